@@ -1,0 +1,272 @@
+"""GB300-native soft-correspondence rigid registration (EM-ICP and Softassign).
+
+Python mirror of the reference's registration API (src/3dregistration.h:39-99):
+``emicp(X, Y, R, t, param)`` and ``softassign(X, Y, R, t, param)`` align point
+set Y (source) to X (target) so that X ~ R Y + t. Both run the sm_103a kernels
+of ``libcesa.so`` through its C ABI (include/cesa.h). There is no CPU path: if
+the library is missing or no GPU is present, the calls raise.
+
+Point clouds are ``(n, 3)`` float arrays. R is 3x3 (row-major when flattened),
+t has 3 entries.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcesa.so")
+
+CESA_OK = 0
+CESA_ERR_INVALID_ARGUMENT = 1
+CESA_ERR_CUDA = 2
+CESA_ERR_TIMEOUT = 3
+CESA_ERR_NO_DEVICE = 4
+CESA_ERR_OUT_OF_MEMORY = 5
+CESA_ERR_UNSUPPORTED = 6
+
+SINKHORN_AUTO = 0
+SINKHORN_MATRIX_FREE = 1
+SINKHORN_MATERIALISED = 2
+
+TRACE_STRIDE = 32
+# trace record fields
+T_STEP, T_SCHED, T_SUM = 0, 1, 2
+T_XC, T_YC, T_S, T_R, T_T = slice(3, 6), slice(6, 9), slice(9, 18), slice(18, 27), slice(27, 30)
+T_GAP, T_LMAX = 30, 31
+
+
+class CesaError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__("%s: %s (%d)" % (what or "cesa", status_string(code) if _lib else code, code))
+
+
+class Params(ctypes.Structure):
+    """Mirror of ``cesa_params`` (registrationParameters fields first)."""
+    _fields_ = [
+        ("JMAX", ctypes.c_int), ("I0", ctypes.c_int), ("I1", ctypes.c_int),
+        ("alpha", ctypes.c_float), ("T_0", ctypes.c_float), ("TFACTOR", ctypes.c_float),
+        ("moutlier", ctypes.c_float),
+        ("sigma_p2", ctypes.c_float), ("sigma_inf", ctypes.c_float),
+        ("sigma_factor", ctypes.c_float), ("d_02", ctypes.c_float),
+        ("maxIteration", ctypes.c_int),
+        ("sinkhorn_form", ctypes.c_int), ("timeout_ms", ctypes.c_int), ("device", ctypes.c_int),
+        ("reserved", ctypes.c_int * 5),
+    ]
+
+    @classmethod
+    def default(cls, **kw):
+        """Reference defaults (src/main.cpp:280-315), overridden by keyword."""
+        p = cls()
+        lib().cesa_params_default(ctypes.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        if "T_0" in kw and "moutlier" not in kw:
+            p.moutlier = float(np.float32(1.0 / np.sqrt(np.float32(p.T_0)) * np.exp(np.float32(-1.0))))
+        return p
+
+
+# registrationParameters is the reference's name for the same record
+registrationParameters = Params
+
+
+class Report(ctypes.Structure):
+    _fields_ = [
+        ("trace", ctypes.c_void_p), ("trace_capacity", ctypes.c_int), ("steps", ctypes.c_int),
+        ("sinkhorn_form", ctypes.c_int), ("grid_blocks", ctypes.c_int), ("device_ms", ctypes.c_float),
+        ("reserved", ctypes.c_int * 3),
+    ]
+
+
+_lib = None
+
+_p = ctypes.c_void_p
+_i = ctypes.c_int
+_f = ctypes.c_float
+
+
+def lib():
+    """The loaded libcesa.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libcesa.so is not built (run: python -m cuda_emicp_softassign_gb300.build)")
+        L = ctypes.CDLL(LIB_PATH)
+        L.cesa_params_default.argtypes = [_p]
+        L.cesa_params_default.restype = None
+        for name in ("cesa_emicp", "cesa_softassign"):
+            fn = getattr(L, name)
+            fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
+            fn.restype = _i
+        for name in ("cesa_emicp_device", "cesa_softassign_device"):
+            fn = getattr(L, name)
+            fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
+            fn.restype = _i
+        L.cesa_stream_status.argtypes = [_p]
+        L.cesa_stream_status.restype = _i
+        L.cesa_emicp_step_device.argtypes = [_p, _i, _p, _i, _p, _p, _f, _f, _p, _p, _p]
+        L.cesa_emicp_step_device.restype = _i
+        L.cesa_softassign_step_device.argtypes = [_p, _i, _p, _i, _p, _p, _f, _f, _i, _i,
+                                                  _p, _p, _p, _p, _p, _p, _p]
+        L.cesa_softassign_step_device.restype = _i
+        L.cesa_find_rt_from_s.argtypes = [_p] * 6
+        L.cesa_find_rt_from_s.restype = _i
+        L.cesa_cloud2data.argtypes = [_p, _i, _i, _p]
+        L.cesa_cloud2data.restype = _i
+        L.cesa_release_workspaces.argtypes = []
+        L.cesa_release_workspaces.restype = None
+        L.cesa_status_string.argtypes = [_i]
+        L.cesa_status_string.restype = ctypes.c_char_p
+        L.cesa_version.restype = _i
+        _lib = L
+    return _lib
+
+
+def status_string(code):
+    return lib().cesa_status_string(int(code)).decode()
+
+
+def _check(rc, what):
+    if rc != CESA_OK:
+        raise CesaError(rc, what)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def cloud2data(points):
+    """(n, 3) points -> SoA float32 [x..., y..., z...] (src/cloud2data.cpp:29-46)."""
+    P = np.ascontiguousarray(points, dtype=np.float32)
+    if P.ndim != 2 or P.shape[1] < 3:
+        raise ValueError("points must be (n, 3)")
+    out = np.empty(3 * P.shape[0], np.float32)
+    _check(lib().cesa_cloud2data(_ptr(P), P.shape[0], P.shape[1], _ptr(out)), "cloud2data")
+    return out
+
+
+def _pose_in(R, t):
+    Rh = np.ascontiguousarray(np.eye(3) if R is None else R, dtype=np.float32).reshape(-1).copy()
+    th = np.ascontiguousarray(np.zeros(3) if t is None else t, dtype=np.float32).reshape(-1).copy()
+    if Rh.size != 9 or th.size != 3:
+        raise ValueError("R must be 3x3 and t must have 3 entries")
+    return Rh, th
+
+
+def _host_call(fn_name, X, Y, R, t, param, trace):
+    Xs, Ys = cloud2data(X), cloud2data(Y)
+    Rh, th = _pose_in(R, t)
+    rep = Report()
+    tr = None
+    if trace:
+        cap = int(trace) if not isinstance(trace, bool) else 100000
+        tr = np.zeros((cap, TRACE_STRIDE))
+        rep.trace = tr.ctypes.data
+        rep.trace_capacity = cap
+    rc = getattr(lib(), fn_name)(_ptr(Xs), len(X), _ptr(Ys), len(Y), _ptr(Rh), _ptr(th),
+                                 ctypes.byref(param), ctypes.byref(rep))
+    _check(rc, fn_name)
+    out = (Rh.reshape(3, 3).astype(np.float64), th.astype(np.float64))
+    if trace:
+        return out + (tr[: min(rep.steps, tr.shape[0])], rep)
+    return out
+
+
+def emicp(X, Y, R=None, t=None, param=None, trace=False):
+    """Annealed EM-ICP on the GPU (replaces emicp(), src/emicp.cu:247-716).
+
+    Returns (R, t), or (R, t, trace, report) when ``trace`` is set.
+    """
+    return _host_call("cesa_emicp", X, Y, R, t, param or Params.default(), trace)
+
+
+def softassign(X, Y, R=None, t=None, param=None, trace=False):
+    """Annealed Softassign on the GPU (replaces softassign(), src/softassign.cu:256-886)."""
+    return _host_call("cesa_softassign", X, Y, R, t, param or Params.default(), trace)
+
+
+def find_rt_from_s(Xc, Yc, S, q_prev=None):
+    """Horn's pose from centres and cross-covariance (replaces findRTfromS)."""
+    xc = np.ascontiguousarray(Xc, dtype=np.float32)
+    yc = np.ascontiguousarray(Yc, dtype=np.float32)
+    s = np.ascontiguousarray(np.asarray(S, dtype=np.float32).reshape(-1))
+    R = np.zeros(9, np.float32)
+    t = np.zeros(3, np.float32)
+    qp = None if q_prev is None else np.ascontiguousarray(q_prev, dtype=np.float32)
+    _check(lib().cesa_find_rt_from_s(_ptr(xc), _ptr(yc), _ptr(s), _ptr(R), _ptr(t),
+                                     _ptr(qp) if qp is not None else None), "find_rt_from_s")
+    return R.reshape(3, 3).astype(np.float64), t.astype(np.float64)
+
+
+# ----------------------------------------------------------------- device API
+# These take torch CUDA tensors (torch only provides the device memory and the
+# stream; the work runs in libcesa.so).
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def emicp_device(dX, dY, dRt, param=None, d_status=None, stream=None):
+    """Enqueue EM-ICP on device SoA tensors; dRt (12 floats, R then t) is in/out."""
+    p = param or Params.default()
+    rc = lib().cesa_emicp_device(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3, _dptr(dRt),
+                                 ctypes.byref(p), _dptr(d_status) if d_status is not None else None,
+                                 ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "emicp_device")
+
+
+def softassign_device(dX, dY, dRt, param=None, d_status=None, stream=None):
+    p = param or Params.default()
+    rc = lib().cesa_softassign_device(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3,
+                                      _dptr(dRt), ctypes.byref(p),
+                                      _dptr(d_status) if d_status is not None else None,
+                                      ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "softassign_device")
+
+
+def stream_status(stream=None):
+    return lib().cesa_stream_status(ctypes.c_void_p(_stream_handle(stream)))
+
+
+def emicp_step(dX, dY, R, t, sigma_p2, d_02, row_out=None, stream=None):
+    """One fused E-step from (R, t). Returns moments[16] = sum(lambda), Xc, Yc, S."""
+    Rh, th = _pose_in(R, t)
+    mom = np.zeros(16)
+    rc = lib().cesa_emicp_step_device(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3,
+                                      _ptr(Rh), _ptr(th), sigma_p2, d_02,
+                                      _dptr(row_out) if row_out is not None else None, _ptr(mom),
+                                      ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "emicp_step")
+    return mom
+
+
+def softassign_step(dX, dY, R, t, T, alpha, I1, s, u, rs=None, cs=None, w=None,
+                    form=SINKHORN_MATRIX_FREE, stream=None):
+    """One Softassign inner iteration; s, u (device) are updated in place."""
+    Rh, th = _pose_in(R, t)
+    mom = np.zeros(16)
+    opt = lambda x: _dptr(x) if x is not None else None  # noqa: E731
+    rc = lib().cesa_softassign_step_device(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3,
+                                           _ptr(Rh), _ptr(th), T, alpha, I1, form, _dptr(s), _dptr(u),
+                                           opt(rs), opt(cs), opt(w), _ptr(mom),
+                                           ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "softassign_step")
+    return mom
+
+
+def release_workspaces():
+    lib().cesa_release_workspaces()
+
+
+def version():
+    return lib().cesa_version()

@@ -1,0 +1,88 @@
+"""Builds libcesa.so (the C ABI declared in include/cesa.h) for sm_103a.
+
+Each ``csrc/*.cu`` file is compiled in parallel with nvcc, then linked into
+``cuda_emicp_softassign_gb300/libcesa.so`` with a static CUDA runtime. A
+version script exports only the ``cesa_*`` symbols. Object files go to
+``cuda_emicp_softassign_gb300/_build/``.
+
+Run ``python -m cuda_emicp_softassign_gb300.build`` or call :func:`build`.
+"""
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libcesa.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE]
+SOURCES = ["cesa_api.cu", "cesa_emicp.cu", "cesa_softassign.cu"]
+HEADERS = ["cesa_common.cuh", "cesa_sweep.cuh", "cesa_pose.h", "cesa_kernels.h", "cesa_prep.cuh"]
+
+
+def nvcc():
+    exe = shutil.which("nvcc")
+    if exe:
+        return exe
+    cand = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(cand):
+        return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcesa.so")
+
+
+def _mtime(p):
+    return os.path.getmtime(p) if os.path.exists(p) else 0.0
+
+
+def _deps_mtime():
+    paths = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "cesa.h"), __file__]
+    return max(_mtime(p) for p in paths)
+
+
+def _compile(src, verbose):
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    s = os.path.join(CSRC, src)
+    if _mtime(obj) >= max(_mtime(s), _deps_mtime()):
+        return obj
+    cmd = [nvcc()] + NVFLAGS + ["-c", s, "-o", obj]
+    if verbose:
+        cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+    if verbose and r.stderr:
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build(force=False, verbose=False):
+    """Compiles and links libcesa.so; returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    if force:
+        for f in os.listdir(BUILD):
+            if f.endswith(".o"):
+                os.remove(os.path.join(BUILD, f))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    if _mtime(LIB) >= max(_mtime(o) for o in objs) and not force:
+        return LIB
+    vs = os.path.join(BUILD, "exports.map")
+    with open(vs, "w") as f:
+        f.write("{ global: cesa_*; local: *; };\n")
+    tmp = LIB + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + [
+        "-Xlinker", "--version-script=" + vs, "-Xcompiler", "-fPIC"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,544 @@
+// C ABI of libcesa.so (declared in include/cesa.h).
+//
+// Host-pointer entry points keep the reference's calling convention: they
+// return only after R,t have been written back. Unlike the reference
+// (src/emicp.cu:713, src/softassign.cu:885), they never reset the device.
+// Device memory (point copies, workspace, trace) is cached per
+// (device, stream) and reused by later calls with the same or smaller sizes.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "../../include/cesa.h"
+#include "cesa_kernels.h"
+#include "cesa_pose.h"
+
+namespace cesa {
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, need);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    bytes = need;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct StreamCtx {
+  DevBuf ws;     // kernel workspace (control block first)
+  DevBuf io;     // point copies + pose + outputs for host-pointer calls
+  DevBuf trace;  // device trace records
+  int last_trace_steps = 0;
+  int last_kind = 0;  // 1 emicp, 2 softassign
+};
+
+std::mutex g_mu;
+std::map<std::pair<int, cudaStream_t>, StreamCtx> g_ctx;
+std::map<int, cudaStream_t> g_own_stream;
+
+StreamCtx& ctx_for(int dev, cudaStream_t st) { return g_ctx[std::make_pair(dev, st)]; }
+
+int map_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return CESA_OK;
+  if (e == cudaErrorMemoryAllocation) return CESA_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return CESA_ERR_NO_DEVICE;
+  if (e == cudaErrorCooperativeLaunchTooLarge) return CESA_ERR_UNSUPPORTED;
+  return CESA_ERR_CUDA;
+}
+
+uint64_t timeout_ns_of(const cesa_params* p) {
+  const int ms = (p && p->timeout_ms > 0) ? p->timeout_ms : 10000;
+  return (uint64_t)ms * 1000000ull;
+}
+
+// Number of sigma steps of src/emicp.cu:443,668 (FP32 loop), or -1 if it
+// would never end.
+long emicp_steps(float sigma_p2, float sigma_inf, float sigma_factor) {
+  long n = 0;
+  float s = sigma_p2;
+  while (s > sigma_inf) {
+    ++n;
+    s *= sigma_factor;
+    if (n > 100000000L) return -1;
+  }
+  return n;
+}
+
+int check_points(const float* X, int N, const float* Y, int M) {
+  if (!X || !Y || N < 1 || M < 1) return CESA_ERR_INVALID_ARGUMENT;
+  if ((long)N * 16 > 0x7fffffffL || (long)M * 16 > 0x7fffffffL) return CESA_ERR_INVALID_ARGUMENT;
+  return CESA_OK;
+}
+
+int check_emicp_params(const cesa_params* p) {
+  if (!p) return CESA_ERR_INVALID_ARGUMENT;
+  if (!(p->sigma_p2 > 0.f) || !(p->sigma_inf > 0.f) || !(p->sigma_factor > 0.f) ||
+      !(p->d_02 >= 0.f) || !isfinite(p->sigma_p2))
+    return CESA_ERR_INVALID_ARGUMENT;
+  if (p->sigma_p2 > p->sigma_inf && !(p->sigma_factor < 1.f)) return CESA_ERR_INVALID_ARGUMENT;
+  return CESA_OK;
+}
+
+int check_sa_params(const cesa_params* p) {
+  if (!p) return CESA_ERR_INVALID_ARGUMENT;
+  if (p->JMAX < 0 || p->I0 < 0 || p->I1 < 1) return CESA_ERR_INVALID_ARGUMENT;
+  if (!(p->T_0 > 0.f) || !(p->TFACTOR > 0.f) || !isfinite(p->alpha) || !(p->moutlier >= 0.f))
+    return CESA_ERR_INVALID_ARGUMENT;
+  if ((long)p->JMAX * (long)p->I0 > 100000000L) return CESA_ERR_INVALID_ARGUMENT;
+  return CESA_OK;
+}
+
+int select_device(const cesa_params* p, int* dev) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return CESA_ERR_NO_DEVICE;
+  if (p && p->device >= 0) {
+    if (p->device >= n) return CESA_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(p->device) != cudaSuccess) return CESA_ERR_CUDA;
+  }
+  if (cudaGetDevice(dev) != cudaSuccess) return CESA_ERR_CUDA;
+  return CESA_OK;
+}
+
+cudaStream_t own_stream(int dev) {
+  auto it = g_own_stream.find(dev);
+  if (it != g_own_stream.end()) return it->second;
+  cudaStream_t s = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  g_own_stream[dev] = s;
+  return s;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Shared body of the two host-pointer entry points.
+int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9], float t[3],
+             const cesa_params* p, cesa_report* rep) {
+  int rc = check_points(X, N, Y, M);
+  if (rc) return rc;
+  if (!R || !t) return CESA_ERR_INVALID_ARGUMENT;
+  rc = kind == 1 ? check_emicp_params(p) : check_sa_params(p);
+  if (rc) return rc;
+  long nsteps = kind == 1 ? emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor)
+                          : (long)p->JMAX * (long)p->I0;
+  if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  rc = select_device(p, &dev);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t st = own_stream(dev);
+  StreamCtx& C = ctx_for(dev, st);
+  const size_t bx = align256(sizeof(float) * 3 * (size_t)N);
+  const size_t by = align256(sizeof(float) * 3 * (size_t)M);
+  cudaError_t e = C.io.ensure(bx + by + 256);
+  if (e != cudaSuccess) return map_cuda(e);
+  float* dX = static_cast<float*>(C.io.p);
+  float* dY = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx);
+  float* dRt = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx + by);
+  const size_t need = kind == 1 ? emicp_ws_need(N, M, dev)
+                                : softassign_ws_need(N, M, p->sinkhorn_form, dev);
+  e = C.ws.ensure(need);
+  if (e != cudaSuccess) return map_cuda(e);
+  const int cap = (rep && rep->trace && rep->trace_capacity > 0) ? rep->trace_capacity : 0;
+  double* dtrace = nullptr;
+  if (cap > 0) {
+    e = C.trace.ensure(sizeof(double) * 32 * (size_t)cap);
+    if (e != cudaSuccess) return map_cuda(e);
+    dtrace = static_cast<double*>(C.trace.p);
+  }
+  float hRt[12];
+  memcpy(hRt, R, sizeof(float) * 9);
+  memcpy(hRt + 9, t, sizeof(float) * 3);
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  e = cudaMemcpyAsync(dX, X, sizeof(float) * 3 * (size_t)N, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dY, Y, sizeof(float) * 3 * (size_t)M, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dRt, hRt, sizeof(hRt), cudaMemcpyHostToDevice, st);
+  int grid = 0;
+  int kerr = 0;
+  if (e == cudaSuccess) {
+    cudaEventRecord(ev0, st);
+    if (kind == 1) {
+      EmicpLaunch L{};
+      L.dX = dX;
+      L.dY = dY;
+      L.N = N;
+      L.M = M;
+      L.sigma_p2 = p->sigma_p2;
+      L.sigma_factor = p->sigma_factor;
+      L.d_02 = p->d_02;
+      L.nsteps = (int)nsteps;
+      L.dRt = dRt;
+      L.trace = dtrace;
+      L.trace_cap = cap;
+      L.timeout_ns = timeout_ns_of(p);
+      kerr = enqueue_emicp(L, C.ws.p, C.ws.bytes, st, &grid);
+    } else {
+      SoftassignLaunch L{};
+      L.dX = dX;
+      L.dY = dY;
+      L.N = N;
+      L.M = M;
+      L.JMAX = p->JMAX;
+      L.I0 = p->I0;
+      L.I1 = p->I1;
+      L.alpha = p->alpha;
+      L.T_0 = p->T_0;
+      L.TFACTOR = p->TFACTOR;
+      L.moutlier = p->moutlier;
+      L.form = CESA_SINKHORN_MATRIX_FREE;
+      L.dRt = dRt;
+      L.trace = dtrace;
+      L.trace_cap = cap;
+      L.timeout_ns = timeout_ns_of(p);
+      kerr = enqueue_softassign(L, C.ws.p, C.ws.bytes, st, &grid);
+    }
+    cudaEventRecord(ev1, st);
+    if (kerr != 0) e = (cudaError_t)kerr;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hRt, dRt, sizeof(hRt), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  int status = 0, steps = 0;
+  if (e == cudaSuccess) e = (cudaError_t)read_ws_status(C.ws.p, st, &status, &steps);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (e != cudaSuccess) return map_cuda(e);
+  if (status != 0) return status;
+  C.last_kind = kind;
+  C.last_trace_steps = steps < cap ? steps : cap;
+  if (cap > 0 && C.last_trace_steps > 0) {
+    e = cudaMemcpy(rep->trace, dtrace, sizeof(double) * 32 * (size_t)C.last_trace_steps,
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return map_cuda(e);
+  }
+  memcpy(R, hRt, sizeof(float) * 9);
+  memcpy(t, hRt + 9, sizeof(float) * 3);
+  if (rep) {
+    rep->steps = (int)nsteps;
+    rep->sinkhorn_form = kind == 2 ? CESA_SINKHORN_MATRIX_FREE : 0;
+    rep->grid_blocks = grid;
+    rep->device_ms = ms;
+  }
+  return CESA_OK;
+}
+
+}  // namespace
+}  // namespace cesa
+
+using namespace cesa;
+
+extern "C" {
+
+void cesa_params_default(cesa_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->JMAX = 100;
+  p->I0 = 5;
+  p->I1 = 3;
+  p->alpha = 3.0f;
+  p->T_0 = 100.0f;
+  p->TFACTOR = 0.95f;
+  p->moutlier = (float)(1 / sqrtf(p->T_0) * expf(-1.0f));
+  p->sigma_p2 = 0.01f;
+  p->sigma_inf = 0.00001f;
+  p->sigma_factor = 0.9f;
+  p->d_02 = 0.01f;
+  p->maxIteration = 30;
+  p->sinkhorn_form = CESA_SINKHORN_AUTO;
+  p->timeout_ms = 0;
+  p->device = -1;
+}
+
+int cesa_emicp(const float* X, int N, const float* Y, int M, float R[9], float t[3],
+               const cesa_params* p, cesa_report* rep) {
+  return run_host(1, X, N, Y, M, R, t, p, rep);
+}
+
+int cesa_softassign(const float* X, int N, const float* Y, int M, float R[9], float t[3],
+                    const cesa_params* p, cesa_report* rep) {
+  return run_host(2, X, N, Y, M, R, t, p, rep);
+}
+
+int cesa_emicp_device(const float* dX, int N, const float* dY, int M, float* dRt,
+                      const cesa_params* p, int* d_status, cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!dRt) return CESA_ERR_INVALID_ARGUMENT;
+  rc = check_emicp_params(p);
+  if (rc) return rc;
+  const long nsteps = emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor);
+  if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(emicp_ws_need(N, M, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  EmicpLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.sigma_p2 = p->sigma_p2;
+  L.sigma_factor = p->sigma_factor;
+  L.d_02 = p->d_02;
+  L.nsteps = (int)nsteps;
+  L.dRt = dRt;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  C.last_kind = 1;
+  C.last_trace_steps = 0;
+  return map_cuda((cudaError_t)enqueue_emicp(L, C.ws.p, C.ws.bytes, st, nullptr));
+}
+
+int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float* dRt,
+                           const cesa_params* p, int* d_status, cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!dRt) return CESA_ERR_INVALID_ARGUMENT;
+  rc = check_sa_params(p);
+  if (rc) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, p->sinkhorn_form, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  SoftassignLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.JMAX = p->JMAX;
+  L.I0 = p->I0;
+  L.I1 = p->I1;
+  L.alpha = p->alpha;
+  L.T_0 = p->T_0;
+  L.TFACTOR = p->TFACTOR;
+  L.moutlier = p->moutlier;
+  L.form = CESA_SINKHORN_MATRIX_FREE;
+  L.dRt = dRt;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  C.last_kind = 2;
+  C.last_trace_steps = 0;
+  return map_cuda((cudaError_t)enqueue_softassign(L, C.ws.p, C.ws.bytes, st, nullptr));
+}
+
+int cesa_stream_status(cesa_stream_t stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_ctx.find(std::make_pair(dev, (cudaStream_t)stream));
+  if (it == g_ctx.end() || !it->second.ws.p) return CESA_ERR_INVALID_ARGUMENT;
+  int status = 0, steps = 0;
+  const int e = read_ws_status(it->second.ws.p, (cudaStream_t)stream, &status, &steps);
+  if (e) return map_cuda((cudaError_t)e);
+  return status;
+}
+
+int cesa_emicp_step_device(const float* dX, int N, const float* dY, int M, const float R[9],
+                           const float t[3], float sigma_p2, float d_02, float* row_out,
+                           double moments[16], cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!R || !t || !(sigma_p2 > 0.f) || !(d_02 >= 0.f)) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(emicp_ws_need(N, M, dev));
+  if (e == cudaSuccess) e = C.io.ensure(256);
+  if (e == cudaSuccess) e = C.trace.ensure(sizeof(double) * 32);
+  if (e != cudaSuccess) return map_cuda(e);
+  float hRt[12];
+  memcpy(hRt, R, sizeof(float) * 9);
+  memcpy(hRt + 9, t, sizeof(float) * 3);
+  float* dRt = static_cast<float*>(C.io.p);
+  e = cudaMemcpyAsync(dRt, hRt, sizeof(hRt), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return map_cuda(e);
+  EmicpLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.sigma_p2 = sigma_p2;
+  L.sigma_factor = 1.f;
+  L.d_02 = d_02;
+  L.nsteps = 1;
+  L.dRt = dRt;
+  L.row_out = row_out;
+  L.trace = static_cast<double*>(C.trace.p);
+  L.trace_cap = 1;
+  L.timeout_ns = 10000000000ull;
+  const int k = enqueue_emicp(L, C.ws.p, C.ws.bytes, st, nullptr);
+  if (k) return map_cuda((cudaError_t)k);
+  double rec[32];
+  e = cudaMemcpyAsync(rec, C.trace.p, sizeof(rec), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return map_cuda(e);
+  int status = 0, steps = 0;
+  read_ws_status(C.ws.p, st, &status, &steps);
+  if (status) return status;
+  if (moments) {
+    moments[0] = rec[2];
+    for (int i = 0; i < 3; ++i) {
+      moments[1 + i] = rec[3 + i];
+      moments[4 + i] = rec[6 + i];
+    }
+    for (int i = 0; i < 9; ++i) moments[7 + i] = rec[9 + i];
+  }
+  return CESA_OK;
+}
+
+int cesa_softassign_step_device(const float* dX, int N, const float* dY, int M, const float R[9],
+                                const float t[3], float T, float alpha, int I1, int sinkhorn_form,
+                                float* s, float* u, float* rs, float* cs, float* w,
+                                double moments[16], cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!R || !t || !s || !u || !(T > 0.f) || I1 < 1) return CESA_ERR_INVALID_ARGUMENT;
+  (void)sinkhorn_form;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, sinkhorn_form, dev));
+  if (e == cudaSuccess) e = C.io.ensure(256);
+  if (e == cudaSuccess) e = C.trace.ensure(sizeof(double) * 32);
+  if (e != cudaSuccess) return map_cuda(e);
+  float hRt[12];
+  memcpy(hRt, R, sizeof(float) * 9);
+  memcpy(hRt + 9, t, sizeof(float) * 3);
+  float* dRt = static_cast<float*>(C.io.p);
+  e = cudaMemcpyAsync(dRt, hRt, sizeof(hRt), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return map_cuda(e);
+  SoftassignLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.JMAX = 1;
+  L.I0 = 1;
+  L.I1 = I1;
+  L.alpha = alpha;
+  L.T_0 = T;
+  L.TFACTOR = 1.f;
+  L.moutlier = 0.f;
+  L.form = CESA_SINKHORN_MATRIX_FREE;
+  L.dRt = dRt;
+  L.s_io = s;
+  L.u_io = u;
+  L.rs_out = rs;
+  L.cs_out = cs;
+  L.w_out = w;
+  L.trace = static_cast<double*>(C.trace.p);
+  L.trace_cap = 1;
+  L.timeout_ns = 10000000000ull;
+  const int k = enqueue_softassign(L, C.ws.p, C.ws.bytes, st, nullptr);
+  if (k) return map_cuda((cudaError_t)k);
+  double rec[32];
+  e = cudaMemcpyAsync(rec, C.trace.p, sizeof(rec), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return map_cuda(e);
+  int status = 0, steps = 0;
+  read_ws_status(C.ws.p, st, &status, &steps);
+  if (status) return status;
+  if (moments) {
+    moments[0] = rec[2];
+    for (int i = 0; i < 3; ++i) {
+      moments[1 + i] = rec[3 + i];
+      moments[4 + i] = rec[6 + i];
+    }
+    for (int i = 0; i < 9; ++i) moments[7 + i] = rec[9 + i];
+  }
+  return CESA_OK;
+}
+
+int cesa_find_rt_from_s(const float Xc[3], const float Yc[3], const float S[9], float R[9],
+                        float t[3], float q_prev[4]) {
+  if (!Xc || !Yc || !S || !R || !t) return CESA_ERR_INVALID_ARGUMENT;
+  HornState<double> st;
+  st.reset();
+  if (q_prev)
+    for (int i = 0; i < 4; ++i) st.q[i] = q_prev[i];
+  double Sd[9], q[4], gap, lmax;
+  for (int i = 0; i < 9; ++i) Sd[i] = S[i];
+  const int fb = horn_quaternion<double>(Sd, st, q, &gap, &lmax);
+  // R from the FP32-rounded quaternion, t = Xc - R Yc in FP32, as the
+  // reference does with its float q (src/findRTfromS.cpp:57,80-96).
+  float qf[4];
+  for (int i = 0; i < 4; ++i) qf[i] = (float)q[i];
+  float xc[3] = {Xc[0], Xc[1], Xc[2]}, yc[3] = {Yc[0], Yc[1], Yc[2]};
+  quat_to_pose<float>(qf, xc, yc, R, t);
+  if (q_prev && !fb)
+    for (int i = 0; i < 4; ++i) q_prev[i] = qf[i];
+  return CESA_OK;
+}
+
+int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_out) {
+  if (n < 0 || (n > 0 && (!points || !soa_out)) || stride_floats < 3) return CESA_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n; ++i) {
+    soa_out[i] = points[(size_t)i * stride_floats + 0];
+    soa_out[n + i] = points[(size_t)i * stride_floats + 1];
+    soa_out[2 * n + i] = points[(size_t)i * stride_floats + 2];
+  }
+  return CESA_OK;
+}
+
+void cesa_release_workspaces(void) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  for (auto& kv : g_ctx) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(kv.first.first);
+    kv.second.ws.release();
+    kv.second.io.release();
+    kv.second.trace.release();
+    cudaSetDevice(cur);
+  }
+  g_ctx.clear();
+}
+
+const char* cesa_status_string(int status) {
+  switch (status) {
+    case CESA_OK: return "ok";
+    case CESA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case CESA_ERR_CUDA: return "CUDA runtime error";
+    case CESA_ERR_TIMEOUT: return "device-side wait timed out";
+    case CESA_ERR_NO_DEVICE: return "no usable CUDA device";
+    case CESA_ERR_OUT_OF_MEMORY: return "out of memory";
+    case CESA_ERR_UNSUPPORTED: return "unsupported request";
+    default: return "unknown status";
+  }
+}
+
+int cesa_version(void) { return 100; }
+
+}  // extern "C"

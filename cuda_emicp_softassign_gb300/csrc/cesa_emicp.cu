@@ -1,0 +1,421 @@
+// Fused, streaming EM-ICP for sm_103a: the whole sigma schedule of emicp()
+// (src/emicp.cu:441-669) in one persistent cooperative launch, with the N x M
+// matrix A never materialised.
+//
+// Reference step (src/emicp.cu:453-635), rows r = Y points, columns c = X:
+//   A_rc = exp(-|x_c - (R y_r + t)|^2 / sigma_p2)               (updateA)
+//   C_r  = sum_c A_rc + exp(-d_02 / sigma_p2)                    (Sgemv + Saxpy)
+//   A_rc <- sqrt(A_rc / C_r)   if C_r > 1e-6, else 1/N           (normalizeRowsOfA)
+//   lambda_r = sum_c A_rc,  X'_r = sum_c A_rc x_c / lambda_r     (Sgemv, Sgemm, division)
+//   Xc = sum lambda X' / sum lambda,  Yc = sum lambda y / sum lambda
+//   S  = sum_r lambda_r (X'_r - Xc)(y_r - Yc)^T,  pose = findRTfromS(Xc, Yc, S)
+// One-pass restatement used here: with e_rc = exp(-d^2 / (2 sigma_p2)) we have
+// A = e^2 and sqrt(A / C) = e / sqrt(C). Per row, three running sums over the
+// columns give everything: sum e^2, sum e, sum e*x. Then
+//   C_r = sum e^2 + outlier,  lambda_r = sum e / sqrt(C_r),  lambda_r X'_r = sum e x / sqrt(C_r).
+// Per element that is 3 FADD (direct differences), FMUL + 2 FFMA (d^2),
+// FMUL (scale), 1 MUFU ex2, and FFMA + FADD + 3 FFMA (accumulators): 12 FP32
+// pipe ops + 1 MUFU op.
+//
+// Coordinates are centred on the device (FP32 offsets oX, oY) before the
+// loop. EM-ICP's S is translation invariant, so only Xc, Yc and t are shifted
+// back; the pose enters and leaves in the caller's frame.
+#include "cesa_kernels.h"
+#include "cesa_pose.h"
+#include "cesa_prep.cuh"
+#include "cesa_sweep.cuh"
+
+namespace cesa {
+
+constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), sum u y^T (9)
+
+struct EmicpArgs {
+  const float4* rows;  // Y' centred (owned), M
+  const float4* cols;  // X' centred (streamed), N
+  int M, N;
+  SweepGeom geo;
+  float sigma0, sigma_factor, d_02;
+  int nsteps;
+  const CenterHdr* hdr;
+  float* dRt;           // PoseIO in/out, caller frame
+  float* part;          // split partials [nblk*S][5][128]
+  unsigned* cnt;        // [nblk]
+  df* bpart;            // [2][grid][kEmNV]
+  Ctl* ctl;
+  double* trace;
+  int trace_cap;
+  float* row_out;       // optional [M][5] (centred-frame u)
+  int* d_status;
+  uint64_t timeout_ns;
+};
+
+// Per-element work of the fused E-step (see the file comment).
+struct EmicpElem {
+  float nk;  // -log2(e) / (2 sigma_p2)
+  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 x,
+                                             float4) const {
+    const float dx = x.x - p[0];
+    const float dy = x.y - p[1];
+    const float dz = x.z - p[2];
+    float d2 = dx * dx;
+    d2 = fmaf(dy, dy, d2);
+    d2 = fmaf(dz, dz, d2);
+    const float e = ex2_approx(d2 * nk);
+    acc[0] = fmaf(e, e, acc[0]);
+    acc[1] += e;
+    acc[2] = fmaf(e, x.x, acc[2]);
+    acc[3] = fmaf(e, x.y, acc[3]);
+    acc[4] = fmaf(e, x.z, acc[4]);
+  }
+};
+
+// Row finalize: C_r, lambda_r, u_r = lambda_r X'_r, and the row's share of the
+// 16 moments (block accumulator, compensated).
+struct EmicpFin {
+  const float4* rows;
+  int M;
+  float outlier;
+  float xm[3];
+  float* row_out;  // caller frame: u = lambda X' + lambda oX
+  float oX[3];
+  df* red;
+  df* acc;
+  __device__ void operator()(int blk, const float (&tot)[5]) const {
+    df v[kEmNV];
+#pragma unroll
+    for (int k = 0; k < kEmNV; ++k) v[k] = df_make(0.f);
+    const int r = blk * kBlockPts + (int)threadIdx.x;
+    if (threadIdx.x < kBlockPts && r < M) {
+      const float4 y = ld_cg(rows + r);
+      const float C = tot[0] + outlier;
+      float lam, uu[3];
+      if (C > 10e-7f) {  // src/emicp.cu:155
+        const float inv = __frsqrt_rn(C);
+        lam = tot[1] * inv;
+        uu[0] = tot[2] * inv;
+        uu[1] = tot[3] * inv;
+        uu[2] = tot[4] * inv;
+      } else {  // A <- 1/N (src/emicp.cu:159): lambda = 1, lambda X' = mean(X)
+        lam = 1.f;
+        uu[0] = xm[0];
+        uu[1] = xm[1];
+        uu[2] = xm[2];
+      }
+      if (row_out) {
+        float* o = row_out + (size_t)r * 5;
+        o[0] = C;
+        o[1] = lam;
+        o[2] = fmaf(lam, oX[0], uu[0]);
+        o[3] = fmaf(lam, oX[1], uu[1]);
+        o[4] = fmaf(lam, oX[2], uu[2]);
+      }
+      const float yy[3] = {y.x, y.y, y.z};
+      df_add(v[0], lam);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        df_add(v[1 + i], uu[i]);
+        df_add_prod(v[4 + i], lam, yy[i]);
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
+    }
+    block_accumulate<kEmNV>(v, red, acc);
+  }
+};
+
+__global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
+  __shared__ float s_pose[12];
+  __shared__ df s_acc[kEmNV];
+  __shared__ df s_red[kThreads];
+  __shared__ df s_tot[kEmNV];
+  __shared__ float s_hdr[12];
+
+  const int tid = threadIdx.x;
+  const unsigned G = gridDim.x;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.full[s], 1);
+    mbar_init_fence();
+    for (int k = 0; k < 3; ++k) {
+      s_hdr[k] = A.hdr->oX[k];
+      s_hdr[3 + k] = A.hdr->oY[k];
+      s_hdr[6 + k] = A.hdr->xmean[k];
+    }
+    float R[9], t[3], tc[3];
+    for (int k = 0; k < 9; ++k) R[k] = A.dRt[k];
+    for (int k = 0; k < 3; ++k) t[k] = A.dRt[9 + k];
+    pose_to_centred(R, t, &s_hdr[0], &s_hdr[3], tc);
+    for (int k = 0; k < 9; ++k) s_pose[k] = R[k];
+    for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
+  }
+  __syncthreads();
+
+  HornState<float> horn;
+  horn.reset();
+  Pipe pipe;
+  pipe_init(pipe);
+  unsigned epoch = 0;
+  const StreamSrc src{A.cols, nullptr, true};
+  float s2 = A.sigma0;
+
+  for (int step = 0; step < A.nsteps; ++step) {
+    const float outlier = expf(-A.d_02 / s2);  // src/emicp.cu:489
+    if (tid < kEmNV) s_acc[tid] = df_make(0.f);
+    float R[9], tc[3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
+    __syncthreads();
+
+    // e = exp(-d2 / (2 s2)) = 2^(nk d2)
+    const EmicpElem elem{-kLog2e / (2.f * s2)};
+    const EmicpFin fin{A.rows,    A.M,
+                       outlier,   {s_hdr[6], s_hdr[7], s_hdr[8]},
+                       A.row_out, {s_hdr[0], s_hdr[1], s_hdr[2]},
+                       s_red,     s_acc};
+    if (!sweep_units<5>(sm, pipe, A.geo, src, A.rows, true, R, tc, (unsigned)step, A.part, A.cnt,
+                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10))
+      break;
+
+    // ---- grid-wide moments -> pose (every block computes the same pose)
+    df* bp = A.bpart + (size_t)(step & 1) * G * kEmNV;
+    if (tid < kEmNV) {
+      const df a = s_acc[tid];
+      __stcg(reinterpret_cast<float2*>(bp + (size_t)blockIdx.x * kEmNV + tid), make_float2(a.hi, a.lo));
+    }
+    if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
+    reduce_block_partials<kEmNV>(bp, (int)G, s_red, s_tot);
+    if (tid == 0) {
+      const float L = df_val(s_tot[0]);
+      float Xc[3], Yc[3], S[9];
+      for (int i = 0; i < 3; ++i) {
+        Xc[i] = df_val(s_tot[1 + i]) / L;
+        Yc[i] = df_val(s_tot[4 + i]) / L;
+      }
+      // S = sum u y^T - L Xc Yc^T (centred frame; S is translation invariant)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+          df a = s_tot[7 + i + 3 * j];
+          df_add_prod(a, -L * Xc[i], Yc[j]);
+          S[i + 3 * j] = df_val(a);
+        }
+      float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
+      horn_quaternion<float>(S, horn, q, &gap, &lmax);
+      quat_to_pose<float>(q, Xc, Yc, Rn, tn);
+      for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];
+      for (int k = 0; k < 3; ++k) s_pose[9 + k] = tn[k];
+      if (blockIdx.x == 0) {
+        if (A.trace && step < A.trace_cap) {
+          double* rec = A.trace + (size_t)step * 32;
+          float to[3];
+          pose_from_centred(Rn, tn, &s_hdr[0], &s_hdr[3], to);
+          rec[0] = step;
+          rec[1] = s2;
+          rec[2] = df_dbl(s_tot[0]);
+          for (int i = 0; i < 3; ++i) {
+            rec[3 + i] = (double)Xc[i] + (double)s_hdr[i];
+            rec[6 + i] = (double)Yc[i] + (double)s_hdr[3 + i];
+            rec[27 + i] = to[i];
+          }
+          for (int k = 0; k < 9; ++k) {
+            rec[9 + k] = S[k];
+            rec[18 + k] = Rn[k];
+          }
+          rec[30] = gap;
+          rec[31] = lmax;
+        }
+        A.ctl->steps_done = step + 1;
+      }
+    }
+    __syncthreads();
+    s2 *= A.sigma_factor;  // FP32, src/emicp.cu:668
+  }
+
+  if (blockIdx.x == 0 && tid == 0) {
+    const int st = ld_status(A.ctl);
+    if (st == kStatusOk) {
+      float R[9], tc[3], t[3];
+      for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
+      for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
+      pose_from_centred(R, tc, &s_hdr[0], &s_hdr[3], t);
+      for (int k = 0; k < 9; ++k) A.dRt[k] = R[k];
+      for (int k = 0; k < 3; ++k) A.dRt[9 + k] = t[k];
+    }
+    if (A.d_status) *A.d_status = st;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+struct Carve {
+  char* p;
+  size_t off = 0;
+  explicit Carve(void* base) : p(static_cast<char*>(base)) {}
+  template <class T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* r = p ? reinterpret_cast<T*>(p + off) : nullptr;
+    off += n * sizeof(T);
+    return r;
+  }
+};
+
+struct EmicpPlan {
+  int grid;
+  SweepGeom geo;
+  size_t smem;
+};
+
+size_t sweep_smem() { return sizeof(SweepSmem); }
+
+EmicpPlan plan_emicp(int N, int M, int device) {
+  EmicpPlan P;
+  P.smem = sweep_smem();
+  const int limit = persistent_grid_limit(device, (const void*)emicp_kernel, P.smem);
+  const SweepGeomH h = plan_sweep(M, N, limit);
+  P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units};
+  P.grid = h.units < limit ? h.units : limit;
+  return P;
+}
+
+struct EmicpCarved {
+  Ctl* ctl;
+  CenterHdr* hdr;
+  float4* rows;
+  float4* cols;
+  float* part;
+  unsigned* cnt;
+  df* bpart;
+};
+
+EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* total) {
+  Carve c(base);
+  EmicpCarved w;
+  w.ctl = c.take<Ctl>(1);
+  w.cnt = c.take<unsigned>((size_t)P.geo.nblk);
+  const size_t zero_end = c.off;  // ctl + counters are cleared per launch
+  w.hdr = c.take<CenterHdr>(1);
+  w.rows = c.take<float4>((size_t)M);
+  w.cols = c.take<float4>((size_t)N);
+  w.part = c.take<float>((size_t)P.geo.units * 5 * kBlockPts);
+  w.bpart = c.take<df>((size_t)2 * P.grid * kEmNV);
+  if (total) *total = c.off;
+  (void)zero_end;
+  return w;
+}
+}  // namespace
+
+size_t emicp_ws_need(int N, int M, int device) {
+  const EmicpPlan P = plan_emicp(N, M, device);
+  size_t total = 0;
+  carve_emicp(nullptr, P, N, M, &total);
+  return total;
+}
+
+int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used) {
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return (int)e;
+  const EmicpPlan P = plan_emicp(L.N, L.M, device);
+  size_t total = 0;
+  EmicpCarved w = carve_emicp(ws, P, L.N, L.M, &total);
+  if (total > ws_bytes) return (int)cudaErrorInvalidValue;
+  if (grid_used) *grid_used = P.grid;
+  // control block + split counters start at zero every launch
+  e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt, 0, sizeof(unsigned) * (size_t)P.geo.nblk, st);
+  if (e != cudaSuccess) return (int)e;
+  prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
+  const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
+  prep_pack_kernel<<<pg_x < 1024 ? pg_x : 1024, pb, 0, st>>>(L.dX, L.N, w.hdr, 0, 0.f, w.cols);
+  prep_pack_kernel<<<pg_y < 1024 ? pg_y : 1024, pb, 0, st>>>(L.dY, L.M, w.hdr, 1, 0.f, w.rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  if (L.nsteps <= 0) return 0;
+
+  EmicpArgs A;
+  A.rows = w.rows;
+  A.cols = w.cols;
+  A.M = L.M;
+  A.N = L.N;
+  A.geo = P.geo;
+  A.sigma0 = L.sigma_p2;
+  A.sigma_factor = L.sigma_factor;
+  A.d_02 = L.d_02;
+  A.nsteps = L.nsteps;
+  A.hdr = w.hdr;
+  A.dRt = L.dRt;
+  A.part = w.part;
+  A.cnt = w.cnt;
+  A.bpart = w.bpart;
+  A.ctl = w.ctl;
+  A.trace = L.trace;
+  A.trace_cap = L.trace_cap;
+  A.row_out = L.row_out;
+  A.d_status = L.d_status;
+  A.timeout_ns = L.timeout_ns;
+  void* args[] = {(void*)&A};
+  e = cudaLaunchCooperativeKernel((const void*)emicp_kernel, dim3(P.grid), dim3(kThreads), args,
+                                  P.smem, st);
+  return (int)e;
+}
+
+int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps) {
+  Ctl h;
+  cudaError_t e = cudaMemcpyAsync(&h, ws, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return (int)e;
+  if (status) *status = h.status;
+  if (steps) *steps = h.steps_done;
+  return 0;
+}
+
+// Smem opt-in and occupancy for a persistent kernel: blocks per SM x SMs.
+int persistent_grid_limit(int device, const void* kernel, size_t smem) {
+  static int cached_dev = -1;
+  static int sms = 0;
+  if (cached_dev != device) {
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cached_dev = device;
+  }
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  if (per_sm > 2) per_sm = 2;
+  return per_sm * (sms > 0 ? sms : 1);
+}
+
+// Unit decomposition: minimise waves x (unit work + fixed cost) over the split S.
+SweepGeomH plan_sweep(int n_own, int n_stream, int grid_limit) {
+  SweepGeomH best{};
+  const int nblk = (n_own + kBlockPts - 1) / kBlockPts;
+  const double fixed = 24000.0;  // per-unit fixed cost in element evaluations
+  double best_cost = 1e300;
+  const int smax_stream = (n_stream + 31) / 32;
+  const int smax = smax_stream < 128 ? smax_stream : 128;
+  for (int S = 1; S <= (smax > 0 ? smax : 1); ++S) {
+    const int slice_len = (n_stream + S - 1) / S;
+    const int s_eff = (n_stream + slice_len - 1) / slice_len;
+    if (s_eff != S) continue;
+    const long units = (long)nblk * S;
+    const int grid = units < grid_limit ? (int)units : grid_limit;
+    const long waves = (units + grid - 1) / grid;
+    const double cost = (double)waves * ((double)kBlockPts * slice_len + fixed) +
+                        (S > 1 ? 4000.0 : 0.0);
+    if (cost < best_cost * 0.999) {
+      best_cost = cost;
+      best = SweepGeomH{n_own, n_stream, nblk, S, slice_len, (int)units};
+    }
+  }
+  if (best.units == 0) best = SweepGeomH{n_own, n_stream, nblk, 1, n_stream, nblk};
+  return best;
+}
+
+}  // namespace cesa

@@ -1,0 +1,84 @@
+// Host-visible launch interface of the registration kernels (internal to
+// libcesa.so; the public C ABI is include/cesa.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cesa {
+
+struct SweepGeomH {
+  int n_own, n_stream, nblk, slices, slice_len, units;
+};
+
+// Centering header computed on the device by prep_center_kernel.
+struct CenterHdr {
+  float oX[4];     // FP32 offset subtracted from X (mean of X rounded to float)
+  float oY[4];     // same for Y
+  float xmean[4];  // mean of the centred X' (used by EM-ICP rows with C_r <= 1e-6)
+  float ymean[4];
+};
+
+// Pose I/O block: R (9, row-major) and t (3) in the caller's frame.
+struct PoseIO {
+  float R[9];
+  float t[3];
+};
+
+struct EmicpLaunch {
+  const float* dX;  // SoA, N
+  const float* dY;  // SoA, M
+  int N, M;
+  float sigma_p2, sigma_factor, d_02;
+  int nsteps;
+  float* dRt;        // PoseIO in/out (device)
+  float* row_out;    // optional [M][5]
+  double* trace;     // optional device trace [cap][32]
+  int trace_cap;
+  int* d_status;     // optional device status mirror
+  uint64_t timeout_ns;
+};
+
+struct SoftassignLaunch {
+  const float* dX;  // SoA, N (rows of the match matrix)
+  const float* dY;  // SoA, M (columns)
+  int N, M;
+  int JMAX, I0, I1;
+  float alpha, T_0, TFACTOR, moutlier;
+  int form;          // CESA_SINKHORN_MATRIX_FREE / _MATERIALISED (resolved)
+  float* dRt;        // PoseIO in/out (device)
+  float* s_io;       // optional slack column in/out [N] (else initialised to moutlier)
+  float* u_io;       // optional slack row in/out [M]
+  float* rs_out;     // optional [N]
+  float* cs_out;     // optional [M]
+  float* w_out;      // optional [N]
+  double* trace;
+  int trace_cap;
+  int* d_status;
+  uint64_t timeout_ns;
+};
+
+// Device workspace carved from one allocation (see api.cu).
+struct Workspace {
+  void* base = nullptr;
+  size_t bytes = 0;
+};
+
+size_t emicp_workspace_bytes(int N, int M, int grid, const SweepGeomH& g);
+size_t softassign_workspace_bytes(int N, int M, int grid, const SweepGeomH& gr, const SweepGeomH& gc,
+                                  int form);
+
+// Plans the persistent grid and the unit decomposition.
+int persistent_grid_limit(int device, const void* kernel, size_t smem);
+SweepGeomH plan_sweep(int n_own, int n_stream, int grid_limit);
+
+// Enqueue a full registration; returns cudaError_t as int.
+int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
+int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st,
+                       int* grid_used);
+size_t emicp_ws_need(int N, int M, int device);
+size_t softassign_ws_need(int N, int M, int form, int device);
+
+// Control-block status of the last launch that used workspace ws.
+int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps);
+
+}  // namespace cesa

@@ -1,0 +1,257 @@
+// Horn's closed-form absolute orientation (unit-quaternion method), the pose
+// update of every registration loop: findRTfromS + eigenvectorOfN,
+// src/findRTfromS.cpp:33-159. The reference builds the symmetric 4x4 matrix N
+// from the 3x3 cross-covariance S, takes the eigenvector of N's largest
+// eigenvalue with LAPACK dsyev_, converts it to R and sets t = Xc - R*Yc.
+//
+// Here the eigenvector comes from a cyclic Jacobi iteration written for a 4x4
+// matrix. It works for T = float (device, one thread per block) and T = double
+// (host C ABI). The device path keeps the previous step's eigenbasis V and
+// starts each solve from B = V^T N V. Consecutive annealing steps change N
+// only slightly, so one or two sweeps reach FP32 round-off. Each solve
+// re-orthonormalises V with one Newton-Schulz step.
+#pragma once
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define CESA_HD __host__ __device__ __forceinline__
+#else
+#define CESA_HD inline
+#endif
+
+namespace cesa {
+
+template <typename T>
+CESA_HD T t_abs(T x) {
+  return x < T(0) ? -x : x;
+}
+template <typename T>
+CESA_HD bool t_finite(T x) {
+  return x == x && t_abs(x) <= T(3.0e38);
+}
+CESA_HD float t_rsqrt(float x) {
+#if defined(__CUDA_ARCH__)
+  return rsqrtf(x);
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+CESA_HD double t_rsqrt(double x) { return 1.0 / sqrt(x); }
+
+template <typename T>
+struct HornState {
+  T V[4][4];   // eigenbasis carried between solves (warm start)
+  T q[4];      // last good quaternion (fallback when N is not finite)
+  CESA_HD void reset() {
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? T(1) : T(0);
+    q[0] = T(1);
+    q[1] = q[2] = q[3] = T(0);
+  }
+};
+
+// One Jacobi rotation of the symmetric B in the (p,q) plane: computes (c, s)
+// that zero B[p][q] (Numerical-Recipes convention theta = (bqq-bpp)/(2 bpq)).
+template <typename T>
+CESA_HD bool jacobi_angle(T bpp, T bqq, T bpq, T tol, T& c, T& s) {
+  if (t_abs(bpq) <= tol) {
+    c = T(1);
+    s = T(0);
+    return false;
+  }
+  const T d = bqq - bpp;
+  // t = 2 bpq sgn(d) / (|d| + sqrt(d^2 + 4 bpq^2)), the smaller root.
+  const T r2 = d * d + T(4) * bpq * bpq;
+  const T r = r2 * t_rsqrt(r2);
+  const T den = t_abs(d) + r;
+  T t = T(2) * bpq / den;
+  if (d < T(0)) t = -t;
+  c = t_rsqrt(T(1) + t * t);
+  s = t * c;
+  return true;
+}
+
+template <typename T, int P, int Q>
+CESA_HD void jacobi_apply(T (&B)[4][4], T (&W)[4][4], T c, T s) {
+  // B <- J^T B J with J = I except J[P][P]=J[Q][Q]=c, J[P][Q]=s, J[Q][P]=-s.
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T bkp = B[k][P], bkq = B[k][Q];
+    B[k][P] = c * bkp - s * bkq;
+    B[k][Q] = s * bkp + c * bkq;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T bpk = B[P][k], bqk = B[Q][k];
+    B[P][k] = c * bpk - s * bqk;
+    B[Q][k] = s * bpk + c * bqk;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T wkp = W[k][P], wkq = W[k][Q];
+    W[k][P] = c * wkp - s * wkq;
+    W[k][Q] = s * wkp + c * wkq;
+  }
+}
+
+// Two disjoint rotations per round: {(0,1),(2,3)}, {(0,2),(1,3)}, {(0,3),(1,2)}.
+template <typename T, int P1, int Q1, int P2, int Q2>
+CESA_HD bool jacobi_round(T (&B)[4][4], T (&W)[4][4], T tol) {
+  T c1, s1, c2, s2;
+  const bool r1 = jacobi_angle<T>(B[P1][P1], B[Q1][Q1], B[P1][Q1], tol, c1, s1);
+  const bool r2 = jacobi_angle<T>(B[P2][P2], B[Q2][Q2], B[P2][Q2], tol, c2, s2);
+  if (r1) jacobi_apply<T, P1, Q1>(B, W, c1, s1);
+  if (r2) jacobi_apply<T, P2, Q2>(B, W, c2, s2);
+  return r1 || r2;
+}
+
+// Horn's N from S in the reference's h_S layout (src/findRTfromS.cpp:38-74).
+template <typename T>
+CESA_HD void horn_matrix(const T S[9], T (&N)[4][4]) {
+  const T Sxx = S[0], Sxy = S[1], Sxz = S[2];
+  const T Syx = S[3], Syy = S[4], Syz = S[5];
+  const T Szx = S[6], Szy = S[7], Szz = S[8];
+  N[0][0] = Sxx + Syy + Szz;
+  N[0][1] = N[1][0] = Syz - Szy;
+  N[0][2] = N[2][0] = Szx - Sxz;
+  N[0][3] = N[3][0] = Sxy - Syx;
+  N[1][1] = Sxx - Syy - Szz;
+  N[1][2] = N[2][1] = Sxy + Syx;
+  N[1][3] = N[3][1] = Szx + Sxz;
+  N[2][2] = Syy - Sxx - Szz;
+  N[2][3] = N[3][2] = Syz + Szy;
+  N[3][3] = Szz - Sxx - Syy;
+}
+
+// Quaternion -> rotation (src/findRTfromS.cpp:83-91) and t = Xc - R Yc (:94-96).
+template <typename T>
+CESA_HD void quat_to_pose(const T q[4], const T Xc[3], const T Yc[3], T R[9], T t[3]) {
+  const T q0 = q[0], qx = q[1], qy = q[2], qz = q[3];
+  R[0] = q0 * q0 + qx * qx - qy * qy - qz * qz;
+  R[1] = T(2) * (qx * qy - q0 * qz);
+  R[2] = T(2) * (qx * qz + q0 * qy);
+  R[3] = T(2) * (qy * qx + q0 * qz);
+  R[4] = q0 * q0 - qx * qx + qy * qy - qz * qz;
+  R[5] = T(2) * (qy * qz - q0 * qx);
+  R[6] = T(2) * (qz * qx - q0 * qy);
+  R[7] = T(2) * (qz * qy + q0 * qx);
+  R[8] = q0 * q0 - qx * qx - qy * qy + qz * qz;
+  for (int i = 0; i < 3; ++i) t[i] = Xc[i] - (R[3 * i] * Yc[0] + R[3 * i + 1] * Yc[1] + R[3 * i + 2] * Yc[2]);
+}
+
+// Top eigenvector of Horn's N for S; warm-started from st.V. Writes q (unit)
+// and returns 0, or returns 1 and the fallback st.q when N is not finite.
+// gap = (l1 - l2)/|l1|, lmax = l1.
+template <typename T>
+CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* lmax) {
+  T N[4][4];
+  horn_matrix<T>(S, N);
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) finite = finite && t_finite(N[i][j]);
+  if (!finite) {
+    for (int i = 0; i < 4; ++i) q[i] = st.q[i];
+    if (gap) *gap = T(0);
+    if (lmax) *lmax = T(0);
+    return 1;
+  }
+  // B = V^T N V
+  T NV[4][4], B[4][4], W[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      NV[i][j] = N[i][0] * st.V[0][j] + N[i][1] * st.V[1][j] + N[i][2] * st.V[2][j] +
+                 N[i][3] * st.V[3][j];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      B[i][j] = st.V[0][i] * NV[0][j] + st.V[1][i] * NV[1][j] + st.V[2][i] * NV[2][j] +
+                st.V[3][i] * NV[3][j];
+      W[i][j] = (i == j) ? T(1) : T(0);
+    }
+  // symmetrise (round-off in the two products)
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      const T m = T(0.5) * (B[i][j] + B[j][i]);
+      B[i][j] = B[j][i] = m;
+    }
+  T scale = T(0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) scale += t_abs(N[i][j]);
+  const T eps = sizeof(T) == 4 ? T(1.2e-7) : T(2.3e-16);
+  const T tol = eps * T(0.0625) * scale + T(1e-37);
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    bool rot = jacobi_round<T, 0, 1, 2, 3>(B, W, tol);
+    rot = jacobi_round<T, 0, 2, 1, 3>(B, W, tol) || rot;
+    rot = jacobi_round<T, 0, 3, 1, 2>(B, W, tol) || rot;
+    if (!rot) break;
+  }
+  // V <- V W, then one Newton-Schulz step V <- V (3I - V^T V)/2
+  T V2[4][4], G[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      V2[i][j] = st.V[i][0] * W[0][j] + st.V[i][1] * W[1][j] + st.V[i][2] * W[2][j] +
+                 st.V[i][3] * W[3][j];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      G[i][j] = (i == j ? T(1.5) : T(0)) -
+                T(0.5) * (V2[0][i] * V2[0][j] + V2[1][i] * V2[1][j] + V2[2][i] * V2[2][j] +
+                          V2[3][i] * V2[3][j]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      st.V[i][j] = V2[i][0] * G[0][j] + V2[i][1] * G[1][j] + V2[i][2] * G[2][j] +
+                   V2[i][3] * G[3][j];
+  int imax = 0;
+  T l1 = B[0][0];
+#pragma unroll
+  for (int i = 1; i < 4; ++i)
+    if (B[i][i] > l1) {
+      l1 = B[i][i];
+      imax = i;
+    }
+  T l2 = T(-3.0e38);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (i != imax && B[i][i] > l2) l2 = B[i][i];
+  T qq[4];
+  T n2 = T(0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qq[i] = st.V[i][imax];
+    n2 += qq[i] * qq[i];
+  }
+  const T inv = t_rsqrt(n2);
+  bool ok = t_finite(inv);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qq[i] *= inv;
+    ok = ok && t_finite(qq[i]);
+  }
+  if (!ok) {
+    for (int i = 0; i < 4; ++i) q[i] = st.q[i];
+    st.reset();
+    if (gap) *gap = T(0);
+    if (lmax) *lmax = T(0);
+    return 1;
+  }
+  for (int i = 0; i < 4; ++i) q[i] = st.q[i] = qq[i];
+  if (gap) *gap = (l1 - l2) / (t_abs(l1) > T(1e-30) ? t_abs(l1) : T(1e-30));
+  if (lmax) *lmax = l1;
+  return 0;
+}
+
+}  // namespace cesa

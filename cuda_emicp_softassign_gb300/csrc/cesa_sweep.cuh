@@ -1,0 +1,338 @@
+// Persistent "sweep" machinery shared by the EM-ICP and Softassign kernels.
+//
+// Both algorithms reduce a dense N x M affinity over one index: a row sum, a
+// column sum, or a weighted row moment. The affinity is never stored. A sweep
+// partitions the work into units of (128 owned points) x (a slice of streamed
+// points):
+//   * owned points live in registers, 4 per lane, 32 lanes -> 128 per unit;
+//   * streamed points are brought into shared memory by 1-D TMA bulk copies
+//     (cp.async.bulk, 2-stage ring, mbarrier completion) in chunks of 512.
+//     The 8 warps split each chunk and every lane reads the same float4
+//     (a broadcast);
+//   * per-owned-point accumulators are reduced across the 8 warps through
+//     shared memory in a fixed order.
+// When a block of owned points is split over S > 1 slices, every unit stores
+// its partial accumulators. The unit that finishes the block last (atomic
+// counter per block, monotonic across sweeps) sums the S partials in slice
+// order and runs the finalize step. Results are therefore deterministic
+// whatever the scheduling.
+//
+// Units are assigned round-robin to the blocks of the persistent grid. The
+// host picks S so that the unit count is close to a multiple of the grid size.
+#pragma once
+#include "cesa_common.cuh"
+
+namespace cesa {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kOwnPerLane = 4;
+constexpr int kBlockPts = 32 * kOwnPerLane;  // owned points per unit
+constexpr int kChunk = 512;                  // streamed points per TMA chunk
+constexpr int kStages = 2;
+constexpr int kMaxAcc = 5;
+
+// Geometry of one sweep type (host-computed).
+struct SweepGeom {
+  int n_own;      // owned points (rows of the reduction)
+  int n_stream;   // streamed points
+  int nblk;       // ceil(n_own / kBlockPts)
+  int slices;     // S
+  int slice_len;  // ceil(n_stream / S)
+  int units;      // nblk * S
+};
+
+struct __align__(16) SweepSmem {
+  float4 raw[kStages][kChunk];   // TMA destination, stream A
+  float4 raw2[kStages][kChunk];  // TMA destination, stream B (optional)
+  float4 prep[kChunk];           // prepared stream A (transformed / weighted)
+  float red[kMaxAcc][kWarps][kBlockPts];
+  uint64_t full[kStages];
+  int flag;
+};
+
+// Per-block pipeline bookkeeping (identical in every thread of the block).
+struct Pipe {
+  unsigned uses[kStages];  // copies issued into each stage
+  int tag[kStages];        // chunk id resident in each stage (static streams), -1 = none
+  int cur;                 // stage of the task being consumed, -1 = none
+};
+
+__device__ __forceinline__ void pipe_init(Pipe& p) {
+  for (int s = 0; s < kStages; ++s) {
+    p.uses[s] = 0;
+    p.tag[s] = -1;
+  }
+  p.cur = -1;
+}
+
+// Streamed source for one sweep.
+struct StreamSrc {
+  const float4* a;  // required
+  const float4* b;  // optional second array (same indexing), nullptr if unused
+  bool is_static;   // contents never change during the launch (enables reuse)
+};
+
+// Chooses the stage for chunk `id`; issues the bulk copy unless a static
+// chunk is already resident. Returns the stage; *need_wait tells the
+// consumer whether to wait on the stage's mbarrier.
+__device__ __forceinline__ int pipe_issue(Pipe& p, SweepSmem& sm, const StreamSrc& src, int id,
+                                          int first, int len, bool& need_wait) {
+  if (src.is_static) {
+    for (int s = 0; s < kStages; ++s)
+      if (p.tag[s] == id) {
+        need_wait = false;
+        return s;
+      }
+  }
+  const int s = (p.cur < 0) ? 0 : (p.cur ^ 1);
+  p.tag[s] = src.is_static ? id : -1;
+  p.uses[s] += 1;
+  need_wait = true;
+  if (threadIdx.x == 0) {
+    const unsigned bytes = (unsigned)len * 16u;
+    mbar_arrive_expect_tx(&sm.full[s], src.b ? 2u * bytes : bytes);
+    bulk_g2s(&sm.raw[s][0], src.a + first, bytes, &sm.full[s]);
+    if (src.b) bulk_g2s(&sm.raw2[s][0], src.b + first, bytes, &sm.full[s]);
+  }
+  return s;
+}
+
+// Owned-point loader: lane's 4 points of block `blk`. Invalid points get
+// `fill` and valid=false.
+__device__ __forceinline__ void load_owned(const float4* own, int n_own, int blk, float4 (&pt)[kOwnPerLane],
+                                           bool (&valid)[kOwnPerLane]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < kOwnPerLane; ++j) {
+    const int i = blk * kBlockPts + lane + 32 * j;
+    valid[j] = i < n_own;
+    pt[j] = valid[j] ? ld_cg(own + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// Writes the warp-level accumulators to shared memory and returns, in threads
+// 0..kBlockPts-1, the sum over warps (fixed order) for owned point threadIdx.x.
+template <int NACC>
+__device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float (&acc)[kOwnPerLane][NACC],
+                                             float (&tot)[NACC]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < kOwnPerLane; ++j)
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) sm.red[a][warp][lane + 32 * j] = acc[j][a];
+  __syncthreads();
+  if (threadIdx.x < kBlockPts) {
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) {
+      float s = sm.red[a][0][threadIdx.x];
+#pragma unroll
+      for (int w = 1; w < kWarps; ++w) s += sm.red[a][w][threadIdx.x];
+      tot[a] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Split-slice completion. Stores this unit's per-point totals; returns true in
+// every thread of the block that must finalize block `blk`, with `tot` (threads
+// < kBlockPts) replaced by the slice-ordered sum over all S partials.
+// part layout: [(blk*S + sl)][NACC][kBlockPts]. cnt[blk] is monotonic; this is
+// the `round`-th sweep of this geometry in the launch (0-based).
+template <int NACC>
+__device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g, int blk, int sl,
+                                               unsigned round, float* part, unsigned* cnt,
+                                               float (&tot)[NACC]) {
+  if (g.slices == 1) return true;
+  float* mine = part + ((size_t)blk * g.slices + sl) * NACC * kBlockPts;
+  if (threadIdx.x < kBlockPts) {
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) __stcg(mine + a * kBlockPts + threadIdx.x, tot[a]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned old = atomicAdd(&cnt[blk], 1u);
+    const unsigned target = (round + 1u) * (unsigned)g.slices;
+    sm.flag = (old + 1u == target) ? 1 : 0;
+    __threadfence();
+  }
+  __syncthreads();
+  const bool last = sm.flag != 0;
+  if (last && threadIdx.x < kBlockPts) {
+    const float* base = part + (size_t)blk * g.slices * NACC * kBlockPts;
+#pragma unroll
+    for (int a = 0; a < NACC; ++a) {
+      float s = 0.f;
+      for (int k = 0; k < g.slices; ++k) s += __ldcg(base + ((size_t)k * NACC + a) * kBlockPts + threadIdx.x);
+      tot[a] = s;
+    }
+  }
+  __syncthreads();
+  return last;
+}
+
+// Accumulates NV per-thread df values (threads that have none pass zeros) into
+// the block accumulator acc[NV] held in shared memory (thread 0 adds).
+template <int NV>
+__device__ __forceinline__ void block_accumulate(df (&v)[NV], df* red_scratch, df* acc) {
+  block_reduce_df<NV>(v, red_scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) df_add(acc[k], v[k]);
+  }
+  __syncthreads();
+}
+
+// Grid-wide sum of NV block partials (df), identical in every block: thread 0
+// of the calling block receives the totals in tot[]. parts: [nblocks][NV].
+template <int NV>
+__device__ __forceinline__ void reduce_block_partials(const df* parts, int nblocks, df* scratch,
+                                                      df* tot) {
+  constexpr int G = kThreads / NV;  // threads per value
+  static_assert(kThreads % NV == 0, "NV must divide the block size");
+  const int v = threadIdx.x % NV, grp = threadIdx.x / NV;
+  df a0 = df_make(0.f), a1 = df_make(0.f);
+  int b = grp;
+  for (; b + G < nblocks; b += 2 * G) {
+    const float2 x0 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
+    const float2 x1 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)(b + G) * NV + v));
+    df_add(a0, df{x0.x, x0.y});
+    df_add(a1, df{x1.x, x1.y});
+  }
+  if (b < nblocks) {
+    const float2 x0 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
+    df_add(a0, df{x0.x, x0.y});
+  }
+  df_add(a0, a1);
+  scratch[grp * NV + v] = a0;
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    df s = scratch[threadIdx.x];
+    for (int k = 1; k < G; ++k) df_add(s, scratch[k * NV + threadIdx.x]);
+    tot[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+
+// Prepare step that uses stream A as loaded.
+struct NoPrep {
+  __device__ __forceinline__ const float4* operator()(SweepSmem& sm, int stage, int len) const {
+    return sm.raw[stage];
+  }
+};
+
+// Runs all units of one sweep assigned to this block (round-robin over the
+// grid). For every unit: owned points -> registers (optionally transformed by
+// R, tc), streamed chunks through the TMA ring, elem() per (owned, streamed)
+// pair, cross-warp reduction, split completion, then fin(blk, tot) in the
+// block that completes the owned block. Returns false if a wait gave up.
+//
+//   Elem: void operator()(float (&acc)[NACC], const float (&p)[3], float4 a, float4 b)
+//   Prep: const float4* operator()(SweepSmem&, int stage, int len)   (block-wide)
+//   Fin:  void operator()(int blk, const float (&tot)[NACC])         (block-wide)
+template <int NACC, class Elem, class Prep, class Fin>
+__device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const SweepGeom& g,
+                                            const StreamSrc& src, const float4* own, bool xform_own,
+                                            const float (&R)[9], const float (&tc)[3], unsigned round,
+                                            float* part, unsigned* cnt, const Elem& elem,
+                                            const Prep& prep, const Fin& fin, Ctl* ctl,
+                                            uint64_t timeout_ns, int where) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int G = (int)gridDim.x;
+  pipe.cur = -1;
+  auto task_range = [&](int uu, int ch, int& first, int& len) -> bool {
+    if (uu >= g.units) return false;
+    const int sl = uu % g.slices;
+    const int sb = sl * g.slice_len;
+    const int se = min(sb + g.slice_len, g.n_stream);
+    first = sb + ch * kChunk;
+    if (first >= se) return false;
+    len = min(kChunk, se - first);
+    return true;
+  };
+  int u = blockIdx.x;
+  int cur_first = 0, cur_len = 0, cur_ch = 0, cur_stage = 0;
+  unsigned cur_par = 0;
+  bool cur_wait = false;
+  bool have = task_range(u, 0, cur_first, cur_len);
+  if (have) {
+    cur_stage = pipe_issue(pipe, sm, src, cur_first, cur_first, cur_len, cur_wait);
+    cur_par = (pipe.uses[cur_stage] - 1u) & 1u;
+  }
+  while (have) {
+    const int blk = u / g.slices, sl = u % g.slices;
+    float4 ow[kOwnPerLane];
+    bool valid[kOwnPerLane];
+    load_owned(own, g.n_own, blk, ow, valid);
+    float p[kOwnPerLane][3];
+#pragma unroll
+    for (int j = 0; j < kOwnPerLane; ++j) {
+      if (xform_own) {
+        p[j][0] = R[0] * ow[j].x + R[1] * ow[j].y + R[2] * ow[j].z + tc[0];
+        p[j][1] = R[3] * ow[j].x + R[4] * ow[j].y + R[5] * ow[j].z + tc[1];
+        p[j][2] = R[6] * ow[j].x + R[7] * ow[j].y + R[8] * ow[j].z + tc[2];
+      } else {
+        p[j][0] = ow[j].x;
+        p[j][1] = ow[j].y;
+        p[j][2] = ow[j].z;
+      }
+    }
+    float acc[kOwnPerLane][NACC];
+#pragma unroll
+    for (int j = 0; j < kOwnPerLane; ++j)
+#pragma unroll
+      for (int a = 0; a < NACC; ++a) acc[j][a] = 0.f;
+
+    for (;;) {
+      int n_first = 0, n_len = 0, n_u = u, n_ch = cur_ch + 1, n_stage = 0;
+      unsigned n_par = 0;
+      bool n_wait = false;
+      bool have_n = task_range(n_u, n_ch, n_first, n_len);
+      if (!have_n) {
+        n_u = u + G;
+        n_ch = 0;
+        have_n = task_range(n_u, 0, n_first, n_len);
+      }
+      pipe.cur = cur_stage;
+      if (have_n) {
+        n_stage = pipe_issue(pipe, sm, src, n_first, n_first, n_len, n_wait);
+        n_par = (pipe.uses[n_stage] - 1u) & 1u;
+      }
+      const bool bad = cur_wait && !mbar_wait(&sm.full[cur_stage], cur_par, ctl, timeout_ns, where);
+      if (__syncthreads_or(bad)) {  // block-uniform decision
+        // leave only after the prefetched copy (if any) has landed
+        if (have_n && n_wait) mbar_wait(&sm.full[n_stage], n_par, ctl, timeout_ns, where + 1);
+        return false;
+      }
+      const float4* __restrict__ bufA = prep(sm, cur_stage, cur_len);
+      const float4* __restrict__ bufB = sm.raw2[cur_stage];
+#pragma unroll 2
+      for (int c = warp; c < cur_len; c += kWarps) {
+        const float4 a = bufA[c];
+        const float4 b = bufB[c];
+#pragma unroll
+        for (int j = 0; j < kOwnPerLane; ++j) elem(acc[j], p[j], a, b);
+      }
+      __syncthreads();
+      const bool unit_done = !(have_n && n_u == u);
+      cur_first = n_first;
+      cur_len = n_len;
+      cur_ch = n_ch;
+      cur_stage = n_stage;
+      cur_par = n_par;
+      cur_wait = n_wait;
+      have = have_n;
+      if (unit_done) break;
+    }
+    float tot[NACC];
+    reduce_warps<NACC>(sm, acc, tot);
+    if (split_complete<NACC>(sm, g, blk, sl, round, part, cnt, tot)) fin(blk, tot);
+    u += G;
+    cur_ch = 0;
+  }
+  return true;
+}
+
+}  // namespace cesa

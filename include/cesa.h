@@ -1,0 +1,177 @@
+/*
+ * cesa.h -- C ABI of the GB300-native soft-correspondence registration library
+ * (libcesa.so): annealed EM-ICP and Softassign rigid registration on one GPU.
+ *
+ * Every entry point takes plain pointers and sizes. Point sets are SoA float
+ * arrays [x0..xn-1, y0..yn-1, z0..zn-1], the layout the reference builds with
+ * cloud2data() (src/cloud2data.cpp:29-46). The rotation R is 9 floats,
+ * row-major (r11 r12 r13 r21 ...), and t is 3 floats (README.md:205-214). On
+ * entry R,t is the initial pose; on exit it is the estimate such that
+ * X ~ R*Y + t (X = target, Y = source).
+ *
+ * All functions return CESA_OK (0) or a CESA_ERR_* code; nothing calls exit().
+ * The reference's functions return void and ignore CUDA errors
+ * (src/3dregistration.h:118); the C++ drop-in layer (3dregistration.h in this
+ * directory) keeps void and reports failures on stderr.
+ */
+#ifndef CESA_H_
+#define CESA_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CESA_OK 0
+#define CESA_ERR_INVALID_ARGUMENT 1 /* bad size, NULL pointer, bad parameter */
+#define CESA_ERR_CUDA 2             /* a CUDA runtime call failed */
+#define CESA_ERR_TIMEOUT 3          /* a device-side wait gave up after its limit */
+#define CESA_ERR_NO_DEVICE 4        /* no usable CUDA device */
+#define CESA_ERR_OUT_OF_MEMORY 5    /* device or host allocation failed */
+#define CESA_ERR_UNSUPPORTED 6      /* the request is outside what this build supports */
+
+/* cudaStream_t without including cuda_runtime.h (same underlying type). */
+typedef struct CUstream_st* cesa_stream_t;
+
+/* Sinkhorn normalisation forms for Softassign (cesa_params.sinkhorn_form). */
+#define CESA_SINKHORN_AUTO 0         /* per-size choice by the built-in tuner */
+#define CESA_SINKHORN_MATRIX_FREE 1  /* scaling vectors, affinities recomputed per sweep */
+#define CESA_SINKHORN_MATERIALISED 2 /* affinity matrix stored once per inner iteration */
+
+/*
+ * Registration parameters. The first twelve fields mirror
+ * registrationParameters (src/3dregistration.h:39-57) in name, type, order and
+ * meaning. The remaining fields control the GPU path and have no counterpart
+ * in the reference. cesa_params_default() fills the reference CLI defaults
+ * (src/main.cpp:280-315).
+ */
+typedef struct cesa_params {
+  /* Softassign */
+  int JMAX;        /* annealing steps; T <- T*TFACTOR after each */
+  int I0;          /* pose updates per temperature */
+  int I1;          /* Sinkhorn row/column passes per pose update (>= 1) */
+  float alpha;     /* outlier parameter */
+  float T_0;       /* initial temperature */
+  float TFACTOR;   /* temperature factor */
+  float moutlier;  /* initial slack-row / slack-column value */
+  /* EM-ICP */
+  float sigma_p2;     /* initial sigma_p^2; sigma_p2 <- sigma_p2*sigma_factor while > sigma_inf */
+  float sigma_inf;    /* stop value of sigma_p2 */
+  float sigma_factor; /* factor for sigma_p2 */
+  float d_02;         /* outlier distance^2 */
+  /* ICP (kept for layout parity; not used by these entry points) */
+  int maxIteration;
+  /* GPU path controls */
+  int sinkhorn_form; /* CESA_SINKHORN_* */
+  int timeout_ms;    /* limit of any device-side wait; 0 selects 10000 ms */
+  int device;        /* CUDA device ordinal for the host-pointer entry points; -1 = current */
+  int reserved[5];
+} cesa_params;
+
+/*
+ * Optional per-call report (may be NULL). trace, when non-NULL, receives one
+ * record of CESA_TRACE_STRIDE doubles per pose update, up to trace_capacity:
+ *   [0] step  [1] sigma_p2 or T  [2] sum(lambda) or sumM  [3..5] Xc  [6..8] Yc
+ *   [9..17] S (reference h_S layout, S[i+3j])  [18..26] R row-major  [27..29] t
+ *   [30] relative eigen-gap of Horn's N  [31] largest eigenvalue of N
+ */
+#define CESA_TRACE_STRIDE 32
+typedef struct cesa_report {
+  double* trace;        /* host buffer or NULL */
+  int trace_capacity;   /* records */
+  int steps;            /* out: pose updates performed */
+  int sinkhorn_form;    /* out: form used (Softassign) */
+  int grid_blocks;      /* out: persistent grid size */
+  float device_ms;      /* out: device time of the registration kernels */
+  int reserved[3];
+} cesa_report;
+
+/* Reference defaults: src/main.cpp:280-315 (moutlier = e^-1 / sqrt(T_0)). */
+void cesa_params_default(cesa_params* p);
+
+/*
+ * Annealed EM-ICP. Replaces emicp(), src/emicp.cu:247-716 (declared at
+ * src/3dregistration.h:87-90). X: N target points, Y: M source points, host
+ * SoA. R, t: host, in/out. Synchronous; device memory is cached between calls.
+ */
+int cesa_emicp(const float* X, int N, const float* Y, int M, float R[9], float t[3],
+               const cesa_params* p, cesa_report* rep);
+
+/*
+ * Annealed Softassign. Replaces softassign(), src/softassign.cu:256-886
+ * (declared at src/3dregistration.h:82-86). Same conventions as cesa_emicp.
+ */
+int cesa_softassign(const float* X, int N, const float* Y, int M, float R[9], float t[3],
+                    const cesa_params* p, cesa_report* rep);
+
+/*
+ * Device-pointer variants (same algorithms as above, inputs already in HBM).
+ * dX, dY: device SoA. dRt: device float[12] = R row-major then t, in/out.
+ * Enqueued on `stream`; the call returns once the work is queued. The
+ * device-side status (CESA_OK or CESA_ERR_TIMEOUT) is written to the device
+ * int *d_status when non-NULL, and is also returned by
+ * cesa_stream_status(stream) after the stream has been synchronised.
+ */
+int cesa_emicp_device(const float* dX, int N, const float* dY, int M, float* dRt,
+                      const cesa_params* p, int* d_status, cesa_stream_t stream);
+int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float* dRt,
+                           const cesa_params* p, int* d_status, cesa_stream_t stream);
+
+/* Status of the last registration enqueued on `stream` (synchronises it). */
+int cesa_stream_status(cesa_stream_t stream);
+
+/*
+ * One EM-ICP sigma step (E-step + weighted moments) from pose (R, t): the
+ * fused kernel's per-row results for parity checks. Device pointers:
+ *   row_out  [M*5]: per Y point r: C_r (row sum incl. outlier term), lambda_r,
+ *            lambda_r * X'_r (3)  (may be NULL)
+ * Host outputs: moments[16] = sum(lambda), Xc[3], Yc[3], S[9].
+ * Replaces one pass of src/emicp.cu:453-624.
+ */
+int cesa_emicp_step_device(const float* dX, int N, const float* dY, int M, const float R[9],
+                           const float t[3], float sigma_p2, float d_02, float* row_out,
+                           double moments[16], cesa_stream_t stream);
+
+/*
+ * One Softassign inner iteration at temperature T from pose (R, t) and slack
+ * (s: N, u: M, device, in/out). Device outputs (may be NULL): rs[N] last row
+ * sums incl. slack, cs[M] last column sums incl. slack, w[N] final row sums.
+ * Host outputs: moments[16] = sumM, Xc[3], Yc[3], S[9].
+ * Replaces one pass of src/softassign.cu:494-798.
+ */
+int cesa_softassign_step_device(const float* dX, int N, const float* dY, int M, const float R[9],
+                                const float t[3], float T, float alpha, int I1, int sinkhorn_form,
+                                float* s, float* u, float* rs, float* cs, float* w,
+                                double moments[16], cesa_stream_t stream);
+
+/*
+ * Horn's pose from the weighted centres and the 3x3 cross-covariance (h_S
+ * layout). Replaces findRTfromS(), src/findRTfromS.cpp:33-97 (declared at
+ * src/3dregistration.h:104-107). q_prev (nullable, in/out) plays the role of
+ * the reference's static q_pre fallback (src/findRTfromS.cpp:110-145).
+ * Host function, FP64 internally like the reference.
+ */
+int cesa_find_rt_from_s(const float Xc[3], const float Yc[3], const float S[9], float R[9],
+                        float t[3], float q_prev[4]);
+
+/*
+ * AoS points (x,y,z at p[i*stride + 0..2]) to SoA. Replaces cloud2data(),
+ * src/cloud2data.cpp:29-67, for callers without PCL.
+ */
+int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_out);
+
+/* Releases cached device workspaces of the calling process. */
+void cesa_release_workspaces(void);
+
+/* Human-readable name of a status code. */
+const char* cesa_status_string(int status);
+
+/* Library version as major*10000 + minor*100 + patch. */
+int cesa_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CESA_H_ */

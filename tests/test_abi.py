@@ -1,0 +1,201 @@
+"""C ABI of libcesa.so without a GPU: exports, layouts, host-side functions,
+argument checks and the loud failure when no device is present."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import REPO, rot_err_deg
+
+HEADER = os.path.join(REPO, "include", "cesa.h")
+GOLD = os.path.join(REPO, "tests", "golden")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cesa_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(cesa):
+    names = declared_functions()
+    assert len(names) >= 12
+    L = cesa.lib()
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", cesa.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (\w+)", out))
+    assert set(names) <= exported
+    assert all(n.startswith("cesa_") for n in exported), "only cesa_* may be exported"
+
+
+def _c_layout(code, extra_inc=()):
+    d = tempfile.mkdtemp()
+    src = os.path.join(d, "l.cpp")
+    exe = os.path.join(d, "l")
+    open(src, "w").write(code)
+    cmd = ["g++", "-std=c++17", "-I", os.path.join(REPO, "include")]
+    for inc in extra_inc:
+        cmd += ["-I", inc]
+    subprocess.run(cmd + [src, "-o", exe], check=True)
+    return subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+
+
+def test_params_mirror_matches_c_layout(cesa):
+    code = r'''
+#include <cstdio>
+#include <cstddef>
+#include "cesa.h"
+#define F(x) printf("%s %zu\n", #x, offsetof(cesa_params, x));
+int main(){ printf("size %zu\n", sizeof(cesa_params));
+F(JMAX)F(I0)F(I1)F(alpha)F(T_0)F(TFACTOR)F(moutlier)F(sigma_p2)F(sigma_inf)F(sigma_factor)F(d_02)
+F(maxIteration)F(sinkhorn_form)F(timeout_ms)F(device)
+printf("report %zu\n", sizeof(cesa_report)); }
+'''
+    got = dict(l.split() for l in _c_layout(code).strip().splitlines())
+    P = cesa.Params
+    assert int(got["size"]) == ctypes.sizeof(P)
+    for name, _ in P._fields_:
+        if name in got:
+            assert int(got[name]) == getattr(P, name).offset, name
+    assert int(got["report"]) == ctypes.sizeof(cesa.Report)
+
+
+def test_registration_parameters_layout_matches_reference():
+    """include/3dregistration.h keeps the reference's registrationParameters
+    field order and offsets (src/3dregistration.h:39-76)."""
+    ref_src = os.path.join(os.environ.get("CESA_REFERENCE_DIR", "/root/reference"), "src")
+    if not os.path.exists(os.path.join(ref_src, "3dregistration.h")):
+        pytest.skip("reference tree not available")
+    fields = ["JMAX", "I0", "I1", "alpha", "T_0", "TFACTOR", "moutlier", "sigma_p2", "sigma_inf",
+              "sigma_factor", "d_02", "maxIteration", "noviewer", "nostop", "notimer", "argc", "argv",
+              "viewer", "source_trans_color", "cloud_source", "cloud_source_trans", "cloud_target"]
+    body = "".join('printf("%%s %%zu\\n", "%s", offsetof(registrationParameters, %s));' % (f, f) for f in fields)
+    code = '#include <cstdio>\n#include <cstddef>\n#include "3dregistration.h"\nint main(){%s printf("size %%zu\\n", sizeof(registrationParameters));}\n' % body
+    ours = _c_layout(code.replace("3dregistration.h", os.path.join(REPO, "include", "3dregistration.h")))
+    theirs = _c_layout(code.replace("3dregistration.h", os.path.join(ref_src, "3dregistration.h")),
+                       extra_inc=[os.path.join(REPO, "oracle", "stubs")])
+    assert ours == theirs
+
+
+def test_params_defaults_are_reference_cli_defaults(cesa):
+    p = cesa.Params.default()
+    assert (p.JMAX, p.I0, p.I1) == (100, 5, 3)
+    assert p.alpha == pytest.approx(3.0) and p.T_0 == pytest.approx(100.0)
+    assert p.TFACTOR == pytest.approx(0.95)
+    assert p.moutlier == pytest.approx(np.exp(-1.0) / 10.0, rel=1e-6)
+    assert p.sigma_p2 == np.float32(0.01) and p.sigma_inf == np.float32(1e-5)
+    assert p.sigma_factor == np.float32(0.9) and p.d_02 == np.float32(0.01)
+    assert p.maxIteration == 30 and p.device == -1
+
+
+def test_find_rt_from_s_matches_reference_golden(cesa, oracle):
+    g = np.load(os.path.join(GOLD, "findrt_reference.npz"))
+    for k in range(len(g["S"])):
+        R, t = cesa.find_rt_from_s(g["Xc"][k], g["Yc"][k], g["S"][k])
+        _, _, info = oracle.find_rt_from_s(g["Xc"][k], g["Yc"][k], g["S"][k])
+        if info["gap"] > 1e-3:
+            assert rot_err_deg(R, g["R"][k]) < 1e-3, k
+            assert np.abs(t - g["t"][k]).max() < 1e-4 * (1 + np.abs(g["t"][k]).max()), k
+
+
+def test_find_rt_from_s_fallback_keeps_previous_quaternion(cesa):
+    q = np.array([np.cos(0.3), 0.0, np.sin(0.3), 0.0], np.float32)
+    R, t = cesa.find_rt_from_s(np.zeros(3), np.ones(3), np.full(9, np.nan), q_prev=q)
+    assert abs(R[1, 1] - 1.0) < 1e-6 and abs(R[0, 0] - np.cos(0.6)) < 1e-6
+
+
+def test_cloud2data_is_soa(cesa):
+    P = np.arange(15, dtype=np.float32).reshape(5, 3)
+    assert np.array_equal(cesa.cloud2data(P), P.T.reshape(-1))
+    P4 = np.c_[P, np.ones(5, np.float32)]  # PCL-style padded points
+    assert np.array_equal(cesa.cloud2data(P4), P.T.reshape(-1))
+
+
+def test_invalid_arguments_are_rejected(cesa):
+    L = cesa.lib()
+    X = np.zeros(6, np.float32)
+    R = np.eye(3, dtype=np.float32).reshape(-1)
+    t = np.zeros(3, np.float32)
+    p = cesa.Params.default()
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    assert L.cesa_emicp(ptr(X), 0, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(p), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    assert L.cesa_emicp(None, 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(p), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    bad = cesa.Params.default(sigma_factor=1.5)  # would never terminate in the reference
+    assert L.cesa_emicp(ptr(X), 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(bad), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    bad = cesa.Params.default(I1=0)  # the reference would read uninitialised column sums
+    assert L.cesa_softassign(ptr(X), 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(bad), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    assert cesa.status_string(cesa.CESA_ERR_TIMEOUT) == "device-side wait timed out"
+
+
+def test_no_cpu_fallback_without_gpu(cesa):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    X = np.random.default_rng(0).uniform(0, 1, (20, 3)).astype(np.float32)
+    with pytest.raises(cesa.CesaError) as e:
+        cesa.emicp(X, X)
+    assert e.value.code == cesa.CESA_ERR_NO_DEVICE
+    with pytest.raises(cesa.CesaError):
+        cesa.softassign(X, X)
+
+
+@pytest.fixture(scope="module")
+def pose_harness():
+    d = tempfile.mkdtemp()
+    so = os.path.join(d, "pose.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I",
+                    os.path.join(REPO, "cuda_emicp_softassign_gb300", "csrc"),
+                    os.path.join(REPO, "tests", "pose_harness.cpp"), "-o", so], check=True)
+    return ctypes.CDLL(so)
+
+
+def _quat_R(q):
+    q0, qx, qy, qz = q
+    return np.array([[q0*q0+qx*qx-qy*qy-qz*qz, 2*(qx*qy-q0*qz), 2*(qx*qz+q0*qy)],
+                     [2*(qy*qx+q0*qz), q0*q0-qx*qx+qy*qy-qz*qz, 2*(qy*qz-q0*qx)],
+                     [2*(qz*qx-q0*qy), 2*(qz*qy+q0*qx), q0*q0-qx*qx-qy*qy+qz*qz]])
+
+
+def test_device_pose_solver_fp32_warm_start(pose_harness, oracle):
+    """The FP32 warm-started Jacobi used on the device, run on the host over an
+    annealing-like sequence of slowly rotating S, against the FP64 oracle."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    rng = np.random.default_rng(9)
+    K = 200
+    base = rng.standard_normal((3, 3)) * 0.05
+    Ss = []
+    for k in range(K):
+        A = W._rot([1.0, 2.0, 0.5], np.radians(40.0 * k / K))
+        S = A * (1.0 + 0.3 * np.sin(k / 7.0)) + base
+        Ss.append(S.reshape(-1, order="F"))
+    S32 = np.ascontiguousarray(np.array(Ss, np.float32))
+    q = np.zeros((K, 4), np.float32)
+    gap = np.zeros(K, np.float32)
+    fb = pose_harness.pose_sequence_f32(S32.ctypes.data_as(ctypes.c_void_p), K,
+                                        q.ctypes.data_as(ctypes.c_void_p), gap.ctypes.data_as(ctypes.c_void_p))
+    assert fb == 0
+    worst = 0.0
+    for k in range(K):
+        Ro, _, info = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), S32[k].astype(np.float64))
+        e = rot_err_deg(_quat_R(q[k].astype(np.float64)), Ro)
+        worst = max(worst, e)
+        assert abs(gap[k] - info["gap"]) < 1e-4 * max(1.0, info["gap"])
+    assert worst < 1e-4, worst
+
+
+def test_device_pose_solver_random_cold(pose_harness, oracle):
+    rng = np.random.default_rng(10)
+    for _ in range(100):
+        S = rng.standard_normal(9)
+        q = np.zeros(4)
+        gap = np.zeros(1)
+        pose_harness.pose_sequence_f64(np.ascontiguousarray(S).ctypes.data_as(ctypes.c_void_p), 1,
+                                       q.ctypes.data_as(ctypes.c_void_p), gap.ctypes.data_as(ctypes.c_void_p))
+        Ro, _, info = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), S)
+        if info["gap"] > 1e-6:
+            assert rot_err_deg(_quat_R(q), Ro) < 1e-7

@@ -1,0 +1,109 @@
+"""Softassign on the GPU through the C ABI, against the FP64 oracle.
+
+Tolerances: slack vectors and row/column sums 1e-5 relative; S relative to
+its largest entry 1e-5 (1e-4 at temperatures where the assignment is nearly
+uniform and S is a small difference of large sums); final R within 1e-3
+degrees and t within 1e-5 x cloud extent for the full default schedule.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err, rot_err_deg, soa_tensor
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,m", [(300, 300), (257, 129), (77, 500)])
+@pytest.mark.parametrize("T", [100.0, 5.0, 0.7])
+def test_inner_iteration_matches_oracle(cesa, oracle, torch_cuda, n, m, T):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    torch = torch_cuda
+    X, Y, Rt, tt = W.surface_pair(n=n, m=m, seed=n + 3 * m)
+    R, t = Rt, tt
+    mo = np.float32(0.0367879)
+    s0 = np.full(n, mo * 0.7, np.float32)  # slack already shrunk by earlier iterations
+    u0 = np.full(m, mo * 0.9, np.float32)
+    ref = oracle.softassign_step(X, Y, R.astype(np.float32), t.astype(np.float32), T, 3.0, 3, s0, u0)
+    s = torch.from_numpy(s0.copy()).cuda()
+    u = torch.from_numpy(u0.copy()).cuda()
+    rs = torch.zeros(n, device="cuda")
+    cs = torch.zeros(m, device="cuda")
+    w = torch.zeros(n, device="cuda")
+    mom = cesa.softassign_step(soa_tensor(torch, X), soa_tensor(torch, Y), R, t, T, 3.0, 3, s, u,
+                               rs=rs, cs=cs, w=w)
+    torch.cuda.synchronize()
+    for name, got in (("s", s), ("u", u), ("rs", rs), ("cs", cs), ("w", w)):
+        g = got.cpu().numpy().astype(np.float64)
+        assert np.all(np.abs(g - ref[name]) <= 1e-5 * np.abs(ref[name]) + 1e-30), name
+    assert abs(mom[0] - ref["sum"]) <= 1e-5 * ref["sum"]
+    extent = float(np.ptp(X, 0).max())
+    assert np.abs(mom[1:4] - ref["Xc"]).max() < 1e-5 * extent
+    assert np.abs(mom[4:7] - ref["Yc"]).max() < 1e-5 * extent
+    tol = 1e-5 if T < 50 else 1e-4
+    assert rel_err(mom[7:16], ref["S"]) < tol
+
+
+@pytest.mark.parametrize("n,m,seed", [(200, 200, 1), (160, 240, 2), (333, 100, 3)])
+def test_full_schedule_matches_oracle(cesa, oracle, n, m, seed):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.surface_pair(n=n, m=m, seed=seed)
+    R, t, tr, rep = cesa.softassign(X, Y, trace=True)
+    Ro, to, tro = oracle.softassign(X, Y)
+    assert rep.steps == 500 and len(tr) == 500
+    assert tro[-1, 30] > 0.05
+    assert rot_err_deg(R, Ro) < 1e-3
+    assert np.abs(t - to).max() < 1e-5 * float(np.ptp(X, 0).max())
+
+
+def test_c2_full_size_matches_oracle(cesa, oracle):
+    """Config 2 (N = M = 2000, default schedule, 500 pose updates)."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
+    R, t = cesa.softassign(X, Y)
+    Ro, to, tro = oracle.softassign(X, Y)
+    assert rot_err_deg(R, Ro) < 1e-3
+    assert np.abs(t - to).max() < 1e-5 * float(np.ptp(X, 0).max())
+
+
+def test_far_from_origin_frame_dependence_is_reproduced(cesa, oracle):
+    """The reference's Softassign S depends on the coordinate origin (X is
+    weighted, then centred); the centred kernels rebuild it exactly."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.surface_pair(n=150, seed=8)
+    off = np.array([3.0, -2.0, 5.0], np.float32)
+    Xo, Yo = X + off, Y + off
+    R, t = cesa.softassign(Xo, Yo, param=cesa.Params.default(JMAX=30))
+    Ro, to, tro = oracle.softassign(Xo, Yo, JMAX=30)
+    R0, _, _ = oracle.softassign(X, Y, JMAX=30)
+    assert rot_err_deg(Ro, R0) > 1e-2  # the origin matters in the reference algorithm
+    assert rot_err_deg(R, Ro) < 1e-3
+    assert np.abs(t - to).max() < 1e-5 * 5.0
+
+
+@pytest.mark.parametrize("n,m", [(1, 1), (2, 5), (16, 17), (129, 33)])
+def test_tiny_sizes(cesa, oracle, n, m):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.surface_pair(n=n, m=m, seed=n * 7 + m)
+    p = cesa.Params.default(JMAX=20)
+    R, t, tr, rep = cesa.softassign(X, Y, param=p, trace=True)
+    Ro, to, tro = oracle.softassign(X, Y, JMAX=20)
+    assert np.all(np.isfinite(R)) and np.all(np.isfinite(t))
+    assert rel_err(tr[-1, 2], tro[-1, 2]) < 1e-5  # sumM
+    if tro[:, 30].min() > 1e-3:
+        assert rot_err_deg(R, Ro) < 1e-3
+
+
+def test_deterministic_and_device_entry(cesa, torch_cuda):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    torch = torch_cuda
+    X, Y, _, _ = W.surface_pair(n=500, seed=5)
+    p = cesa.Params.default(JMAX=10)
+    R1, t1 = cesa.softassign(X, Y, param=p)
+    R2, t2 = cesa.softassign(X, Y, param=p)
+    assert np.array_equal(R1, R2) and np.array_equal(t1, t2)
+    dRt = torch.tensor(np.r_[np.eye(3).reshape(-1), np.zeros(3)], dtype=torch.float32, device="cuda")
+    cesa.softassign_device(soa_tensor(torch, X), soa_tensor(torch, Y), dRt, param=p)
+    torch.cuda.synchronize()
+    assert cesa.stream_status() == 0
+    out = dRt.cpu().numpy().astype(np.float64)
+    assert np.array_equal(out[:9].reshape(3, 3), R1) and np.array_equal(out[9:], t1)
