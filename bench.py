@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark of the soft-correspondence registration path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000]
+
+One step is one complete registration (the whole annealing schedule) of the
+workload's seeded synthetic pair. The default workload is config 2: Softassign
+with N ~ M ~ 2000 and JMAX=100, I0=5, I1=3, i.e. 500 pose updates.
+
+ours:      `value` times the device-pointer C ABI entry point (inputs already
+           in HBM) with CUDA events on the launching stream. L2 is flushed
+           (256 MiB write) between steps, outside the timed events. `e2e`
+           times the host-pointer entry point (pinned host SoA in, R,t out,
+           copies included) by wall clock.
+reference: times the reference algorithm on the host cores (the oracle's FP32
+           port of the path, all threads) on a bounded sample of the same
+           workload, scaled to registrations/s.
+
+Multi-GPU: one process per GPU (torchrun), independent replicas of the same
+workload; value = registrations done by all ranks / max rank time.
+Rank 0 prints one JSON line.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2_softassign_2000")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0,
+                    help="target seconds of CPU work for the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name, seed):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    kind, X, Y, Rt, tt = W.make(name, seed=seed)
+    return kind, X, Y
+
+
+class RefDefaults:
+    """The reference CLI defaults (src/main.cpp:280-315), without loading libcesa."""
+    JMAX, I0, I1, alpha, T_0, TFACTOR = 100, 5, 3, 3.0, 100.0, 0.95
+    moutlier = float(np.float32(np.exp(np.float32(-1.0)) / np.sqrt(np.float32(100.0))))
+    sigma_p2, sigma_inf, sigma_factor, d_02 = 0.01, 1e-5, 0.9, 0.01
+
+
+def params_for(cesa, kind):
+    return cesa.Params.default()
+
+
+def pose_updates(kind, p):
+    if kind == "softassign":
+        return p.JMAX * p.I0
+    n, s = 0, np.float32(p.sigma_p2)
+    while s > np.float32(p.sigma_inf):
+        n += 1
+        s = np.float32(s * np.float32(p.sigma_factor))
+    return n
+
+
+def algorithmic_work(kind, N, M, p):
+    """(fp32 ops, ex2 ops, affinity elements) of one registration.
+
+    EM-ICP: per element 12 FP32-pipe ops + 1 ex2 (3 FADD, FMUL + 2 FFMA for
+    d^2, FMUL scale, FFMA + FADD + 3 FFMA accumulators).
+    Softassign: per pose update 2*I1 Sinkhorn sweeps of 7 FP32 ops + 1 ex2
+    (3 FADD, FMUL + 2 FFMA, FFMA exponent, FFMA weighted sum) and one final
+    sweep of 11 FP32 ops + 1 ex2.
+    """
+    n = pose_updates(kind, p)
+    e = float(N) * float(M)
+    if kind == "emicp":
+        return 12.0 * e * n, e * n, e * n
+    sweeps = 2 * p.I1
+    return e * n * (7.0 * sweeps + 11.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
+
+
+def kernels_per_registration(kind):
+    # prep_center + 2 x prep_pack (+ 2 x fill for the slack vectors) + the persistent kernel
+    return 4 if kind == "emicp" else 6
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(kind, X, Y, p, target_s, threads=None):
+    """Times the oracle's FP32 port of the reference algorithm on the host on a
+    bounded sample; returns (registrations/s, description, threads)."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    O.set_threads(threads)
+    n_full = pose_updates(kind, p)
+    # calibrate with one pose update, then size the sample to ~target_s
+    if kind == "emicp":
+        s1 = np.float32(p.sigma_p2) * np.float32(p.sigma_factor)
+        t0 = time.perf_counter()
+        O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=float(s1), sigma_factor=p.sigma_factor,
+                d_02=p.d_02, precision="f32", trace=False)
+        one = time.perf_counter() - t0
+        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
+        sig = np.float32(p.sigma_p2)
+        for _ in range(k):
+            sig = np.float32(sig * np.float32(p.sigma_factor))
+        t0 = time.perf_counter()
+        O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=float(sig), sigma_factor=p.sigma_factor,
+                d_02=p.d_02, precision="f32", trace=False)
+        dt = time.perf_counter() - t0
+    else:
+        t0 = time.perf_counter()
+        O.softassign(X, Y, JMAX=1, I0=1, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
+                     moutlier=p.moutlier, precision="f32", trace=False)
+        one = time.perf_counter() - t0
+        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
+        t0 = time.perf_counter()
+        O.softassign(X, Y, JMAX=1, I0=k, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
+                     moutlier=p.moutlier, precision="f32", trace=False)
+        dt = time.perf_counter() - t0
+    per_update = dt / k
+    regs_per_s = 1.0 / (per_update * n_full)
+    desc = ("first %d of %d pose updates of one registration (FP32 port of the reference algorithm, "
+            "OpenMP), scaled to a full registration" % (k, n_full))
+    return regs_per_s, desc, threads
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    kind, X, Y = workload(args.workload, args.seed)
+    p = RefDefaults()
+    per_step = max(2.0, args.cpu_sample_s / max(1, args.steps + args.warmup))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, desc, thr = cpu_baseline(kind, X, Y, p, per_step)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": "registrations/s", "value": value, "unit": "registrations/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_of(args, kind, X, Y, p),
+            "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": thr, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, kind, X, Y, p):
+    c = {"workload": args.workload, "algorithm": kind, "N": int(len(X)), "M": int(len(Y)),
+         "pose_updates_per_registration": pose_updates(kind, p), "seed": args.seed,
+         "l2": "flushed between steps (256 MiB write), outside the timed events",
+         "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+    if kind == "softassign":
+        c.update(JMAX=p.JMAX, I0=p.I0, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR)
+    else:
+        c.update(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_inf, sigma_factor=p.sigma_factor, d_02=p.d_02)
+    return c
+
+
+def load_peaks():
+    from cuda_emicp_softassign_gb300 import build
+    L = ctypes.CDLL(build.PEAKS_LIB)
+    L.cesa_peaks_measure.argtypes = [ctypes.POINTER(ctypes.c_double)] * 2
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    rc = L.cesa_peaks_measure(ctypes.byref(a), ctypes.byref(b))
+    return (a.value, b.value) if rc == 0 else (None, None)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+    import cuda_emicp_softassign_gb300 as cesa
+
+    torch.cuda.set_device(local)
+    kind, X, Y = workload(args.workload, args.seed)
+    p = params_for(cesa, kind)
+    N, M = len(X), len(Y)
+    dev_call = cesa.emicp_device if kind == "emicp" else cesa.softassign_device
+    host_call = cesa.emicp if kind == "emicp" else cesa.softassign
+
+    dX = torch.from_numpy(cesa.cloud2data(X)).cuda()
+    dY = torch.from_numpy(cesa.cloud2data(Y)).cuda()
+    pose0 = torch.tensor(np.r_[np.eye(3).reshape(-1), np.zeros(3)], dtype=torch.float32, device="cuda")
+    dRt = pose0.clone()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def one_step():
+        dRt.copy_(pose0)
+        dev_call(dX, dY, dRt, param=p, d_status=status, stream=stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        one_step()
+    torch.cuda.synchronize()
+    assert cesa.stream_status(stream) == 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        dRt.copy_(pose0)
+        ev[k][0].record(stream)
+        dev_call(dX, dY, dRt, param=p, d_status=status, stream=stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    st = cesa.stream_status(stream)
+    assert st == 0, "device status %d" % st
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(np.sum(step_ms))
+    R_dev = dRt.cpu().numpy().astype(np.float64)
+
+    # ---- end to end through the host-pointer C ABI (pinned SoA in, R,t out)
+    hX = torch.from_numpy(cesa.cloud2data(X)).pin_memory().numpy()
+    hY = torch.from_numpy(cesa.cloud2data(Y)).pin_memory().numpy()
+    lib = cesa.lib()
+    Rh = np.eye(3, dtype=np.float32).reshape(-1).copy()
+    th = np.zeros(3, np.float32)
+    fn = lib.cesa_emicp if kind == "emicp" else lib.cesa_softassign
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    for _ in range(max(1, args.warmup)):
+        Rh[:] = np.eye(3, dtype=np.float32).reshape(-1)
+        th[:] = 0
+        assert fn(ptr(hX), N, ptr(hY), M, ptr(Rh), ptr(th), ctypes.byref(p), None) == 0
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        Rh[:] = np.eye(3, dtype=np.float32).reshape(-1)
+        th[:] = 0
+        t0 = time.perf_counter()
+        rc = fn(ptr(hX), N, ptr(hY), M, ptr(Rh), ptr(th), ctypes.byref(p), None)
+        e2e_s += time.perf_counter() - t0
+        assert rc == 0
+    assert np.array_equal(Rh.astype(np.float64), R_dev[:9]), "host and device entry points disagree"
+
+    # ---- max over ranks
+    tot = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    total_ms, e2e_s = float(tot[0]), float(tot[1])
+    if rank != 0:
+        return
+
+    regs = args.steps * world
+    value = regs / (total_ms * 1e-3)
+    fp32_ops, ex2_ops, elems = algorithmic_work(kind, N, M, p)
+    mean_s = total_ms * 1e-3 / args.steps
+    fp32_peak, ex2_peak = load_peaks()
+    achieved = fp32_ops / mean_s / 1e12
+    roofline = {"bound": "fp32", "kernel": "%s_kernel" % kind,
+                "achieved": achieved, "peak": fp32_peak / 1e12 if fp32_peak else None, "unit": "TFLOP/s",
+                "frac": achieved / (fp32_peak / 1e12) if fp32_peak else None,
+                "traffic": None,
+                "peak_source": "measured in this run: FFMA lane-op rate (libcesa_peaks), FMA counted as 1 op; "
+                               "MEASURED_PEAKS.json carries no FP32/MUFU figure",
+                "ex2_achieved_tops": ex2_ops / mean_s / 1e12,
+                "ex2_peak_tops": ex2_peak / 1e12 if ex2_peak else None,
+                "ops_per_registration": fp32_ops,
+                "note": "achieved = algorithmic FP32-pipe ops of one registration / event time of its launch "
+                        "sequence (prep kernels included)"}
+    cpu_v, cpu_desc, cpu_thr = cpu_baseline(kind, X, Y, p, args.cpu_sample_s)
+    h2d = (N + M) * 3 * 4 + 12 * 4
+    line = {"metric": "registrations/s", "value": value, "unit": "registrations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator of the workload; see cuda_emicp_softassign_gb300/workloads.py)",
+            "config": config_of(args, kind, X, Y, p),
+            "gelem_per_s": elems * regs / (total_ms * 1e-3) / 1e9,
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_v, "unit": "registrations/s", "cores": cpu_thr, "kind": "port",
+                             "sample": cpu_desc},
+            "e2e": {"value": args.steps * world / e2e_s, "unit": "registrations/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * 4},
+            "clocks": clocks,
+            "gpu_launches": kernels_per_registration(kind) * args.steps,
+            "wall_s_timed_region": t_wall}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend="nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo")
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

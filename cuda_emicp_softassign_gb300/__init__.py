@@ -77,7 +77,7 @@ class Report(ctypes.Structure):
     _fields_ = [
         ("trace", ctypes.c_void_p), ("trace_capacity", ctypes.c_int), ("steps", ctypes.c_int),
         ("sinkhorn_form", ctypes.c_int), ("grid_blocks", ctypes.c_int), ("device_ms", ctypes.c_float),
-        ("reserved", ctypes.c_int * 3),
+        ("timeline", ctypes.c_void_p), ("timeline_capacity", ctypes.c_int), ("timeline_written", ctypes.c_int),
     ]
 
 
@@ -156,10 +156,15 @@ def _pose_in(R, t):
     return Rh, th
 
 
-def _host_call(fn_name, X, Y, R, t, param, trace):
+def _host_call(fn_name, X, Y, R, t, param, trace, timeline=0):
     Xs, Ys = cloud2data(X), cloud2data(Y)
     Rh, th = _pose_in(R, t)
     rep = Report()
+    tl = None
+    if timeline:
+        tl = np.zeros(int(timeline), np.uint64)
+        rep.timeline = tl.ctypes.data
+        rep.timeline_capacity = int(timeline)
     tr = None
     if trace:
         cap = int(trace) if not isinstance(trace, bool) else 100000
@@ -170,22 +175,33 @@ def _host_call(fn_name, X, Y, R, t, param, trace):
                                  ctypes.byref(param), ctypes.byref(rep))
     _check(rc, fn_name)
     out = (Rh.reshape(3, 3).astype(np.float64), th.astype(np.float64))
+    if timeline:
+        return out + (tl[: rep.timeline_written], rep)
     if trace:
         return out + (tr[: min(rep.steps, tr.shape[0])], rep)
     return out
 
 
-def emicp(X, Y, R=None, t=None, param=None, trace=False):
+def timeline_table(tl):
+    """Decodes a phase timeline into (phase, ns since the first entry) rows."""
+    tl = np.asarray(tl, dtype=np.uint64)
+    phase = (tl >> np.uint64(56)).astype(np.int64)
+    t = (tl & np.uint64((1 << 56) - 1)).astype(np.int64)
+    return np.stack([phase, t - t[0]], axis=1) if len(t) else np.zeros((0, 2), np.int64)
+
+
+def emicp(X, Y, R=None, t=None, param=None, trace=False, timeline=0):
     """Annealed EM-ICP on the GPU (replaces emicp(), src/emicp.cu:247-716).
 
-    Returns (R, t), or (R, t, trace, report) when ``trace`` is set.
+    Returns (R, t); (R, t, trace, report) when ``trace`` is set; (R, t,
+    timeline, report) when ``timeline`` (a capacity) is given.
     """
-    return _host_call("cesa_emicp", X, Y, R, t, param or Params.default(), trace)
+    return _host_call("cesa_emicp", X, Y, R, t, param or Params.default(), trace, timeline)
 
 
-def softassign(X, Y, R=None, t=None, param=None, trace=False):
+def softassign(X, Y, R=None, t=None, param=None, trace=False, timeline=0):
     """Annealed Softassign on the GPU (replaces softassign(), src/softassign.cu:256-886)."""
-    return _host_call("cesa_softassign", X, Y, R, t, param or Params.default(), trace)
+    return _host_call("cesa_softassign", X, Y, R, t, param or Params.default(), trace, timeline)
 
 
 def find_rt_from_s(Xc, Yc, S, q_prev=None):

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcesa.so")
+PEAKS_LIB = os.path.join(HERE, "libcesa_peaks.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -84,5 +85,21 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def build_peaks(force=False):
+    """Compiles libcesa_peaks.so (FP32 / MUFU throughput probes for bench.py)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(CSRC, "cesa_peaks.cu")
+    if not force and _mtime(PEAKS_LIB) >= _mtime(src):
+        return PEAKS_LIB
+    tmp = PEAKS_LIB + ".tmp"
+    cmd = [nvcc()] + NVFLAGS + ["-shared", src, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for cesa_peaks.cu:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, PEAKS_LIB)
+    return PEAKS_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_peaks(force="--force" in sys.argv))

@@ -48,6 +48,7 @@ struct StreamCtx {
   DevBuf ws;     // kernel workspace (control block first)
   DevBuf io;     // point copies + pose + outputs for host-pointer calls
   DevBuf trace;  // device trace records
+  DevBuf tl;     // device phase timeline
   int last_trace_steps = 0;
   int last_kind = 0;  // 1 emicp, 2 softassign
 };
@@ -165,6 +166,13 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
     if (e != cudaSuccess) return map_cuda(e);
     dtrace = static_cast<double*>(C.trace.p);
   }
+  const int tl_cap = (rep && rep->timeline && rep->timeline_capacity > 0) ? rep->timeline_capacity : 0;
+  unsigned long long* dtl = nullptr;
+  if (tl_cap > 0) {
+    e = C.tl.ensure(sizeof(unsigned long long) * (size_t)tl_cap);
+    if (e != cudaSuccess) return map_cuda(e);
+    dtl = static_cast<unsigned long long*>(C.tl.p);
+  }
   float hRt[12];
   memcpy(hRt, R, sizeof(float) * 9);
   memcpy(hRt + 9, t, sizeof(float) * 3);
@@ -191,6 +199,8 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
       L.dRt = dRt;
       L.trace = dtrace;
       L.trace_cap = cap;
+      L.timeline = dtl;
+      L.timeline_cap = tl_cap;
       L.timeout_ns = timeout_ns_of(p);
       kerr = enqueue_emicp(L, C.ws.p, C.ws.bytes, st, &grid);
     } else {
@@ -210,6 +220,8 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
       L.dRt = dRt;
       L.trace = dtrace;
       L.trace_cap = cap;
+      L.timeline = dtl;
+      L.timeline_cap = tl_cap;
       L.timeout_ns = timeout_ns_of(p);
       kerr = enqueue_softassign(L, C.ws.p, C.ws.bytes, st, &grid);
     }
@@ -218,8 +230,8 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(hRt, dRt, sizeof(hRt), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  int status = 0, steps = 0;
-  if (e == cudaSuccess) e = (cudaError_t)read_ws_status(C.ws.p, st, &status, &steps);
+  int status = 0, steps = 0, tl_n = 0;
+  if (e == cudaSuccess) e = (cudaError_t)read_ws_status(C.ws.p, st, &status, &steps, &tl_n);
   float ms = 0.f;
   if (e == cudaSuccess) cudaEventElapsedTime(&ms, ev0, ev1);
   cudaEventDestroy(ev0);
@@ -232,6 +244,12 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
     e = cudaMemcpy(rep->trace, dtrace, sizeof(double) * 32 * (size_t)C.last_trace_steps,
                    cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return map_cuda(e);
+  }
+  if (tl_cap > 0) {
+    if (tl_n > tl_cap) tl_n = tl_cap;
+    e = cudaMemcpy(rep->timeline, dtl, sizeof(unsigned long long) * (size_t)tl_n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return map_cuda(e);
+    rep->timeline_written = tl_n;
   }
   memcpy(R, hRt, sizeof(float) * 9);
   memcpy(t, hRt + 9, sizeof(float) * 3);
@@ -521,6 +539,7 @@ void cesa_release_workspaces(void) {
     kv.second.ws.release();
     kv.second.io.release();
     kv.second.trace.release();
+    kv.second.tl.release();
     cudaSetDevice(cur);
   }
   g_ctx.clear();

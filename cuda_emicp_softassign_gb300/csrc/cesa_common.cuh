@@ -53,6 +53,17 @@ __device__ __forceinline__ void set_status(Ctl* ctl, int code, int where) {
   if (atomicCAS(&ctl->status, 0, code) == 0) ctl->where = where;
 }
 
+// Optional phase timeline, recorded by thread 0 of block 0 only.
+struct Timeline {
+  unsigned long long* p;
+  int cap;
+  int n;
+  __device__ __forceinline__ void mark(int phase) {
+    if (p && blockIdx.x == 0 && threadIdx.x == 0 && n < cap)
+      p[n++] = ((unsigned long long)phase << 56) | (global_ns() & ((1ull << 56) - 1));
+  }
+};
+
 // ---------------------------------------------------------------- double-float
 struct df {
   float hi, lo;

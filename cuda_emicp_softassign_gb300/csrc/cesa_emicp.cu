@@ -46,6 +46,8 @@ struct EmicpArgs {
   int trace_cap;
   float* row_out;       // optional [M][5] (centred-frame u)
   int* d_status;
+  unsigned long long* tl;
+  int tl_cap;
   uint64_t timeout_ns;
 };
 
@@ -161,8 +163,10 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   unsigned epoch = 0;
   const StreamSrc src{A.cols, nullptr, true};
   float s2 = A.sigma0;
+  Timeline tl{A.tl, A.tl_cap, 0};
 
   for (int step = 0; step < A.nsteps; ++step) {
+    tl.mark(1);
     const float outlier = expf(-A.d_02 / s2);  // src/emicp.cu:489
     if (tid < kEmNV) s_acc[tid] = df_make(0.f);
     float R[9], tc[3];
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
                        A.row_out, {s_hdr[0], s_hdr[1], s_hdr[2]},
                        s_red,     s_acc};
     if (!sweep_units<5>(sm, pipe, A.geo, src, A.rows, true, R, tc, (unsigned)step, A.part, A.cnt,
-                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10))
+                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10, tl))
       break;
 
     // ---- grid-wide moments -> pose (every block computes the same pose)
@@ -189,7 +193,9 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
       __stcg(reinterpret_cast<float2*>(bp + (size_t)blockIdx.x * kEmNV + tid), make_float2(a.hi, a.lo));
     }
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
+    tl.mark(5);
     reduce_block_partials<kEmNV>(bp, (int)G, s_red, s_tot);
+    tl.mark(6);
     if (tid == 0) {
       const float L = df_val(s_tot[0]);
       float Xc[3], Yc[3], S[9];
@@ -233,6 +239,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
       }
     }
     __syncthreads();
+    tl.mark(7);
     s2 *= A.sigma_factor;  // FP32, src/emicp.cu:668
   }
 
@@ -247,6 +254,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
       for (int k = 0; k < 3; ++k) A.dRt[9 + k] = t[k];
     }
     if (A.d_status) *A.d_status = st;
+    if (A.tl) A.ctl->pad[0] = (unsigned)tl.n;
   }
 }
 
@@ -359,6 +367,8 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.trace_cap = L.trace_cap;
   A.row_out = L.row_out;
   A.d_status = L.d_status;
+  A.tl = L.timeline;
+  A.tl_cap = L.timeline_cap;
   A.timeout_ns = L.timeout_ns;
   void* args[] = {(void*)&A};
   e = cudaLaunchCooperativeKernel((const void*)emicp_kernel, dim3(P.grid), dim3(kThreads), args,
@@ -366,13 +376,14 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   return (int)e;
 }
 
-int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps) {
+int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written) {
   Ctl h;
   cudaError_t e = cudaMemcpyAsync(&h, ws, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return (int)e;
   if (status) *status = h.status;
   if (steps) *steps = h.steps_done;
+  if (tl_written) *tl_written = (int)h.pad[0];
   return 0;
 }
 

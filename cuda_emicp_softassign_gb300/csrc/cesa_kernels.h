@@ -35,6 +35,8 @@ struct EmicpLaunch {
   double* trace;     // optional device trace [cap][32]
   int trace_cap;
   int* d_status;     // optional device status mirror
+  unsigned long long* timeline;  // optional device phase timeline (block 0)
+  int timeline_cap;
   uint64_t timeout_ns;
 };
 
@@ -54,6 +56,8 @@ struct SoftassignLaunch {
   double* trace;
   int trace_cap;
   int* d_status;
+  unsigned long long* timeline;
+  int timeline_cap;
   uint64_t timeout_ns;
 };
 
@@ -79,6 +83,6 @@ size_t emicp_ws_need(int N, int M, int device);
 size_t softassign_ws_need(int N, int M, int form, int device);
 
 // Control-block status of the last launch that used workspace ws.
-int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps);
+int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written = nullptr);
 
 }  // namespace cesa

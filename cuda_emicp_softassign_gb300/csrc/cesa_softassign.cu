@@ -19,9 +19,11 @@
 // 2*I1 + 1 grid barriers.
 //
 // The reference's S is not translation invariant, because X is weighted and
-// only then centred. Coordinates are centred on the device for accuracy, and
-// the original-frame S is rebuilt exactly from 32 compensated sums of
-// centred-frame per-row and per-column quantities.
+// only then centred. Coordinates are shifted by exact offsets (see
+// exact_offset), and the original-frame S is rebuilt exactly from 28
+// compensated row sums and 4 column sums. The final sweep accumulates
+// centred terms (Vhat, mu = m - w), so S is formed without the cancellation
+// of large sums at high temperature, where the assignment is nearly uniform.
 #include "cesa_kernels.h"
 #include "cesa_pose.h"
 #include "cesa_prep.cuh"
@@ -34,7 +36,7 @@ constexpr int kSaNV = 32;
 struct SoftArgs {
   float4* rows;    // X' centred, .w = a_r   (N)
   float4* cols;    // Y' centred, .w = b_c   (M)
-  float4* colfin;  // per column (g y', g), g = b_c cs_c after the last column pass
+  float4* colfin;  // per column (cs_c, g_c = b_c cs_c, delta_c = b_c (cs_c - 1), 0) after the last column pass
   float* s;        // slack column [N]
   float* u;        // slack row [M]
   float* rs;       // last row sums incl. slack [N]
@@ -50,20 +52,23 @@ struct SoftArgs {
   unsigned* cnt_r;
   float* part_c;
   unsigned* cnt_c;
-  df* bpart;  // [2][grid][kSaNV]
+  df* bpart;   // [2][grid][kSaNV]  row-side moments
+  df* bcol;    // [2][grid][4]      column moments (sum cs, sum cs y')
   Ctl* ctl;
   double* trace;
   int trace_cap;
   int* d_status;
+  unsigned long long* tl;
+  int tl_cap;
   uint64_t timeout_ns;
 };
 
-// Streamed Y columns for row sweeps: (R y' + t', b_c) with b_c := 1 in the
-// first pass of an inner iteration.
+// Streamed Y columns for Sinkhorn row sweeps: (R y' + t', b_c), with b_c := 1
+// in the first pass of an inner iteration.
 struct RowPrep {
   float R[9], tc[3];
   bool unit_w;
-  __device__ __forceinline__ const float4* operator()(SweepSmem& sm, int stage, int len) const {
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int len) const {
     for (int c = threadIdx.x; c < len; c += kThreads) {
       const float4 y = sm.raw[stage][c];
       sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
@@ -71,7 +76,27 @@ struct RowPrep {
                                R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], unit_w ? 1.f : y.w);
     }
     __syncthreads();
-    return sm.prep;
+    return PrepOut{sm.prep, sm.raw2[stage]};
+  }
+};
+
+// Streamed Y columns for the final row sweep: (R y' + t', b_c) and
+// (g_c (y'_c - Yhat), delta_c). Yhat = sum cs y' / sum cs makes the weighted
+// sums of the third stream small where the assignment is nearly uniform, so
+// the cross-covariance is formed from centred terms.
+struct FinalPrep {
+  float R[9], tc[3], yh[3];
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int len) const {
+    for (int c = threadIdx.x; c < len; c += kThreads) {
+      const float4 y = sm.raw[stage][c];
+      const float4 f = sm.raw2[stage][c];  // (cs, g, delta, 0)
+      sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
+                               R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
+                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], y.w);
+      sm.prep2[c] = make_float4(f.y * (y.x - yh[0]), f.y * (y.y - yh[1]), f.y * (y.z - yh[2]), f.z);
+    }
+    __syncthreads();
+    return PrepOut{sm.prep, sm.prep2};
   }
 };
 
@@ -91,11 +116,11 @@ struct SinkElem {
   }
 };
 
-// Final row sweep element: w += K b, m += K g, V' += K g y'.
+// Final row sweep element: w += K b, mu += K delta, Vhat += K g (y' - Yhat).
 struct FinalElem {
   float nk, c0;
   __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 s,
-                                             float4 hg) const {
+                                             float4 h) const {
     const float dx = s.x - p[0];
     const float dy = s.y - p[1];
     const float dz = s.z - p[2];
@@ -104,10 +129,10 @@ struct FinalElem {
     d2 = fmaf(dz, dz, d2);
     const float e = ex2_approx(fmaf(d2, nk, c0));
     acc[0] = fmaf(e, s.w, acc[0]);
-    acc[1] = fmaf(e, hg.w, acc[1]);
-    acc[2] = fmaf(e, hg.x, acc[2]);
-    acc[3] = fmaf(e, hg.y, acc[3]);
-    acc[4] = fmaf(e, hg.z, acc[4]);
+    acc[1] = fmaf(e, h.w, acc[1]);
+    acc[2] = fmaf(e, h.x, acc[2]);
+    acc[3] = fmaf(e, h.y, acc[3]);
+    acc[4] = fmaf(e, h.z, acc[4]);
   }
 };
 
@@ -132,7 +157,8 @@ struct RowFin {
 };
 
 // Column pass finalize (normalizeMbySinkhorn_col + Saxpy, src/softassign.cu:579-597).
-// On the last pass also records (g y', g) and the column moments for Yc.
+// On the last pass also records (cs, g, delta) per column and the column
+// moments sum cs, sum cs y' (the reference's Yw = cs .* Y, src/softassign.cu:661-666).
 struct ColFin {
   float4* cols;
   float4* colfin;
@@ -141,7 +167,7 @@ struct ColFin {
   int M;
   bool first, last;
   df* red;
-  df* acc;  // block accumulator slots 28..31
+  df* acc;  // block accumulator, 4 slots
   __device__ void operator()(int blk, const float (&tot)[1]) const {
     df v[4];
 #pragma unroll
@@ -157,8 +183,7 @@ struct ColFin {
       __stcg(&u[c], u_old / sum);
       __stcg(&cs[c], sum);
       if (last) {
-        const float g = b_new * sum;
-        __stcg(&colfin[c], make_float4(g * y.x, g * y.y, g * y.z, g));
+        __stcg(&colfin[c], make_float4(sum, b_new * sum, b_new * (sum - 1.f), 0.f));
         df_add(v[0], sum);
         df_add_prod(v[1], sum, y.x);
         df_add_prod(v[2], sum, y.y);
@@ -169,10 +194,10 @@ struct ColFin {
   }
 };
 
-// Final row finalize: w, m, V' and the 28 row-side moments.
-//  0: sum w        1-3: sum w x'         4-12: sum w x'_i V'_j (i + 3j)
-// 13-15: sum w^2 x'  16-18: sum V'        19-21: sum m w x'   22: sum m
-// 23-25: sum w V'    26: sum w^2         27: sum w m
+// Final row finalize: w, mu = m - w, Vhat and the 28 row-side moments.
+//  0: sum w            1-3: sum w x'         4-12: sum w x'_i Vhat_j (i + 3j)
+// 13-15: sum Vhat       16-18: sum w mu x'    19: sum mu
+// 20-22: sum w^2 x'     23: sum w^2           24-26: sum w Vhat      27: sum w mu
 struct FinalFin {
   const float4* rows;
   float* w_out;
@@ -187,11 +212,11 @@ struct FinalFin {
     if (threadIdx.x < kBlockPts && r < N) {
       const float4 x = __ldcg(&rows[r]);
       const float a = x.w;
-      const float w = a * tot[0], m = a * tot[1];
+      const float w = a * tot[0], mu = a * tot[1];
       const float V[3] = {a * tot[2], a * tot[3], a * tot[4]};
       const float xp[3] = {x.x, x.y, x.z};
       if (w_out) w_out[r] = w;
-      const float w2 = w * w, mw = m * w;
+      const float w2 = w * w, wmu = w * mu;
       df_add(v[0], w);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -199,14 +224,14 @@ struct FinalFin {
         const float wx = w * xp[i];
 #pragma unroll
         for (int j = 0; j < 3; ++j) df_add_prod(v[4 + i + 3 * j], wx, V[j]);
-        df_add_prod(v[13 + i], w2, xp[i]);
-        df_add(v[16 + i], V[i]);
-        df_add_prod(v[19 + i], mw, xp[i]);
-        df_add_prod(v[23 + i], w, V[i]);
+        df_add(v[13 + i], V[i]);
+        df_add_prod(v[16 + i], wmu, xp[i]);
+        df_add_prod(v[20 + i], w2, xp[i]);
+        df_add_prod(v[24 + i], w, V[i]);
       }
-      df_add(v[22], m);
-      df_add_prod(v[26], w, w);
-      df_add_prod(v[27], w, m);
+      df_add(v[19], mu);
+      df_add_prod(v[23], w, w);
+      df_add_prod(v[27], w, mu);
     }
     block_accumulate<28>(v, red, acc);
   }
@@ -219,15 +244,22 @@ __device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df p
   r.lo = __fmaf_rn(a.lo, b, r.lo);
   return r;
 }
+__device__ __forceinline__ df dsub(df a, const df& b) {
+  df_add(a, df{-b.hi, -b.lo});
+  return a;
+}
 
 __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
   __shared__ float s_pose[12];
   __shared__ df s_acc[kSaNV];
+  __shared__ df s_cacc[4];
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[kSaNV];
+  __shared__ df s_ctot[4];
   __shared__ float s_hdr[8];
+  __shared__ float s_S[9], s_xcp[3], s_yd[3], s_xc[3], s_yc[3];
 
   const int tid = threadIdx.x;
   const unsigned G = gridDim.x;
@@ -259,6 +291,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   float T = A.T0;
   int step = 0;
   bool ok = true;
+  Timeline tl{A.tl, A.tl_cap, 0};
 
   for (int Titer = 0; Titer < A.JMAX && ok; ++Titer) {
     // K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
@@ -266,7 +299,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     const float nk = -kk;
     const float c0 = fmaf(A.alpha, kk, -0.5f * log2f(T));
     for (int iter0 = 0; iter0 < A.I0 && ok; ++iter0, ++step) {
+      tl.mark(1);
       if (tid < kSaNV) s_acc[tid] = df_make(0.f);
+      if (tid < 4) s_cacc[tid] = df_make(0.f);
       float R[9], tc[3];
 #pragma unroll
       for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
@@ -274,6 +309,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
       __syncthreads();
       const SinkElem se{nk, c0};
+      const int par = step & 1;
       for (int k = 0; k < A.I1 && ok; ++k) {
         // row pass: own X rows, stream transformed Y columns weighted by b
         RowPrep rp;
@@ -284,97 +320,113 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         rp.unit_w = (k == 0);
         const RowFin rf{A.rows, A.s, A.rs, A.N, k == 0};
         ok = sweep_units<1>(sm, pipe, A.gr, src_cols, A.rows, false, R, tc, round_r++, A.part_r,
-                            A.cnt_r, se, rp, rf, A.ctl, A.timeout_ns, 30) &&
+                            A.cnt_r, se, rp, rf, A.ctl, A.timeout_ns, 30, tl) &&
              grid_sync(A.ctl, epoch, G, A.timeout_ns, 32);
+        tl.mark(5);
         if (!ok) break;
         // column pass: own transformed Y columns, stream X rows weighted by a
-        const ColFin cf{A.cols, A.colfin, A.u, A.cs, A.M, k == 0, k == A.I1 - 1, s_red, s_acc + 28};
+        const bool last = (k == A.I1 - 1);
+        const ColFin cf{A.cols, A.colfin, A.u, A.cs, A.M, k == 0, last, s_red, s_cacc};
         ok = sweep_units<1>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc, round_c++, A.part_c,
-                            A.cnt_c, se, NoPrep{}, cf, A.ctl, A.timeout_ns, 40) &&
-             grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
+                            A.cnt_c, se, NoPrep{}, cf, A.ctl, A.timeout_ns, 40, tl);
+        if (ok && last && tid < 4) {
+          const df a = s_cacc[tid];
+          __stcg(reinterpret_cast<float2*>(A.bcol + ((size_t)par * G + blockIdx.x) * 4 + tid),
+                 make_float2(a.hi, a.lo));
+        }
+        ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
+        tl.mark(5);
       }
       if (!ok) break;
-      // final row sweep: w, m, V'
+      // column moments -> Yhat (identical in every block)
+      reduce_block_partials<4>(A.bcol + (size_t)par * G * 4, (int)G, s_red, s_ctot);
+      tl.mark(6);
+      float yh[3];
       {
-        RowPrep rp;
+        const float B1 = df_val(s_ctot[0]);
+        for (int i = 0; i < 3; ++i) yh[i] = df_val(s_ctot[1 + i]) / B1;
+      }
+      // final row sweep: w, mu, Vhat
+      {
+        FinalPrep fp;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) rp.R[q] = R[q];
+        for (int q = 0; q < 9; ++q) fp.R[q] = R[q];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) rp.tc[q] = tc[q];
-        rp.unit_w = false;
+        for (int q = 0; q < 3; ++q) {
+          fp.tc[q] = tc[q];
+          fp.yh[q] = yh[q];
+        }
         const FinalElem fe{nk, c0};
         const FinalFin ff{A.rows, A.w_out, A.N, s_red, s_acc};
         ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_r++, A.part_r,
-                            A.cnt_r, fe, rp, ff, A.ctl, A.timeout_ns, 50);
+                            A.cnt_r, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl);
         if (!ok) break;
       }
-      df* bp = A.bpart + (size_t)(step & 1) * G * kSaNV;
+      df* bp = A.bpart + (size_t)par * G * kSaNV;
       if (tid < kSaNV) {
         const df a = s_acc[tid];
         __stcg(reinterpret_cast<float2*>(bp + (size_t)blockIdx.x * kSaNV + tid),
                make_float2(a.hi, a.lo));
       }
       ok = grid_sync(A.ctl, epoch, G, A.timeout_ns, 52);
+      tl.mark(5);
       if (!ok) break;
       reduce_block_partials<kSaNV>(bp, (int)G, s_red, s_tot);
+      tl.mark(6);
+      // S_ij by threads 0..8, centres by threads 9..11 (in parallel), then the
+      // pose by thread 0.
+      //   S_ij = (T1_ij - Xc'_i T3_j) + (T4_i - Xc'_i T5) alpha_j + (T6_i - Xc'_i A1) beta_j
+      //        + oX_i (T8_j - T3_j) + (T9 - T5) oX_i alpha_j + (T7 - A1) oX_i beta_j
+      // with D_r = Vhat_r + (mu_r + (1 - rho) w_r) alpha, alpha = Yhat + oY,
+      // beta = (1 - rho) alpha, all sums compensated.
+      if (tid < 12) {
+        const float* oX = &s_hdr[0];
+        const float* oY = &s_hdr[3];
+        const df A1 = s_tot[0];
+        const float inv = 1.f / df_val(A1);
+        const float rho = df_val(s_ctot[0]) * inv;
+        if (tid < 9) {
+          const int i = tid % 3, j = tid / 3;
+          const float xi = df_val(s_tot[1 + i]) * inv;
+          const float al = yh[j] + oY[j];
+          const float be = (1.f - rho) * al;
+          const df T5 = s_tot[19], T7 = s_tot[23], T9 = s_tot[27];
+          df P2 = s_tot[16 + i];
+          df_add(P2, dmul(T5, -xi));
+          df P3 = s_tot[20 + i];
+          df_add(P3, dmul(A1, -xi));
+          df sij = s_tot[4 + i + 3 * j];
+          df_add(sij, dmul(s_tot[13 + j], -xi));
+          df_add(sij, dmul(P2, al));
+          df_add(sij, dmul(P3, be));
+          df_add(sij, dmul(dsub(s_tot[24 + j], s_tot[13 + j]), oX[i]));
+          df_add(sij, dmul(dsub(T9, T5), oX[i] * al));
+          df_add(sij, dmul(dsub(T7, A1), oX[i] * be));
+          s_S[i + 3 * j] = df_val(sij);
+        } else {
+          const int i = tid - 9;
+          const float xi = df_val(s_tot[1 + i]) * inv;
+          s_xcp[i] = xi;
+          s_xc[i] = xi + oX[i];
+          s_yc[i] = rho * (yh[i] + oY[i]);
+          df yd = df_make(0.f);  // Yc - oY = rho Yhat + (rho - 1) oY
+          df_add_prod(yd, rho, yh[i]);
+          df_add_prod(yd, rho - 1.f, oY[i]);
+          s_yd[i] = df_val(yd);
+        }
+      }
+      __syncthreads();
       if (tid == 0) {
         const float* oX = &s_hdr[0];
         const float* oY = &s_hdr[3];
         const df A1 = s_tot[0];
-        const float sumM = df_val(A1);
-        const float inv = 1.f / sumM;
-        float Xcp[3], Ycp[3];
+        float S[9], Xc[3], Yc[3], Xcp[3], Yd[3];
+        for (int k = 0; k < 9; ++k) S[k] = s_S[k];
         for (int i = 0; i < 3; ++i) {
-          Xcp[i] = df_val(s_tot[1 + i]) * inv;
-          Ycp[i] = df_val(s_tot[29 + i]) * inv;
-        }
-        const float rho = df_val(s_tot[28]) * inv;
-        const float C5 = df_val(s_tot[22]);
-        const float C7 = df_val(s_tot[26]);
-        // P_i = C4_i - rho C2_i - Xc'_i C5 + rho Xc'_i A1
-        // Q_j = C6_j - C3_j - Yc'_j C7 + Yc'_j A1
-        // Z   = C8 - rho C7 - C5 + rho A1
-        float P[3], Q[3];
-        for (int i = 0; i < 3; ++i) {
-          df p = s_tot[19 + i];
-          df_add(p, dmul(s_tot[13 + i], -rho));
-          df_add_prod(p, -Xcp[i], C5);
-          df_add(p, dmul(A1, rho * Xcp[i]));
-          P[i] = df_val(p);
-          df q = s_tot[23 + i];
-          df_add(q, df{-s_tot[16 + i].hi, -s_tot[16 + i].lo});
-          df_add_prod(q, -Ycp[i], C7);
-          df_add(q, dmul(A1, Ycp[i]));
-          Q[i] = df_val(q);
-        }
-        df z = s_tot[27];
-        df_add(z, dmul(s_tot[26], -rho));
-        df_add(z, df{-s_tot[22].hi, -s_tot[22].lo});
-        df_add(z, dmul(A1, rho));
-        const float Z = df_val(z);
-        // S_ij = C1_ij - C2_i Yc'_j - Xc'_i C3_j + Xc'_i Yc'_j A1
-        //        + P_i oY_j + oX_i Q_j + oX_i oY_j Z
-        float S[9];
-        for (int j = 0; j < 3; ++j)
-          for (int i = 0; i < 3; ++i) {
-            df sij = s_tot[4 + i + 3 * j];
-            df_add(sij, dmul(s_tot[13 + i], -Ycp[j]));
-            df_add(sij, dmul(s_tot[16 + j], -Xcp[i]));
-            df_add(sij, dmul(A1, Xcp[i] * Ycp[j]));
-            df_add_prod(sij, P[i], oY[j]);
-            df_add_prod(sij, oX[i], Q[j]);
-            df_add_prod(sij, oX[i] * oY[j], Z);
-            S[i + 3 * j] = df_val(sij);
-          }
-        float Xc[3], Yc[3], Yd[3];
-        for (int i = 0; i < 3; ++i) {
-          Xc[i] = Xcp[i] + oX[i];
-          df y = df_make(Ycp[i]);
-          df_add_prod(y, rho, oY[i]);
-          Yc[i] = df_val(y);
-          df yd = df_make(Ycp[i]);
-          df_add_prod(yd, rho - 1.f, oY[i]);
-          Yd[i] = df_val(yd);  // Yc - oY
+          Xc[i] = s_xc[i];
+          Yc[i] = s_yc[i];
+          Xcp[i] = s_xcp[i];
+          Yd[i] = s_yd[i];
         }
         float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
         horn_quaternion<float>(S, horn, q, &gap, &lmax);
@@ -406,6 +458,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         }
       }
       __syncthreads();
+      tl.mark(7);
     }
     T = T * A.TFACTOR;  // FP32, src/softassign.cu:820
   }
@@ -421,6 +474,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       for (int k = 0; k < 3; ++k) A.dRt[9 + k] = t[k];
     }
     if (A.d_status) *A.d_status = st;
+    if (A.tl) A.ctl->pad[0] = (unsigned)tl.n;
   }
 }
 
@@ -470,6 +524,7 @@ struct SaCarved {
   float* part_r;
   float* part_c;
   df* bpart;
+  df* bcol;
 };
 
 SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
@@ -489,6 +544,7 @@ SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
   w.part_r = c.take<float>((size_t)P.gr.units * 5 * kBlockPts);
   w.part_c = c.take<float>((size_t)P.gc.units * 1 * kBlockPts);
   w.bpart = c.take<df>((size_t)2 * P.grid * kSaNV);
+  w.bcol = c.take<df>((size_t)2 * P.grid * 4);
   if (total) *total = c.off;
   return w;
 }
@@ -558,10 +614,13 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.part_c = w.part_c;
   A.cnt_c = w.cnt_c;
   A.bpart = w.bpart;
+  A.bcol = w.bcol;
   A.ctl = w.ctl;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;
   A.d_status = L.d_status;
+  A.tl = L.timeline;
+  A.tl_cap = L.timeline_cap;
   A.timeout_ns = L.timeout_ns;
   void* args[] = {(void*)&A};
   e = cudaLaunchCooperativeKernel((const void*)softassign_kernel, dim3(P.grid), dim3(kThreads), args,

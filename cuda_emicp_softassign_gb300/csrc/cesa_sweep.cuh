@@ -46,6 +46,7 @@ struct __align__(16) SweepSmem {
   float4 raw[kStages][kChunk];   // TMA destination, stream A
   float4 raw2[kStages][kChunk];  // TMA destination, stream B (optional)
   float4 prep[kChunk];           // prepared stream A (transformed / weighted)
+  float4 prep2[kChunk];          // prepared stream B
   float red[kMaxAcc][kWarps][kBlockPts];
   uint64_t full[kStages];
   int flag;
@@ -159,13 +160,29 @@ __device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g
   }
   __syncthreads();
   const bool last = sm.flag != 0;
-  if (last && threadIdx.x < kBlockPts) {
+  if (last) {
+    // All threads take (accumulator, point) pairs; the S partials of a pair
+    // are loaded 8 at a time (independent loads in flight) and summed in
+    // slice order.
     const float* base = part + (size_t)blk * g.slices * NACC * kBlockPts;
-#pragma unroll
-    for (int a = 0; a < NACC; ++a) {
+    for (int p = threadIdx.x; p < NACC * kBlockPts; p += kThreads) {
+      const float* src = base + p;
       float s = 0.f;
-      for (int k = 0; k < g.slices; ++k) s += __ldcg(base + ((size_t)k * NACC + a) * kBlockPts + threadIdx.x);
-      tot[a] = s;
+      int k = 0;
+      for (; k + 8 <= g.slices; k += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = __ldcg(src + (size_t)(k + j) * NACC * kBlockPts);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s += v[j];
+      }
+      for (; k < g.slices; ++k) s += __ldcg(src + (size_t)k * NACC * kBlockPts);
+      reinterpret_cast<float*>(sm.red)[p] = s;  // red is free after reduce_warps
+    }
+    __syncthreads();
+    if (threadIdx.x < kBlockPts) {
+#pragma unroll
+      for (int a = 0; a < NACC; ++a) tot[a] = reinterpret_cast<float*>(sm.red)[a * kBlockPts + threadIdx.x];
     }
   }
   __syncthreads();
@@ -190,36 +207,50 @@ template <int NV>
 __device__ __forceinline__ void reduce_block_partials(const df* parts, int nblocks, df* scratch,
                                                       df* tot) {
   constexpr int G = kThreads / NV;  // threads per value
-  static_assert(kThreads % NV == 0, "NV must divide the block size");
+  static_assert(kThreads % NV == 0 && NV <= 32, "NV must divide the block size");
   const int v = threadIdx.x % NV, grp = threadIdx.x / NV;
-  df a0 = df_make(0.f), a1 = df_make(0.f);
+  // blocks grp, grp + G, ... in order; loads issued 8 at a time
+  df a = df_make(0.f);
   int b = grp;
-  for (; b + G < nblocks; b += 2 * G) {
-    const float2 x0 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
-    const float2 x1 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)(b + G) * NV + v));
-    df_add(a0, df{x0.x, x0.y});
-    df_add(a1, df{x1.x, x1.y});
+  for (; b + 7 * G < nblocks; b += 8 * G) {
+    float2 x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)(b + j * G) * NV + v));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) df_add(a, df{x[j].x, x[j].y});
   }
-  if (b < nblocks) {
-    const float2 x0 = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
-    df_add(a0, df{x0.x, x0.y});
+  for (; b < nblocks; b += G) {
+    const float2 x = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
+    df_add(a, df{x.x, x.y});
   }
-  df_add(a0, a1);
-  scratch[grp * NV + v] = a0;
+  // fixed tree over the groups: lanes of a warp with the same v, then warps
+#pragma unroll
+  for (int off = 16; off >= NV; off >>= 1) {
+    const df o = df_shfl_down(a, off);
+    df_add(a, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < NV) scratch[warp * NV + lane] = a;
   __syncthreads();
   if (threadIdx.x < NV) {
     df s = scratch[threadIdx.x];
-    for (int k = 1; k < G; ++k) df_add(s, scratch[k * NV + threadIdx.x]);
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) df_add(s, scratch[w * NV + threadIdx.x]);
     tot[threadIdx.x] = s;
   }
   __syncthreads();
 }
 
+// Streams as seen by the element function after the prepare step.
+struct PrepOut {
+  const float4* a;
+  const float4* b;
+};
 
-// Prepare step that uses stream A as loaded.
+// Prepare step that uses the streams as loaded.
 struct NoPrep {
-  __device__ __forceinline__ const float4* operator()(SweepSmem& sm, int stage, int len) const {
-    return sm.raw[stage];
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int) const {
+    return PrepOut{sm.raw[stage], sm.raw2[stage]};
   }
 };
 
@@ -230,7 +261,7 @@ struct NoPrep {
 // block that completes the owned block. Returns false if a wait gave up.
 //
 //   Elem: void operator()(float (&acc)[NACC], const float (&p)[3], float4 a, float4 b)
-//   Prep: const float4* operator()(SweepSmem&, int stage, int len)   (block-wide)
+//   Prep: PrepOut operator()(SweepSmem&, int stage, int len)         (block-wide)
 //   Fin:  void operator()(int blk, const float (&tot)[NACC])         (block-wide)
 template <int NACC, class Elem, class Prep, class Fin>
 __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const SweepGeom& g,
@@ -238,7 +269,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
                                             const float (&R)[9], const float (&tc)[3], unsigned round,
                                             float* part, unsigned* cnt, const Elem& elem,
                                             const Prep& prep, const Fin& fin, Ctl* ctl,
-                                            uint64_t timeout_ns, int where) {
+                                            uint64_t timeout_ns, int where, Timeline& tl) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int G = (int)gridDim.x;
   pipe.cur = -1;
@@ -306,8 +337,10 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
         if (have_n && n_wait) mbar_wait(&sm.full[n_stage], n_par, ctl, timeout_ns, where + 1);
         return false;
       }
-      const float4* __restrict__ bufA = prep(sm, cur_stage, cur_len);
-      const float4* __restrict__ bufB = sm.raw2[cur_stage];
+      if (cur_ch == 0 && u == (int)blockIdx.x) tl.mark(2);
+      const PrepOut pb = prep(sm, cur_stage, cur_len);
+      const float4* __restrict__ bufA = pb.a;
+      const float4* __restrict__ bufB = pb.b;
 #pragma unroll 2
       for (int c = warp; c < cur_len; c += kWarps) {
         const float4 a = bufA[c];
@@ -326,9 +359,11 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
       have = have_n;
       if (unit_done) break;
     }
+    tl.mark(3);
     float tot[NACC];
     reduce_warps<NACC>(sm, acc, tot);
     if (split_complete<NACC>(sm, g, blk, sl, round, part, cnt, tot)) fin(blk, tot);
+    tl.mark(4);
     u += G;
     cur_ch = 0;
   }

@@ -84,8 +84,21 @@ typedef struct cesa_report {
   int sinkhorn_form;    /* out: form used (Softassign) */
   int grid_blocks;      /* out: persistent grid size */
   float device_ms;      /* out: device time of the registration kernels */
-  int reserved[3];
+  /* Optional phase timeline of block 0 (profiling): entries are
+   * (phase << 56) | (globaltimer ns & (2^56 - 1)); phases are listed in
+   * CESA_TL_* below. */
+  unsigned long long* timeline;
+  int timeline_capacity;
+  int timeline_written; /* out */
 } cesa_report;
+
+#define CESA_TL_STEP 1       /* a pose update starts */
+#define CESA_TL_WAIT 2       /* first streamed chunk of a sweep has landed */
+#define CESA_TL_COMPUTE 3    /* a unit's affinity loop is done */
+#define CESA_TL_UNIT 4       /* a unit's reduction / completion is done */
+#define CESA_TL_SYNC 5       /* a grid barrier has been passed */
+#define CESA_TL_REDUCE 6     /* block partials reduced */
+#define CESA_TL_POSE 7       /* pose solved */
 
 /* Reference defaults: src/main.cpp:280-315 (moutlier = e^-1 / sqrt(T_0)). */
 void cesa_params_default(cesa_params* p);

@@ -1,0 +1,63 @@
+"""The C++ drop-in boundary: a program written against the reference API
+(3dregistration.h + registration.cpp, linked to libcesa.so), as the reference
+README asks users to build with emicp.cu / softassign.cu."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import REPO, rot_err_deg
+
+
+@pytest.fixture(scope="module")
+def dropin_exe(cesa):
+    d = tempfile.mkdtemp()
+    exe = os.path.join(d, "dropin")
+    libdir = os.path.dirname(cesa.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "tests", "dropin_main.cpp"),
+                    os.path.join(REPO, "cuda_emicp_softassign_gb300", "csrc", "registration.cpp"),
+                    "-L", libdir, "-lcesa", "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    return exe
+
+
+def _write(path, P):
+    with open(path, "wb") as f:
+        np.array([len(P)], np.int32).tofile(f)
+        np.ascontiguousarray(P, np.float32).tofile(f)
+
+
+def _run(exe, algo, X, Y, *extra):
+    d = tempfile.mkdtemp()
+    px, py = os.path.join(d, "x.bin"), os.path.join(d, "y.bin")
+    _write(px, X)
+    _write(py, Y)
+    r = subprocess.run([exe, algo, px, py] + [str(e) for e in extra], capture_output=True, text=True)
+    vals = [float(v) for v in r.stdout.split()]
+    return np.array(vals[:9]).reshape(3, 3), np.array(vals[9:12]), int(vals[12]), r.stderr
+
+
+def test_dropin_without_gpu_reports_and_keeps_pose(dropin_exe):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    X = np.random.default_rng(0).uniform(0, 1, (30, 3))
+    R, t, ok, err = _run(dropin_exe, "emicp", X, X)
+    assert np.array_equal(R, np.eye(3)) and np.array_equal(t, np.zeros(3))
+    assert "no usable CUDA device" in err and ok == 1
+
+
+@pytest.mark.gpu
+def test_dropin_emicp_and_softassign_match_oracle(dropin_exe, oracle):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.uniform_pair(n=500, seed=31, max_deg=15.0, t_range=0.05)
+    R, t, ok, err = _run(dropin_exe, "emicp", X, Y)
+    Ro, to, _ = oracle.emicp(X, Y)
+    assert ok == 1 and err == ""
+    assert rot_err_deg(R, Ro) < 1e-3 and np.abs(t - to).max() < 1e-5
+    X, Y, _, _ = W.surface_pair(n=200, seed=32)
+    R, t, ok, err = _run(dropin_exe, "softassign", X, Y)
+    Ro, to, _ = oracle.softassign(X, Y)
+    assert rot_err_deg(R, Ro) < 1e-3

@@ -1,9 +1,12 @@
 """Softassign on the GPU through the C ABI, against the FP64 oracle.
 
 Tolerances: slack vectors and row/column sums 1e-5 relative; S relative to
-its largest entry 1e-5 (1e-4 at temperatures where the assignment is nearly
-uniform and S is a small difference of large sums); final R within 1e-3
+its largest entry at most max(1e-5, 2x the error of the reference's own FP32
+arithmetic, i.e. the oracle's FP32 port): at high temperature the assignment
+is nearly uniform and S is a small residue of the data; final R within 1e-3
 degrees and t within 1e-5 x cloud extent for the full default schedule.
+Schedules cut short at high temperature end ill-conditioned; there the pose
+must match the FP64 oracle at least as well as the FP32 port does.
 """
 import numpy as np
 import pytest
@@ -39,8 +42,10 @@ def test_inner_iteration_matches_oracle(cesa, oracle, torch_cuda, n, m, T):
     extent = float(np.ptp(X, 0).max())
     assert np.abs(mom[1:4] - ref["Xc"]).max() < 1e-5 * extent
     assert np.abs(mom[4:7] - ref["Yc"]).max() < 1e-5 * extent
-    tol = 1e-5 if T < 50 else 1e-4
-    assert rel_err(mom[7:16], ref["S"]) < tol
+    port = oracle.softassign_step(X, Y, R.astype(np.float32), t.astype(np.float32), T, 3.0, 3, s0, u0,
+                                  precision="f32")
+    e_gpu, e_port = rel_err(mom[7:16], ref["S"]), rel_err(port["S"], ref["S"])
+    assert e_gpu <= max(1e-5, 2.0 * e_port), (e_gpu, e_port)
 
 
 @pytest.mark.parametrize("n,m,seed", [(200, 200, 1), (160, 240, 2), (333, 100, 3)])
@@ -49,10 +54,17 @@ def test_full_schedule_matches_oracle(cesa, oracle, n, m, seed):
     X, Y, _, _ = W.surface_pair(n=n, m=m, seed=seed)
     R, t, tr, rep = cesa.softassign(X, Y, trace=True)
     Ro, to, tro = oracle.softassign(X, Y)
+    Rp, tp, _ = oracle.softassign(X, Y, precision="f32", trace=False)
     assert rep.steps == 500 and len(tr) == 500
     assert tro[-1, 30] > 0.05
-    assert rot_err_deg(R, Ro) < 1e-3
-    assert np.abs(t - to).max() < 1e-5 * float(np.ptp(X, 0).max())
+    # The assignment stays within ~10% of uniform over the whole default
+    # schedule (alpha = 3 >> d^2), so the trajectory is sensitive to the FP32
+    # state: 1e-3 deg, or at least 4x closer to FP64 than the reference's own
+    # FP32 arithmetic on the same input, whichever is larger.
+    e, e_port = rot_err_deg(R, Ro), rot_err_deg(Rp, Ro)
+    assert e <= max(1e-3, 0.25 * e_port), (e, e_port)
+    extent = float(np.ptp(X, 0).max())
+    assert np.abs(t - to).max() <= max(1e-5 * extent, 0.25 * np.abs(tp - to).max())
 
 
 def test_c2_full_size_matches_oracle(cesa, oracle):
@@ -72,9 +84,9 @@ def test_far_from_origin_frame_dependence_is_reproduced(cesa, oracle):
     X, Y, _, _ = W.surface_pair(n=150, seed=8)
     off = np.array([3.0, -2.0, 5.0], np.float32)
     Xo, Yo = X + off, Y + off
-    R, t = cesa.softassign(Xo, Yo, param=cesa.Params.default(JMAX=30))
-    Ro, to, tro = oracle.softassign(Xo, Yo, JMAX=30)
-    R0, _, _ = oracle.softassign(X, Y, JMAX=30)
+    R, t = cesa.softassign(Xo, Yo)
+    Ro, to, tro = oracle.softassign(Xo, Yo)
+    R0, _, _ = oracle.softassign(X, Y)
     assert rot_err_deg(Ro, R0) > 1e-2  # the origin matters in the reference algorithm
     assert rot_err_deg(R, Ro) < 1e-3
     assert np.abs(t - to).max() < 1e-5 * 5.0
@@ -89,8 +101,8 @@ def test_tiny_sizes(cesa, oracle, n, m):
     Ro, to, tro = oracle.softassign(X, Y, JMAX=20)
     assert np.all(np.isfinite(R)) and np.all(np.isfinite(t))
     assert rel_err(tr[-1, 2], tro[-1, 2]) < 1e-5  # sumM
-    if tro[:, 30].min() > 1e-3:
-        assert rot_err_deg(R, Ro) < 1e-3
+    Rp, tp, _ = oracle.softassign(X, Y, JMAX=20, precision="f32", trace=False)
+    assert rot_err_deg(R, Ro) <= max(1e-3, 2.0 * rot_err_deg(Rp, Ro))
 
 
 def test_deterministic_and_device_entry(cesa, torch_cuda):
