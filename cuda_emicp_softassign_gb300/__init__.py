@@ -176,18 +176,25 @@ def _host_call(fn_name, X, Y, R, t, param, trace, timeline=0):
     _check(rc, fn_name)
     out = (Rh.reshape(3, 3).astype(np.float64), th.astype(np.float64))
     if timeline:
-        return out + (tl[: rep.timeline_written], rep)
+        return out + (tl, rep)
     if trace:
         return out + (tr[: min(rep.steps, tr.shape[0])], rep)
     return out
 
 
-def timeline_table(tl):
-    """Decodes a phase timeline into (phase, ns since the first entry) rows."""
+def timeline_table(tl, grid_blocks=1, block=None):
+    """Decodes a phase timeline into rows (block, phase, ns since the earliest
+    entry of any block); `block` selects one block's rows."""
     tl = np.asarray(tl, dtype=np.uint64)
-    phase = (tl >> np.uint64(56)).astype(np.int64)
-    t = (tl & np.uint64((1 << 56) - 1)).astype(np.int64)
-    return np.stack([phase, t - t[0]], axis=1) if len(t) else np.zeros((0, 2), np.int64)
+    per = len(tl) // max(grid_blocks, 1)
+    tl = tl[: per * grid_blocks].reshape(grid_blocks, per)
+    blk = np.repeat(np.arange(grid_blocks), per).reshape(grid_blocks, per)
+    used = tl != 0
+    phase = (tl >> np.uint64(56)).astype(np.int64)[used]
+    t = (tl & np.uint64((1 << 56) - 1)).astype(np.int64)[used]
+    b = blk[used]
+    rows = np.stack([b, phase, t - (t.min() if len(t) else 0)], axis=1)
+    return rows if block is None else rows[rows[:, 0] == block][:, 1:]
 
 
 def emicp(X, Y, R=None, t=None, param=None, trace=False, timeline=0):

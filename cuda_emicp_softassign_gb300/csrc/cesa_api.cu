@@ -170,6 +170,7 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   unsigned long long* dtl = nullptr;
   if (tl_cap > 0) {
     e = C.tl.ensure(sizeof(unsigned long long) * (size_t)tl_cap);
+    if (e == cudaSuccess) e = cudaMemsetAsync(C.tl.p, 0, sizeof(unsigned long long) * (size_t)tl_cap, st);
     if (e != cudaSuccess) return map_cuda(e);
     dtl = static_cast<unsigned long long*>(C.tl.p);
   }
@@ -246,8 +247,8 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
     if (e != cudaSuccess) return map_cuda(e);
   }
   if (tl_cap > 0) {
-    if (tl_n > tl_cap) tl_n = tl_cap;
-    e = cudaMemcpy(rep->timeline, dtl, sizeof(unsigned long long) * (size_t)tl_n, cudaMemcpyDeviceToHost);
+    // every block owns tl_cap / grid entries; unused entries stay zero
+    e = cudaMemcpy(rep->timeline, dtl, sizeof(unsigned long long) * (size_t)tl_cap, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return map_cuda(e);
     rep->timeline_written = tl_n;
   }

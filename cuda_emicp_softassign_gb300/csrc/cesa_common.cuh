@@ -53,14 +53,16 @@ __device__ __forceinline__ void set_status(Ctl* ctl, int code, int where) {
   if (atomicCAS(&ctl->status, 0, code) == 0) ctl->where = where;
 }
 
-// Optional phase timeline, recorded by thread 0 of block 0 only.
+// Optional phase timeline, recorded by thread 0 of every block into its own
+// region of cap / gridDim.x entries.
 struct Timeline {
   unsigned long long* p;
   int cap;
   int n;
   __device__ __forceinline__ void mark(int phase) {
-    if (p && blockIdx.x == 0 && threadIdx.x == 0 && n < cap)
-      p[n++] = ((unsigned long long)phase << 56) | (global_ns() & ((1ull << 56) - 1));
+    const int per = cap / (int)gridDim.x;
+    if (p && threadIdx.x == 0 && n < per)
+      p[(size_t)blockIdx.x * per + n++] = ((unsigned long long)phase << 56) | (global_ns() & ((1ull << 56) - 1));
   }
 };
 

@@ -156,8 +156,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   }
   __syncthreads();
 
-  HornState<float> horn;
-  horn.reset();
+  __shared__ HornState<float> horn;  // carried eigenbasis (thread 0)
+  if (tid == 0) horn.reset();
   Pipe pipe;
   pipe_init(pipe);
   unsigned epoch = 0;
@@ -403,11 +403,15 @@ int persistent_grid_limit(int device, const void* kernel, size_t smem) {
   return per_sm * (sms > 0 ? sms : 1);
 }
 
-// Unit decomposition: minimise waves x (unit work + fixed cost) over the split S.
+// Unit decomposition over the split S. Modelled time, in element
+// evaluations of one block (~20 per ns): waves x (unit work + fixed cost per
+// unit: streamed-chunk latency, reductions) + the completion of split owned
+// blocks (partials written, the last unit loads S partials per accumulator,
+// 16 in flight).
 SweepGeomH plan_sweep(int n_own, int n_stream, int grid_limit) {
   SweepGeomH best{};
   const int nblk = (n_own + kBlockPts - 1) / kBlockPts;
-  const double fixed = 24000.0;  // per-unit fixed cost in element evaluations
+  const double fixed = 40000.0;
   double best_cost = 1e300;
   const int smax_stream = (n_stream + 31) / 32;
   const int smax = smax_stream < 128 ? smax_stream : 128;
@@ -418,8 +422,8 @@ SweepGeomH plan_sweep(int n_own, int n_stream, int grid_limit) {
     const long units = (long)nblk * S;
     const int grid = units < grid_limit ? (int)units : grid_limit;
     const long waves = (units + grid - 1) / grid;
-    const double cost = (double)waves * ((double)kBlockPts * slice_len + fixed) +
-                        (S > 1 ? 4000.0 : 0.0);
+    const double split = S > 1 ? 30000.0 + 15000.0 * ((S + 15) / 16) : 0.0;
+    const double cost = (double)waves * ((double)kBlockPts * slice_len + fixed) + split;
     if (cost < best_cost * 0.999) {
       best_cost = cost;
       best = SweepGeomH{n_own, n_stream, nblk, S, slice_len, (int)units};

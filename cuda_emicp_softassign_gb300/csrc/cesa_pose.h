@@ -37,6 +37,17 @@ CESA_HD float t_rsqrt(float x) {
 #endif
 }
 CESA_HD double t_rsqrt(double x) { return 1.0 / sqrt(x); }
+// a / b; the device FP32 path uses the approximate (MUFU) division: Jacobi
+// only needs each rotation to be orthogonal (c = rsqrt(1 + t^2), s = t c),
+// not the exact angle.
+CESA_HD float t_div(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+CESA_HD double t_div(double a, double b) { return a / b; }
 
 template <typename T>
 struct HornState {
@@ -64,7 +75,7 @@ CESA_HD bool jacobi_angle(T bpp, T bqq, T bpq, T tol, T& c, T& s) {
   const T r2 = d * d + T(4) * bpq * bpq;
   const T r = r2 * t_rsqrt(r2);
   const T den = t_abs(d) + r;
-  T t = T(2) * bpq / den;
+  T t = t_div(T(2) * bpq, den);
   if (d < T(0)) t = -t;
   c = t_rsqrt(T(1) + t * t);
   s = t * c;
@@ -157,20 +168,24 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
     if (lmax) *lmax = T(0);
     return 1;
   }
+  // Work on register copies (static indices only) of the carried basis.
+  T V[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) V[i][j] = st.V[i][j];
   // B = V^T N V
   T NV[4][4], B[4][4], W[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      NV[i][j] = N[i][0] * st.V[0][j] + N[i][1] * st.V[1][j] + N[i][2] * st.V[2][j] +
-                 N[i][3] * st.V[3][j];
+      NV[i][j] = N[i][0] * V[0][j] + N[i][1] * V[1][j] + N[i][2] * V[2][j] + N[i][3] * V[3][j];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      B[i][j] = st.V[0][i] * NV[0][j] + st.V[1][i] * NV[1][j] + st.V[2][i] * NV[2][j] +
-                st.V[3][i] * NV[3][j];
+      B[i][j] = V[0][i] * NV[0][j] + V[1][i] * NV[1][j] + V[2][i] * NV[2][j] + V[3][i] * NV[3][j];
       W[i][j] = (i == j) ? T(1) : T(0);
     }
   // symmetrise (round-off in the two products)
@@ -181,13 +196,14 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
       const T m = T(0.5) * (B[i][j] + B[j][i]);
       B[i][j] = B[j][i] = m;
     }
+  // rotations stop once the off-diagonal entries are at round-off level
   T scale = T(0);
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) scale += t_abs(N[i][j]);
+    for (int j = 0; j < 4; ++j) scale = t_abs(N[i][j]) > scale ? t_abs(N[i][j]) : scale;
   const T eps = sizeof(T) == 4 ? T(1.2e-7) : T(2.3e-16);
-  const T tol = eps * T(0.0625) * scale + T(1e-37);
+  const T tol = T(4) * eps * scale + T(1e-37);
   for (int sweep = 0; sweep < 16; ++sweep) {
     bool rot = jacobi_round<T, 0, 1, 2, 3>(B, W, tol);
     rot = jacobi_round<T, 0, 2, 1, 3>(B, W, tol) || rot;
@@ -200,8 +216,7 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      V2[i][j] = st.V[i][0] * W[0][j] + st.V[i][1] * W[1][j] + st.V[i][2] * W[2][j] +
-                 st.V[i][3] * W[3][j];
+      V2[i][j] = V[i][0] * W[0][j] + V[i][1] * W[1][j] + V[i][2] * W[2][j] + V[i][3] * W[3][j];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -213,17 +228,20 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      st.V[i][j] = V2[i][0] * G[0][j] + V2[i][1] * G[1][j] + V2[i][2] * G[2][j] +
-                   V2[i][3] * G[3][j];
+      V[i][j] = V2[i][0] * G[0][j] + V2[i][1] * G[1][j] + V2[i][2] * G[2][j] + V2[i][3] * G[3][j];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) st.V[i][j] = V[i][j];
+  // largest eigenvalue; its column selected without dynamic indexing
+  T l1 = B[0][0], l2 = T(-3.0e38);
   int imax = 0;
-  T l1 = B[0][0];
 #pragma unroll
   for (int i = 1; i < 4; ++i)
     if (B[i][i] > l1) {
       l1 = B[i][i];
       imax = i;
     }
-  T l2 = T(-3.0e38);
 #pragma unroll
   for (int i = 0; i < 4; ++i)
     if (i != imax && B[i][i] > l2) l2 = B[i][i];
@@ -231,7 +249,7 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
   T n2 = T(0);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    qq[i] = st.V[i][imax];
+    qq[i] = imax == 0 ? V[i][0] : imax == 1 ? V[i][1] : imax == 2 ? V[i][2] : V[i][3];
     n2 += qq[i] * qq[i];
   }
   const T inv = t_rsqrt(n2);
@@ -249,7 +267,7 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
     return 1;
   }
   for (int i = 0; i < 4; ++i) q[i] = st.q[i] = qq[i];
-  if (gap) *gap = (l1 - l2) / (t_abs(l1) > T(1e-30) ? t_abs(l1) : T(1e-30));
+  if (gap) *gap = t_div(l1 - l2, t_abs(l1) > T(1e-30) ? t_abs(l1) : T(1e-30));
   if (lmax) *lmax = l1;
   return 0;
 }

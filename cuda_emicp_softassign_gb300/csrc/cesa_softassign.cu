@@ -280,8 +280,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   }
   __syncthreads();
 
-  HornState<float> horn;
-  horn.reset();
+  __shared__ HornState<float> horn;  // carried eigenbasis (thread 0)
+  if (tid == 0) horn.reset();
   Pipe pipe;
   pipe_init(pipe);
   unsigned epoch = 0, round_r = 0, round_c = 0;

@@ -169,14 +169,21 @@ __device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g
       const float* src = base + p;
       float s = 0.f;
       int k = 0;
-      for (; k + 8 <= g.slices; k += 8) {
-        float v[8];
+      for (; k + 16 <= g.slices; k += 16) {
+        float v[16];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = __ldcg(src + (size_t)(k + j) * NACC * kBlockPts);
+        for (int j = 0; j < 16; ++j) v[j] = __ldcg(src + (size_t)(k + j) * NACC * kBlockPts);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) s += v[j];
+        for (int j = 0; j < 16; ++j) s += v[j];
       }
-      for (; k < g.slices; ++k) s += __ldcg(src + (size_t)k * NACC * kBlockPts);
+      if (k < g.slices) {
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          v[j] = (k + j < g.slices) ? __ldcg(src + (size_t)(k + j) * NACC * kBlockPts) : 0.f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s += v[j];  // zero padding does not change the sum
+      }
       reinterpret_cast<float*>(sm.red)[p] = s;  // red is free after reduce_warps
     }
     __syncthreads();
@@ -192,11 +199,27 @@ __device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g
 // Accumulates NV per-thread df values (threads that have none pass zeros) into
 // the block accumulator acc[NV] held in shared memory (thread 0 adds).
 template <int NV>
-__device__ __forceinline__ void block_accumulate(df (&v)[NV], df* red_scratch, df* acc) {
-  block_reduce_df<NV>(v, red_scratch);
-  if (threadIdx.x == 0) {
+__device__ __forceinline__ void block_accumulate(df (&v)[NV], df* red, df* acc) {
+  static_assert(NV <= kThreads, "one thread per value");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) df_add(acc[k], v[k]);
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const df o = df_shfl_down(v[k], off);
+      df_add(v[k], o);
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[k * kWarps + warp] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {  // value k summed over the warps by thread k, fixed order
+    df s = red[threadIdx.x * kWarps];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) df_add(s, red[threadIdx.x * kWarps + w]);
+    df_add(acc[threadIdx.x], s);
   }
   __syncthreads();
 }

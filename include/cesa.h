@@ -84,12 +84,13 @@ typedef struct cesa_report {
   int sinkhorn_form;    /* out: form used (Softassign) */
   int grid_blocks;      /* out: persistent grid size */
   float device_ms;      /* out: device time of the registration kernels */
-  /* Optional phase timeline of block 0 (profiling): entries are
-   * (phase << 56) | (globaltimer ns & (2^56 - 1)); phases are listed in
-   * CESA_TL_* below. */
+  /* Optional phase timeline (profiling): block b of the persistent grid
+   * records into entries [b * per, (b + 1) * per), per = timeline_capacity /
+   * grid_blocks; an entry is (phase << 56) | (globaltimer ns & (2^56 - 1)),
+   * 0 when unused. Phases are listed in CESA_TL_* below. */
   unsigned long long* timeline;
   int timeline_capacity;
-  int timeline_written; /* out */
+  int timeline_written; /* out: entries written by block 0 */
 } cesa_report;
 
 #define CESA_TL_STEP 1       /* a pose update starts */
