@@ -24,6 +24,7 @@ CESA_ERR_TIMEOUT = 3
 CESA_ERR_NO_DEVICE = 4
 CESA_ERR_OUT_OF_MEMORY = 5
 CESA_ERR_UNSUPPORTED = 6
+CESA_ERR_NOALLOC_LIMIT = 7
 
 SINKHORN_AUTO = 0
 SINKHORN_MATRIX_FREE = 1
@@ -255,6 +256,19 @@ def softassign_device(dX, dY, dRt, param=None, d_status=None, stream=None):
                                       _dptr(d_status) if d_status is not None else None,
                                       ctypes.c_void_p(_stream_handle(stream)))
     _check(rc, "softassign_device")
+
+
+def emicp_device_noalloc(dX, dY, dRt, param=None, d_status=None, stream=None):
+    """EM-ICP on device tensors without any device allocation (fixed 16 MiB
+    scratch inside libcesa.so); for callers that cannot call cudaMalloc.
+    Returns the C status code instead of raising, so callers can test the
+    size limit (CESA_ERR_NOALLOC_LIMIT)."""
+    p = param or Params.default()
+    fn = lib().cesa_emicp_device_noalloc
+    fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
+    fn.restype = _i
+    return fn(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3, _dptr(dRt), ctypes.byref(p),
+              _dptr(d_status) if d_status is not None else None, ctypes.c_void_p(_stream_handle(stream)))
 
 
 def stream_status(stream=None):

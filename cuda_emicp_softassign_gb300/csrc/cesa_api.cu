@@ -555,6 +555,7 @@ const char* cesa_status_string(int status) {
     case CESA_ERR_NO_DEVICE: return "no usable CUDA device";
     case CESA_ERR_OUT_OF_MEMORY: return "out of memory";
     case CESA_ERR_UNSUPPORTED: return "unsupported request";
+    case CESA_ERR_NOALLOC_LIMIT: return "problem exceeds the 16 MiB fixed scratch of cesa_emicp_device_noalloc";
     default: return "unknown status";
   }
 }

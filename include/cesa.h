@@ -30,6 +30,7 @@ extern "C" {
 #define CESA_ERR_NO_DEVICE 4        /* no usable CUDA device */
 #define CESA_ERR_OUT_OF_MEMORY 5    /* device or host allocation failed */
 #define CESA_ERR_UNSUPPORTED 6      /* the request is outside what this build supports */
+#define CESA_ERR_NOALLOC_LIMIT 7    /* too large for the fixed scratch of cesa_emicp_device_noalloc */
 
 /* cudaStream_t without including cuda_runtime.h (same underlying type). */
 typedef struct CUstream_st* cesa_stream_t;
@@ -131,6 +132,27 @@ int cesa_emicp_device(const float* dX, int N, const float* dY, int M, float* dRt
                       const cesa_params* p, int* d_status, cesa_stream_t stream);
 int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float* dRt,
                            const cesa_params* p, int* d_status, cesa_stream_t stream);
+
+/*
+ * EM-ICP with no device allocation. No counterpart in the reference: this is
+ * for callers that cannot call cudaMalloc, such as a plugin inside a host
+ * application that owns no device heap, a real-time pipeline that forbids
+ * allocation after start-up, or code recorded between cudaStreamBeginCapture
+ * and cudaStreamEndCapture. It computes the same result as
+ * cesa_emicp_device (same arguments and conventions), but its scratch is a
+ * fixed 16 MiB device array inside libcesa.so, held on every GPU that loads
+ * the library until the process exits. That is enough for about N = M =
+ * 100,000 points. Larger problems return CESA_ERR_NOALLOC_LIMIT, and nothing
+ * is enqueued. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Every call on a device shares the one array: calls that overlap on the GPU
+ * (different streams, or a second call enqueued before the first has
+ * finished on another stream) race and corrupt each other's results.
+ * Serialise them on one stream or synchronise between them. No cudaMalloc,
+ * cudaFree or allocating library routine is called.
+ */
+int cesa_emicp_device_noalloc(const float* dX, int N, const float* dY, int M, float* dRt,
+                              const cesa_params* p, int* d_status, cesa_stream_t stream);
 
 /* Status of the last registration enqueued on `stream` (synchronises it). */
 int cesa_stream_status(cesa_stream_t stream);
