@@ -346,6 +346,12 @@ def run_ours(args, rank, world, local):
                 "ops_per_registration": fp32_ops,
                 "note": "achieved = algorithmic FP32-pipe ops of one registration / event time of its launch "
                         "sequence (prep kernels included)"}
+    traffic_file = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    if os.path.exists(traffic_file):
+        entry = json.load(open(traffic_file)).get(args.workload)
+        if entry:
+            roofline["traffic"] = entry["bytes_per_launch"]
+            roofline["traffic_source"] = "ncu dram bytes per launch, profiles/ncu_traffic.json"
     cpu_v, cpu_desc, cpu_thr = cpu_baseline(kind, X, Y, p, args.cpu_sample_s)
     h2d = (N + M) * 3 * 4 + 12 * 4
     line = {"metric": "registrations/s", "value": value, "unit": "registrations/s", "n_gpus": world,
