@@ -47,8 +47,9 @@ __device__ __forceinline__ float exact_offset(double mean, float lo, float hi) {
 
 static __global__ void prep_center_kernel(const float* __restrict__ X, int N, const float* __restrict__ Y,
                                           int M, CenterHdr* hdr) {
-  // One block: means (df) and extents of X and Y, exact offsets, and the mean
-  // of the centred X (EM-ICP rows with C_r <= 1e-6 use it).
+  // One block: means (df) and extents of X and Y, exact offsets, and the means
+  // of the centred clouds (EM-ICP rows with C_r <= 1e-6 use mean(X'); the
+  // Softassign final sweep centres its Y moments on mean(Y')).
   __shared__ df red[6 * (1024 / 32)];
   __shared__ float s_lo[12][32], s_hi[12][32];
   __shared__ float s_o[6];
@@ -98,17 +99,19 @@ static __global__ void prep_center_kernel(const float* __restrict__ X, int N, co
     }
   }
   __syncthreads();
-  df w[3];
-  for (int k = 0; k < 3; ++k) w[k] = df_make(0.f);
+  df w[6];
+  for (int k = 0; k < 6; ++k) w[k] = df_make(0.f);
   for (int i = threadIdx.x; i < N; i += blockDim.x)
     for (int k = 0; k < 3; ++k) df_add(w[k], __fsub_rn(X[k * N + i], s_o[k]));
-  block_reduce_df<3>(w, red);
+  for (int i = threadIdx.x; i < M; i += blockDim.x)
+    for (int k = 0; k < 3; ++k) df_add(w[3 + k], __fsub_rn(Y[k * M + i], s_o[3 + k]));
+  block_reduce_df<6>(w, red);
   if (threadIdx.x == 0) {
     for (int k = 0; k < 3; ++k) {
       hdr->oX[k] = s_o[k];
       hdr->oY[k] = s_o[3 + k];
       hdr->xmean[k] = (float)(df_dbl(w[k]) / (double)N);
-      hdr->ymean[k] = 0.f;
+      hdr->ymean[k] = (float)(df_dbl(w[3 + k]) / (double)M);
     }
     hdr->oX[3] = hdr->oY[3] = hdr->xmean[3] = hdr->ymean[3] = 0.f;
   }

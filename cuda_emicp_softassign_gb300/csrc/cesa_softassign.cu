@@ -13,7 +13,11 @@
 //
 // Matrix-free form: M_rc = K_rc a_r b_c. K is recomputed in every sweep and
 // never stored. Row sweeps own 128 X points and stream Y. Column sweeps own
-// 128 Y points and stream X. Each sweep element costs 3 FADD + FMUL + 2 FFMA
+// 128 Y points and stream X. A Sinkhorn pass only stores its per-slice partial
+// sums. The next pass completes it while preparing the points it streams
+// (deferred completion: no completion counters or serial finalize on the
+// critical path). A designated unit per point stores the new scaling and slack
+// in ping-pong buffers. Each sweep element costs 3 FADD + FMUL + 2 FFMA
 // (direct-difference d^2), 1 FFMA (exponent), 1 MUFU ex2 and 1 FFMA (weighted
 // sum): 7 FP32 ops + 1 MUFU op. Per pose update there are 2*I1 + 1 sweeps and
 // 2*I1 + 1 grid barriers.
@@ -34,26 +38,26 @@ namespace cesa {
 constexpr int kSaNV = 32;
 
 struct SoftArgs {
-  float4* rows;    // X' centred, .w = a_r   (N)
-  float4* cols;    // Y' centred, .w = b_c   (M)
-  float4* colfin;  // per column (cs_c, g_c = b_c cs_c, delta_c = b_c (cs_c - 1), 0) after the last column pass
-  float* s;        // slack column [N]
-  float* u;        // slack row [M]
-  float* rs;       // last row sums incl. slack [N]
-  float* cs;       // last column sums incl. slack [M]
-  float* w_out;    // optional [N]
-  int N, M;
-  SweepGeom gr, gc;  // row sweeps (own X, stream Y) / column sweeps (own Y, stream X)
+  const float4* rows;  // X' centred (N)
+  const float4* cols;  // Y' centred (M)
+  float* abuf;         // [2][Np] row scalings a^(k), k = 1..I1 at [k & 1]
+  float* bbuf;         // [2][Mp] column scalings b^(k), k = 1..I1 at [k & 1]
+  float* sbuf;         // [2][Np] slack column (ping-pong, persistent)
+  float* ubuf;         // [2][Mp] slack row (ping-pong, persistent)
+  float* rs;           // [Np] last row sums incl. slack
+  float* cs;           // [Mp] last column sums incl. slack
+  float* w_out;        // optional [N]
+  int N, M, Np, Mp;
+  SweepGeom gr, gc;    // row sweeps (own X, stream Y) / column sweeps (own Y, stream X)
   int JMAX, I0, I1;
   float alpha, T0, TFACTOR;
   const CenterHdr* hdr;
   float* dRt;
-  float* part_r;
-  unsigned* cnt_r;
-  float* part_c;
-  unsigned* cnt_c;
-  df* bpart;   // [2][grid][kSaNV]  row-side moments
-  df* bcol;    // [2][grid][4]      column moments (sum cs, sum cs y')
+  float* pr;           // row-pass partials [S_r][Np]
+  float* pc;           // column-pass partials [S_c][Mp]
+  float* part_f;       // final-sweep split partials [units_r][5][128]
+  unsigned* cnt_f;     // [nblk_r]
+  df* bpart;           // [2][grid][kSaNV]
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -63,37 +67,129 @@ struct SoftArgs {
   uint64_t timeout_ns;
 };
 
-// Streamed Y columns for Sinkhorn row sweeps: (R y' + t', b_c), with b_c := 1
-// in the first pass of an inner iteration.
+// Sum of the S slice partials of point i (deferred completion), 8 loads in flight.
+__device__ __forceinline__ float slice_sum(const float* part, int S, int ld, int i) {
+  float s = 0.f;
+  int k = 0;
+  for (; k + 8 <= S; k += 8) {
+    float v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldcg(part + (size_t)(k + j) * ld + i);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += v[j];
+  }
+  for (; k < S; ++k) s += __ldcg(part + (size_t)k * ld + i);
+  return s;
+}
+
+// Completion of a column pass for column c, done by whoever streams c next
+// (normalizeMbySinkhorn_col + Saxpy, src/softassign.cu:579-597):
+//   cs = b_old * (column sum of K a) + u_old,  b_new = b_old / cs,  u_new = u_old / cs.
+// The unit designated for c (block index 0 of its sweep) stores the results.
+struct ColDone {
+  const float* pc;
+  int S, ld;
+  const float* b_old;  // nullptr: b_old = 1 (first pass of an inner iteration)
+  const float* u_old;
+  float* b_new;
+  float* u_new;
+  float* cs_out;
+  __device__ __forceinline__ void operator()(int c, bool store, float& bn, float& csv) const {
+    const float sum = slice_sum(pc, S, ld, c);
+    const float bo = b_old ? __ldcg(b_old + c) : 1.f;
+    const float uo = __ldcg(u_old + c);
+    csv = fmaf(bo, sum, uo);
+    bn = bo / csv;
+    if (store) {
+      __stcg(b_new + c, bn);
+      __stcg(u_new + c, uo / csv);
+      __stcg(cs_out + c, csv);
+    }
+  }
+};
+
+// Streamed Y columns for Sinkhorn row sweeps: (R y' + t', b_c). b_c := 1 in
+// the first pass of an inner iteration, else the completed previous column pass.
 struct RowPrep {
   float R[9], tc[3];
-  bool unit_w;
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int len) const {
+  bool fresh;
+  ColDone cd;
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
+                                                int blk) const {
     for (int c = threadIdx.x; c < len; c += kThreads) {
       const float4 y = sm.raw[stage][c];
+      float w = 1.f, csv;
+      if (!fresh) cd(first + c, blk == 0, w, csv);
       sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
                                R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], unit_w ? 1.f : y.w);
+                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w);
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.raw2[stage]};
   }
 };
 
-// Streamed Y columns for the final row sweep: (R y' + t', b_c) and
-// (g_c (y'_c - Yhat), delta_c). Yhat = sum cs y' / sum cs makes the weighted
-// sums of the third stream small where the assignment is nearly uniform, so
-// the cross-covariance is formed from centred terms.
+// Streamed X rows for Sinkhorn column sweeps: (x', a_r), completing the
+// previous row pass (normalizeMbySinkhorn_row + Saxpy, src/softassign.cu:538-561):
+//   rs = a_old * (row sum of K b) + s_old,  a_new = a_old / rs,  s_new = s_old / rs.
+struct ColPrep {
+  const float* pr;
+  int S, ld;
+  const float* a_old;  // nullptr: a_old = 1
+  const float* s_old;
+  float* a_new;
+  float* s_new;
+  float* rs_out;
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
+                                                int blk) const {
+    for (int c = threadIdx.x; c < len; c += kThreads) {
+      const int r = first + c;
+      const float4 x = sm.raw[stage][c];
+      const float sum = slice_sum(pr, S, ld, r);
+      const float ao = a_old ? __ldcg(a_old + r) : 1.f;
+      const float so = __ldcg(s_old + r);
+      const float rsv = fmaf(ao, sum, so);
+      const float an = ao / rsv;
+      if (blk == 0) {
+        __stcg(a_new + r, an);
+        __stcg(s_new + r, so / rsv);
+        __stcg(rs_out + r, rsv);
+      }
+      sm.prep[c] = make_float4(x.x, x.y, x.z, an);
+    }
+    __syncthreads();
+    return PrepOut{sm.prep, sm.raw2[stage]};
+  }
+};
+
+// Streamed Y columns for the final row sweep, completing the last column pass:
+// (R y' + t', b_c) and (g_c (y'_c - Yhat), delta_c) with g = b cs,
+// delta = b (cs - 1) and Yhat = mean(Y') (any centre is exact; this one keeps
+// the third stream small). The designated units also accumulate the column
+// moments sum cs and sum cs y' (per thread, df, in shared memory).
 struct FinalPrep {
   float R[9], tc[3], yh[3];
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int len) const {
+  ColDone cd;
+  df* colacc;  // [kThreads][4]
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
+                                                int blk) const {
     for (int c = threadIdx.x; c < len; c += kThreads) {
       const float4 y = sm.raw[stage][c];
-      const float4 f = sm.raw2[stage][c];  // (cs, g, delta, 0)
+      float bn, csv;
+      cd(first + c, blk == 0, bn, csv);
+      const float g = bn * csv;
       sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
                                R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], y.w);
-      sm.prep2[c] = make_float4(f.y * (y.x - yh[0]), f.y * (y.y - yh[1]), f.y * (y.z - yh[2]), f.z);
+                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn);
+      sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]),
+                                bn * (csv - 1.f));
+      if (blk == 0) {
+        df* a = colacc + threadIdx.x * 4;
+        df_add(a[0], csv);
+        df_add_prod(a[1], csv, y.x);
+        df_add_prod(a[2], csv, y.y);
+        df_add_prod(a[3], csv, y.z);
+      }
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.prep2};
@@ -136,70 +232,13 @@ struct FinalElem {
   }
 };
 
-// Row pass finalize (normalizeMbySinkhorn_row + Saxpy, src/softassign.cu:538-561).
-struct RowFin {
-  float4* rows;
-  float* s;
-  float* rs;
-  int N;
-  bool first;
-  __device__ void operator()(int blk, const float (&tot)[1]) const {
-    const int r = blk * kBlockPts + (int)threadIdx.x;
-    if (threadIdx.x < kBlockPts && r < N) {
-      const float a_old = first ? 1.f : __ldcg(&rows[r].w);
-      const float s_old = __ldcg(&s[r]);
-      const float sum = fmaf(a_old, tot[0], s_old);
-      __stcg(&rows[r].w, a_old / sum);
-      __stcg(&s[r], s_old / sum);
-      __stcg(&rs[r], sum);
-    }
-  }
-};
-
-// Column pass finalize (normalizeMbySinkhorn_col + Saxpy, src/softassign.cu:579-597).
-// On the last pass also records (cs, g, delta) per column and the column
-// moments sum cs, sum cs y' (the reference's Yw = cs .* Y, src/softassign.cu:661-666).
-struct ColFin {
-  float4* cols;
-  float4* colfin;
-  float* u;
-  float* cs;
-  int M;
-  bool first, last;
-  df* red;
-  df* acc;  // block accumulator, 4 slots
-  __device__ void operator()(int blk, const float (&tot)[1]) const {
-    df v[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = df_make(0.f);
-    const int c = blk * kBlockPts + (int)threadIdx.x;
-    if (threadIdx.x < kBlockPts && c < M) {
-      const float4 y = __ldcg(&cols[c]);
-      const float b_old = first ? 1.f : y.w;
-      const float u_old = __ldcg(&u[c]);
-      const float sum = fmaf(b_old, tot[0], u_old);
-      const float b_new = b_old / sum;
-      __stcg(&cols[c].w, b_new);
-      __stcg(&u[c], u_old / sum);
-      __stcg(&cs[c], sum);
-      if (last) {
-        __stcg(&colfin[c], make_float4(sum, b_new * sum, b_new * (sum - 1.f), 0.f));
-        df_add(v[0], sum);
-        df_add_prod(v[1], sum, y.x);
-        df_add_prod(v[2], sum, y.y);
-        df_add_prod(v[3], sum, y.z);
-      }
-    }
-    if (last) block_accumulate<4>(v, red, acc);
-  }
-};
-
-// Final row finalize: w, mu = m - w, Vhat and the 28 row-side moments.
+// Final row finalize: w, mu = m - w, Vhat (times a_r) and the 28 row-side moments.
 //  0: sum w            1-3: sum w x'         4-12: sum w x'_i Vhat_j (i + 3j)
 // 13-15: sum Vhat       16-18: sum w mu x'    19: sum mu
 // 20-22: sum w^2 x'     23: sum w^2           24-26: sum w Vhat      27: sum w mu
 struct FinalFin {
   const float4* rows;
+  const float* a;  // a^(I1)
   float* w_out;
   int N;
   df* red;
@@ -211,9 +250,9 @@ struct FinalFin {
     const int r = blk * kBlockPts + (int)threadIdx.x;
     if (threadIdx.x < kBlockPts && r < N) {
       const float4 x = __ldcg(&rows[r]);
-      const float a = x.w;
-      const float w = a * tot[0], mu = a * tot[1];
-      const float V[3] = {a * tot[2], a * tot[3], a * tot[4]};
+      const float ar = __ldcg(a + r);
+      const float w = ar * tot[0], mu = ar * tot[1];
+      const float V[3] = {ar * tot[2], ar * tot[3], ar * tot[4]};
       const float xp[3] = {x.x, x.y, x.z};
       if (w_out) w_out[r] = w;
       const float w2 = w * w, wmu = w * mu;
@@ -237,7 +276,7 @@ struct FinalFin {
   }
 };
 
-// df helpers for the (thread 0) moment assembly
+// df helpers for the moment assembly
 __device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df precision
   df r = df_make(0.f);
   df_add_prod(r, a.hi, b);
@@ -254,11 +293,10 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
   __shared__ float s_pose[12];
   __shared__ df s_acc[kSaNV];
-  __shared__ df s_cacc[4];
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[kSaNV];
-  __shared__ df s_ctot[4];
-  __shared__ float s_hdr[8];
+  __shared__ df s_colacc[kThreads * 4];
+  __shared__ float s_hdr[12];
   __shared__ float s_S[9], s_xcp[3], s_yd[3], s_xc[3], s_yc[3];
 
   const int tid = threadIdx.x;
@@ -270,6 +308,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     for (int k = 0; k < 3; ++k) {
       s_hdr[k] = A.hdr->oX[k];
       s_hdr[3 + k] = A.hdr->oY[k];
+      s_hdr[6 + k] = A.hdr->ymean[k];
     }
     float R[9], t[3], tc[3];
     for (int k = 0; k < 9; ++k) R[k] = A.dRt[k];
@@ -278,20 +317,21 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     for (int k = 0; k < 9; ++k) s_pose[k] = R[k];
     for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
   }
-  __syncthreads();
-
   __shared__ HornState<float> horn;  // carried eigenbasis (thread 0)
   if (tid == 0) horn.reset();
+  __syncthreads();
+
   Pipe pipe;
   pipe_init(pipe);
-  unsigned epoch = 0, round_r = 0, round_c = 0;
+  unsigned epoch = 0, round_f = 0;
+  int sp = 0, up = 0;  // current slack buffers
   const StreamSrc src_cols{A.cols, nullptr, false};
   const StreamSrc src_rows{A.rows, nullptr, false};
-  const StreamSrc src_final{A.cols, A.colfin, false};
   float T = A.T0;
   int step = 0;
   bool ok = true;
   Timeline tl{A.tl, A.tl_cap, 0};
+  const int Np = A.Np, Mp = A.Mp;
 
   for (int Titer = 0; Titer < A.JMAX && ok; ++Titer) {
     // K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
@@ -301,7 +341,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     for (int iter0 = 0; iter0 < A.I0 && ok; ++iter0, ++step) {
       tl.mark(1);
       if (tid < kSaNV) s_acc[tid] = df_make(0.f);
-      if (tid < 4) s_cacc[tid] = df_make(0.f);
+      for (int k = tid; k < kThreads * 4; k += kThreads) s_colacc[k] = df_make(0.f);
       float R[9], tc[3];
 #pragma unroll
       for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
@@ -309,44 +349,47 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
       __syncthreads();
       const SinkElem se{nk, c0};
-      const int par = step & 1;
       for (int k = 0; k < A.I1 && ok; ++k) {
-        // row pass: own X rows, stream transformed Y columns weighted by b
+        // row pass k: own X rows, stream Y columns weighted by b^(k); row partials -> pr
         RowPrep rp;
 #pragma unroll
         for (int q = 0; q < 9; ++q) rp.R[q] = R[q];
 #pragma unroll
         for (int q = 0; q < 3; ++q) rp.tc[q] = tc[q];
-        rp.unit_w = (k == 0);
-        const RowFin rf{A.rows, A.s, A.rs, A.N, k == 0};
-        ok = sweep_units<1>(sm, pipe, A.gr, src_cols, A.rows, false, R, tc, round_r++, A.part_r,
-                            A.cnt_r, se, rp, rf, A.ctl, A.timeout_ns, 30, tl) &&
+        rp.fresh = (k == 0);
+        rp.cd = ColDone{A.pc,
+                        A.gc.slices,
+                        Mp,
+                        k >= 2 ? A.bbuf + (size_t)((k - 1) & 1) * Mp : nullptr,
+                        A.ubuf + (size_t)up * Mp,
+                        A.bbuf + (size_t)(k & 1) * Mp,
+                        A.ubuf + (size_t)(up ^ 1) * Mp,
+                        A.cs};
+        ok = sweep_units<1, SinkElem, RowPrep, NoFin, true>(sm, pipe, A.gr, src_cols, A.rows, false, R,
+                                                            tc, 0u, A.pr, nullptr, se, rp, NoFin{},
+                                                            A.ctl, A.timeout_ns, 30, tl, Np) &&
              grid_sync(A.ctl, epoch, G, A.timeout_ns, 32);
         tl.mark(5);
         if (!ok) break;
-        // column pass: own transformed Y columns, stream X rows weighted by a
-        const bool last = (k == A.I1 - 1);
-        const ColFin cf{A.cols, A.colfin, A.u, A.cs, A.M, k == 0, last, s_red, s_cacc};
-        ok = sweep_units<1>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc, round_c++, A.part_c,
-                            A.cnt_c, se, NoPrep{}, cf, A.ctl, A.timeout_ns, 40, tl);
-        if (ok && last && tid < 4) {
-          const df a = s_cacc[tid];
-          __stcg(reinterpret_cast<float2*>(A.bcol + ((size_t)par * G + blockIdx.x) * 4 + tid),
-                 make_float2(a.hi, a.lo));
-        }
-        ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
+        if (k >= 1) up ^= 1;  // the row pass completed column pass k-1
+        // column pass k: own Y columns, stream X rows weighted by a^(k+1)
+        const ColPrep cp{A.pr,
+                         A.gr.slices,
+                         Np,
+                         k >= 1 ? A.abuf + (size_t)(k & 1) * Np : nullptr,
+                         A.sbuf + (size_t)sp * Np,
+                         A.abuf + (size_t)((k + 1) & 1) * Np,
+                         A.sbuf + (size_t)(sp ^ 1) * Np,
+                         A.rs};
+        ok = sweep_units<1, SinkElem, ColPrep, NoFin, true>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
+                                                           0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
+                                                           A.timeout_ns, 40, tl, Mp) &&
+             grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
         tl.mark(5);
+        sp ^= 1;
       }
       if (!ok) break;
-      // column moments -> Yhat (identical in every block)
-      reduce_block_partials<4>(A.bcol + (size_t)par * G * 4, (int)G, s_red, s_ctot);
-      tl.mark(6);
-      float yh[3];
-      {
-        const float B1 = df_val(s_ctot[0]);
-        for (int i = 0; i < 3; ++i) yh[i] = df_val(s_ctot[1 + i]) / B1;
-      }
-      // final row sweep: w, mu, Vhat
+      // final row sweep: completes the last column pass, accumulates w, mu, Vhat
       {
         FinalPrep fp;
 #pragma unroll
@@ -354,14 +397,32 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
           fp.tc[q] = tc[q];
-          fp.yh[q] = yh[q];
+          fp.yh[q] = s_hdr[6 + q];
         }
+        const int kl = A.I1 - 1;
+        fp.cd = ColDone{A.pc,
+                        A.gc.slices,
+                        Mp,
+                        kl >= 1 ? A.bbuf + (size_t)(kl & 1) * Mp : nullptr,
+                        A.ubuf + (size_t)up * Mp,
+                        A.bbuf + (size_t)(A.I1 & 1) * Mp,
+                        A.ubuf + (size_t)(up ^ 1) * Mp,
+                        A.cs};
+        fp.colacc = s_colacc;
         const FinalElem fe{nk, c0};
-        const FinalFin ff{A.rows, A.w_out, A.N, s_red, s_acc};
-        ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_r++, A.part_r,
-                            A.cnt_r, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl);
+        const FinalFin ff{A.rows, A.abuf + (size_t)(A.I1 & 1) * Np, A.w_out, A.N, s_red, s_acc};
+        const StreamSrc src_final{A.cols, nullptr, false};
+        ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_f++, A.part_f,
+                            A.cnt_f, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl);
         if (!ok) break;
+        up ^= 1;
+        // column moments of the designated units -> slots 28..31
+        df cv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cv[q] = s_colacc[tid * 4 + q];
+        block_accumulate<4>(cv, s_red, s_acc + 28);
       }
+      const int par = step & 1;
       df* bp = A.bpart + (size_t)par * G * kSaNV;
       if (tid < kSaNV) {
         const df a = s_acc[tid];
@@ -373,23 +434,25 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       if (!ok) break;
       reduce_block_partials<kSaNV>(bp, (int)G, s_red, s_tot);
       tl.mark(6);
-      // S_ij by threads 0..8, centres by threads 9..11 (in parallel), then the
-      // pose by thread 0.
+      // S_ij by threads 0..8, centres by threads 9..11, then the pose by thread 0.
+      //   Yc = (B2 + oY B1)/A1, alpha = Yhat + oY, beta = alpha - Yc,
       //   S_ij = (T1_ij - Xc'_i T3_j) + (T4_i - Xc'_i T5) alpha_j + (T6_i - Xc'_i A1) beta_j
       //        + oX_i (T8_j - T3_j) + (T9 - T5) oX_i alpha_j + (T7 - A1) oX_i beta_j
-      // with D_r = Vhat_r + (mu_r + (1 - rho) w_r) alpha, alpha = Yhat + oY,
-      // beta = (1 - rho) alpha, all sums compensated.
       if (tid < 12) {
         const float* oX = &s_hdr[0];
         const float* oY = &s_hdr[3];
+        const float* yh = &s_hdr[6];
         const df A1 = s_tot[0];
         const float inv = 1.f / df_val(A1);
-        const float rho = df_val(s_ctot[0]) * inv;
+        const float rho = df_val(s_tot[28]) * inv;
         if (tid < 9) {
           const int i = tid % 3, j = tid / 3;
           const float xi = df_val(s_tot[1 + i]) * inv;
           const float al = yh[j] + oY[j];
-          const float be = (1.f - rho) * al;
+          df bj = df_make(yh[j]);  // beta_j = (Yhat_j - B2_j/A1) - (rho - 1) oY_j
+          df_add(bj, -df_val(s_tot[29 + j]) * inv);
+          df_add_prod(bj, 1.f - rho, oY[j]);
+          const float be = df_val(bj);
           const df T5 = s_tot[19], T7 = s_tot[23], T9 = s_tot[27];
           df P2 = s_tot[16 + i];
           df_add(P2, dmul(T5, -xi));
@@ -408,18 +471,18 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
           const float xi = df_val(s_tot[1 + i]) * inv;
           s_xcp[i] = xi;
           s_xc[i] = xi + oX[i];
-          s_yc[i] = rho * (yh[i] + oY[i]);
-          df yd = df_make(0.f);  // Yc - oY = rho Yhat + (rho - 1) oY
-          df_add_prod(yd, rho, yh[i]);
+          df yd = df_make(df_val(s_tot[29 + i]) * inv);  // Yc - oY = B2/A1 + (rho - 1) oY
           df_add_prod(yd, rho - 1.f, oY[i]);
           s_yd[i] = df_val(yd);
+          df yc = yd;
+          df_add(yc, oY[i]);
+          s_yc[i] = df_val(yc);
         }
       }
       __syncthreads();
       if (tid == 0) {
         const float* oX = &s_hdr[0];
         const float* oY = &s_hdr[3];
-        const df A1 = s_tot[0];
         float S[9], Xc[3], Yc[3], Xcp[3], Yd[3];
         for (int k = 0; k < 9; ++k) S[k] = s_S[k];
         for (int i = 0; i < 3; ++i) {
@@ -441,7 +504,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
             pose_from_centred(Rn, tn, oX, oY, to);
             rec[0] = step;
             rec[1] = T;
-            rec[2] = df_dbl(A1);
+            rec[2] = df_dbl(s_tot[0]);
             for (int i = 0; i < 3; ++i) {
               rec[3 + i] = Xc[i];
               rec[6 + i] = Yc[i];
@@ -514,37 +577,38 @@ SaPlan plan_sa(int N, int M, int device) {
 
 struct SaCarved {
   Ctl* ctl;
-  unsigned* cnt_r;
-  unsigned* cnt_c;
+  unsigned* cnt_f;
   CenterHdr* hdr;
   float4* rows;
   float4* cols;
-  float4* colfin;
-  float *s, *u, *rs, *cs;
-  float* part_r;
-  float* part_c;
+  float *abuf, *bbuf, *sbuf, *ubuf, *rs, *cs;
+  float* pr;
+  float* pc;
+  float* part_f;
   df* bpart;
-  df* bcol;
+  int Np, Mp;
 };
 
 SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
   Carve c(base);
   SaCarved w;
+  w.Np = (N + 3) & ~3;
+  w.Mp = (M + 3) & ~3;
   w.ctl = c.take<Ctl>(1);
-  w.cnt_r = c.take<unsigned>((size_t)P.gr.nblk);
-  w.cnt_c = c.take<unsigned>((size_t)P.gc.nblk);
+  w.cnt_f = c.take<unsigned>((size_t)P.gr.nblk);
   w.hdr = c.take<CenterHdr>(1);
   w.rows = c.take<float4>((size_t)N);
   w.cols = c.take<float4>((size_t)M);
-  w.colfin = c.take<float4>((size_t)M);
-  w.s = c.take<float>((size_t)N);
-  w.u = c.take<float>((size_t)M);
-  w.rs = c.take<float>((size_t)N);
-  w.cs = c.take<float>((size_t)M);
-  w.part_r = c.take<float>((size_t)P.gr.units * 5 * kBlockPts);
-  w.part_c = c.take<float>((size_t)P.gc.units * 1 * kBlockPts);
+  w.abuf = c.take<float>((size_t)2 * w.Np);
+  w.bbuf = c.take<float>((size_t)2 * w.Mp);
+  w.sbuf = c.take<float>((size_t)2 * w.Np);
+  w.ubuf = c.take<float>((size_t)2 * w.Mp);
+  w.rs = c.take<float>((size_t)w.Np);
+  w.cs = c.take<float>((size_t)w.Mp);
+  w.pr = c.take<float>((size_t)P.gr.slices * w.Np);
+  w.pc = c.take<float>((size_t)P.gc.slices * w.Mp);
+  w.part_f = c.take<float>((size_t)P.gr.units * 5 * kBlockPts);
   w.bpart = c.take<df>((size_t)2 * P.grid * kSaNV);
-  w.bcol = c.take<df>((size_t)2 * P.grid * 4);
   if (total) *total = c.off;
   return w;
 }
@@ -569,21 +633,20 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   if (total > ws_bytes) return (int)cudaErrorInvalidValue;
   if (grid_used) *grid_used = P.grid;
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt_r, 0, sizeof(unsigned) * (size_t)P.gr.nblk, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt_c, 0, sizeof(unsigned) * (size_t)P.gc.nblk, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt_f, 0, sizeof(unsigned) * (size_t)P.gr.nblk, st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
-  prep_pack_kernel<<<pg_x < 1024 ? pg_x : 1024, pb, 0, st>>>(L.dX, L.N, w.hdr, 0, 1.f, w.rows);
-  prep_pack_kernel<<<pg_y < 1024 ? pg_y : 1024, pb, 0, st>>>(L.dY, L.M, w.hdr, 1, 1.f, w.cols);
+  prep_pack_kernel<<<pg_x < 1024 ? pg_x : 1024, pb, 0, st>>>(L.dX, L.N, w.hdr, 0, 0.f, w.rows);
+  prep_pack_kernel<<<pg_y < 1024 ? pg_y : 1024, pb, 0, st>>>(L.dY, L.M, w.hdr, 1, 0.f, w.cols);
   if (L.s_io)
-    e = cudaMemcpyAsync(w.s, L.s_io, sizeof(float) * (size_t)L.N, cudaMemcpyDeviceToDevice, st);
+    e = cudaMemcpyAsync(w.sbuf, L.s_io, sizeof(float) * (size_t)L.N, cudaMemcpyDeviceToDevice, st);
   else
-    fill_kernel<<<pg_x < 1024 ? pg_x : 1024, pb, 0, st>>>(w.s, L.N, L.moutlier);
+    fill_kernel<<<pg_x < 1024 ? pg_x : 1024, pb, 0, st>>>(w.sbuf, L.N, L.moutlier);
   if (e == cudaSuccess && L.u_io)
-    e = cudaMemcpyAsync(w.u, L.u_io, sizeof(float) * (size_t)L.M, cudaMemcpyDeviceToDevice, st);
+    e = cudaMemcpyAsync(w.ubuf, L.u_io, sizeof(float) * (size_t)L.M, cudaMemcpyDeviceToDevice, st);
   else if (e == cudaSuccess)
-    fill_kernel<<<pg_y < 1024 ? pg_y : 1024, pb, 0, st>>>(w.u, L.M, L.moutlier);
+    fill_kernel<<<pg_y < 1024 ? pg_y : 1024, pb, 0, st>>>(w.ubuf, L.M, L.moutlier);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (L.JMAX <= 0 || L.I0 <= 0) return 0;
@@ -591,14 +654,17 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   SoftArgs A;
   A.rows = w.rows;
   A.cols = w.cols;
-  A.colfin = w.colfin;
-  A.s = w.s;
-  A.u = w.u;
+  A.abuf = w.abuf;
+  A.bbuf = w.bbuf;
+  A.sbuf = w.sbuf;
+  A.ubuf = w.ubuf;
   A.rs = w.rs;
   A.cs = w.cs;
   A.w_out = L.w_out;
   A.N = L.N;
   A.M = L.M;
+  A.Np = w.Np;
+  A.Mp = w.Mp;
   A.gr = P.gr;
   A.gc = P.gc;
   A.JMAX = L.JMAX;
@@ -609,12 +675,11 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.TFACTOR = L.TFACTOR;
   A.hdr = w.hdr;
   A.dRt = L.dRt;
-  A.part_r = w.part_r;
-  A.cnt_r = w.cnt_r;
-  A.part_c = w.part_c;
-  A.cnt_c = w.cnt_c;
+  A.pr = w.pr;
+  A.pc = w.pc;
+  A.part_f = w.part_f;
+  A.cnt_f = w.cnt_f;
   A.bpart = w.bpart;
-  A.bcol = w.bcol;
   A.ctl = w.ctl;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;
@@ -626,10 +691,13 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   e = cudaLaunchCooperativeKernel((const void*)softassign_kernel, dim3(P.grid), dim3(kThreads), args,
                                   P.smem, st);
   if (e != cudaSuccess) return (int)e;
-  // optional vector outputs
-  if (L.s_io) e = cudaMemcpyAsync(L.s_io, w.s, sizeof(float) * (size_t)L.N, cudaMemcpyDeviceToDevice, st);
+  // the slack buffers toggle once per row / column pass completion
+  const long passes = (long)L.JMAX * L.I0 * L.I1;
+  const float* s_fin = w.sbuf + (size_t)(passes & 1) * w.Np;
+  const float* u_fin = w.ubuf + (size_t)(passes & 1) * w.Mp;
+  if (L.s_io) e = cudaMemcpyAsync(L.s_io, s_fin, sizeof(float) * (size_t)L.N, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess && L.u_io)
-    e = cudaMemcpyAsync(L.u_io, w.u, sizeof(float) * (size_t)L.M, cudaMemcpyDeviceToDevice, st);
+    e = cudaMemcpyAsync(L.u_io, u_fin, sizeof(float) * (size_t)L.M, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess && L.rs_out)
     e = cudaMemcpyAsync(L.rs_out, w.rs, sizeof(float) * (size_t)L.N, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess && L.cs_out)

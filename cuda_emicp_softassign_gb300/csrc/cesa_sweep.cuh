@@ -272,9 +272,16 @@ struct PrepOut {
 
 // Prepare step that uses the streams as loaded.
 struct NoPrep {
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int) const {
+  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int, int, int) const {
     return PrepOut{sm.raw[stage], sm.raw2[stage]};
   }
+};
+
+// Finalize step of a deferred sweep: the owned totals stay in the partial
+// buffer and are combined by the consumer of the next sweep.
+struct NoFin {
+  template <int NACC>
+  __device__ __forceinline__ void operator()(int, const float (&)[NACC]) const {}
 };
 
 // Runs all units of one sweep assigned to this block (round-robin over the
@@ -284,15 +291,19 @@ struct NoPrep {
 // block that completes the owned block. Returns false if a wait gave up.
 //
 //   Elem: void operator()(float (&acc)[NACC], const float (&p)[3], float4 a, float4 b)
-//   Prep: PrepOut operator()(SweepSmem&, int stage, int len)         (block-wide)
-//   Fin:  void operator()(int blk, const float (&tot)[NACC])         (block-wide)
-template <int NACC, class Elem, class Prep, class Fin>
+//   Prep: PrepOut operator()(SweepSmem&, int stage, int first, int len, int blk)  (block-wide)
+//   Fin:  void operator()(int blk, const float (&tot)[NACC])                      (block-wide)
+// kDeferred: the owned totals of slice sl are stored at part[sl * part_ld + point]
+// and nothing is finalized here (no completion counter, no Fin); the sweep
+// that streams these points next sums the S slices itself.
+template <int NACC, class Elem, class Prep, class Fin, bool kDeferred = false>
 __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const SweepGeom& g,
                                             const StreamSrc& src, const float4* own, bool xform_own,
                                             const float (&R)[9], const float (&tc)[3], unsigned round,
                                             float* part, unsigned* cnt, const Elem& elem,
                                             const Prep& prep, const Fin& fin, Ctl* ctl,
-                                            uint64_t timeout_ns, int where, Timeline& tl) {
+                                            uint64_t timeout_ns, int where, Timeline& tl,
+                                            int part_ld = 0) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int G = (int)gridDim.x;
   pipe.cur = -1;
@@ -361,7 +372,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
         return false;
       }
       if (cur_ch == 0 && u == (int)blockIdx.x) tl.mark(2);
-      const PrepOut pb = prep(sm, cur_stage, cur_len);
+      const PrepOut pb = prep(sm, cur_stage, cur_first, cur_len, blk);
       const float4* __restrict__ bufA = pb.a;
       const float4* __restrict__ bufB = pb.b;
 #pragma unroll 2
@@ -385,7 +396,15 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
     tl.mark(3);
     float tot[NACC];
     reduce_warps<NACC>(sm, acc, tot);
-    if (split_complete<NACC>(sm, g, blk, sl, round, part, cnt, tot)) fin(blk, tot);
+    if (kDeferred) {
+      const int i = blk * kBlockPts + (int)threadIdx.x;
+      if (threadIdx.x < kBlockPts && i < g.n_own) {
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) __stcg(part + ((size_t)a * g.slices + sl) * part_ld + i, tot[a]);
+      }
+    } else if (split_complete<NACC>(sm, g, blk, sl, round, part, cnt, tot)) {
+      fin(blk, tot);
+    }
     tl.mark(4);
     u += G;
     cur_ch = 0;
