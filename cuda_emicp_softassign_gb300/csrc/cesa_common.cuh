@@ -134,10 +134,31 @@ __device__ __forceinline__ void block_reduce_df(df (&v)[NV], df* red) {
 }
 
 // ---------------------------------------------------------------- grid barrier
+// Release add (no return value): orders this thread's earlier writes, and the
+// block's writes it observed through __syncthreads, before the add.
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Acquire-release add returning the old value.
+__device__ __forceinline__ unsigned atom_acq_rel_add(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // Monotonic-counter barrier across all blocks of a cooperative launch.
 // `epoch` counts the barriers this block has passed (kept by the caller).
+// Thread 0 arrives with a release add and polls with acquire loads; the
+// __syncthreads on either side extend the ordering to the whole block.
 // Returns false when the wait exceeded timeout_ns or another block recorded an
-// error; the caller must then leave the kernel.
+// error while this one waited; the caller must then leave the kernel.
 __device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nblocks,
                                           uint64_t timeout_ns, int where) {
   __shared__ int s_ok;
@@ -145,15 +166,11 @@ __device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nb
   epoch += 1;
   if (threadIdx.x == 0) {
     const unsigned target = epoch * nblocks;
-    __threadfence();
-    atomicAdd(&ctl->bar, 1u);
+    red_release_add(&ctl->bar, 1u);
     int ok = 1;
     uint64_t t0 = 0;
     unsigned spins = 0;
-    for (;;) {
-      unsigned v;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&ctl->bar) : "memory");
-      if ((int)(v - target) >= 0) break;
+    while ((int)(ld_acquire(&ctl->bar) - target) < 0) {
       if ((++spins & 31u) == 0) {
         if (ld_status(ctl) != kStatusOk) {
           ok = 0;
@@ -169,8 +186,6 @@ __device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nb
         }
       }
     }
-    __threadfence();
-    if (ok && ld_status(ctl) != kStatusOk) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

@@ -40,7 +40,7 @@ struct EmicpArgs {
   float* dRt;           // PoseIO in/out, caller frame
   float* part;          // split partials [nblk*S][5][128]
   unsigned* cnt;        // [nblk]
-  df* bpart;            // [2][grid][kEmNV]
+  df* rbpart;           // [2][nblk][kEmNV] moments per owned block (step parity)
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -80,8 +80,8 @@ struct EmicpFin {
   float xm[3];
   float* row_out;  // caller frame: u = lambda X' + lambda oX
   float oX[3];
-  df* red;
-  df* acc;
+  df* scratch;     // shared, >= 17 * 128 dfs
+  df* rbpart;      // this step's [nblk][kEmNV]
   __device__ void operator()(int blk, const float (&tot)[5]) const {
     df v[kEmNV];
 #pragma unroll
@@ -123,7 +123,7 @@ struct EmicpFin {
 #pragma unroll
         for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
     }
-    block_accumulate<kEmNV>(v, red, acc);
+    owned_block_sum<kEmNV>(v, scratch, rbpart + (size_t)blk * kEmNV);
   }
 };
 
@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
   __shared__ float s_pose[12];
-  __shared__ df s_acc[kEmNV];
   __shared__ df s_red[kThreads];
+  __shared__ OwnCache oc_rows;
   __shared__ df s_tot[kEmNV];
   __shared__ float s_hdr[12];
 
@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     pose_to_centred(R, t, &s_hdr[0], &s_hdr[3], tc);
     for (int k = 0; k < 9; ++k) s_pose[k] = R[k];
     for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
+    oc_rows.blk = -1;
   }
   __syncthreads();
 
@@ -168,7 +169,6 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   for (int step = 0; step < A.nsteps; ++step) {
     tl.mark(1);
     const float outlier = expf(-A.d_02 / s2);  // src/emicp.cu:489
-    if (tid < kEmNV) s_acc[tid] = df_make(0.f);
     float R[9], tc[3];
 #pragma unroll
     for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
@@ -178,23 +178,19 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
 
     // e = exp(-d2 / (2 s2)) = 2^(nk d2)
     const EmicpElem elem{-kLog2e / (2.f * s2)};
+    df* rb = A.rbpart + (size_t)(step & 1) * A.geo.nblk * kEmNV;
     const EmicpFin fin{A.rows,    A.M,
                        outlier,   {s_hdr[6], s_hdr[7], s_hdr[8]},
                        A.row_out, {s_hdr[0], s_hdr[1], s_hdr[2]},
-                       s_red,     s_acc};
+                       reinterpret_cast<df*>(sm.prep), rb};
     if (!sweep_units<5>(sm, pipe, A.geo, src, A.rows, true, R, tc, (unsigned)step, A.part, A.cnt,
-                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10, tl))
+                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10, tl, 0, &oc_rows))
       break;
 
     // ---- grid-wide moments -> pose (every block computes the same pose)
-    df* bp = A.bpart + (size_t)(step & 1) * G * kEmNV;
-    if (tid < kEmNV) {
-      const df a = s_acc[tid];
-      __stcg(reinterpret_cast<float2*>(bp + (size_t)blockIdx.x * kEmNV + tid), make_float2(a.hi, a.lo));
-    }
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
     tl.mark(5);
-    reduce_block_partials<kEmNV>(bp, (int)G, s_red, s_tot);
+    reduce_block_partials<kEmNV>(rb, A.geo.nblk, s_red, s_tot);
     tl.mark(6);
     if (tid == 0) {
       const float L = df_val(s_tot[0]);
@@ -299,7 +295,7 @@ struct EmicpCarved {
   float4* cols;
   float* part;
   unsigned* cnt;
-  df* bpart;
+  df* rbpart;
 };
 
 EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* total) {
@@ -312,7 +308,7 @@ EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* to
   w.rows = c.take<float4>((size_t)M);
   w.cols = c.take<float4>((size_t)N);
   w.part = c.take<float>((size_t)P.geo.units * 5 * kBlockPts);
-  w.bpart = c.take<df>((size_t)2 * P.grid * kEmNV);
+  w.rbpart = c.take<df>((size_t)2 * P.geo.nblk * kEmNV);
   if (total) *total = c.off;
   (void)zero_end;
   return w;
@@ -361,7 +357,7 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.dRt = L.dRt;
   A.part = w.part;
   A.cnt = w.cnt;
-  A.bpart = w.bpart;
+  A.rbpart = w.rbpart;
   A.ctl = w.ctl;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;

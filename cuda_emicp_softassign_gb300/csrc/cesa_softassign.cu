@@ -57,7 +57,7 @@ struct SoftArgs {
   float* pc;           // column-pass partials [S_c][Mp]
   float* part_f;       // final-sweep split partials [units_r][5][128]
   unsigned* cnt_f;     // [nblk_r]
-  df* bpart;           // [2][grid][kSaNV]
+  df* mom;             // [2][nblk_r + S_c][32] moment records: row blocks, then column slices
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -127,6 +127,7 @@ struct RowPrep {
     __syncthreads();
     return PrepOut{sm.prep, sm.raw2[stage]};
   }
+  __device__ __forceinline__ void unit_end(int, int) const {}
 };
 
 // Streamed X rows for Sinkhorn column sweeps: (x', a_r), completing the
@@ -160,17 +161,22 @@ struct ColPrep {
     __syncthreads();
     return PrepOut{sm.prep, sm.raw2[stage]};
   }
+  __device__ __forceinline__ void unit_end(int, int) const {}
 };
 
 // Streamed Y columns for the final row sweep, completing the last column pass:
 // (R y' + t', b_c) and (g_c (y'_c - Yhat), delta_c) with g = b cs,
 // delta = b (cs - 1) and Yhat = mean(Y') (any centre is exact; this one keeps
-// the third stream small). The designated units also accumulate the column
-// moments sum cs and sum cs y' (per thread, df, in shared memory).
+// the third stream small). The designated units (block 0 of each slice) also
+// accumulate the column moments sum cs and sum cs y' of their slice and store
+// them as one moment record per slice.
 struct FinalPrep {
   float R[9], tc[3], yh[3];
   ColDone cd;
-  df* colacc;  // [kThreads][4]
+  df* colacc;   // shared [kThreads][4], per-thread running sums
+  df* red;      // shared scratch (kThreads dfs)
+  df* tmp;      // shared df[4]
+  df* colrec;   // this update's column records [S_c][32] (slots 28..31 used)
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
     for (int c = threadIdx.x; c < len; c += kThreads) {
@@ -193,6 +199,22 @@ struct FinalPrep {
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.prep2};
+  }
+  __device__ __forceinline__ void unit_end(int blk, int sl) const {
+    if (blk != 0) return;  // uniform per unit
+    df v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[q] = colacc[threadIdx.x * 4 + q];
+      colacc[threadIdx.x * 4 + q] = df_make(0.f);
+    }
+    if (threadIdx.x < 4) tmp[threadIdx.x] = df_make(0.f);
+    __syncthreads();
+    block_accumulate<4>(v, red, tmp);
+    if (threadIdx.x < 32) {
+      const df o = threadIdx.x >= 28 ? tmp[threadIdx.x - 28] : df_make(0.f);
+      __stcg(reinterpret_cast<float2*>(colrec + (size_t)sl * 32 + threadIdx.x), make_float2(o.hi, o.lo));
+    }
   }
 };
 
@@ -241,12 +263,12 @@ struct FinalFin {
   const float* a;  // a^(I1)
   float* w_out;
   int N;
-  df* red;
-  df* acc;
+  df* scratch;     // shared, >= 33 * 128 dfs
+  df* rbpart;      // this update's row-block records [nblk_r][32] (slots 0..27 used)
   __device__ void operator()(int blk, const float (&tot)[5]) const {
-    df v[28];
+    df v[32];
 #pragma unroll
-    for (int k = 0; k < 28; ++k) v[k] = df_make(0.f);
+    for (int k = 0; k < 32; ++k) v[k] = df_make(0.f);
     const int r = blk * kBlockPts + (int)threadIdx.x;
     if (threadIdx.x < kBlockPts && r < N) {
       const float4 x = __ldcg(&rows[r]);
@@ -272,7 +294,7 @@ struct FinalFin {
       df_add_prod(v[23], w, w);
       df_add_prod(v[27], w, mu);
     }
-    block_accumulate<28>(v, red, acc);
+    owned_block_sum<32>(v, scratch, rbpart + (size_t)blk * 32);
   }
 };
 
@@ -292,10 +314,11 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
   __shared__ float s_pose[12];
-  __shared__ df s_acc[kSaNV];
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[kSaNV];
   __shared__ df s_colacc[kThreads * 4];
+  __shared__ df s_tmp4[4];
+  __shared__ OwnCache oc_rows, oc_cols;
   __shared__ float s_hdr[12];
   __shared__ float s_S[9], s_xcp[3], s_yd[3], s_xc[3], s_yc[3];
 
@@ -318,7 +341,12 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
   }
   __shared__ HornState<float> horn;  // carried eigenbasis (thread 0)
-  if (tid == 0) horn.reset();
+  if (tid == 0) {
+    horn.reset();
+    oc_rows.blk = -1;
+    oc_cols.blk = -1;
+  }
+  for (int k = tid; k < kThreads * 4; k += kThreads) s_colacc[k] = df_make(0.f);
   __syncthreads();
 
   Pipe pipe;
@@ -340,8 +368,6 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     const float c0 = fmaf(A.alpha, kk, -0.5f * log2f(T));
     for (int iter0 = 0; iter0 < A.I0 && ok; ++iter0, ++step) {
       tl.mark(1);
-      if (tid < kSaNV) s_acc[tid] = df_make(0.f);
-      for (int k = tid; k < kThreads * 4; k += kThreads) s_colacc[k] = df_make(0.f);
       float R[9], tc[3];
 #pragma unroll
       for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
@@ -367,8 +393,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.cs};
         ok = sweep_units<1, SinkElem, RowPrep, NoFin, true>(sm, pipe, A.gr, src_cols, A.rows, false, R,
                                                             tc, 0u, A.pr, nullptr, se, rp, NoFin{},
-                                                            A.ctl, A.timeout_ns, 30, tl, Np) &&
-             grid_sync(A.ctl, epoch, G, A.timeout_ns, 32);
+                                                            A.ctl, A.timeout_ns, 30, tl, Np, &oc_rows);
+        if (ok) sweep_prefetch(pipe, sm, A.gc, src_rows);
+        ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 32);
         tl.mark(5);
         if (!ok) break;
         if (k >= 1) up ^= 1;  // the row pass completed column pass k-1
@@ -383,8 +410,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                          A.rs};
         ok = sweep_units<1, SinkElem, ColPrep, NoFin, true>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
                                                            0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
-                                                           A.timeout_ns, 40, tl, Mp) &&
-             grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
+                                                           A.timeout_ns, 40, tl, Mp, &oc_cols);
+        if (ok) sweep_prefetch(pipe, sm, A.gr, src_cols);  // the next row pass or the final sweep
+        ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
         tl.mark(5);
         sp ^= 1;
       }
@@ -408,31 +436,29 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.bbuf + (size_t)(A.I1 & 1) * Mp,
                         A.ubuf + (size_t)(up ^ 1) * Mp,
                         A.cs};
+        df* mom = A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32;
         fp.colacc = s_colacc;
+        fp.red = s_red;
+        fp.tmp = s_tmp4;
+        fp.colrec = mom + (size_t)A.gr.nblk * 32;
         const FinalElem fe{nk, c0};
-        const FinalFin ff{A.rows, A.abuf + (size_t)(A.I1 & 1) * Np, A.w_out, A.N, s_red, s_acc};
+        // owned_block_sum<32> scratch (32 * (128 + 8) dfs) spans prep, prep2 and red
+        static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >= 32 * (kBlockPts + 8) * sizeof(df),
+                      "moment scratch does not fit");
+        const FinalFin ff{A.rows, A.abuf + (size_t)(A.I1 & 1) * Np, A.w_out, A.N,
+                          reinterpret_cast<df*>(sm.prep), mom};
         const StreamSrc src_final{A.cols, nullptr, false};
         ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_f++, A.part_f,
-                            A.cnt_f, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl);
+                            A.cnt_f, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl, 0, &oc_rows);
         if (!ok) break;
         up ^= 1;
-        // column moments of the designated units -> slots 28..31
-        df cv[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) cv[q] = s_colacc[tid * 4 + q];
-        block_accumulate<4>(cv, s_red, s_acc + 28);
-      }
-      const int par = step & 1;
-      df* bp = A.bpart + (size_t)par * G * kSaNV;
-      if (tid < kSaNV) {
-        const df a = s_acc[tid];
-        __stcg(reinterpret_cast<float2*>(bp + (size_t)blockIdx.x * kSaNV + tid),
-               make_float2(a.hi, a.lo));
+        sweep_prefetch(pipe, sm, A.gr, src_cols);  // the next pose update's first row pass
       }
       ok = grid_sync(A.ctl, epoch, G, A.timeout_ns, 52);
       tl.mark(5);
       if (!ok) break;
-      reduce_block_partials<kSaNV>(bp, (int)G, s_red, s_tot);
+      reduce_block_partials<32>(A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32,
+                                A.gr.nblk + A.gr.slices, s_red, s_tot);
       tl.mark(6);
       // S_ij by threads 0..8, centres by threads 9..11, then the pose by thread 0.
       //   Yc = (B2 + oY B1)/A1, alpha = Yhat + oY, beta = alpha - Yc,
@@ -526,6 +552,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     T = T * A.TFACTOR;  // FP32, src/softassign.cu:820
   }
 
+  // a copy issued ahead for a pose update that never came must land before exit
+  if (pipe.pre_valid && pipe.pre_wait)
+    mbar_wait(&sm.full[pipe.pre_stage], pipe.pre_par, A.ctl, A.timeout_ns, 60);
   if (blockIdx.x == 0 && tid == 0) {
     const int st = ld_status(A.ctl);
     if (st == kStatusOk) {
@@ -585,7 +614,7 @@ struct SaCarved {
   float* pr;
   float* pc;
   float* part_f;
-  df* bpart;
+  df* mom;
   int Np, Mp;
 };
 
@@ -608,7 +637,7 @@ SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
   w.pr = c.take<float>((size_t)P.gr.slices * w.Np);
   w.pc = c.take<float>((size_t)P.gc.slices * w.Mp);
   w.part_f = c.take<float>((size_t)P.gr.units * 5 * kBlockPts);
-  w.bpart = c.take<df>((size_t)2 * P.grid * kSaNV);
+  w.mom = c.take<df>((size_t)2 * (P.gr.nblk + P.gr.slices) * 32);
   if (total) *total = c.off;
   return w;
 }
@@ -679,7 +708,7 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.pc = w.pc;
   A.part_f = w.part_f;
   A.cnt_f = w.cnt_f;
-  A.bpart = w.bpart;
+  A.mom = w.mom;
   A.ctl = w.ctl;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;

@@ -57,6 +57,11 @@ struct Pipe {
   unsigned uses[kStages];  // copies issued into each stage
   int tag[kStages];        // chunk id resident in each stage (static streams), -1 = none
   int cur;                 // stage of the task being consumed, -1 = none
+  // first task of the next sweep, issued before the grid barrier that precedes it
+  const float4* pre_src;
+  int pre_stage, pre_first, pre_len;
+  unsigned pre_par;
+  bool pre_wait, pre_valid;
 };
 
 __device__ __forceinline__ void pipe_init(Pipe& p) {
@@ -65,7 +70,15 @@ __device__ __forceinline__ void pipe_init(Pipe& p) {
     p.tag[s] = -1;
   }
   p.cur = -1;
+  p.pre_valid = false;
 }
+
+// Owned points of the last unit a block processed in a sweep type, kept in
+// shared memory (owned arrays never change during a launch).
+struct OwnCache {
+  float4 pts[kBlockPts];
+  int blk;
+};
 
 // Streamed source for one sweep.
 struct StreamSrc {
@@ -97,6 +110,24 @@ __device__ __forceinline__ int pipe_issue(Pipe& p, SweepSmem& sm, const StreamSr
     if (src.b) bulk_g2s(&sm.raw2[s][0], src.b + first, bytes, &sm.full[s]);
   }
   return s;
+}
+
+// Owned points of block `blk` from the cache, filling it from global memory on
+// a miss (block-wide). Invalid points read as zero.
+__device__ __forceinline__ void load_owned_cached(OwnCache& oc, const float4* own, int n_own, int blk,
+                                                  float4 (&pt)[kOwnPerLane]) {
+  if (oc.blk != blk) {  // uniform: every thread reads the same tag
+    __syncthreads();
+    if (threadIdx.x < kBlockPts) {
+      const int i = blk * kBlockPts + (int)threadIdx.x;
+      oc.pts[threadIdx.x] = i < n_own ? ld_cg(own + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) oc.blk = blk;
+  }
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < kOwnPerLane; ++j) pt[j] = oc.pts[lane + 32 * j];
 }
 
 // Owned-point loader: lane's 4 points of block `blk`. Invalid points get
@@ -152,11 +183,9 @@ __device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned old = atomicAdd(&cnt[blk], 1u);
+    const unsigned old = atom_acq_rel_add(&cnt[blk], 1u);
     const unsigned target = (round + 1u) * (unsigned)g.slices;
     sm.flag = (old + 1u == target) ? 1 : 0;
-    __threadfence();
   }
   __syncthreads();
   const bool last = sm.flag != 0;
@@ -224,41 +253,79 @@ __device__ __forceinline__ void block_accumulate(df (&v)[NV], df* red, df* acc) 
   __syncthreads();
 }
 
+// Sum over the 128 owned points of NV per-point df values (thread i < 128
+// holds point i; other threads pass zeros or nothing), written to dst[NV] in
+// global memory. Goes through shared memory (`scratch`, >= NV*128 dfs) in
+// a fixed order: 8 partial sums of 16 points per value, then 8 -> 1.
+template <int NV>
+__device__ __forceinline__ void owned_block_sum(const df (&v)[NV], df* scratch, df* dst) {
+  static_assert(NV * 8 <= kThreads * 2, "two passes of the block at most");
+  if (threadIdx.x < kBlockPts) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * kBlockPts + threadIdx.x] = v[k];
+  }
+  __syncthreads();
+  df* part = scratch + NV * kBlockPts;  // [NV][8]
+  for (int p = threadIdx.x; p < NV * 8; p += kThreads) {
+    const int k = p >> 3, g = p & 7;
+    const df* src = scratch + k * kBlockPts + g * 16;
+    df s = src[0];
+#pragma unroll
+    for (int j = 1; j < 16; ++j) df_add(s, src[j]);
+    part[p] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    df s = part[threadIdx.x * 8];
+#pragma unroll
+    for (int g = 1; g < 8; ++g) df_add(s, part[threadIdx.x * 8 + g]);
+    __stcg(reinterpret_cast<float2*>(dst + threadIdx.x), make_float2(s.hi, s.lo));
+  }
+  __syncthreads();
+}
+
 // Grid-wide sum of NV block partials (df), identical in every block: thread 0
 // of the calling block receives the totals in tot[]. parts: [nblocks][NV].
+__host__ __device__ constexpr int pow2_ceil(int v) { return v <= 1 ? 1 : 2 * pow2_ceil((v + 1) / 2); }
+
 template <int NV>
 __device__ __forceinline__ void reduce_block_partials(const df* parts, int nblocks, df* scratch,
                                                       df* tot) {
-  constexpr int G = kThreads / NV;  // threads per value
-  static_assert(kThreads % NV == 0 && NV <= 32, "NV must divide the block size");
-  const int v = threadIdx.x % NV, grp = threadIdx.x / NV;
+  constexpr int NVP = pow2_ceil(NV);  // lanes per group (values >= NV idle)
+  constexpr int G = kThreads / NVP;   // threads per value
+  static_assert(NVP <= 32, "at most 32 values");
+  const int v = threadIdx.x % NVP, grp = threadIdx.x / NVP;
+  const bool live = v < NV;
   // blocks grp, grp + G, ... in order; loads issued 8 at a time
   df a = df_make(0.f);
   int b = grp;
   for (; b + 7 * G < nblocks; b += 8 * G) {
     float2 x[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) x[j] = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)(b + j * G) * NV + v));
+    for (int j = 0; j < 8; ++j)
+      x[j] = live ? __ldcg(reinterpret_cast<const float2*>(parts + (size_t)(b + j * G) * NV + v))
+                  : make_float2(0.f, 0.f);
 #pragma unroll
     for (int j = 0; j < 8; ++j) df_add(a, df{x[j].x, x[j].y});
   }
   for (; b < nblocks; b += G) {
-    const float2 x = __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v));
+    const float2 x = live ? __ldcg(reinterpret_cast<const float2*>(parts + (size_t)b * NV + v))
+                          : make_float2(0.f, 0.f);
     df_add(a, df{x.x, x.y});
   }
   // fixed tree over the groups: lanes of a warp with the same v, then warps
 #pragma unroll
-  for (int off = 16; off >= NV; off >>= 1) {
+  for (int off = 16; off >= NVP; off >>= 1) {
     const df o = df_shfl_down(a, off);
     df_add(a, o);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane < NV) scratch[warp * NV + lane] = a;
+  if (lane < NVP) scratch[warp * NVP + lane] = a;
   __syncthreads();
   if (threadIdx.x < NV) {
     df s = scratch[threadIdx.x];
 #pragma unroll
-    for (int w = 1; w < kWarps; ++w) df_add(s, scratch[w * NV + threadIdx.x]);
+    for (int w = 1; w < kWarps; ++w) df_add(s, scratch[w * NVP + threadIdx.x]);
     tot[threadIdx.x] = s;
   }
   __syncthreads();
@@ -275,6 +342,7 @@ struct NoPrep {
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int, int, int) const {
     return PrepOut{sm.raw[stage], sm.raw2[stage]};
   }
+  __device__ __forceinline__ void unit_end(int, int) const {}
 };
 
 // Finalize step of a deferred sweep: the owned totals stay in the partial
@@ -284,6 +352,31 @@ struct NoFin {
   __device__ __forceinline__ void operator()(int, const float (&)[NACC]) const {}
 };
 
+// Issues, ahead of a sweep, the bulk copy of the first streamed chunk this
+// block will need in it. Called block-wide after the previous sweep's last
+// unit, before the grid barrier, so the copy lands while the barrier waits.
+// Only for streams whose contents are final at that point (the coordinate
+// arrays, which never change during a launch).
+__device__ __forceinline__ void sweep_prefetch(Pipe& p, SweepSmem& sm, const SweepGeom& g,
+                                               const StreamSrc& src) {
+  const int u = blockIdx.x;
+  if (u >= g.units || p.pre_valid) return;
+  const int sl = u % g.slices;
+  const int sb = sl * g.slice_len;
+  const int se = min(sb + g.slice_len, g.n_stream);
+  const int first = sb, len = min(kChunk, se - sb);
+  p.cur = -1;
+  bool w = false;
+  const int st = pipe_issue(p, sm, src, first, first, len, w);
+  p.pre_src = src.a;
+  p.pre_stage = st;
+  p.pre_par = (p.uses[st] - 1u) & 1u;
+  p.pre_first = first;
+  p.pre_len = len;
+  p.pre_wait = w;
+  p.pre_valid = true;
+}
+
 // Runs all units of one sweep assigned to this block (round-robin over the
 // grid). For every unit: owned points -> registers (optionally transformed by
 // R, tc), streamed chunks through the TMA ring, elem() per (owned, streamed)
@@ -292,6 +385,7 @@ struct NoFin {
 //
 //   Elem: void operator()(float (&acc)[NACC], const float (&p)[3], float4 a, float4 b)
 //   Prep: PrepOut operator()(SweepSmem&, int stage, int first, int len, int blk)  (block-wide)
+//         void unit_end(int blk, int slice)                                       (block-wide)
 //   Fin:  void operator()(int blk, const float (&tot)[NACC])                      (block-wide)
 // kDeferred: the owned totals of slice sl are stored at part[sl * part_ld + point]
 // and nothing is finalized here (no completion counter, no Fin); the sweep
@@ -303,7 +397,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
                                             float* part, unsigned* cnt, const Elem& elem,
                                             const Prep& prep, const Fin& fin, Ctl* ctl,
                                             uint64_t timeout_ns, int where, Timeline& tl,
-                                            int part_ld = 0) {
+                                            int part_ld = 0, OwnCache* oc = nullptr) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int G = (int)gridDim.x;
   pipe.cur = -1;
@@ -322,15 +416,32 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
   unsigned cur_par = 0;
   bool cur_wait = false;
   bool have = task_range(u, 0, cur_first, cur_len);
-  if (have) {
+  const bool pre_hit = have && pipe.pre_valid && pipe.pre_src == src.a && pipe.pre_first == cur_first &&
+                       pipe.pre_len == cur_len;
+  if (pipe.pre_valid && !pre_hit && pipe.pre_wait) {  // unused prefetch: let it land
+    if (!mbar_wait(&sm.full[pipe.pre_stage], pipe.pre_par, ctl, timeout_ns, where + 2)) {
+      pipe.pre_valid = false;
+      return false;
+    }
+  }
+  if (pre_hit) {
+    cur_stage = pipe.pre_stage;
+    cur_par = pipe.pre_par;
+    cur_wait = pipe.pre_wait;
+  } else if (have) {
     cur_stage = pipe_issue(pipe, sm, src, cur_first, cur_first, cur_len, cur_wait);
     cur_par = (pipe.uses[cur_stage] - 1u) & 1u;
   }
+  pipe.pre_valid = false;
   while (have) {
     const int blk = u / g.slices, sl = u % g.slices;
     float4 ow[kOwnPerLane];
-    bool valid[kOwnPerLane];
-    load_owned(own, g.n_own, blk, ow, valid);
+    if (oc) {
+      load_owned_cached(*oc, own, g.n_own, blk, ow);
+    } else {
+      bool valid[kOwnPerLane];
+      load_owned(own, g.n_own, blk, ow, valid);
+    }
     float p[kOwnPerLane][3];
 #pragma unroll
     for (int j = 0; j < kOwnPerLane; ++j) {
@@ -394,6 +505,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
       if (unit_done) break;
     }
     tl.mark(3);
+    prep.unit_end(blk, sl);
     float tot[NACC];
     reduce_warps<NACC>(sm, acc, tot);
     if (kDeferred) {
