@@ -242,6 +242,23 @@ def load_peaks():
     return (a.value, b.value) if rc == 0 else (None, None)
 
 
+def max_over_ranks(values, world, device):
+    """Element-wise maximum of this rank's timings over all ranks (each rank
+    runs an independent replica; the slowest one sets the job time)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_rate(steps, world, seconds):
+    """Registrations per second of the whole job: every rank registers `steps`
+    pairs, and the job takes the slowest rank's time."""
+    return steps * world / seconds
+
+
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -322,15 +339,12 @@ def run_ours(args, rank, world, local):
     assert np.array_equal(Rh.astype(np.float64), R_dev[:9]), "host and device entry points disagree"
 
     # ---- max over ranks
-    tot = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
-    total_ms, e2e_s = float(tot[0]), float(tot[1])
+    total_ms, e2e_s = max_over_ranks([total_ms, e2e_s], world, "cuda")
     if rank != 0:
         return
 
     regs = args.steps * world
-    value = regs / (total_ms * 1e-3)
+    value = whole_job_rate(args.steps, world, total_ms * 1e-3)
     fp32_ops, ex2_ops, elems = algorithmic_work(kind, N, M, p)
     mean_s = total_ms * 1e-3 / args.steps
     fp32_peak, ex2_peak = load_peaks()
@@ -363,7 +377,7 @@ def run_ours(args, rank, world, local):
             "roofline": roofline,
             "cpu_baseline": {"value": cpu_v, "unit": "registrations/s", "cores": cpu_thr, "kind": "port",
                              "sample": cpu_desc},
-            "e2e": {"value": args.steps * world / e2e_s, "unit": "registrations/s",
+            "e2e": {"value": whole_job_rate(args.steps, world, e2e_s), "unit": "registrations/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * 4},
             "clocks": clocks,
             "gpu_launches": kernels_per_registration(kind) * args.steps,

@@ -73,6 +73,19 @@ class Params(ctypes.Structure):
 # registrationParameters is the reference's name for the same record
 registrationParameters = Params
 
+ALGO_EMICP = 0
+ALGO_SOFTASSIGN = 1
+MAX_BATCH = 1024
+
+
+class Pair(ctypes.Structure):
+    """Mirror of ``cesa_pair``: one registration of a batch."""
+    _fields_ = [
+        ("algorithm", ctypes.c_int), ("N", ctypes.c_int), ("M", ctypes.c_int),
+        ("X", ctypes.c_void_p), ("Y", ctypes.c_void_p), ("Rt", ctypes.c_void_p),
+        ("params", Params),
+    ]
+
 
 class Report(ctypes.Structure):
     _fields_ = [
@@ -122,6 +135,12 @@ def lib():
         L.cesa_status_string.argtypes = [_i]
         L.cesa_status_string.restype = ctypes.c_char_p
         L.cesa_version.restype = _i
+        L.cesa_register_batch_device.argtypes = [_p, _i, _p, _p]
+        L.cesa_register_batch_device.restype = _i
+        L.cesa_register_batch.argtypes = [_p, _i, _p]
+        L.cesa_register_batch.restype = _i
+        L.cesa_self_test_waits.argtypes = [_i, _i, _p, _p]
+        L.cesa_self_test_waits.restype = _i
         _lib = L
     return _lib
 
@@ -271,6 +290,56 @@ def emicp_device_noalloc(dX, dY, dRt, param=None, d_status=None, stream=None):
               _dptr(d_status) if d_status is not None else None, ctypes.c_void_p(_stream_handle(stream)))
 
 
+def register_batch(pairs, report=False):
+    """Batched registration on host clouds, one persistent launch.
+
+    pairs: sequence of (algorithm, X, Y, params) or (algorithm, X, Y, params,
+    R0, t0), with algorithm ALGO_EMICP or ALGO_SOFTASSIGN and X, Y (n, 3).
+    Returns a list of (R, t); with ``report`` also the Report.
+    """
+    n = len(pairs)
+    arr = (Pair * n)()
+    keep = []
+    for i, pr in enumerate(pairs):
+        algo, X, Y, prm = pr[:4]
+        R0, t0 = (pr[4], pr[5]) if len(pr) > 4 else (None, None)
+        Xs, Ys = cloud2data(X), cloud2data(Y)
+        Rh, th = _pose_in(R0, t0)
+        rt = np.concatenate([Rh, th]).astype(np.float32)
+        keep.append((Xs, Ys, rt))
+        arr[i].algorithm = int(algo)
+        arr[i].N = len(X)
+        arr[i].M = len(Y)
+        arr[i].X = Xs.ctypes.data
+        arr[i].Y = Ys.ctypes.data
+        arr[i].Rt = rt.ctypes.data
+        arr[i].params = prm if prm is not None else Params.default()
+    rep = Report()
+    _check(lib().cesa_register_batch(ctypes.cast(arr, ctypes.c_void_p), n, ctypes.byref(rep)), "register_batch")
+    out = [(k[2][:9].reshape(3, 3).astype(np.float64), k[2][9:].astype(np.float64)) for k in keep]
+    return (out, rep) if report else out
+
+
+def register_batch_device(pairs, d_status=None, stream=None):
+    """Batched registration on device tensors: pairs of (algorithm, dX, dY,
+    dRt, params) with SoA float32 dX (3N), dY (3M) and dRt (12, in/out).
+    Enqueues on `stream` (default: torch's current stream)."""
+    n = len(pairs)
+    arr = (Pair * n)()
+    for i, (algo, dX, dY, dRt, prm) in enumerate(pairs):
+        arr[i].algorithm = int(algo)
+        arr[i].N = dX.numel() // 3
+        arr[i].M = dY.numel() // 3
+        arr[i].X = dX.data_ptr()
+        arr[i].Y = dY.data_ptr()
+        arr[i].Rt = dRt.data_ptr()
+        arr[i].params = prm if prm is not None else Params.default()
+    rc = lib().cesa_register_batch_device(ctypes.cast(arr, ctypes.c_void_p), n,
+                                          _dptr(d_status) if d_status is not None else None,
+                                          ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "register_batch_device")
+
+
 def stream_status(stream=None):
     return lib().cesa_stream_status(ctypes.c_void_p(_stream_handle(stream)))
 
@@ -303,6 +372,17 @@ def softassign_step(dX, dY, R, t, T, alpha, I1, s, u, rs=None, cs=None, w=None,
 
 def release_workspaces():
     lib().cesa_release_workspaces()
+
+
+def self_test_waits(which, timeout_us=1000):
+    """Runs the grid barrier (which=0) or the mbarrier wait (which=1) of the
+    kernels on a barrier that nothing completes. Returns (rc, status, where):
+    rc is CESA_OK when the probe ran and the device still works afterwards;
+    status is the code the expired wait recorded (CESA_ERR_TIMEOUT)."""
+    st = ctypes.c_int(-1)
+    wh = ctypes.c_int(-1)
+    rc = lib().cesa_self_test_waits(int(which), int(timeout_us), ctypes.byref(st), ctypes.byref(wh))
+    return rc, st.value, wh.value
 
 
 def version():

@@ -13,6 +13,7 @@
 #include <map>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "../../include/cesa.h"
 #include "cesa_kernels.h"
@@ -263,6 +264,61 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   return CESA_OK;
 }
 
+// Validates a batch and converts it to launch records (device pointers are
+// taken from the pairs unless dX/dY/dRt overrides are given).
+int batch_records(const cesa_pair* pairs, int npairs, std::vector<BatchLaunchPair>& out) {
+  if (!pairs || npairs < 1 || npairs > CESA_MAX_BATCH) return CESA_ERR_INVALID_ARGUMENT;
+  out.resize((size_t)npairs);
+  for (int i = 0; i < npairs; ++i) {
+    const cesa_pair& q = pairs[i];
+    int rc = check_points(q.X, q.N, q.Y, q.M);
+    if (rc) return rc;
+    if (!q.Rt) return CESA_ERR_INVALID_ARGUMENT;
+    BatchLaunchPair& L = out[(size_t)i];
+    L = BatchLaunchPair{};
+    L.N = q.N;
+    L.M = q.M;
+    L.dX = q.X;
+    L.dY = q.Y;
+    L.dRt = q.Rt;
+    if (q.algorithm == CESA_ALGO_EMICP) {
+      rc = check_emicp_params(&q.params);
+      if (rc) return rc;
+      const long n = emicp_steps(q.params.sigma_p2, q.params.sigma_inf, q.params.sigma_factor);
+      if (n < 0 || n > 1000000L) return CESA_ERR_INVALID_ARGUMENT;
+      L.algo = 0;
+      L.nsteps = (int)n;
+      L.sigma_p2 = q.params.sigma_p2;
+      L.sigma_factor = q.params.sigma_factor;
+      L.d_02 = q.params.d_02;
+    } else if (q.algorithm == CESA_ALGO_SOFTASSIGN) {
+      rc = check_sa_params(&q.params);
+      if (rc) return rc;
+      if ((long)q.params.JMAX * q.params.I0 * (2L * q.params.I1 + 2) > 100000000L) return CESA_ERR_INVALID_ARGUMENT;
+      L.algo = 1;
+      L.JMAX = q.params.JMAX;
+      L.I0 = q.params.I0;
+      L.I1 = q.params.I1;
+      L.alpha = q.params.alpha;
+      L.T_0 = q.params.T_0;
+      L.TFACTOR = q.params.TFACTOR;
+      L.moutlier = q.params.moutlier;
+    } else {
+      return CESA_ERR_INVALID_ARGUMENT;
+    }
+  }
+  return CESA_OK;
+}
+
+uint64_t batch_timeout_ns(const cesa_pair* pairs, int npairs) {
+  uint64_t t = 0;
+  for (int i = 0; i < npairs; ++i) {
+    const uint64_t v = timeout_ns_of(&pairs[i].params);
+    if (v > t) t = v;
+  }
+  return t;
+}
+
 }  // namespace
 }  // namespace cesa
 
@@ -366,6 +422,98 @@ int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float
   C.last_kind = 2;
   C.last_trace_steps = 0;
   return map_cuda((cudaError_t)enqueue_softassign(L, C.ws.p, C.ws.bytes, st, nullptr));
+}
+
+int cesa_register_batch_device(const cesa_pair* pairs, int npairs, int* d_status, cesa_stream_t stream) {
+  std::vector<BatchLaunchPair> rec;
+  int rc = batch_records(pairs, npairs, rec);
+  if (rc) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(batch_ws_need(rec.data(), npairs));
+  if (e != cudaSuccess) return map_cuda(e);
+  C.last_kind = 3;
+  C.last_trace_steps = 0;
+  return map_cuda((cudaError_t)enqueue_batch(rec.data(), npairs, d_status, batch_timeout_ns(pairs, npairs),
+                                             C.ws.p, C.ws.bytes, st, nullptr, nullptr));
+}
+
+int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* rep) {
+  std::vector<BatchLaunchPair> rec;
+  int rc = batch_records(pairs, npairs, rec);
+  if (rc) return rc;
+  int dev = 0;
+  rc = select_device(&pairs[0].params, &dev);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t st = own_stream(dev);
+  StreamCtx& C = ctx_for(dev, st);
+  // device copies: X, Y of every pair, then the poses
+  std::vector<size_t> ox((size_t)npairs), oy((size_t)npairs);
+  size_t off = 0;
+  for (int i = 0; i < npairs; ++i) {
+    ox[(size_t)i] = off;
+    off += align256(sizeof(float) * 3 * (size_t)pairs[i].N);
+    oy[(size_t)i] = off;
+    off += align256(sizeof(float) * 3 * (size_t)pairs[i].M);
+  }
+  const size_t opose = off;
+  off += align256(sizeof(float) * 12 * (size_t)npairs);
+  cudaError_t e = C.io.ensure(off);
+  if (e != cudaSuccess) return map_cuda(e);
+  char* io = static_cast<char*>(C.io.p);
+  float* dpose = reinterpret_cast<float*>(io + opose);
+  std::vector<float> hpose((size_t)npairs * 12);
+  for (int i = 0; i < npairs; ++i) {
+    BatchLaunchPair& L = rec[(size_t)i];
+    float* dx = reinterpret_cast<float*>(io + ox[(size_t)i]);
+    float* dy = reinterpret_cast<float*>(io + oy[(size_t)i]);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dx, pairs[i].X, sizeof(float) * 3 * (size_t)L.N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dy, pairs[i].Y, sizeof(float) * 3 * (size_t)L.M, cudaMemcpyHostToDevice, st);
+    L.dX = dx;
+    L.dY = dy;
+    L.dRt = dpose + (size_t)i * 12;
+    memcpy(&hpose[(size_t)i * 12], pairs[i].Rt, sizeof(float) * 12);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dpose, hpose.data(), sizeof(float) * hpose.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = C.ws.ensure(batch_ws_need(rec.data(), npairs));
+  if (e != cudaSuccess) return map_cuda(e);
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  int grid = 0, rounds = 0;
+  cudaEventRecord(ev0, st);
+  int kerr = enqueue_batch(rec.data(), npairs, nullptr, batch_timeout_ns(pairs, npairs), C.ws.p, C.ws.bytes, st,
+                           &grid, &rounds);
+  cudaEventRecord(ev1, st);
+  if (kerr != 0) e = (cudaError_t)kerr;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hpose.data(), dpose, sizeof(float) * hpose.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  int status = 0, steps = 0;
+  if (e == cudaSuccess) e = (cudaError_t)read_ws_status(C.ws.p, st, &status, &steps);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (e != cudaSuccess) return map_cuda(e);
+  if (status != 0) return status;
+  C.last_kind = 3;
+  C.last_trace_steps = 0;
+  for (int i = 0; i < npairs; ++i) memcpy(pairs[i].Rt, &hpose[(size_t)i * 12], sizeof(float) * 12);
+  if (rep) {
+    rep->steps = rounds;
+    rep->sinkhorn_form = CESA_SINKHORN_MATRIX_FREE;
+    rep->grid_blocks = grid;
+    rep->device_ms = ms;
+  }
+  return CESA_OK;
 }
 
 int cesa_stream_status(cesa_stream_t stream) {

@@ -21,13 +21,11 @@
 // loop. EM-ICP's S is translation invariant, so only Xc, Yc and t are shifted
 // back; the pose enters and leaves in the caller's frame.
 #include "cesa_kernels.h"
+#include "cesa_ops.cuh"
 #include "cesa_pose.h"
 #include "cesa_prep.cuh"
-#include "cesa_sweep.cuh"
 
 namespace cesa {
-
-constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), sum u y^T (9)
 
 struct EmicpArgs {
   const float4* rows;  // Y' centred (owned), M
@@ -49,82 +47,6 @@ struct EmicpArgs {
   unsigned long long* tl;
   int tl_cap;
   uint64_t timeout_ns;
-};
-
-// Per-element work of the fused E-step (see the file comment).
-struct EmicpElem {
-  float nk;  // -log2(e) / (2 sigma_p2)
-  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 x,
-                                             float4) const {
-    const float dx = x.x - p[0];
-    const float dy = x.y - p[1];
-    const float dz = x.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(d2 * nk);
-    acc[0] = fmaf(e, e, acc[0]);
-    acc[1] += e;
-    acc[2] = fmaf(e, x.x, acc[2]);
-    acc[3] = fmaf(e, x.y, acc[3]);
-    acc[4] = fmaf(e, x.z, acc[4]);
-  }
-};
-
-// Row finalize: C_r, lambda_r, u_r = lambda_r X'_r, and the row's share of the
-// 16 moments (block accumulator, compensated).
-struct EmicpFin {
-  const float4* rows;
-  int M;
-  float outlier;
-  float xm[3];
-  float* row_out;  // caller frame: u = lambda X' + lambda oX
-  float oX[3];
-  df* scratch;     // shared, >= 17 * 128 dfs
-  df* rbpart;      // this step's [nblk][kEmNV]
-  __device__ void operator()(int blk, const float (&tot)[5]) const {
-    df v[kEmNV];
-#pragma unroll
-    for (int k = 0; k < kEmNV; ++k) v[k] = df_make(0.f);
-    const int r = blk * kBlockPts + (int)threadIdx.x;
-    if (threadIdx.x < kBlockPts && r < M) {
-      const float4 y = ld_cg(rows + r);
-      const float C = tot[0] + outlier;
-      float lam, uu[3];
-      if (C > 10e-7f) {  // src/emicp.cu:155
-        const float inv = __frsqrt_rn(C);
-        lam = tot[1] * inv;
-        uu[0] = tot[2] * inv;
-        uu[1] = tot[3] * inv;
-        uu[2] = tot[4] * inv;
-      } else {  // A <- 1/N (src/emicp.cu:159): lambda = 1, lambda X' = mean(X)
-        lam = 1.f;
-        uu[0] = xm[0];
-        uu[1] = xm[1];
-        uu[2] = xm[2];
-      }
-      if (row_out) {
-        float* o = row_out + (size_t)r * 5;
-        o[0] = C;
-        o[1] = lam;
-        o[2] = fmaf(lam, oX[0], uu[0]);
-        o[3] = fmaf(lam, oX[1], uu[1]);
-        o[4] = fmaf(lam, oX[2], uu[2]);
-      }
-      const float yy[3] = {y.x, y.y, y.z};
-      df_add(v[0], lam);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        df_add(v[1 + i], uu[i]);
-        df_add_prod(v[4 + i], lam, yy[i]);
-      }
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
-    }
-    owned_block_sum<kEmNV>(v, scratch, rbpart + (size_t)blk * kEmNV);
-  }
 };
 
 __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
@@ -193,19 +115,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     reduce_block_partials<kEmNV>(rb, A.geo.nblk, s_red, s_tot);
     tl.mark(6);
     if (tid == 0) {
-      const float L = df_val(s_tot[0]);
       float Xc[3], Yc[3], S[9];
-      for (int i = 0; i < 3; ++i) {
-        Xc[i] = df_val(s_tot[1 + i]) / L;
-        Yc[i] = df_val(s_tot[4 + i]) / L;
-      }
-      // S = sum u y^T - L Xc Yc^T (centred frame; S is translation invariant)
-      for (int j = 0; j < 3; ++j)
-        for (int i = 0; i < 3; ++i) {
-          df a = s_tot[7 + i + 3 * j];
-          df_add_prod(a, -L * Xc[i], Yc[j]);
-          S[i + 3 * j] = df_val(a);
-        }
+      em_moments_to_S(s_tot, Xc, Yc, S);
       float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
       horn_quaternion<float>(S, horn, q, &gap, &lmax);
       quat_to_pose<float>(q, Xc, Yc, Rn, tn);

@@ -61,6 +61,20 @@ struct SoftassignLaunch {
   uint64_t timeout_ns;
 };
 
+// One pair of a batched launch (device pointers).
+constexpr int kMaxBatchPairs = 1024;
+struct BatchLaunchPair {
+  int algo;  // 0 EM-ICP, 1 Softassign
+  int N, M;
+  const float* dX;  // SoA, N
+  const float* dY;  // SoA, M
+  float* dRt;       // PoseIO in/out (device)
+  int nsteps;       // EM-ICP sigma steps
+  float sigma_p2, sigma_factor, d_02;
+  int JMAX, I0, I1;  // Softassign
+  float alpha, T_0, TFACTOR, moutlier;
+};
+
 // Device workspace carved from one allocation (see api.cu).
 struct Workspace {
   void* base = nullptr;
@@ -81,6 +95,11 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
                        int* grid_used);
 size_t emicp_ws_need(int N, int M, int device);
 size_t softassign_ws_need(int N, int M, int form, int device);
+
+// Batched registration: all pairs in one persistent launch.
+size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs);
+int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint64_t timeout_ns, void* ws,
+                  size_t ws_bytes, cudaStream_t st, int* grid_used, int* rounds_out);
 
 // Control-block status of the last launch that used workspace ws.
 int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written = nullptr);

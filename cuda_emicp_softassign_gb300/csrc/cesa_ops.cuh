@@ -1,0 +1,246 @@
+// Per-element functors, row finalizers and moment assembly shared by the
+// single-pair and the batched registration kernels (sm_103a).
+#pragma once
+#include "cesa_sweep.cuh"
+
+namespace cesa {
+
+// ------------------------------------------------------------------ EM-ICP
+constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), sum u y^T (9)
+
+// Per-element work of the fused one-pass E-step, with e = exp(-d^2 / (2 sigma_p2)):
+// running sums of e^2, e and e x over the streamed X points of one owned Y row.
+struct EmicpElem {
+  float nk;  // -log2(e) / (2 sigma_p2)
+  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 x,
+                                             float4) const {
+    const float dx = x.x - p[0];
+    const float dy = x.y - p[1];
+    const float dz = x.z - p[2];
+    float d2 = dx * dx;
+    d2 = fmaf(dy, dy, d2);
+    d2 = fmaf(dz, dz, d2);
+    const float e = ex2_approx(d2 * nk);
+    acc[0] = fmaf(e, e, acc[0]);
+    acc[1] += e;
+    acc[2] = fmaf(e, x.x, acc[2]);
+    acc[3] = fmaf(e, x.y, acc[3]);
+    acc[4] = fmaf(e, x.z, acc[4]);
+  }
+};
+
+// Row finalize: C_r, lambda_r, u_r = lambda_r X'_r, and the row's share of the
+// 16 moments (block accumulator, compensated).
+struct EmicpFin {
+  const float4* rows;
+  int M;
+  float outlier;
+  float xm[3];
+  float* row_out;  // caller frame: u = lambda X' + lambda oX
+  float oX[3];
+  df* scratch;     // shared, >= 17 * 128 dfs
+  df* rbpart;      // this step's [nblk][kEmNV]
+  __device__ void operator()(int blk, const float (&tot)[5]) const {
+    df v[kEmNV];
+#pragma unroll
+    for (int k = 0; k < kEmNV; ++k) v[k] = df_make(0.f);
+    const int r = blk * kBlockPts + (int)threadIdx.x;
+    if (threadIdx.x < kBlockPts && r < M) {
+      const float4 y = ld_cg(rows + r);
+      const float C = tot[0] + outlier;
+      float lam, uu[3];
+      if (C > 10e-7f) {  // src/emicp.cu:155
+        const float inv = __frsqrt_rn(C);
+        lam = tot[1] * inv;
+        uu[0] = tot[2] * inv;
+        uu[1] = tot[3] * inv;
+        uu[2] = tot[4] * inv;
+      } else {  // A <- 1/N (src/emicp.cu:159): lambda = 1, lambda X' = mean(X)
+        lam = 1.f;
+        uu[0] = xm[0];
+        uu[1] = xm[1];
+        uu[2] = xm[2];
+      }
+      if (row_out) {
+        float* o = row_out + (size_t)r * 5;
+        o[0] = C;
+        o[1] = lam;
+        o[2] = fmaf(lam, oX[0], uu[0]);
+        o[3] = fmaf(lam, oX[1], uu[1]);
+        o[4] = fmaf(lam, oX[2], uu[2]);
+      }
+      const float yy[3] = {y.x, y.y, y.z};
+      df_add(v[0], lam);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        df_add(v[1 + i], uu[i]);
+        df_add_prod(v[4 + i], lam, yy[i]);
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
+    }
+    owned_block_sum<kEmNV>(v, scratch, rbpart + (size_t)blk * kEmNV);
+  }
+};
+
+// Centres and cross-covariance from the 16 EM-ICP moments (centred frame):
+// Xc = sum u / L, Yc = sum lambda y / L, S = sum u y^T - L Xc Yc^T
+// (S is translation invariant).
+__device__ __forceinline__ void em_moments_to_S(const df* tot, float Xc[3], float Yc[3], float S[9]) {
+  const float L = df_val(tot[0]);
+  for (int i = 0; i < 3; ++i) {
+    Xc[i] = df_val(tot[1 + i]) / L;
+    Yc[i] = df_val(tot[4 + i]) / L;
+  }
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) {
+      df a = tot[7 + i + 3 * j];
+      df_add_prod(a, -L * Xc[i], Yc[j]);
+      S[i + 3 * j] = df_val(a);
+    }
+}
+
+// ------------------------------------------------------------------ Softassign
+constexpr int kSaNV = 32;
+
+// Sinkhorn sweep element: acc += K * weight(streamed).
+struct SinkElem {
+  float nk, c0;  // K = 2^(c0 + nk d^2)
+  __device__ __forceinline__ void operator()(float (&acc)[1], const float (&p)[3], float4 s,
+                                             float4) const {
+    const float dx = s.x - p[0];
+    const float dy = s.y - p[1];
+    const float dz = s.z - p[2];
+    float d2 = dx * dx;
+    d2 = fmaf(dy, dy, d2);
+    d2 = fmaf(dz, dz, d2);
+    const float e = ex2_approx(fmaf(d2, nk, c0));
+    acc[0] = fmaf(e, s.w, acc[0]);
+  }
+};
+
+// Final row sweep element: w += K b, mu += K delta, Vhat += K g (y' - Yhat).
+struct FinalElem {
+  float nk, c0;
+  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 s,
+                                             float4 h) const {
+    const float dx = s.x - p[0];
+    const float dy = s.y - p[1];
+    const float dz = s.z - p[2];
+    float d2 = dx * dx;
+    d2 = fmaf(dy, dy, d2);
+    d2 = fmaf(dz, dz, d2);
+    const float e = ex2_approx(fmaf(d2, nk, c0));
+    acc[0] = fmaf(e, s.w, acc[0]);
+    acc[1] = fmaf(e, h.w, acc[1]);
+    acc[2] = fmaf(e, h.x, acc[2]);
+    acc[3] = fmaf(e, h.y, acc[3]);
+    acc[4] = fmaf(e, h.z, acc[4]);
+  }
+};
+
+// Final row finalize: w, mu = m - w, Vhat (times a_r) and the 28 row-side moments.
+//  0: sum w            1-3: sum w x'         4-12: sum w x'_i Vhat_j (i + 3j)
+// 13-15: sum Vhat       16-18: sum w mu x'    19: sum mu
+// 20-22: sum w^2 x'     23: sum w^2           24-26: sum w Vhat      27: sum w mu
+struct FinalFin {
+  const float4* rows;
+  const float* a;  // a^(I1)
+  float* w_out;
+  int N;
+  df* scratch;     // shared, >= 33 * 128 dfs
+  df* rbpart;      // this update's row-block records [nblk_r][32] (slots 0..27 used)
+  __device__ void operator()(int blk, const float (&tot)[5]) const {
+    df v[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = df_make(0.f);
+    const int r = blk * kBlockPts + (int)threadIdx.x;
+    if (threadIdx.x < kBlockPts && r < N) {
+      const float4 x = __ldcg(&rows[r]);
+      const float ar = __ldcg(a + r);
+      const float w = ar * tot[0], mu = ar * tot[1];
+      const float V[3] = {ar * tot[2], ar * tot[3], ar * tot[4]};
+      const float xp[3] = {x.x, x.y, x.z};
+      if (w_out) w_out[r] = w;
+      const float w2 = w * w, wmu = w * mu;
+      df_add(v[0], w);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        df_add_prod(v[1 + i], w, xp[i]);
+        const float wx = w * xp[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) df_add_prod(v[4 + i + 3 * j], wx, V[j]);
+        df_add(v[13 + i], V[i]);
+        df_add_prod(v[16 + i], wmu, xp[i]);
+        df_add_prod(v[20 + i], w2, xp[i]);
+        df_add_prod(v[24 + i], w, V[i]);
+      }
+      df_add(v[19], mu);
+      df_add_prod(v[23], w, w);
+      df_add_prod(v[27], w, mu);
+    }
+    owned_block_sum<32>(v, scratch, rbpart + (size_t)blk * 32);
+  }
+};
+
+// df helpers for the moment assembly
+__device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df precision
+  df r = df_make(0.f);
+  df_add_prod(r, a.hi, b);
+  r.lo = __fmaf_rn(a.lo, b, r.lo);
+  return r;
+}
+__device__ __forceinline__ df dsub(df a, const df& b) {
+  df_add(a, df{-b.hi, -b.lo});
+  return a;
+}
+
+// Softassign S and centres from the 32 moments, one value per thread
+// (tid 0..8: S_ij, tid 9..11: centres). oX, oY: centring offsets; yh: mean(Y').
+//   Yc = (B2 + oY B1)/A1, alpha = Yhat + oY, beta = alpha - Yc,
+//   S_ij = (T1_ij - Xc'_i T3_j) + (T4_i - Xc'_i T5) alpha_j + (T6_i - Xc'_i A1) beta_j
+//        + oX_i (T8_j - T3_j) + (T9 - T5) oX_i alpha_j + (T7 - A1) oX_i beta_j
+__device__ __forceinline__ void sa_moments_to_S(int tid, const df* s_tot, const float* oX, const float* oY,
+                                                const float* yh, float* s_S, float* s_xcp, float* s_yd,
+                                                float* s_xc, float* s_yc) {
+  const df A1 = s_tot[0];
+  const float inv = 1.f / df_val(A1);
+  const float rho = df_val(s_tot[28]) * inv;
+  if (tid < 9) {
+    const int i = tid % 3, j = tid / 3;
+    const float xi = df_val(s_tot[1 + i]) * inv;
+    const float al = yh[j] + oY[j];
+    df bj = df_make(yh[j]);  // beta_j = (Yhat_j - B2_j/A1) - (rho - 1) oY_j
+    df_add(bj, -df_val(s_tot[29 + j]) * inv);
+    df_add_prod(bj, 1.f - rho, oY[j]);
+    const float be = df_val(bj);
+    const df T5 = s_tot[19], T7 = s_tot[23], T9 = s_tot[27];
+    df P2 = s_tot[16 + i];
+    df_add(P2, dmul(T5, -xi));
+    df P3 = s_tot[20 + i];
+    df_add(P3, dmul(A1, -xi));
+    df sij = s_tot[4 + i + 3 * j];
+    df_add(sij, dmul(s_tot[13 + j], -xi));
+    df_add(sij, dmul(P2, al));
+    df_add(sij, dmul(P3, be));
+    df_add(sij, dmul(dsub(s_tot[24 + j], s_tot[13 + j]), oX[i]));
+    df_add(sij, dmul(dsub(T9, T5), oX[i] * al));
+    df_add(sij, dmul(dsub(T7, A1), oX[i] * be));
+    s_S[i + 3 * j] = df_val(sij);
+  } else {
+    const int i = tid - 9;
+    const float xi = df_val(s_tot[1 + i]) * inv;
+    s_xcp[i] = xi;
+    s_xc[i] = xi + oX[i];
+    df yd = df_make(df_val(s_tot[29 + i]) * inv);  // Yc - oY = B2/A1 + (rho - 1) oY
+    df_add_prod(yd, rho - 1.f, oY[i]);
+    s_yd[i] = df_val(yd);
+    df yc = yd;
+    df_add(yc, oY[i]);
+    s_yc[i] = df_val(yc);
+  }
+}
+
+}  // namespace cesa

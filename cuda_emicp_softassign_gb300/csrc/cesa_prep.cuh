@@ -45,11 +45,11 @@ __device__ __forceinline__ float exact_offset(double mean, float lo, float hi) {
   return (float)(rint(mean / (double)q) * (double)q);
 }
 
-static __global__ void prep_center_kernel(const float* __restrict__ X, int N, const float* __restrict__ Y,
-                                          int M, CenterHdr* hdr) {
-  // One block: means (df) and extents of X and Y, exact offsets, and the means
-  // of the centred clouds (EM-ICP rows with C_r <= 1e-6 use mean(X'); the
-  // Softassign final sweep centres its Y moments on mean(Y')).
+// One block of up to 1024 threads: means (df) and extents of X and Y, exact
+// offsets, and the means of the centred clouds (EM-ICP rows with C_r <= 1e-6
+// use mean(X'); the Softassign final sweep centres its Y moments on mean(Y')).
+__device__ __forceinline__ void center_block(const float* __restrict__ X, int N, const float* __restrict__ Y,
+                                             int M, CenterHdr* hdr) {
   __shared__ df red[6 * (1024 / 32)];
   __shared__ float s_lo[12][32], s_hi[12][32];
   __shared__ float s_o[6];
@@ -115,6 +115,11 @@ static __global__ void prep_center_kernel(const float* __restrict__ X, int N, co
     }
     hdr->oX[3] = hdr->oY[3] = hdr->xmean[3] = hdr->ymean[3] = 0.f;
   }
+}
+
+static __global__ void __launch_bounds__(1024) prep_center_kernel(const float* __restrict__ X, int N, const float* __restrict__ Y,
+                                          int M, CenterHdr* hdr) {
+  center_block(X, N, Y, M, hdr);
 }
 
 // SoA -> centred float4 (x - o, w0).

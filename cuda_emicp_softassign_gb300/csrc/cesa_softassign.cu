@@ -29,13 +29,11 @@
 // centred terms (Vhat, mu = m - w), so S is formed without the cancellation
 // of large sums at high temperature, where the assignment is nearly uniform.
 #include "cesa_kernels.h"
+#include "cesa_ops.cuh"
 #include "cesa_pose.h"
 #include "cesa_prep.cuh"
-#include "cesa_sweep.cuh"
 
 namespace cesa {
-
-constexpr int kSaNV = 32;
 
 struct SoftArgs {
   const float4* rows;  // X' centred (N)
@@ -218,98 +216,6 @@ struct FinalPrep {
   }
 };
 
-// Sinkhorn sweep element: acc += K * weight(streamed).
-struct SinkElem {
-  float nk, c0;  // K = 2^(c0 + nk d^2)
-  __device__ __forceinline__ void operator()(float (&acc)[1], const float (&p)[3], float4 s,
-                                             float4) const {
-    const float dx = s.x - p[0];
-    const float dy = s.y - p[1];
-    const float dz = s.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(fmaf(d2, nk, c0));
-    acc[0] = fmaf(e, s.w, acc[0]);
-  }
-};
-
-// Final row sweep element: w += K b, mu += K delta, Vhat += K g (y' - Yhat).
-struct FinalElem {
-  float nk, c0;
-  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 s,
-                                             float4 h) const {
-    const float dx = s.x - p[0];
-    const float dy = s.y - p[1];
-    const float dz = s.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(fmaf(d2, nk, c0));
-    acc[0] = fmaf(e, s.w, acc[0]);
-    acc[1] = fmaf(e, h.w, acc[1]);
-    acc[2] = fmaf(e, h.x, acc[2]);
-    acc[3] = fmaf(e, h.y, acc[3]);
-    acc[4] = fmaf(e, h.z, acc[4]);
-  }
-};
-
-// Final row finalize: w, mu = m - w, Vhat (times a_r) and the 28 row-side moments.
-//  0: sum w            1-3: sum w x'         4-12: sum w x'_i Vhat_j (i + 3j)
-// 13-15: sum Vhat       16-18: sum w mu x'    19: sum mu
-// 20-22: sum w^2 x'     23: sum w^2           24-26: sum w Vhat      27: sum w mu
-struct FinalFin {
-  const float4* rows;
-  const float* a;  // a^(I1)
-  float* w_out;
-  int N;
-  df* scratch;     // shared, >= 33 * 128 dfs
-  df* rbpart;      // this update's row-block records [nblk_r][32] (slots 0..27 used)
-  __device__ void operator()(int blk, const float (&tot)[5]) const {
-    df v[32];
-#pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] = df_make(0.f);
-    const int r = blk * kBlockPts + (int)threadIdx.x;
-    if (threadIdx.x < kBlockPts && r < N) {
-      const float4 x = __ldcg(&rows[r]);
-      const float ar = __ldcg(a + r);
-      const float w = ar * tot[0], mu = ar * tot[1];
-      const float V[3] = {ar * tot[2], ar * tot[3], ar * tot[4]};
-      const float xp[3] = {x.x, x.y, x.z};
-      if (w_out) w_out[r] = w;
-      const float w2 = w * w, wmu = w * mu;
-      df_add(v[0], w);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        df_add_prod(v[1 + i], w, xp[i]);
-        const float wx = w * xp[i];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) df_add_prod(v[4 + i + 3 * j], wx, V[j]);
-        df_add(v[13 + i], V[i]);
-        df_add_prod(v[16 + i], wmu, xp[i]);
-        df_add_prod(v[20 + i], w2, xp[i]);
-        df_add_prod(v[24 + i], w, V[i]);
-      }
-      df_add(v[19], mu);
-      df_add_prod(v[23], w, w);
-      df_add_prod(v[27], w, mu);
-    }
-    owned_block_sum<32>(v, scratch, rbpart + (size_t)blk * 32);
-  }
-};
-
-// df helpers for the moment assembly
-__device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df precision
-  df r = df_make(0.f);
-  df_add_prod(r, a.hi, b);
-  r.lo = __fmaf_rn(a.lo, b, r.lo);
-  return r;
-}
-__device__ __forceinline__ df dsub(df a, const df& b) {
-  df_add(a, df{-b.hi, -b.lo});
-  return a;
-}
-
 __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
@@ -461,50 +367,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                                 A.gr.nblk + A.gr.slices, s_red, s_tot);
       tl.mark(6);
       // S_ij by threads 0..8, centres by threads 9..11, then the pose by thread 0.
-      //   Yc = (B2 + oY B1)/A1, alpha = Yhat + oY, beta = alpha - Yc,
-      //   S_ij = (T1_ij - Xc'_i T3_j) + (T4_i - Xc'_i T5) alpha_j + (T6_i - Xc'_i A1) beta_j
-      //        + oX_i (T8_j - T3_j) + (T9 - T5) oX_i alpha_j + (T7 - A1) oX_i beta_j
-      if (tid < 12) {
-        const float* oX = &s_hdr[0];
-        const float* oY = &s_hdr[3];
-        const float* yh = &s_hdr[6];
-        const df A1 = s_tot[0];
-        const float inv = 1.f / df_val(A1);
-        const float rho = df_val(s_tot[28]) * inv;
-        if (tid < 9) {
-          const int i = tid % 3, j = tid / 3;
-          const float xi = df_val(s_tot[1 + i]) * inv;
-          const float al = yh[j] + oY[j];
-          df bj = df_make(yh[j]);  // beta_j = (Yhat_j - B2_j/A1) - (rho - 1) oY_j
-          df_add(bj, -df_val(s_tot[29 + j]) * inv);
-          df_add_prod(bj, 1.f - rho, oY[j]);
-          const float be = df_val(bj);
-          const df T5 = s_tot[19], T7 = s_tot[23], T9 = s_tot[27];
-          df P2 = s_tot[16 + i];
-          df_add(P2, dmul(T5, -xi));
-          df P3 = s_tot[20 + i];
-          df_add(P3, dmul(A1, -xi));
-          df sij = s_tot[4 + i + 3 * j];
-          df_add(sij, dmul(s_tot[13 + j], -xi));
-          df_add(sij, dmul(P2, al));
-          df_add(sij, dmul(P3, be));
-          df_add(sij, dmul(dsub(s_tot[24 + j], s_tot[13 + j]), oX[i]));
-          df_add(sij, dmul(dsub(T9, T5), oX[i] * al));
-          df_add(sij, dmul(dsub(T7, A1), oX[i] * be));
-          s_S[i + 3 * j] = df_val(sij);
-        } else {
-          const int i = tid - 9;
-          const float xi = df_val(s_tot[1 + i]) * inv;
-          s_xcp[i] = xi;
-          s_xc[i] = xi + oX[i];
-          df yd = df_make(df_val(s_tot[29 + i]) * inv);  // Yc - oY = B2/A1 + (rho - 1) oY
-          df_add_prod(yd, rho - 1.f, oY[i]);
-          s_yd[i] = df_val(yd);
-          df yc = yd;
-          df_add(yc, oY[i]);
-          s_yc[i] = df_val(yc);
-        }
-      }
+      if (tid < 12)
+        sa_moments_to_S(tid, s_tot, &s_hdr[0], &s_hdr[3], &s_hdr[6], s_S, s_xcp, s_yd, s_xc, s_yc);
       __syncthreads();
       if (tid == 0) {
         const float* oX = &s_hdr[0];

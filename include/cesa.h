@@ -133,6 +133,43 @@ int cesa_emicp_device(const float* dX, int N, const float* dY, int M, float* dRt
 int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float* dRt,
                            const cesa_params* p, int* d_status, cesa_stream_t stream);
 
+/* Algorithms of a batched registration (cesa_pair.algorithm). */
+#define CESA_ALGO_EMICP 0
+#define CESA_ALGO_SOFTASSIGN 1
+#define CESA_MAX_BATCH 1024 /* pairs per batched call */
+
+/* One registration of a batch: emicp() or softassign() of X (target) and Y
+ * (source), src/3dregistration.h:82-90. X, Y and Rt are device pointers for
+ * cesa_register_batch_device and host pointers for cesa_register_batch. Rt
+ * holds R (row-major, 9 floats) then t (3): the initial guess on entry, the
+ * estimate on return. params: the pair's registrationParameters fields; the
+ * sigma_* and d_02 fields drive EM-ICP, JMAX, I0, I1, alpha, T_0, TFACTOR and
+ * moutlier drive Softassign. */
+typedef struct cesa_pair {
+  int algorithm; /* CESA_ALGO_* */
+  int N;         /* points in X */
+  int M;         /* points in Y */
+  const float* X;
+  const float* Y;
+  float* Rt;
+  cesa_params params;
+} cesa_pair;
+
+/*
+ * Batched registration: every pair of `pairs` (uneven sizes, EM-ICP and
+ * Softassign mixed) in one persistent launch, replacing one emicp() or
+ * softassign() call per pair. The pairs advance in lock step through their own
+ * schedules; each step of every pair is split into (pair, tile) units that all
+ * blocks of the GPU share. Each pair's result equals a single-pair call of the
+ * same algorithm up to FP32 rounding of the summation order (the Sinkhorn
+ * passes complete in a different place). npairs <= CESA_MAX_BATCH. The device
+ * variant enqueues on `stream` and writes the device status to *d_status when
+ * non-NULL; the host variant copies the clouds in and the poses out and
+ * returns when they are written.
+ */
+int cesa_register_batch_device(const cesa_pair* pairs, int npairs, int* d_status, cesa_stream_t stream);
+int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* report);
+
 /*
  * EM-ICP with no device allocation. No counterpart in the reference: this is
  * for callers that cannot call cudaMalloc, such as a plugin inside a host
@@ -202,6 +239,15 @@ void cesa_release_workspaces(void);
 
 /* Human-readable name of a status code. */
 const char* cesa_status_string(int status);
+
+/* Self-test of the bounded device-side waits (no counterpart in the
+ * reference). Runs, on the current device, the grid barrier (which = 0) or the
+ * mbarrier wait (which = 1) used by the registration kernels on a barrier that
+ * nothing completes, with a limit of timeout_us microseconds. The wait gives
+ * up, records CESA_ERR_TIMEOUT in its control block and returns; *status_out
+ * receives that code and *where_out the waiting site's tag. Returns CESA_OK
+ * when the probe ran and the device is still usable afterwards. */
+int cesa_self_test_waits(int which, int timeout_us, int* status_out, int* where_out);
 
 /* Library version as major*10000 + minor*100 + patch. */
 int cesa_version(void);

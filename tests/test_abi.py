@@ -54,7 +54,10 @@ def test_params_mirror_matches_c_layout(cesa):
 int main(){ printf("size %zu\n", sizeof(cesa_params));
 F(JMAX)F(I0)F(I1)F(alpha)F(T_0)F(TFACTOR)F(moutlier)F(sigma_p2)F(sigma_inf)F(sigma_factor)F(d_02)
 F(maxIteration)F(sinkhorn_form)F(timeout_ms)F(device)
-printf("report %zu\n", sizeof(cesa_report)); }
+printf("report %zu\n", sizeof(cesa_report));
+printf("pair %zu\n", sizeof(cesa_pair));
+printf("pair_params %zu\n", offsetof(cesa_pair, params));
+printf("pair_Rt %zu\n", offsetof(cesa_pair, Rt)); }
 '''
     got = dict(l.split() for l in _c_layout(code).strip().splitlines())
     P = cesa.Params
@@ -63,6 +66,9 @@ printf("report %zu\n", sizeof(cesa_report)); }
         if name in got:
             assert int(got[name]) == getattr(P, name).offset, name
     assert int(got["report"]) == ctypes.sizeof(cesa.Report)
+    assert int(got["pair"]) == ctypes.sizeof(cesa.Pair)
+    assert int(got["pair_params"]) == cesa.Pair.params.offset
+    assert int(got["pair_Rt"]) == cesa.Pair.Rt.offset
 
 
 def test_registration_parameters_layout_matches_reference():
@@ -130,6 +136,32 @@ def test_invalid_arguments_are_rejected(cesa):
     bad = cesa.Params.default(I1=0)  # the reference would read uninitialised column sums
     assert L.cesa_softassign(ptr(X), 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(bad), None) == cesa.CESA_ERR_INVALID_ARGUMENT
     assert cesa.status_string(cesa.CESA_ERR_TIMEOUT) == "device-side wait timed out"
+
+
+def test_invalid_batches_are_rejected(cesa):
+    L = cesa.lib()
+    X = np.zeros(6, np.float32)
+    rt = np.zeros(12, np.float32)
+    arr = (cesa.Pair * 2)()
+    for k in range(2):
+        arr[k].algorithm = cesa.ALGO_EMICP
+        arr[k].N = arr[k].M = 2
+        arr[k].X = arr[k].Y = X.ctypes.data
+        arr[k].Rt = rt.ctypes.data
+        arr[k].params = cesa.Params.default()
+    call = lambda n: L.cesa_register_batch(ctypes.cast(arr, ctypes.c_void_p), n, None)  # noqa: E731
+    assert call(0) == cesa.CESA_ERR_INVALID_ARGUMENT
+    arr[1].algorithm = 7
+    assert call(2) == cesa.CESA_ERR_INVALID_ARGUMENT
+    arr[1].algorithm = cesa.ALGO_SOFTASSIGN
+    arr[1].params = cesa.Params.default(I1=0)
+    assert call(2) == cesa.CESA_ERR_INVALID_ARGUMENT
+    arr[1].params = cesa.Params.default()
+    arr[1].M = 0
+    assert call(2) == cesa.CESA_ERR_INVALID_ARGUMENT
+    assert L.cesa_register_batch(None, 1, None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    assert L.cesa_register_batch_device(ctypes.cast(arr, ctypes.c_void_p), cesa.MAX_BATCH + 1, None,
+                                        None) == cesa.CESA_ERR_INVALID_ARGUMENT
 
 
 def test_no_cpu_fallback_without_gpu(cesa):
