@@ -433,7 +433,7 @@ int cesa_register_batch_device(const cesa_pair* pairs, int npairs, int* d_status
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  cudaError_t e = C.ws.ensure(batch_ws_need(rec.data(), npairs));
+  cudaError_t e = C.ws.ensure(batch_ws_need(rec.data(), npairs, dev));
   if (e != cudaSuccess) return map_cuda(e);
   C.last_kind = 3;
   C.last_trace_steps = 0;
@@ -482,7 +482,7 @@ int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* rep) {
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(dpose, hpose.data(), sizeof(float) * hpose.size(), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = C.ws.ensure(batch_ws_need(rec.data(), npairs));
+  if (e == cudaSuccess) e = C.ws.ensure(batch_ws_need(rec.data(), npairs, dev));
   if (e != cudaSuccess) return map_cuda(e);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEventCreate(&ev0);

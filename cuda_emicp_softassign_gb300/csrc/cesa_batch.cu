@@ -24,6 +24,7 @@
 // two agree to rounding, not bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "cesa_kernels.h"
@@ -43,8 +44,10 @@ constexpr int kStateFloats = 64;
 constexpr int kStateHorn = 16;
 static_assert(sizeof(HornState<float>) == 20 * sizeof(float), "Horn state layout");
 
-// Streamed points per unit slice (two TMA chunks).
-constexpr int kBatchSlice = 2 * kChunk;
+// Streamed points per unit slice: from one to kMaxSliceChunks TMA chunks,
+// chosen so that a round holds about kUnitsPerBlock units per block.
+constexpr int kMaxSliceChunks = 8;
+constexpr double kUnitsPerBlock = 8.0;
 
 struct BPair {
   int algo;  // 0 EM-ICP, 1 Softassign
@@ -76,6 +79,7 @@ struct BatchArgs {
   const BPair* pairs;
   int npairs;
   int rounds;  // max over pairs
+  unsigned* rctr;  // [rounds] units handed out beyond the first G of each round
   Ctl* ctl;
   int* d_status;
   uint64_t timeout_ns;
@@ -174,17 +178,39 @@ __device__ __forceinline__ int pair_of_unit(const int* pref, int npairs, int u) 
   return lo;
 }
 
+// Where a unit's data lands in the stage buffers: streamed points in
+// raw[stage]; in raw2[stage] the streamed points' weights (floats [0, 512) and
+// [512, 1024)) and, with a unit's first chunk, its owned points (float4
+// [256, 384)).
+constexpr int kOwnSlot = 256;
+// With a unit's first chunk also the pair's state block (pose, sigma_p2 or T:
+// 16 floats) and centring header (16 floats), at float4 [384, 392).
+constexpr int kMetaSlot = kOwnSlot + kBlockPts;
+static_assert(kOwnSlot * 4 >= 2 * kChunk && kMetaSlot + 8 <= kChunk, "stage buffer layout");
+static_assert(sizeof(CenterHdr) == 16 * sizeof(float), "centring header layout");
+
 struct UnitRef {
   int p;
   Ph ph;
   int blk, sl;
   SweepGeom g;
   const float4* src;  // streamed points (nullptr for a Z unit)
+  const float4* own;  // owned points of the pair (all blocks)
+  const float* w0;    // weights of the streamed points, or nullptr
+  const float* w1;
+  const float* state;  // the pair's state block
+  const CenterHdr* hdr;
 };
 
 struct Task {
   const float4* src;  // nullptr: none
   int first, len;
+  const float* w0;
+  const float* w1;
+  const float4* own;  // first chunk of a unit: its owned points, else nullptr
+  int own_n;
+  const float* state;  // first chunk: the pair's state block and centring header
+  const CenterHdr* hdr;
 };
 
 __device__ __forceinline__ UnitRef resolve(const BPair* pairs, const Sched* sched, const int* pref, int npairs,
@@ -197,29 +223,56 @@ __device__ __forceinline__ UnitRef resolve(const BPair* pairs, const Sched* sche
   U.g = (U.ph.phase == kPhSaCol) ? P.g1 : P.g0;
   U.blk = lu / U.g.slices;
   U.sl = lu - U.blk * U.g.slices;
+  U.w0 = nullptr;
+  U.w1 = nullptr;
+  U.state = P.state;
+  U.hdr = P.hdr;
   switch (U.ph.phase) {
     case kPhEmE:
+      U.src = P.own1;
+      U.own = P.own0;
+      break;
     case kPhSaRow:
+      U.src = P.own1;
+      U.own = P.own0;
+      U.w0 = U.ph.k == 0 ? nullptr : P.b;
+      break;
     case kPhSaFin:
       U.src = P.own1;
+      U.own = P.own0;
+      U.w0 = P.b;
+      U.w1 = P.cs;
       break;
     case kPhSaCol:
       U.src = P.own0;
+      U.own = P.own1;
+      U.w0 = P.a;
       break;
     default:
       U.src = nullptr;
+      U.own = nullptr;
   }
   return U;
 }
 
-__device__ __forceinline__ Task first_task(const UnitRef& U) {
-  Task t{U.src, 0, 0};
-  if (!U.src) return t;
-  const int sb = U.sl * U.g.slice_len;
-  const int se = min(sb + U.g.slice_len, U.g.n_stream);
-  t.first = sb;
-  t.len = min(kChunk, se - sb);
+// The unit's chunk starting at `first` (the first chunk also carries the
+// owned points).
+__device__ __forceinline__ Task chunk_task(const UnitRef& U, int first, bool with_own) {
+  Task t{U.src, first, 0, U.w0, U.w1, nullptr, 0, nullptr, nullptr};
+  const int se = min(U.sl * U.g.slice_len + U.g.slice_len, U.g.n_stream);
+  t.len = min(kChunk, se - first);
+  if (with_own) {
+    t.own = U.own + (size_t)U.blk * kBlockPts;
+    t.own_n = min(kBlockPts, U.g.n_own - U.blk * kBlockPts);
+    t.state = U.state;
+    t.hdr = U.hdr;
+  }
   return t;
+}
+
+__device__ __forceinline__ Task first_task(const UnitRef& U) {
+  if (!U.src) return Task{nullptr, 0, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr};
+  return chunk_task(U, U.sl * U.g.slice_len, true);
 }
 
 // Two-stage ring of TMA destinations; copies alternate between the stages.
@@ -234,46 +287,49 @@ struct Slot {
   bool valid;
 };
 
+// Issues the bulk copies of one task on the next stage's mbarrier. Weight
+// copies are rounded up to 4 floats (16 bytes): slices start at multiples of
+// 4 points and the weight arrays are padded to a multiple of 4.
 __device__ __forceinline__ Slot ring_issue(Ring& rg, SweepSmem& sm, const Task& t) {
   Slot s{rg.next, 0u, true};
   rg.next ^= 1;
   rg.uses[s.stage] += 1;
   s.par = (rg.uses[s.stage] - 1u) & 1u;
   if (threadIdx.x == 0) {
-    const unsigned bytes = (unsigned)t.len * 16u;
-    mbar_arrive_expect_tx(&sm.full[s.stage], bytes);
-    bulk_g2s(&sm.raw[s.stage][0], t.src + t.first, bytes, &sm.full[s.stage]);
+    const unsigned pbytes = (unsigned)t.len * 16u;
+    const unsigned wbytes = (unsigned)((t.len + 3) & ~3) * 4u;
+    const unsigned obytes = (unsigned)t.own_n * 16u;
+    const unsigned total = pbytes + (t.w0 ? wbytes : 0u) + (t.w1 ? wbytes : 0u) + (t.own ? obytes : 0u) +
+                           (t.state ? 128u : 0u);
+    mbar_arrive_expect_tx(&sm.full[s.stage], total);
+    bulk_g2s(&sm.raw[s.stage][0], t.src + t.first, pbytes, &sm.full[s.stage]);
+    float* wd = reinterpret_cast<float*>(&sm.raw2[s.stage][0]);
+    if (t.w0) bulk_g2s(wd, t.w0 + t.first, wbytes, &sm.full[s.stage]);
+    if (t.w1) bulk_g2s(wd + kChunk, t.w1 + t.first, wbytes, &sm.full[s.stage]);
+    if (t.own) bulk_g2s(&sm.raw2[s.stage][kOwnSlot], t.own, obytes, &sm.full[s.stage]);
+    if (t.state) {
+      bulk_g2s(&sm.raw2[s.stage][kMetaSlot], t.state, 64u, &sm.full[s.stage]);
+      bulk_g2s(&sm.raw2[s.stage][kMetaSlot + 4], t.hdr, 64u, &sm.full[s.stage]);
+    }
   }
   return s;
 }
 
 // One sweep unit: owned points (optionally posed), the slice streamed through
-// the ring chunk by chunk, then split completion. The unit's first chunk is in
-// `cur`; during its last chunk the first chunk of the block's next unit (`tn`)
-// is issued into `nslot`.
-template <int NACC, class Elem, class Prep, class Fin>
-__device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, const float4* own, bool xform,
-                               const float (&R)[9], const float (&tc)[3], Slot cur, const Task& tn, Slot& nslot,
-                               float* part, unsigned* cnt, const Elem& elem, const Prep& prep, const Fin& fin,
-                               Ctl* ctl, uint64_t timeout_ns, int where) {
-  const int warp = threadIdx.x >> 5;
+// the ring chunk by chunk, then split completion. The unit's first chunk
+// brings its owned points and the pair's state and centring header (copied to
+// `meta`: 16 state floats, then the header). `Ops` supplies the element
+// constants, the prepare step (reading the pose from meta) and the finalize
+// step. During the unit's last chunk the first chunk of the block's next unit
+// (`tn`) is issued into `nslot`.
+template <int NACC, class Ops>
+__device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool xform, Slot cur, const Task& tn,
+                               Slot& nslot, float* part, unsigned* cnt, const Ops& ops, float* meta, Ctl* ctl,
+                               uint64_t timeout_ns, int where) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const SweepGeom& g = U.g;
-  float4 ow[kOwnPerLane];
-  bool valid[kOwnPerLane];
-  load_owned(own, g.n_own, U.blk, ow, valid);
+  typename Ops::Elem elem;
   float p[kOwnPerLane][3];
-#pragma unroll
-  for (int j = 0; j < kOwnPerLane; ++j) {
-    if (xform) {
-      p[j][0] = R[0] * ow[j].x + R[1] * ow[j].y + R[2] * ow[j].z + tc[0];
-      p[j][1] = R[3] * ow[j].x + R[4] * ow[j].y + R[5] * ow[j].z + tc[1];
-      p[j][2] = R[6] * ow[j].x + R[7] * ow[j].y + R[8] * ow[j].z + tc[2];
-    } else {
-      p[j][0] = ow[j].x;
-      p[j][1] = ow[j].y;
-      p[j][2] = ow[j].z;
-    }
-  }
   float acc[kOwnPerLane][NACC];
 #pragma unroll
   for (int j = 0; j < kOwnPerLane; ++j)
@@ -285,7 +341,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, const 
     const int len = min(kChunk, se - first);
     Slot nx{0, 0u, false};
     if (first + kChunk < se) {
-      nx = ring_issue(rg, sm, Task{U.src, first + kChunk, min(kChunk, se - first - kChunk)});
+      nx = ring_issue(rg, sm, chunk_task(U, first + kChunk, false));
     } else if (tn.src) {
       nslot = ring_issue(rg, sm, tn);
     }
@@ -296,7 +352,27 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, const 
       nslot.valid = false;
       return false;
     }
-    const PrepOut pb = prep(sm, cur.stage, first, len, U.blk);
+    if (first == sb) {  // owned points, state and header arrived with the first chunk
+      const float* m = reinterpret_cast<const float*>(&sm.raw2[cur.stage][kMetaSlot]);
+      if (threadIdx.x < 32) meta[threadIdx.x] = m[threadIdx.x];
+      elem = ops.elem(m);
+      const float4* os = &sm.raw2[cur.stage][kOwnSlot];
+#pragma unroll
+      for (int j = 0; j < kOwnPerLane; ++j) {
+        const int i = lane + 32 * j;
+        const float4 o = (U.blk * kBlockPts + i < g.n_own) ? os[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (xform) {
+          p[j][0] = m[0] * o.x + m[1] * o.y + m[2] * o.z + m[9];
+          p[j][1] = m[3] * o.x + m[4] * o.y + m[5] * o.z + m[10];
+          p[j][2] = m[6] * o.x + m[7] * o.y + m[8] * o.z + m[11];
+        } else {
+          p[j][0] = o.x;
+          p[j][1] = o.y;
+          p[j][2] = o.z;
+        }
+      }
+    }
+    const PrepOut pb = ops.prep(sm, cur.stage, len, meta);
     const float4* __restrict__ bufA = pb.a;
     const float4* __restrict__ bufB = pb.b;
 #pragma unroll 2
@@ -311,62 +387,52 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, const 
   }
   float tot[NACC];
   reduce_warps<NACC>(sm, acc, tot);
-  if (split_complete<NACC>(sm, g, U.blk, U.sl, U.ph.geo_round, part, cnt, tot)) fin(U.blk, tot);
+  if (split_complete<NACC>(sm, g, U.blk, U.sl, U.ph.geo_round, part, cnt, tot)) ops.fin(U.blk, tot, meta);
   return true;
 }
 
-// ---------------------------------------------------------------- Softassign
-// Streamed Y' for a row pass: (R y' + t', b_c), b = 1 in the first pass of a
-// pose update.
-struct BRowPrep {
-  float R[9], tc[3];
-  const float* b;  // nullptr: 1
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len, int) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const float4 y = sm.raw[stage][c];
-      const float w = b ? __ldcg(b + first + c) : 1.f;
-      sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
-                               R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w);
-    }
-    __syncthreads();
-    return PrepOut{sm.prep, sm.raw2[stage]};
+// E-step: the streamed X' as loaded.
+__device__ __forceinline__ PrepOut prep_raw(SweepSmem& sm, int stage) { return PrepOut{sm.raw[stage], sm.raw[stage]}; }
+
+// Streamed Y' posed by (R, t') = meta[0..11]: (R y' + t', w) with w from the
+// stage's weights, or 1.
+__device__ __forceinline__ PrepOut prep_posed(SweepSmem& sm, int stage, int len, const float* m, bool unit_weight) {
+  const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
+  for (int c = threadIdx.x; c < len; c += kThreads) {
+    const float4 y = sm.raw[stage][c];
+    sm.prep[c] = make_float4(m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9], m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10],
+                             m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11], unit_weight ? 1.f : w[c]);
   }
-};
+  __syncthreads();
+  return PrepOut{sm.prep, sm.prep};
+}
 
 // Streamed X' for a column pass: (x', a_r) with a from the completed row pass.
-struct BColPrep {
-  const float* a;
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len, int) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const float4 x = sm.raw[stage][c];
-      sm.prep[c] = make_float4(x.x, x.y, x.z, __ldcg(a + first + c));
-    }
-    __syncthreads();
-    return PrepOut{sm.prep, sm.raw2[stage]};
+__device__ __forceinline__ PrepOut prep_weighted(SweepSmem& sm, int stage, int len) {
+  const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
+  for (int c = threadIdx.x; c < len; c += kThreads) {
+    const float4 x = sm.raw[stage][c];
+    sm.prep[c] = make_float4(x.x, x.y, x.z, w[c]);
   }
-};
+  __syncthreads();
+  return PrepOut{sm.prep, sm.prep};
+}
 
 // Streamed Y' for the final sweep: (R y' + t', b) and (g (y' - Yhat), b (cs - 1))
-// with g = b cs, from the completed last column pass.
-struct BFinPrep {
-  float R[9], tc[3], yh[3];
-  const float* b;
-  const float* cs;
-  __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len, int) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const float4 y = sm.raw[stage][c];
-      const float bn = __ldcg(b + first + c), csv = __ldcg(cs + first + c);
-      const float g = bn * csv;
-      sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
-                               R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn);
-      sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]), bn * (csv - 1.f));
-    }
-    __syncthreads();
-    return PrepOut{sm.prep, sm.prep2};
+// with g = b cs, from the completed last column pass; Yhat = meta[28..30].
+__device__ __forceinline__ PrepOut prep_final(SweepSmem& sm, int stage, int len, const float* m) {
+  const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
+  for (int c = threadIdx.x; c < len; c += kThreads) {
+    const float4 y = sm.raw[stage][c];
+    const float bn = w[c], csv = w[kChunk + c];
+    const float g = bn * csv;
+    sm.prep[c] = make_float4(m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9], m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10],
+                             m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11], bn);
+    sm.prep2[c] = make_float4(g * (y.x - m[28]), g * (y.y - m[29]), g * (y.z - m[30]), bn * (csv - 1.f));
   }
-};
+  __syncthreads();
+  return PrepOut{sm.prep, sm.prep2};
+}
 
 // Row pass completion (normalizeMbySinkhorn_row + Saxpy, src/softassign.cu:538-561):
 //   rs = a_old (K b row sum) + s_old,  a = a_old / rs,  s = s_old / rs.
@@ -427,15 +493,79 @@ struct BColFin {
   }
 };
 
-// ---------------------------------------------------------------- pose tasks
-__device__ __forceinline__ void load_pose(const float* state, float* s_pose) {
-  if (threadIdx.x < 12) s_pose[threadIdx.x] = __ldcg(state + threadIdx.x);
-  __syncthreads();
+// Per-phase operations of a sweep unit. meta: state floats [0..15] (R, t',
+// sigma_p2 or T at [12]), centring header [16..31] (oX, oY, xmean, ymean).
+struct EmOps {  // EM-ICP E-step
+  using Elem = EmicpElem;
+  const BPair* P;
+  df* scratch;
+  __device__ __forceinline__ Elem elem(const float* m) const { return EmicpElem{-kLog2e / (2.f * m[12])}; }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int, const float*) const {
+    return prep_raw(sm, stage);
+  }
+  __device__ __forceinline__ void fin(int blk, const float (&tot)[5], const float* m) const {
+    const EmicpFin f{P->own0, P->M, expf(-P->d_02 / m[12]),  // src/emicp.cu:489
+                     {m[24], m[25], m[26]}, nullptr, {m[16], m[17], m[18]}, scratch, P->rec};
+    f(blk, tot);
+  }
+};
+
+// K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
+__device__ __forceinline__ SinkElem sink_elem(float alpha, float T) {
+  const float kk = kLog2e / T;
+  return SinkElem{-kk, fmaf(alpha, kk, -0.5f * log2f(T))};
 }
 
+struct RowOps {  // Sinkhorn row pass k
+  using Elem = SinkElem;
+  const BPair* P;
+  bool first;
+  __device__ __forceinline__ Elem elem(const float* m) const { return sink_elem(P->alpha, m[12]); }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
+    return prep_posed(sm, stage, len, m, first);
+  }
+  __device__ __forceinline__ void fin(int blk, const float (&tot)[1], const float*) const {
+    const BRowFin f{P->a, P->s, P->rs, P->N, first};
+    f(blk, tot);
+  }
+};
+
+struct ColOps {  // Sinkhorn column pass k
+  using Elem = SinkElem;
+  const BPair* P;
+  bool first, last;
+  df* scratch;
+  __device__ __forceinline__ Elem elem(const float* m) const { return sink_elem(P->alpha, m[12]); }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float*) const {
+    return prep_weighted(sm, stage, len);
+  }
+  __device__ __forceinline__ void fin(int blk, const float (&tot)[1], const float*) const {
+    const BColFin f{P->b, P->u, P->cs, P->M, first, last, P->own1, scratch, P->rec + (size_t)P->g0.nblk * 32};
+    f(blk, tot);
+  }
+};
+
+struct FinOps {  // Softassign final sweep
+  using Elem = FinalElem;
+  const BPair* P;
+  df* scratch;
+  __device__ __forceinline__ Elem elem(const float* m) const {
+    const SinkElem e = sink_elem(P->alpha, m[12]);
+    return FinalElem{e.nk, e.c0};
+  }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
+    return prep_final(sm, stage, len, m);
+  }
+  __device__ __forceinline__ void fin(int blk, const float (&tot)[5], const float*) const {
+    const FinalFin f{P->own0, P->a, nullptr, P->N, scratch, P->rec};
+    f(blk, tot);
+  }
+};
+
+// ---------------------------------------------------------------- pose tasks
 // Horn solve + pose store by thread 0; the carried eigenbasis lives in the
 // pair's state block between solves.
-__device__ void horn_update(const BPair& P, const float S[9], const float Xcp[3], const float Yd[3], int step,
+__device__ __noinline__ void horn_update(const BPair& P, const float S[9], const float Xcp[3], const float Yd[3], int step,
                             bool last) {
   HornState<float> st;
   float* sv = reinterpret_cast<float*>(&st);
@@ -455,7 +585,7 @@ __device__ void horn_update(const BPair& P, const float S[9], const float Xcp[3]
   (void)step;
 }
 
-__device__ void em_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot) {
+__device__ __noinline__ void em_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot) {
   reduce_block_partials<kEmNV>(P.rec, P.g0.nblk, s_red, s_tot);
   if (threadIdx.x == 0) {
     float Xc[3], Yc[3], S[9];
@@ -466,7 +596,7 @@ __device__ void em_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot) 
   __syncthreads();
 }
 
-__device__ void sa_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot, float* s_S, float* s_v) {
+__device__ __noinline__ void sa_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot, float* s_S, float* s_v) {
   reduce_block_partials<kSaNV>(P.rec, P.g0.nblk + P.g1.nblk, s_red, s_tot);
   if (threadIdx.x < 12) {
     const CenterHdr* h = P.hdr;
@@ -493,7 +623,7 @@ __global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchArgs A) {
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
   Sched* s_sched = reinterpret_cast<Sched*>(smem_raw + sizeof(SweepSmem));
   int* s_pref = reinterpret_cast<int*>(s_sched + A.npairs);
-  __shared__ float s_pose[12];
+  __shared__ float s_meta[32];
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[kSaNV];
   __shared__ float s_S[9], s_v[12];
@@ -513,23 +643,45 @@ __global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchArgs A) {
   Ring rg{{0u, 0u}, 0};
   unsigned epoch = 0;
   bool ok = true;
+  // Units of a round: block b starts with unit b; further units are handed
+  // out by the round's counter. Thread 0 requests one unit ahead, so the
+  // atomic's latency is hidden behind the current unit (and the first request
+  // of a round is issued before the previous round's barrier).
+  __shared__ int s_next;
+  __shared__ UnitRef s_cur;
+  __shared__ Task s_tn;
+  unsigned pending = 0;  // thread 0: next unit of this round
+  if (tid == 0) pending = (unsigned)G + atomicAdd(&A.rctr[0], 1u);
   for (int r = 0; r < A.rounds && ok; ++r) {
+    // Weights copied by TMA this round were written by other blocks in earlier
+    // rounds (generic proxy, ordered by the grid barrier); the proxy fence
+    // makes them visible to the async proxy of the copies thread 0 issues.
+    if (tid == 0 && r > 0) asm volatile("fence.proxy.async.global;" ::: "memory");
     round_prefix(s_sched, A.npairs, r, s_pref);
     const int total = s_pref[A.npairs];
     int u = blockIdx.x;
     if (u < total) {
-      UnitRef cur = resolve(A.pairs, s_sched, s_pref, A.npairs, r, u);
       Slot slot{0, 0u, false};
-      const Task t0 = first_task(cur);
-      if (t0.src) slot = ring_issue(rg, sm, t0);
+      {
+        const Task t0 = first_task(resolve(A.pairs, s_sched, s_pref, A.npairs, r, u));
+        if (t0.src) slot = ring_issue(rg, sm, t0);
+      }
       for (;;) {
-        const int un = u + G;
-        UnitRef nxt{};
-        Task tn{nullptr, 0, 0};
-        if (un < total) {
-          nxt = resolve(A.pairs, s_sched, s_pref, A.npairs, r, un);
-          tn = first_task(nxt);
+        // The unit and the next unit's first copy are block-uniform: thread 0
+        // resolves them into shared memory (read where used, not held in
+        // registers across the streaming loop).
+        if (tid == 0) {
+          const int nxt = (int)min(pending, 0x7fffffffu);
+          pending = (unsigned)G + atomicAdd(&A.rctr[r], 1u);
+          s_next = nxt;
+          s_cur = resolve(A.pairs, s_sched, s_pref, A.npairs, r, u);
+          s_tn = nxt < total ? first_task(resolve(A.pairs, s_sched, s_pref, A.npairs, r, nxt))
+                             : Task{nullptr, 0, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr};
         }
+        __syncthreads();
+        const UnitRef& cur = s_cur;
+        const int un = s_next;
+        const Task& tn = s_tn;
         const BPair& P = A.pairs[cur.p];
         Slot ns{0, 0u, false};
         if (cur.ph.phase == kPhEmZ || cur.ph.phase == kPhSaZ) {
@@ -537,67 +689,30 @@ __global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchArgs A) {
           if (cur.ph.phase == kPhEmZ) em_finalize(P, cur.ph, s_red, s_tot);
           else sa_finalize(P, cur.ph, s_red, s_tot, s_S, s_v);
         } else {
-          load_pose(P.state, s_pose);
-          float R[9], tc[3];
-#pragma unroll
-          for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
-          const float par = __ldcg(P.state + 12);  // sigma_p2 or T
           df* scratch = reinterpret_cast<df*>(sm.prep);
-          if (cur.ph.phase == kPhEmE) {
-            const EmicpElem elem{-kLog2e / (2.f * par)};
-            const CenterHdr* h = P.hdr;
-            const EmicpFin fin{P.own0, P.M, expf(-P.d_02 / par),  // src/emicp.cu:489
-                               {h->xmean[0], h->xmean[1], h->xmean[2]}, nullptr,
-                               {h->oX[0], h->oX[1], h->oX[2]}, scratch, P.rec};
-            ok = run_sweep_unit<5>(sm, rg, cur, P.own0, true, R, tc, slot, tn, ns, P.part, P.cnt0, elem,
-                                   NoPrep{}, fin, A.ctl, A.timeout_ns, 10);
-          } else {
-            // K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
-            const float kk = kLog2e / par;
-            const float c0 = fmaf(P.alpha, kk, -0.5f * log2f(par));
-            if (cur.ph.phase == kPhSaRow) {
-              BRowPrep prep;
-#pragma unroll
-              for (int k = 0; k < 9; ++k) prep.R[k] = R[k];
-#pragma unroll
-              for (int k = 0; k < 3; ++k) prep.tc[k] = tc[k];
-              prep.b = cur.ph.k == 0 ? nullptr : P.b;
-              const BRowFin fin{P.a, P.s, P.rs, P.N, cur.ph.k == 0};
-              ok = run_sweep_unit<1>(sm, rg, cur, P.own0, false, R, tc, slot, tn, ns, P.part, P.cnt0,
-                                     SinkElem{-kk, c0}, prep, fin, A.ctl, A.timeout_ns, 30);
-            } else if (cur.ph.phase == kPhSaCol) {
-              const BColFin fin{P.b, P.u, P.cs, P.M, cur.ph.k == 0, cur.ph.k == P.I1 - 1, P.own1, scratch,
-                                P.rec + (size_t)P.g0.nblk * 32};
-              ok = run_sweep_unit<1>(sm, rg, cur, P.own1, true, R, tc, slot, tn, ns, P.part, P.cnt1,
-                                     SinkElem{-kk, c0}, BColPrep{P.a}, fin, A.ctl, A.timeout_ns, 40);
-            } else {
-              BFinPrep prep;
-#pragma unroll
-              for (int k = 0; k < 9; ++k) prep.R[k] = R[k];
-#pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                prep.tc[k] = tc[k];
-                prep.yh[k] = P.hdr->ymean[k];
-              }
-              prep.b = P.b;
-              prep.cs = P.cs;
-              static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >=
-                                32 * (kBlockPts + 8) * sizeof(df),
-                            "moment scratch does not fit");
-              const FinalFin fin{P.own0, P.a, nullptr, P.N, scratch, P.rec};
-              ok = run_sweep_unit<5>(sm, rg, cur, P.own0, false, R, tc, slot, tn, ns, P.part, P.cnt0,
-                                     FinalElem{-kk, c0}, prep, fin, A.ctl, A.timeout_ns, 50);
-            }
-          }
+          static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >= 32 * (kBlockPts + 8) * sizeof(df),
+                        "moment scratch does not fit");
+          const BPair* PP = &A.pairs[cur.p];
+          const int k = cur.ph.k;
+          if (cur.ph.phase == kPhEmE)
+            ok = run_sweep_unit<5>(sm, rg, cur, true, slot, tn, ns, P.part, P.cnt0, EmOps{PP, scratch}, s_meta,
+                                   A.ctl, A.timeout_ns, 10);
+          else if (cur.ph.phase == kPhSaRow)
+            ok = run_sweep_unit<1>(sm, rg, cur, false, slot, tn, ns, P.part, P.cnt0, RowOps{PP, k == 0}, s_meta,
+                                   A.ctl, A.timeout_ns, 30);
+          else if (cur.ph.phase == kPhSaCol)
+            ok = run_sweep_unit<1>(sm, rg, cur, true, slot, tn, ns, P.part, P.cnt1,
+                                   ColOps{PP, k == 0, k == P.I1 - 1, scratch}, s_meta, A.ctl, A.timeout_ns, 40);
+          else
+            ok = run_sweep_unit<5>(sm, rg, cur, false, slot, tn, ns, P.part, P.cnt0, FinOps{PP, scratch}, s_meta,
+                                   A.ctl, A.timeout_ns, 50);
         }
         if (!ok || un >= total) break;
         u = un;
-        cur = nxt;
         slot = ns;
       }
     }
+    if (tid == 0 && r + 1 < A.rounds) pending = (unsigned)G + atomicAdd(&A.rctr[r + 1], 1u);
     ok = ok && grid_sync(A.ctl, epoch, (unsigned)G, A.timeout_ns, 70);
   }
   if (blockIdx.x == 0 && tid == 0) {
@@ -657,14 +772,14 @@ struct Carve {
   }
 };
 
-SweepGeom batch_geom(int n_own, int n_stream) {
+SweepGeom batch_geom(int n_own, int n_stream, int slice) {
   SweepGeom g;
   g.n_own = n_own;
   g.n_stream = n_stream;
   g.nblk = (n_own + kBlockPts - 1) / kBlockPts;
-  int S = (n_stream + kBatchSlice - 1) / kBatchSlice;
+  int S = (n_stream + slice - 1) / slice;
   if (S < 1) S = 1;
-  g.slice_len = (n_stream + S - 1) / S;
+  g.slice_len = (((n_stream + S - 1) / S) + 3) & ~3;  // slices start at multiples of 4 points
   g.slices = (n_stream + g.slice_len - 1) / g.slice_len;
   g.units = g.nblk * g.slices;
   return g;
@@ -673,21 +788,45 @@ SweepGeom batch_geom(int n_own, int n_stream) {
 // Lays out the workspace: control block, all split counters (cleared per
 // launch), the pair table, then each pair's buffers. With base == nullptr
 // only sizes are computed.
-size_t carve_batch(void* base, const BatchLaunchPair* in, int npairs, std::vector<BPair>* out, Ctl** ctl,
-                   size_t* zero_bytes, BPair** dpairs, int* rounds) {
+// Slice length for a batch on a grid of G blocks: the largest sweep round
+// (sum of N M over the pairs) in about kUnitsPerBlock * G units of 128 owned
+// points, in whole TMA chunks.
+int batch_slice(const BatchLaunchPair* in, int npairs, int G) {
+  double work = 0.0;
+  for (int i = 0; i < npairs; ++i) work += (double)in[i].N * (double)in[i].M;
+  double chunks = work / (kUnitsPerBlock * (double)G * kBlockPts * kChunk);
+  int c = (int)(chunks + 0.5);
+  if (c < 1) c = 1;
+  if (c > kMaxSliceChunks) c = kMaxSliceChunks;
+  return c * kChunk;
+}
+
+// Lays out the workspace: control block, all split counters and the round
+// counters (cleared per launch), the pair table, then each pair's buffers.
+// The pair table is ordered by decreasing size, so the largest units of a
+// round are handed out first. With base == nullptr only sizes are computed.
+size_t carve_batch(void* base, const BatchLaunchPair* in, int npairs, int G, std::vector<BPair>* out, Ctl** ctl,
+                   size_t* zero_bytes, BPair** dpairs, int* rounds, unsigned** rctr) {
   Carve c(base);
   *ctl = c.take<Ctl>(1);
+  const int slice = batch_slice(in, npairs, G);
+  std::vector<int> order((size_t)npairs);
+  for (int i = 0; i < npairs; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (double)in[a].N * in[a].M > (double)in[b].N * in[b].M;
+  });
   std::vector<BPair> v((size_t)npairs);
   size_t ncnt = 0;
+  int rmax = 0;
   for (int i = 0; i < npairs; ++i) {
-    const BatchLaunchPair& L = in[i];
+    const BatchLaunchPair& L = in[order[(size_t)i]];
     BPair& P = v[(size_t)i];
     P = BPair{};
     P.algo = L.algo;
     P.N = L.N;
     P.M = L.M;
     if (L.algo == 0) {
-      P.g0 = batch_geom(L.M, L.N);
+      P.g0 = batch_geom(L.M, L.N, slice);
       P.g1 = SweepGeom{0, 0, 0, 1, 0, 0};
       P.nsteps = L.nsteps;
       P.rounds = 2 * L.nsteps;
@@ -697,8 +836,8 @@ size_t carve_batch(void* base, const BatchLaunchPair* in, int npairs, std::vecto
       P.I0 = 1;
       P.I1 = 1;
     } else {
-      P.g0 = batch_geom(L.N, L.M);
-      P.g1 = batch_geom(L.M, L.N);
+      P.g0 = batch_geom(L.N, L.M, slice);
+      P.g1 = batch_geom(L.M, L.N, slice);
       P.nsteps = L.JMAX * L.I0;
       P.rounds = (2 * L.I1 + 2) * P.nsteps;
       P.init = L.T_0;
@@ -712,11 +851,12 @@ size_t carve_batch(void* base, const BatchLaunchPair* in, int npairs, std::vecto
     P.X = L.dX;
     P.Y = L.dY;
     P.dRt = L.dRt;
+    if (P.rounds > rmax) rmax = P.rounds;
   }
   unsigned* cnt = c.take<unsigned>(ncnt > 0 ? ncnt : 1);
+  *rctr = c.take<unsigned>((size_t)rmax + 1);
   *zero_bytes = c.off;
   *dpairs = c.take<BPair>((size_t)npairs);
-  int rmax = 0;
   size_t co = 0;
   for (int i = 0; i < npairs; ++i) {
     BPair& P = v[(size_t)i];
@@ -734,15 +874,16 @@ size_t carve_batch(void* base, const BatchLaunchPair* in, int npairs, std::vecto
     P.part = c.take<float>(part0 > part1 ? part0 : part1);
     P.rec = c.take<df>((size_t)(P.g0.nblk + P.g1.nblk) * 32);
     if (P.algo == 1) {
-      P.a = c.take<float>((size_t)P.N);
-      P.s = c.take<float>((size_t)P.N);
-      P.rs = c.take<float>((size_t)P.N);
-      P.b = c.take<float>((size_t)P.M);
-      P.u = c.take<float>((size_t)P.M);
-      P.cs = c.take<float>((size_t)P.M);
+      // padded to 4 floats: weight copies are whole 16-byte groups
+      const size_t Np = ((size_t)P.N + 3) & ~size_t(3), Mp = ((size_t)P.M + 3) & ~size_t(3);
+      P.a = c.take<float>(Np);
+      P.s = c.take<float>(Np);
+      P.rs = c.take<float>(Np);
+      P.b = c.take<float>(Mp);
+      P.u = c.take<float>(Mp);
+      P.cs = c.take<float>(Mp);
     }
     P.state = c.take<float>(kStateFloats);
-    if (P.rounds > rmax) rmax = P.rounds;
   }
   if (out) out->swap(v);
   *rounds = rmax;
@@ -755,12 +896,14 @@ size_t batch_smem(int npairs) {
 
 }  // namespace
 
-size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs) {
+size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs, int device) {
   Ctl* ctl = nullptr;
   size_t zb = 0;
   BPair* dp = nullptr;
   int rounds = 0;
-  return carve_batch(nullptr, pairs, npairs, nullptr, &ctl, &zb, &dp, &rounds);
+  unsigned* rctr = nullptr;
+  const int G = persistent_grid_limit(device, (const void*)batch_kernel, batch_smem(npairs));
+  return carve_batch(nullptr, pairs, npairs, G, nullptr, &ctl, &zb, &dp, &rounds, &rctr);
 }
 
 int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint64_t timeout_ns, void* ws,
@@ -774,7 +917,10 @@ int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint6
   size_t zero_bytes = 0;
   BPair* dpairs = nullptr;
   int rounds = 0;
-  const size_t need = carve_batch(ws, pairs, npairs, &host, &ctl, &zero_bytes, &dpairs, &rounds);
+  unsigned* rctr = nullptr;
+  const size_t smem = batch_smem(npairs);
+  const int limit = persistent_grid_limit(device, (const void*)batch_kernel, smem);
+  const size_t need = carve_batch(ws, pairs, npairs, limit, &host, &ctl, &zero_bytes, &dpairs, &rounds, &rctr);
   if (need > ws_bytes) return (int)cudaErrorInvalidValue;
   if (rounds_out) *rounds_out = rounds;
   e = cudaMemsetAsync(ws, 0, zero_bytes, st);
@@ -785,14 +931,13 @@ int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint6
   batch_pack_kernel<<<dim3(16, npairs), 256, 0, st>>>(dpairs);
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
-  const size_t smem = batch_smem(npairs);
-  const int limit = persistent_grid_limit(device, (const void*)batch_kernel, smem);
   if (grid_used) *grid_used = limit;
   if (rounds == 0) return 0;
   BatchArgs A;
   A.pairs = dpairs;
   A.npairs = npairs;
   A.rounds = rounds;
+  A.rctr = rctr;
   A.ctl = ctl;
   A.d_status = d_status;
   A.timeout_ns = timeout_ns;

@@ -97,7 +97,7 @@ size_t emicp_ws_need(int N, int M, int device);
 size_t softassign_ws_need(int N, int M, int form, int device);
 
 // Batched registration: all pairs in one persistent launch.
-size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs);
+size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs, int device);
 int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint64_t timeout_ns, void* ws,
                   size_t ws_bytes, cudaStream_t st, int* grid_used, int* rounds_out);
 
