@@ -2,7 +2,8 @@
 """Benchmark of the soft-correspondence registration path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000]
+                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000|
+                                c4_batch_256]
 
 One step is one complete registration (the whole annealing schedule) of the
 workload's seeded synthetic pair. The default workload is config 2: Softassign
@@ -16,6 +17,10 @@ ours:      `value` times the device-pointer C ABI entry point (inputs already
 reference: times the reference algorithm on the host cores (the oracle's FP32
            port of the path, all threads) on a bounded sample of the same
            workload, scaled to registrations/s.
+
+c4_batch_256: one step is one batched launch (cesa_register_batch_device) of
+the 256 pairs of config 4; value counts every pair as one registration. The
+line also reports the same pairs registered one pair per launch.
 
 Multi-GPU: one process per GPU (torchrun), independent replicas of the same
 workload; value = registrations done by all ranks / max rank time.
@@ -90,16 +95,16 @@ def algorithmic_work(kind, N, M, p):
 
     EM-ICP: per element 12 FP32-pipe ops + 1 ex2 (3 FADD, FMUL + 2 FFMA for
     d^2, FMUL scale, FFMA + FADD + 3 FFMA accumulators).
-    Softassign: per pose update 2*I1 Sinkhorn sweeps of 7 FP32 ops + 1 ex2
+    Softassign: per pose update 2*I1 Sinkhorn sweeps of 8 FP32 ops + 1 ex2
     (3 FADD, FMUL + 2 FFMA, FFMA exponent, FFMA weighted sum) and one final
-    sweep of 11 FP32 ops + 1 ex2.
+    sweep of 12 FP32 ops + 1 ex2 (the same with 5 weighted sums).
     """
     n = pose_updates(kind, p)
     e = float(N) * float(M)
     if kind == "emicp":
         return 12.0 * e * n, e * n, e * n
     sweeps = 2 * p.I1
-    return e * n * (7.0 * sweeps + 11.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
+    return e * n * (8.0 * sweeps + 12.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
 
 
 def kernels_per_registration(kind):
@@ -202,6 +207,24 @@ def cpu_baseline(kind, X, Y, p, target_s, threads=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    if args.workload == BATCH_WORKLOAD:
+        pairs = batch_workload(args.seed)
+        per_step = max(2.0, args.cpu_sample_s / max(1, args.steps + args.warmup))
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, desc, thr = batch_cpu_baseline(pairs, per_step)
+            if i >= args.warmup:
+                vals.append(v)
+        value = float(np.mean(vals))
+        line = {"impl": "reference", "metric": "registrations/s", "value": value, "unit": "registrations/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(pairs) / value,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": batch_config(args, pairs),
+                "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": thr, "kind": "port",
+                                 "sample": desc},
+                "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     kind, X, Y = workload(args.workload, args.seed)
     p = RefDefaults()
     per_step = max(2.0, args.cpu_sample_s / max(1, args.steps + args.warmup))
@@ -257,6 +280,194 @@ def whole_job_rate(steps, world, seconds):
     """Registrations per second of the whole job: every rank registers `steps`
     pairs, and the job takes the slowest rank's time."""
     return steps * world / seconds
+
+
+BATCH_WORKLOAD = "c4_batch_256"
+
+
+def batch_workload(seed, count=256):
+    """Config 4: 256 pairs, N and M log-uniform in [500, 20000], config-1
+    generator per pair; even pairs EM-ICP (default parameters), odd pairs
+    Softassign (config-2 parameters, JMAX = 60)."""
+    import cuda_emicp_softassign_gb300 as cesa
+    from cuda_emicp_softassign_gb300 import workloads as W
+    out = []
+    for kind, X, Y, _, _ in W.batch_pairs(count=count, seed=seed):
+        if kind == "emicp":
+            out.append((cesa.ALGO_EMICP, X, Y, cesa.Params.default()))
+        else:
+            out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa.Params.default(JMAX=60)))
+    return out
+
+
+def batch_work(pairs):
+    """(fp32 ops, ex2 ops, affinity elements) of one batched registration of all pairs."""
+    f = x = e = 0.0
+    for algo, X, Y, p in pairs:
+        kind = "emicp" if algo == 0 else "softassign"
+        a, b, c = algorithmic_work(kind, len(X), len(Y), p)
+        f, x, e = f + a, x + b, e + c
+    return f, x, e
+
+
+def batch_config(args, pairs):
+    n = [len(X) for _, X, _, _ in pairs]
+    m = [len(Y) for _, _, Y, _ in pairs]
+    return {"workload": BATCH_WORKLOAD, "pairs": len(pairs),
+            "emicp_pairs": sum(1 for a, _, _, _ in pairs if a == 0),
+            "softassign_pairs": sum(1 for a, _, _, _ in pairs if a == 1),
+            "N_range": [int(min(n)), int(max(n))], "M_range": [int(min(m)), int(max(m))],
+            "softassign_JMAX": 60, "seed": args.seed,
+            "l2": "flushed between steps (256 MiB write), outside the timed events",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def batch_cpu_baseline(pairs, target_s):
+    """FP32 port of the reference algorithm on the host: time per affinity
+    element measured on the first pose updates of a few pairs of the batch,
+    scaled to the batch's total elements. Returns (registrations/s, desc, threads)."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    _, _, total = batch_work(pairs)
+    spent = 0.0
+    elems = 0.0
+    used = 0
+    for algo, X, Y, p in pairs[:8]:
+        if spent > target_s:
+            break
+        t0 = time.perf_counter()
+        if algo == 0:
+            O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=p.sigma_p2 * 0.5, sigma_factor=p.sigma_factor,
+                    d_02=p.d_02, precision="f32", trace=False)
+            n = pose_updates("emicp", type("P", (), dict(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_p2 * 0.5,
+                                                          sigma_factor=p.sigma_factor))())
+            elems += float(len(X)) * len(Y) * n
+        else:
+            O.softassign(X, Y, JMAX=1, I0=1, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
+                         moutlier=p.moutlier, precision="f32", trace=False)
+            elems += float(len(X)) * len(Y) * (2 * p.I1 + 1)
+        spent += time.perf_counter() - t0
+        used += 1
+    per_elem = spent / elems
+    regs = len(pairs) / (per_elem * total)
+    desc = ("first pose updates of %d of the %d pairs (FP32 port of the reference algorithm, OpenMP): "
+            "%.3g s per affinity element, scaled to the batch's %.3g elements" % (used, len(pairs), per_elem, total))
+    return regs, desc, threads
+
+
+def run_batch(args, rank, world, local):
+    """Config 4: one step = one batched registration of all 256 pairs
+    (cesa_register_batch_device, inputs resident). Also reported: the same
+    pairs registered one pair per launch with the single-pair kernels."""
+    import torch
+    import cuda_emicp_softassign_gb300 as cesa
+
+    torch.cuda.set_device(local)
+    pairs = batch_workload(args.seed)
+    dev = []
+    pose0 = torch.tensor(np.r_[np.eye(3).reshape(-1), np.zeros(3)], dtype=torch.float32, device="cuda")
+    for algo, X, Y, p in pairs:
+        dX = torch.from_numpy(cesa.cloud2data(X)).cuda()
+        dY = torch.from_numpy(cesa.cloud2data(Y)).cuda()
+        dev.append([algo, dX, dY, pose0.clone(), p])
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def reset():
+        for d in dev:
+            d[3].copy_(pose0)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        reset()
+        cesa.register_batch_device([tuple(d) for d in dev], d_status=status, stream=stream)
+    torch.cuda.synchronize()
+    assert cesa.stream_status(stream) == 0
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        reset()
+        ev[k][0].record(stream)
+        cesa.register_batch_device([tuple(d) for d in dev], d_status=status, stream=stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    assert cesa.stream_status(stream) == 0 and int(status.item()) == 0
+    total_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+
+    # the same pairs, one pair per launch (single-pair device entry points)
+    single_ms = 0.0
+    for algo, dX, dY, dRt, p in dev:
+        dRt.copy_(pose0)
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        (cesa.emicp_device if algo == 0 else cesa.softassign_device)(dX, dY, dRt, param=p, d_status=status,
+                                                                      stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        single_ms += e0.elapsed_time(e1)
+
+    # end to end through the host-pointer batch entry point
+    e2e_steps = max(1, min(args.steps, 3))
+    cesa.register_batch(pairs)
+    e2e_s = 0.0
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cesa.register_batch(pairs)
+        e2e_s += time.perf_counter() - t0
+    e2e_s /= e2e_steps
+
+    total_ms, e2e_s, single_ms = max_over_ranks([total_ms, e2e_s, single_ms], world, "cuda")
+    if rank != 0:
+        return
+    npairs = len(pairs)
+    mean_s = total_ms * 1e-3 / args.steps
+    value = whole_job_rate(args.steps * npairs, world, total_ms * 1e-3)
+    fp32_ops, ex2_ops, elems = batch_work(pairs)
+    fp32_peak, ex2_peak = load_peaks()
+    achieved = fp32_ops / mean_s / 1e12
+    roofline = {"bound": "fp32", "kernel": "batch_kernel", "achieved": achieved,
+                "peak": fp32_peak / 1e12 if fp32_peak else None, "unit": "TFLOP/s",
+                "frac": achieved / (fp32_peak / 1e12) if fp32_peak else None, "traffic": None,
+                "peak_source": "measured in this run: FFMA lane-op rate (libcesa_peaks), FMA counted as 1 op",
+                "ex2_achieved_tops": ex2_ops / mean_s / 1e12,
+                "ex2_peak_tops": ex2_peak / 1e12 if ex2_peak else None,
+                "ops_per_batch": fp32_ops}
+    cpu_v, cpu_desc, cpu_thr = batch_cpu_baseline(pairs, args.cpu_sample_s)
+    h2d = sum((len(X) + len(Y)) * 3 * 4 + 48 for _, X, Y, _ in pairs)
+    line = {"metric": "registrations/s", "value": value, "unit": "registrations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator of config 4; see cuda_emicp_softassign_gb300/workloads.py)",
+            "config": batch_config(args, pairs),
+            "gelem_per_s": elems * args.steps * world / (total_ms * 1e-3) / 1e9,
+            "one_pair_per_launch": {"value": world * npairs / (single_ms * 1e-3), "unit": "registrations/s",
+                                    "ms": single_ms, "batched_speedup": single_ms / (total_ms / args.steps)},
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_v, "unit": "registrations/s", "cores": cpu_thr, "kind": "port",
+                             "sample": cpu_desc},
+            "e2e": {"value": world * npairs / e2e_s, "unit": "registrations/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 48 * npairs},
+            "clocks": clocks,
+            "gpu_launches": 3 * args.steps,
+            "wall_s_timed_region": t_wall}
+    print(json.dumps(line), flush=True)
 
 
 def run_ours(args, rank, world, local):
@@ -397,6 +608,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, rank, world)
+        elif args.workload == BATCH_WORKLOAD:
+            run_batch(args, rank, world, local)
         else:
             run_ours(args, rank, world, local)
     finally:

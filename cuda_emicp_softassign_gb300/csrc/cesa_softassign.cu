@@ -19,7 +19,7 @@
 // critical path). A designated unit per point stores the new scaling and slack
 // in ping-pong buffers. Each sweep element costs 3 FADD + FMUL + 2 FFMA
 // (direct-difference d^2), 1 FFMA (exponent), 1 MUFU ex2 and 1 FFMA (weighted
-// sum): 7 FP32 ops + 1 MUFU op. Per pose update there are 2*I1 + 1 sweeps and
+// sum): 8 FP32 ops + 1 MUFU op. Per pose update there are 2*I1 + 1 sweeps and
 // 2*I1 + 1 grid barriers.
 //
 // The reference's S is not translation invariant, because X is weighted and
