@@ -329,12 +329,12 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const SweepGeom& g = U.g;
   typename Ops::Elem elem;
-  float p[kOwnPerLane][3];
-  float acc[kOwnPerLane][NACC];
+  float2 q[kPairs][3];
+  float2 acc[kPairs][NACC];
 #pragma unroll
-  for (int j = 0; j < kOwnPerLane; ++j)
+  for (int k = 0; k < kPairs; ++k)
 #pragma unroll
-    for (int a = 0; a < NACC; ++a) acc[j][a] = 0.f;
+    for (int a = 0; a < NACC; ++a) acc[k][a] = make_float2(0.f, 0.f);
   nslot.valid = false;
   const int sb = U.sl * g.slice_len, se = min(sb + g.slice_len, g.n_stream);
   for (int first = sb; first < se; first += kChunk) {
@@ -357,6 +357,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
       if (threadIdx.x < 32) meta[threadIdx.x] = m[threadIdx.x];
       elem = ops.elem(m);
       const float4* os = &sm.raw2[cur.stage][kOwnSlot];
+      float p[kOwnPerLane][3];
 #pragma unroll
       for (int j = 0; j < kOwnPerLane; ++j) {
         const int i = lane + 32 * j;
@@ -371,6 +372,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
           p[j][2] = o.z;
         }
       }
+      pack_owned(p, q);
     }
     const PrepOut pb = ops.prep(sm, cur.stage, len, meta);
     const float4* __restrict__ bufA = pb.a;
@@ -380,7 +382,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
       const float4 a = bufA[c];
       const float4 b = bufB[c];
 #pragma unroll
-      for (int j = 0; j < kOwnPerLane; ++j) elem(acc[j], p[j], a, b);
+      for (int k = 0; k < kPairs; ++k) elem(acc[k], q[k], a, b);
     }
     __syncthreads();
     cur = nx;

@@ -5,6 +5,26 @@
 
 namespace cesa {
 
+// Element functors work on two owned points at once with packed FP32 pairs
+// (FFMA2/FADD2/FMUL2 on sm_100+: the same round-to-nearest operations as the
+// scalar code, so results are unchanged, at half the issued instructions).
+// q holds the negated coordinates of the two owned points; s is the streamed
+// point and h its second record.
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// Squared distances |s - p|^2 of one streamed point to two owned points:
+// 3 FADD, FMUL + 2 FFMA each, as direct differences.
+__device__ __forceinline__ float2 dist2_pair(const float2 (&q)[3], float4 s) {
+  const float2 dx = __fadd2_rn(dup2(s.x), q[0]);
+  const float2 dy = __fadd2_rn(dup2(s.y), q[1]);
+  const float2 dz = __fadd2_rn(dup2(s.z), q[2]);
+  float2 d2 = __fmul2_rn(dx, dx);
+  d2 = __ffma2_rn(dy, dy, d2);
+  return __ffma2_rn(dz, dz, d2);
+}
+
+__device__ __forceinline__ float2 ex2_pair(float2 t) { return make_float2(ex2_approx(t.x), ex2_approx(t.y)); }
+
 // ------------------------------------------------------------------ EM-ICP
 constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), sum u y^T (9)
 
@@ -12,20 +32,13 @@ constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), 
 // running sums of e^2, e and e x over the streamed X points of one owned Y row.
 struct EmicpElem {
   float nk;  // -log2(e) / (2 sigma_p2)
-  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 x,
-                                             float4) const {
-    const float dx = x.x - p[0];
-    const float dy = x.y - p[1];
-    const float dz = x.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(d2 * nk);
-    acc[0] = fmaf(e, e, acc[0]);
-    acc[1] += e;
-    acc[2] = fmaf(e, x.x, acc[2]);
-    acc[3] = fmaf(e, x.y, acc[3]);
-    acc[4] = fmaf(e, x.z, acc[4]);
+  __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 x, float4) const {
+    const float2 e = ex2_pair(__fmul2_rn(dist2_pair(q, x), dup2(nk)));
+    acc[0] = __ffma2_rn(e, e, acc[0]);
+    acc[1] = __fadd2_rn(acc[1], e);
+    acc[2] = __ffma2_rn(e, dup2(x.x), acc[2]);
+    acc[3] = __ffma2_rn(e, dup2(x.y), acc[3]);
+    acc[4] = __ffma2_rn(e, dup2(x.z), acc[4]);
   }
 };
 
@@ -108,36 +121,22 @@ constexpr int kSaNV = 32;
 // Sinkhorn sweep element: acc += K * weight(streamed).
 struct SinkElem {
   float nk, c0;  // K = 2^(c0 + nk d^2)
-  __device__ __forceinline__ void operator()(float (&acc)[1], const float (&p)[3], float4 s,
-                                             float4) const {
-    const float dx = s.x - p[0];
-    const float dy = s.y - p[1];
-    const float dz = s.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(fmaf(d2, nk, c0));
-    acc[0] = fmaf(e, s.w, acc[0]);
+  __device__ __forceinline__ void operator()(float2 (&acc)[1], const float2 (&q)[3], float4 s, float4) const {
+    const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q, s), dup2(nk), dup2(c0)));
+    acc[0] = __ffma2_rn(e, dup2(s.w), acc[0]);
   }
 };
 
 // Final row sweep element: w += K b, mu += K delta, Vhat += K g (y' - Yhat).
 struct FinalElem {
   float nk, c0;
-  __device__ __forceinline__ void operator()(float (&acc)[5], const float (&p)[3], float4 s,
-                                             float4 h) const {
-    const float dx = s.x - p[0];
-    const float dy = s.y - p[1];
-    const float dz = s.z - p[2];
-    float d2 = dx * dx;
-    d2 = fmaf(dy, dy, d2);
-    d2 = fmaf(dz, dz, d2);
-    const float e = ex2_approx(fmaf(d2, nk, c0));
-    acc[0] = fmaf(e, s.w, acc[0]);
-    acc[1] = fmaf(e, h.w, acc[1]);
-    acc[2] = fmaf(e, h.x, acc[2]);
-    acc[3] = fmaf(e, h.y, acc[3]);
-    acc[4] = fmaf(e, h.z, acc[4]);
+  __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 s, float4 h) const {
+    const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q, s), dup2(nk), dup2(c0)));
+    acc[0] = __ffma2_rn(e, dup2(s.w), acc[0]);
+    acc[1] = __ffma2_rn(e, dup2(h.w), acc[1]);
+    acc[2] = __ffma2_rn(e, dup2(h.x), acc[2]);
+    acc[3] = __ffma2_rn(e, dup2(h.y), acc[3]);
+    acc[4] = __ffma2_rn(e, dup2(h.z), acc[4]);
   }
 };
 

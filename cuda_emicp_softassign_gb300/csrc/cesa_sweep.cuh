@@ -143,6 +143,18 @@ __device__ __forceinline__ void load_owned(const float4* own, int n_own, int blk
   }
 }
 
+// Owned points of a lane in packed pairs: pair k holds the lane's points
+// (2k, 2k + 1), i.e. owned indices lane + 64 k and lane + 64 k + 32.
+constexpr int kPairs = kOwnPerLane / 2;
+
+// Negated coordinates of the lane's owned points, packed by pair.
+__device__ __forceinline__ void pack_owned(const float (&p)[kOwnPerLane][3], float2 (&q)[kPairs][3]) {
+#pragma unroll
+  for (int k = 0; k < kPairs; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) q[k][c] = make_float2(-p[2 * k][c], -p[2 * k + 1][c]);
+}
+
 // Writes the warp-level accumulators to shared memory and returns, in threads
 // 0..kBlockPts-1, the sum over warps (fixed order) for owned point threadIdx.x.
 template <int NACC>
@@ -164,6 +176,19 @@ __device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float (&acc)[k
     }
   }
   __syncthreads();
+}
+
+template <int NACC>
+__device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float2 (&acc)[kPairs][NACC], float (&tot)[NACC]) {
+  float a[kOwnPerLane][NACC];
+#pragma unroll
+  for (int k = 0; k < kPairs; ++k)
+#pragma unroll
+    for (int v = 0; v < NACC; ++v) {
+      a[2 * k][v] = acc[k][v].x;
+      a[2 * k + 1][v] = acc[k][v].y;
+    }
+  reduce_warps<NACC>(sm, a, tot);
 }
 
 // Split-slice completion. Stores this unit's per-point totals; returns true in
@@ -383,7 +408,8 @@ __device__ __forceinline__ void sweep_prefetch(Pipe& p, SweepSmem& sm, const Swe
 // pair, cross-warp reduction, split completion, then fin(blk, tot) in the
 // block that completes the owned block. Returns false if a wait gave up.
 //
-//   Elem: void operator()(float (&acc)[NACC], const float (&p)[3], float4 a, float4 b)
+//   Elem: void operator()(float2 (&acc)[NACC], const float2 (&q)[3], float4 a, float4 b)
+//         (two owned points, packed; q = their negated coordinates)
 //   Prep: PrepOut operator()(SweepSmem&, int stage, int first, int len, int blk)  (block-wide)
 //         void unit_end(int blk, int slice)                                       (block-wide)
 //   Fin:  void operator()(int blk, const float (&tot)[NACC])                      (block-wide)
@@ -455,11 +481,13 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
         p[j][2] = ow[j].z;
       }
     }
-    float acc[kOwnPerLane][NACC];
+    float2 q[kPairs][3];
+    pack_owned(p, q);
+    float2 acc[kPairs][NACC];
 #pragma unroll
-    for (int j = 0; j < kOwnPerLane; ++j)
+    for (int k = 0; k < kPairs; ++k)
 #pragma unroll
-      for (int a = 0; a < NACC; ++a) acc[j][a] = 0.f;
+      for (int a = 0; a < NACC; ++a) acc[k][a] = make_float2(0.f, 0.f);
 
     for (;;) {
       int n_first = 0, n_len = 0, n_u = u, n_ch = cur_ch + 1, n_stage = 0;
@@ -491,7 +519,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
         const float4 a = bufA[c];
         const float4 b = bufB[c];
 #pragma unroll
-        for (int j = 0; j < kOwnPerLane; ++j) elem(acc[j], p[j], a, b);
+        for (int k = 0; k < kPairs; ++k) elem(acc[k], q[k], a, b);
       }
       __syncthreads();
       const bool unit_done = !(have_n && n_u == u);
