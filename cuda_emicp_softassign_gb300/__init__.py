@@ -139,6 +139,8 @@ def lib():
         L.cesa_register_batch_device.restype = _i
         L.cesa_register_batch.argtypes = [_p, _i, _p]
         L.cesa_register_batch.restype = _i
+        L.cesa_tune_sinkhorn.argtypes = [_i, _i, _p, _p, _p, _p]
+        L.cesa_tune_sinkhorn.restype = _i
         L.cesa_self_test_waits.argtypes = [_i, _i, _p, _p]
         L.cesa_self_test_waits.restype = _i
         _lib = L
@@ -368,6 +370,18 @@ def softassign_step(dX, dY, R, t, T, alpha, I1, s, u, rs=None, cs=None, w=None,
                                            ctypes.c_void_p(_stream_handle(stream)))
     _check(rc, "softassign_step")
     return mom
+
+
+def tune_sinkhorn(N, M, param=None):
+    """Times both Sinkhorn forms for N x M on the current device and records
+    the faster one for CESA_SINKHORN_AUTO. Returns (form, ms per pose update
+    matrix-free, ms per pose update materialised or -1)."""
+    f = ctypes.c_int(0)
+    a = ctypes.c_float(0)
+    b = ctypes.c_float(0)
+    _check(lib().cesa_tune_sinkhorn(int(N), int(M), ctypes.byref(param) if param is not None else None,
+                                    ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)), "tune_sinkhorn")
+    return f.value, a.value, b.value
 
 
 def release_workspaces():

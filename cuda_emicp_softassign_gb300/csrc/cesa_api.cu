@@ -132,6 +132,41 @@ cudaStream_t own_stream(int dev) {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+static_assert(kFormMatrixFree == CESA_SINKHORN_MATRIX_FREE && kFormMaterialised == CESA_SINKHORN_MATERIALISED,
+              "Sinkhorn form values");
+
+// Sinkhorn form chosen per size by the tuner (cesa_tune_sinkhorn): measured
+// decisions per device and half-octave size bucket of (N, M).
+struct TuneKey {
+  int dev, bn, bm;
+  bool operator<(const TuneKey& o) const {
+    return dev != o.dev ? dev < o.dev : (bn != o.bn ? bn < o.bn : bm < o.bm);
+  }
+};
+std::map<TuneKey, int> g_tuned;  // guarded by g_mu
+
+int size_bucket(int n) { return (int)floor(2.0 * log2((double)(n > 1 ? n : 1))); }
+
+// The materialised form needs its N x M matrix: never chosen when that would
+// take more than half of the device's free memory.
+bool materialised_fits(int N, int M) {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+  const double k_bytes = (double)((N + 127) / 128 * 128) * (double)M * 4.0;
+  return k_bytes < 0.5 * (double)free_b;
+}
+
+// Form for a request; AUTO takes the tuner's decision for the size bucket,
+// else the matrix-free form (measured faster wherever the tuner has run on
+// GB300; the materialised form streams 28 bytes per element per update).
+int resolve_form(int requested, int N, int M, int dev) {
+  if (requested == CESA_SINKHORN_MATRIX_FREE) return kFormMatrixFree;
+  if (requested == CESA_SINKHORN_MATERIALISED) return kFormMaterialised;
+  auto it = g_tuned.find(TuneKey{dev, size_bucket(N), size_bucket(M)});
+  if (it != g_tuned.end() && (it->second != kFormMaterialised || materialised_fits(N, M))) return it->second;
+  return kFormMatrixFree;
+}
+
 // Shared body of the two host-pointer entry points.
 int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9], float t[3],
              const cesa_params* p, cesa_report* rep) {
@@ -156,8 +191,8 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   float* dX = static_cast<float*>(C.io.p);
   float* dY = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx);
   float* dRt = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx + by);
-  const size_t need = kind == 1 ? emicp_ws_need(N, M, dev)
-                                : softassign_ws_need(N, M, p->sinkhorn_form, dev);
+  const int form = kind == 1 ? 0 : resolve_form(p->sinkhorn_form, N, M, dev);
+  const size_t need = kind == 1 ? emicp_ws_need(N, M, dev) : softassign_ws_need(N, M, form, dev);
   e = C.ws.ensure(need);
   if (e != cudaSuccess) return map_cuda(e);
   const int cap = (rep && rep->trace && rep->trace_capacity > 0) ? rep->trace_capacity : 0;
@@ -218,7 +253,7 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
       L.T_0 = p->T_0;
       L.TFACTOR = p->TFACTOR;
       L.moutlier = p->moutlier;
-      L.form = CESA_SINKHORN_MATRIX_FREE;
+      L.form = form;
       L.dRt = dRt;
       L.trace = dtrace;
       L.trace_cap = cap;
@@ -257,7 +292,7 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   memcpy(t, hRt + 9, sizeof(float) * 3);
   if (rep) {
     rep->steps = (int)nsteps;
-    rep->sinkhorn_form = kind == 2 ? CESA_SINKHORN_MATRIX_FREE : 0;
+    rep->sinkhorn_form = form;
     rep->grid_blocks = grid;
     rep->device_ms = ms;
   }
@@ -401,7 +436,8 @@ int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, p->sinkhorn_form, dev));
+  const int form = resolve_form(p->sinkhorn_form, N, M, dev);
+  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, form, dev));
   if (e != cudaSuccess) return map_cuda(e);
   SoftassignLaunch L{};
   L.dX = dX;
@@ -415,7 +451,7 @@ int cesa_softassign_device(const float* dX, int N, const float* dY, int M, float
   L.T_0 = p->T_0;
   L.TFACTOR = p->TFACTOR;
   L.moutlier = p->moutlier;
-  L.form = CESA_SINKHORN_MATRIX_FREE;
+  L.form = form;
   L.dRt = dRt;
   L.d_status = d_status;
   L.timeout_ns = timeout_ns_of(p);
@@ -516,6 +552,99 @@ int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* rep) {
   return CESA_OK;
 }
 
+int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
+                       float* ms_materialised) {
+  if (N < 1 || M < 1 || (long)N * 16 > 0x7fffffffL || (long)M * 16 > 0x7fffffffL) return CESA_ERR_INVALID_ARGUMENT;
+  cesa_params q;
+  if (p) {
+    q = *p;
+  } else {
+    cesa_params_default(&q);
+  }
+  if (check_sa_params(&q)) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  int rc = select_device(&q, &dev);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  cudaStream_t st = own_stream(dev);
+  // synthetic clouds of the requested sizes (timing does not depend on the
+  // values: the sweeps have no data-dependent branches)
+  std::vector<float> hx(3 * (size_t)N), hy(3 * (size_t)M);
+  unsigned long long z = 0x9e3779b97f4a7c15ull;
+  auto next = [&z]() {
+    z = z * 6364136223846793005ull + 1442695040888963407ull;
+    return (float)((z >> 40) & 0xffffff) / 16777216.f;
+  };
+  for (auto& v : hx) v = next();
+  for (auto& v : hy) v = next();
+  const bool try_mat = materialised_fits(N, M);
+  const size_t need_f = softassign_ws_need(N, M, kFormMatrixFree, dev);
+  const size_t need_m = try_mat ? softassign_ws_need(N, M, kFormMaterialised, dev) : 0;
+  const size_t need = need_f > need_m ? need_f : need_m;
+  void* mem = nullptr;
+  const size_t bx = align256(sizeof(float) * hx.size()), by = align256(sizeof(float) * hy.size());
+  cudaError_t e = cudaMalloc(&mem, bx + by + 256 + need);
+  if (e != cudaSuccess) return map_cuda(e);
+  char* base = static_cast<char*>(mem);
+  float* dX = reinterpret_cast<float*>(base);
+  float* dY = reinterpret_cast<float*>(base + bx);
+  float* dRt = reinterpret_cast<float*>(base + bx + by);
+  void* ws = base + bx + by + 256;
+  const float pose[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  e = cudaMemcpyAsync(dX, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dY, hy.data(), sizeof(float) * hy.size(), cudaMemcpyHostToDevice, st);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float ms[2] = {-1.f, -1.f};
+  for (int f = 0; f < 2 && e == cudaSuccess; ++f) {
+    const int form = f == 0 ? kFormMatrixFree : kFormMaterialised;
+    if (form == kFormMaterialised && !try_mat) break;
+    SoftassignLaunch L{};
+    L.dX = dX;
+    L.dY = dY;
+    L.N = N;
+    L.M = M;
+    L.JMAX = 1;
+    L.I0 = 2;
+    L.I1 = q.I1;
+    L.alpha = q.alpha;
+    L.T_0 = q.T_0;
+    L.TFACTOR = q.TFACTOR;
+    L.moutlier = q.moutlier;
+    L.form = form;
+    L.dRt = dRt;
+    L.timeout_ns = timeout_ns_of(&q);
+    float best = 0.f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {  // first run is the warm-up
+      e = cudaMemcpyAsync(dRt, pose, sizeof(pose), cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+      if (e == cudaSuccess) e = (cudaError_t)enqueue_softassign(L, ws, need, st, nullptr);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float t = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+      if (rep == 1 || (rep > 1 && t < best)) best = t;
+    }
+    int status = 0, steps = 0;
+    if (e == cudaSuccess) e = (cudaError_t)read_ws_status(ws, st, &status, &steps);
+    if (e == cudaSuccess && status) rc = status;
+    ms[f] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  cudaFree(mem);
+  if (e != cudaSuccess) return map_cuda(e);
+  if (rc) return rc;
+  const int form = (ms[1] >= 0.f && ms[1] < ms[0]) ? kFormMaterialised : kFormMatrixFree;
+  g_tuned[TuneKey{dev, size_bucket(N), size_bucket(M)}] = form;
+  if (form_out) *form_out = form;
+  if (ms_matrix_free) *ms_matrix_free = ms[0] * 0.5f;  // per pose update
+  if (ms_materialised) *ms_materialised = ms[1] >= 0.f ? ms[1] * 0.5f : -1.f;
+  return CESA_OK;
+}
+
 int cesa_stream_status(cesa_stream_t stream) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
@@ -590,13 +719,13 @@ int cesa_softassign_step_device(const float* dX, int N, const float* dY, int M, 
   int rc = check_points(dX, N, dY, M);
   if (rc) return rc;
   if (!R || !t || !s || !u || !(T > 0.f) || I1 < 1) return CESA_ERR_INVALID_ARGUMENT;
-  (void)sinkhorn_form;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, sinkhorn_form, dev));
+  const int form = resolve_form(sinkhorn_form, N, M, dev);
+  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, form, dev));
   if (e == cudaSuccess) e = C.io.ensure(256);
   if (e == cudaSuccess) e = C.trace.ensure(sizeof(double) * 32);
   if (e != cudaSuccess) return map_cuda(e);
@@ -618,7 +747,7 @@ int cesa_softassign_step_device(const float* dX, int N, const float* dY, int M, 
   L.T_0 = T;
   L.TFACTOR = 1.f;
   L.moutlier = 0.f;
-  L.form = CESA_SINKHORN_MATRIX_FREE;
+  L.form = form;
   L.dRt = dRt;
   L.s_io = s;
   L.u_io = u;

@@ -75,6 +75,10 @@ struct BatchLaunchPair {
   float alpha, T_0, TFACTOR, moutlier;
 };
 
+// Sinkhorn forms of SoftassignLaunch.form (the CESA_SINKHORN_* values).
+constexpr int kFormMatrixFree = 1;
+constexpr int kFormMaterialised = 2;
+
 // Device workspace carved from one allocation (see api.cu).
 struct Workspace {
   void* base = nullptr;
@@ -95,6 +99,8 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
                        int* grid_used);
 size_t emicp_ws_need(int N, int M, int device);
 size_t softassign_ws_need(int N, int M, int form, int device);
+size_t softassign_mat_ws_need(int N, int M, int device);
+int enqueue_softassign_mat(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
 
 // Batched registration: all pairs in one persistent launch.
 size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs, int device);

@@ -508,7 +508,7 @@ SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
 }  // namespace
 
 size_t softassign_ws_need(int N, int M, int form, int device) {
-  (void)form;
+  if (form == kFormMaterialised) return softassign_mat_ws_need(N, M, device);
   const SaPlan P = plan_sa(N, M, device);
   size_t total = 0;
   carve_sa(nullptr, P, N, M, &total);
@@ -517,6 +517,7 @@ size_t softassign_ws_need(int N, int M, int form, int device) {
 
 int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st,
                        int* grid_used) {
+  if (L.form == kFormMaterialised) return enqueue_softassign_mat(L, ws, ws_bytes, st, grid_used);
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return (int)e;

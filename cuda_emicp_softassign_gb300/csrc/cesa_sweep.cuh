@@ -157,9 +157,9 @@ __device__ __forceinline__ void pack_owned(const float (&p)[kOwnPerLane][3], flo
 
 // Writes the warp-level accumulators to shared memory and returns, in threads
 // 0..kBlockPts-1, the sum over warps (fixed order) for owned point threadIdx.x.
-template <int NACC>
-__device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float (&acc)[kOwnPerLane][NACC],
-                                             float (&tot)[NACC]) {
+// (Smem: any shared-memory block with red[kMaxAcc][kWarps][kBlockPts] and flag.)
+template <int NACC, class Smem>
+__device__ __forceinline__ void reduce_warps(Smem& sm, const float (&acc)[kOwnPerLane][NACC], float (&tot)[NACC]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < kOwnPerLane; ++j)
@@ -178,8 +178,8 @@ __device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float (&acc)[k
   __syncthreads();
 }
 
-template <int NACC>
-__device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float2 (&acc)[kPairs][NACC], float (&tot)[NACC]) {
+template <int NACC, class Smem>
+__device__ __forceinline__ void reduce_warps(Smem& sm, const float2 (&acc)[kPairs][NACC], float (&tot)[NACC]) {
   float a[kOwnPerLane][NACC];
 #pragma unroll
   for (int k = 0; k < kPairs; ++k)
@@ -196,8 +196,8 @@ __device__ __forceinline__ void reduce_warps(SweepSmem& sm, const float2 (&acc)[
 // < kBlockPts) replaced by the slice-ordered sum over all S partials.
 // part layout: [(blk*S + sl)][NACC][kBlockPts]. cnt[blk] is monotonic; this is
 // the `round`-th sweep of this geometry in the launch (0-based).
-template <int NACC>
-__device__ __forceinline__ bool split_complete(SweepSmem& sm, const SweepGeom& g, int blk, int sl,
+template <int NACC, class Smem>
+__device__ __forceinline__ bool split_complete(Smem& sm, const SweepGeom& g, int blk, int sl,
                                                unsigned round, float* part, unsigned* cnt,
                                                float (&tot)[NACC]) {
   if (g.slices == 1) return true;

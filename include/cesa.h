@@ -234,6 +234,21 @@ int cesa_find_rt_from_s(const float Xc[3], const float Yc[3], const float S[9], 
  */
 int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_out);
 
+/*
+ * Autotuner of the Softassign Sinkhorn form. Times both forms (two pose
+ * updates each, after a warm-up) on synthetic clouds of N and M points with
+ * the schedule parameters of *p (NULL: defaults) on the current device, and
+ * records the faster one for the size bucket (half-octaves of N and M).
+ * Later calls with sinkhorn_form = CESA_SINKHORN_AUTO and sizes in that bucket
+ * use it; without a recorded decision AUTO uses the matrix-free form. The
+ * materialised form is skipped when its N x M matrix would take more than half
+ * of the free device memory. Outputs (may be NULL): the chosen form and the
+ * milliseconds per pose update of each form (-1 when not run). No counterpart
+ * in the reference, which has one (materialised) form.
+ */
+int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
+                       float* ms_materialised);
+
 /* Releases cached device workspaces of the calling process. */
 void cesa_release_workspaces(void);
 
