@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0,
                     help="target seconds of CPU work for the CPU-baseline sample")
+    ap.add_argument("--sinkhorn-form", default="auto", choices=["auto", "matrix_free", "materialised"],
+                    help="Softassign Sinkhorn form (auto: the autotuner's choice for the size)")
     return ap.parse_args()
 
 
@@ -76,8 +78,17 @@ class RefDefaults:
     sigma_p2, sigma_inf, sigma_factor, d_02 = 0.01, 1e-5, 0.9, 0.01
 
 
-def params_for(cesa, kind):
-    return cesa.Params.default()
+FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2}
+
+
+def params_for(cesa, kind, form="auto"):
+    return cesa.Params.default(sinkhorn_form=FORMS[form])
+
+
+def materialised_bytes(N, M, p):
+    """HBM bytes of one registration in the materialised form: per pose update
+    4 B per element written (K) and 4 B read by each of the 2*I1 later passes."""
+    return 4.0 * (1 + 2 * p.I1) * float(N) * float(M) * p.JMAX * p.I0
 
 
 def pose_updates(kind, p):
@@ -477,8 +488,13 @@ def run_ours(args, rank, world, local):
 
     torch.cuda.set_device(local)
     kind, X, Y = workload(args.workload, args.seed)
-    p = params_for(cesa, kind)
+    p = params_for(cesa, kind, args.sinkhorn_form)
     N, M = len(X), len(Y)
+    tuned = None
+    if kind == "softassign":
+        f, ms_free, ms_mat = cesa.tune_sinkhorn(N, M, p)  # records the choice used by "auto"
+        tuned = {"chosen": "materialised" if f == 2 else "matrix_free",
+                 "ms_per_update_matrix_free": ms_free, "ms_per_update_materialised": ms_mat}
     dev_call = cesa.emicp_device if kind == "emicp" else cesa.softassign_device
     host_call = cesa.emicp if kind == "emicp" else cesa.softassign
 
@@ -571,9 +587,28 @@ def run_ours(args, rank, world, local):
                 "ops_per_registration": fp32_ops,
                 "note": "achieved = algorithmic FP32-pipe ops of one registration / event time of its launch "
                         "sequence (prep kernels included)"}
+    form_used = None
+    if kind == "softassign":
+        form_used = {0: "matrix_free", 1: "matrix_free", 2: "materialised"}[
+            FORMS[args.sinkhorn_form] if args.sinkhorn_form != "auto" else (2 if tuned["chosen"] == "materialised" else 1)]
+    if form_used == "materialised":
+        hbm_peak = None
+        try:
+            hbm_peak = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        except (OSError, KeyError, ValueError):
+            pass
+        gbs = materialised_bytes(N, M, p) / mean_s / 1e9
+        roofline = {"bound": "hbm", "kernel": "softassign_mat_kernel", "achieved": gbs,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak if hbm_peak else None,
+                    "traffic": None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
+                    "bytes_per_registration": materialised_bytes(N, M, p),
+                    "note": "achieved = algorithmic HBM bytes (4 B per element written once and read by "
+                            "each of the 2*I1 later passes, per pose update) / event time"}
     traffic_file = os.path.join(HERE, "profiles", "ncu_traffic.json")
     if os.path.exists(traffic_file):
-        entry = json.load(open(traffic_file)).get(args.workload)
+        key = args.workload + (":materialised" if form_used == "materialised" else "")
+        entry = json.load(open(traffic_file)).get(key)
         if entry:
             roofline["traffic"] = entry["bytes_per_launch"]
             roofline["traffic_source"] = "ncu dram bytes per launch, profiles/ncu_traffic.json"
@@ -593,6 +628,9 @@ def run_ours(args, rank, world, local):
             "clocks": clocks,
             "gpu_launches": kernels_per_registration(kind) * args.steps,
             "wall_s_timed_region": t_wall}
+    if kind == "softassign":
+        line["config"]["sinkhorn_form"] = form_used
+        line["config"]["sinkhorn_tuner"] = tuned
     print(json.dumps(line), flush=True)
 
 
