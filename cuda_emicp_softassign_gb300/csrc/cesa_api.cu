@@ -552,6 +552,123 @@ int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* rep) {
   return CESA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Layout of an EM-ICP tape buffer: centring header, packed X' and Y', the
+// step records, the per-step row records.
+struct TapeLayout {
+  size_t hdr, cols, rows, steps, row_tape, total;
+};
+TapeLayout tape_layout(int N, int M, long nsteps) {
+  TapeLayout t;
+  size_t off = 0;
+  t.hdr = off;
+  off += align256(sizeof(CenterHdr));
+  t.cols = off;
+  off += align256(sizeof(float4) * (size_t)N);
+  t.rows = off;
+  off += align256(sizeof(float4) * (size_t)M);
+  t.steps = off;
+  off += align256(sizeof(float) * kEmTape * (size_t)nsteps);
+  t.row_tape = off;
+  off += align256(sizeof(float) * 5 * (size_t)M * (size_t)nsteps);
+  t.total = off;
+  return t;
+}
+}  // namespace
+
+extern "C" {
+
+size_t cesa_emicp_tape_bytes(int N, int M, const cesa_params* p) {
+  if (N < 1 || M < 1 || check_emicp_params(p)) return 0;
+  const long n = emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor);
+  if (n < 0) return 0;
+  return tape_layout(N, M, n).total;
+}
+
+int cesa_emicp_forward_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
+                              void* tape, int* d_status, cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!dRt || !tape) return CESA_ERR_INVALID_ARGUMENT;
+  rc = check_emicp_params(p);
+  if (rc) return rc;
+  const long nsteps = emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor);
+  if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(emicp_ws_need(N, M, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  const TapeLayout T = tape_layout(N, M, nsteps);
+  char* tb = static_cast<char*>(tape);
+  EmicpLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.sigma_p2 = p->sigma_p2;
+  L.sigma_factor = p->sigma_factor;
+  L.d_02 = p->d_02;
+  L.nsteps = (int)nsteps;
+  L.dRt = dRt;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  L.tape = reinterpret_cast<float*>(tb + T.steps);
+  L.row_tape = reinterpret_cast<float*>(tb + T.row_tape);
+  C.last_kind = 1;
+  C.last_trace_steps = 0;
+  int k = enqueue_emicp(L, C.ws.p, C.ws.bytes, st, nullptr);
+  if (k) return map_cuda((cudaError_t)k);
+  // the packed clouds and offsets the forward used
+  CenterHdr* hdr = nullptr;
+  float4 *rows = nullptr, *cols = nullptr;
+  emicp_ws_views(C.ws.p, N, M, dev, &hdr, &rows, &cols);
+  e = cudaMemcpyAsync(tb + T.hdr, hdr, sizeof(CenterHdr), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tb + T.cols, cols, sizeof(float4) * (size_t)N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tb + T.rows, rows, sizeof(float4) * (size_t)M, cudaMemcpyDeviceToDevice, st);
+  return map_cuda(e);
+}
+
+int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* tape, const float* d_gRt,
+                               float* d_gX, float* d_gY, float* d_gRt0, int* d_status, cesa_stream_t stream) {
+  if (N < 1 || M < 1 || !tape || !d_gRt || !d_gX || !d_gY || !d_gRt0) return CESA_ERR_INVALID_ARGUMENT;
+  int rc = check_emicp_params(p);
+  if (rc) return rc;
+  const long nsteps = emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor);
+  if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(emicp_adjoint_ws_need(N, M, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  const TapeLayout T = tape_layout(N, M, nsteps);
+  const char* tb = static_cast<const char*>(tape);
+  EmicpAdjointLaunch L{};
+  L.rows = reinterpret_cast<const float4*>(tb + T.rows);
+  L.cols = reinterpret_cast<const float4*>(tb + T.cols);
+  L.hdr = reinterpret_cast<const CenterHdr*>(tb + T.hdr);
+  L.N = N;
+  L.M = M;
+  L.nsteps = (int)nsteps;
+  L.tape = reinterpret_cast<const float*>(tb + T.steps);
+  L.row_tape = reinterpret_cast<const float*>(tb + T.row_tape);
+  L.g_out = d_gRt;
+  L.gX = d_gX;
+  L.gY = d_gY;
+  L.g_in = d_gRt0;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  C.last_kind = 1;
+  C.last_trace_steps = 0;
+  return map_cuda((cudaError_t)enqueue_emicp_adjoint(L, C.ws.p, C.ws.bytes, st));
+}
+
 int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
                        float* ms_materialised) {
   if (N < 1 || M < 1 || (long)N * 16 > 0x7fffffffL || (long)M * 16 > 0x7fffffffL) return CESA_ERR_INVALID_ARGUMENT;

@@ -43,6 +43,8 @@ struct EmicpArgs {
   double* trace;
   int trace_cap;
   float* row_out;       // optional [M][5] (centred-frame u)
+  float* tape;          // optional [nsteps][kEmTape]
+  float* row_tape;      // optional [nsteps][M][5]
   int* d_status;
   unsigned long long* tl;
   int tl_cap;
@@ -104,7 +106,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     const EmicpFin fin{A.rows,    A.M,
                        outlier,   {s_hdr[6], s_hdr[7], s_hdr[8]},
                        A.row_out, {s_hdr[0], s_hdr[1], s_hdr[2]},
-                       reinterpret_cast<df*>(sm.prep), rb};
+                       reinterpret_cast<df*>(sm.prep), rb,
+                       A.row_tape ? A.row_tape + (size_t)step * A.M * 5 : nullptr};
     if (!sweep_units<5>(sm, pipe, A.geo, src, A.rows, true, R, tc, (unsigned)step, A.part, A.cnt,
                         elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10, tl, 0, &oc_rows))
       break;
@@ -120,6 +123,18 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
       float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
       horn_quaternion<float>(S, horn, q, &gap, &lmax);
       quat_to_pose<float>(q, Xc, Yc, Rn, tn);
+      if (A.tape && blockIdx.x == 0) {  // the step's inputs and solve for the adjoint
+        float* rec = A.tape + (size_t)step * kEmTape;
+        for (int k = 0; k < 12; ++k) rec[k] = s_pose[k];
+        rec[12] = s2;
+        for (int k = 0; k < kEmNV; ++k) {
+          rec[16 + 2 * k] = s_tot[k].hi;
+          rec[17 + 2 * k] = s_tot[k].lo;
+        }
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) rec[48 + 4 * i + j] = horn.V[i][j];
+        for (int k = 0; k < 4; ++k) rec[64 + k] = q[k];
+      }
       for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];
       for (int k = 0; k < 3; ++k) s_pose[9 + k] = tn[k];
       if (blockIdx.x == 0) {
@@ -226,6 +241,14 @@ EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* to
 }
 }  // namespace
 
+void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols) {
+  const EmicpPlan P = plan_emicp(N, M, device);
+  EmicpCarved w = carve_emicp(ws, P, N, M, nullptr);
+  *hdr = w.hdr;
+  *rows = w.rows;
+  *cols = w.cols;
+}
+
 size_t emicp_ws_need(int N, int M, int device) {
   const EmicpPlan P = plan_emicp(N, M, device);
   size_t total = 0;
@@ -273,6 +296,8 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;
   A.row_out = L.row_out;
+  A.tape = L.tape;
+  A.row_tape = L.row_tape;
   A.d_status = L.d_status;
   A.tl = L.timeline;
   A.tl_cap = L.timeline_cap;

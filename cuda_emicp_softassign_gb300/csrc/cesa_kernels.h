@@ -38,7 +38,14 @@ struct EmicpLaunch {
   unsigned long long* timeline;  // optional device phase timeline (block 0)
   int timeline_cap;
   uint64_t timeout_ns;
+  float* tape;       // optional [nsteps][kEmTape] step records for the adjoint
+  float* row_tape;   // optional [nsteps][M][5] per-row (C, lambda, u), centred frame
 };
+
+// EM-ICP tape record per step (floats): [0..8] R in, [9..11] t' in (centred
+// frame), [12] sigma_p2, [16..47] the 16 moments as (hi, lo), [48..63] Horn
+// eigenbasis V (row-major, columns are eigenvectors), [64..67] q.
+constexpr int kEmTape = 80;
 
 struct SoftassignLaunch {
   const float* dX;  // SoA, N (rows of the match matrix)
@@ -106,6 +113,26 @@ int enqueue_softassign_mat(const SoftassignLaunch& L, void* ws, size_t ws_bytes,
 size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs, int device);
 int enqueue_batch(const BatchLaunchPair* pairs, int npairs, int* d_status, uint64_t timeout_ns, void* ws,
                   size_t ws_bytes, cudaStream_t st, int* grid_used, int* rounds_out);
+
+// EM-ICP adjoint over a recorded forward (tape).
+struct EmicpAdjointLaunch {
+  const float4* rows;  // Y' centred (M), as packed by the forward
+  const float4* cols;  // X' centred (N)
+  const CenterHdr* hdr;
+  int N, M, nsteps;
+  const float* tape;      // [nsteps][kEmTape]
+  const float* row_tape;  // [nsteps][M][5]
+  const float* g_out;     // device [12]: dL/dR (9), dL/dt (3) of the final pose, caller frame
+  float* gX;              // device SoA [3N] (written)
+  float* gY;              // device SoA [3M] (written)
+  float* g_in;            // device [12]: dL/dR0, dL/dt0 of the initial pose, caller frame
+  int* d_status;
+  uint64_t timeout_ns;
+};
+size_t emicp_adjoint_ws_need(int N, int M, int device);
+int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st);
+// The forward workspace's packed clouds and centring header (for the tape).
+void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);
 
 // Control-block status of the last launch that used workspace ws.
 int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written = nullptr);

@@ -53,6 +53,7 @@ struct EmicpFin {
   float oX[3];
   df* scratch;     // shared, >= 17 * 128 dfs
   df* rbpart;      // this step's [nblk][kEmNV]
+  float* row_tape; // optional: this step's [M][5] (C, lambda, u) in the centred frame
   __device__ void operator()(int blk, const float (&tot)[5]) const {
     df v[kEmNV];
 #pragma unroll
@@ -73,6 +74,14 @@ struct EmicpFin {
         uu[0] = xm[0];
         uu[1] = xm[1];
         uu[2] = xm[2];
+      }
+      if (row_tape) {
+        float* o = row_tape + (size_t)r * 5;
+        o[0] = C;
+        o[1] = lam;
+        o[2] = uu[0];
+        o[3] = uu[1];
+        o[4] = uu[2];
       }
       if (row_out) {
         float* o = row_out + (size_t)r * 5;

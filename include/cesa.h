@@ -249,6 +249,24 @@ int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_ou
 int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
                        float* ms_materialised);
 
+/*
+ * Adjoint of EM-ICP (no counterpart in the reference). A forward pass that
+ * also records a tape (per sigma step: input pose, moments, Horn eigenbasis;
+ * per step and Y point: C_r, lambda_r, u_r; the packed clouds; no N x M
+ * affinity is stored) and a backward pass that, given dL/dR (9, row-major) and
+ * dL/dt (3) of the returned pose, writes dL/dX (SoA 3N), dL/dY (SoA 3M) and
+ * dL/dR0, dL/dt0 of the initial pose (12). The backward recomputes the
+ * affinities step by step. All pointers are device pointers;
+ * cesa_emicp_forward_device returns the same pose as cesa_emicp_device. The
+ * gradient of a rows' C_r <= 1e-6 branch (lambda = 1, u = mean X) is that of
+ * the branch taken, as in any piecewise function.
+ */
+size_t cesa_emicp_tape_bytes(int N, int M, const cesa_params* p);
+int cesa_emicp_forward_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
+                              void* tape, int* d_status, cesa_stream_t stream);
+int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* tape, const float* d_gRt,
+                               float* d_gX, float* d_gY, float* d_gRt0, int* d_status, cesa_stream_t stream);
+
 /* Releases cached device workspaces of the calling process. */
 void cesa_release_workspaces(void);
 
