@@ -754,7 +754,8 @@ int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float*
   cudaFree(mem);
   if (e != cudaSuccess) return map_cuda(e);
   if (rc) return rc;
-  const int form = (ms[1] >= 0.f && ms[1] < ms[0]) ? kFormMaterialised : kFormMatrixFree;
+  // the materialised form also holds N x M floats: it must win by 10%
+  const int form = (ms[1] >= 0.f && ms[1] < 0.9f * ms[0]) ? kFormMaterialised : kFormMatrixFree;
   g_tuned[TuneKey{dev, size_bucket(N), size_bucket(M)}] = form;
   if (form_out) *form_out = form;
   if (ms_matrix_free) *ms_matrix_free = ms[0] * 0.5f;  // per pose update

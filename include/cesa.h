@@ -243,8 +243,10 @@ int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_ou
  * use it; without a recorded decision AUTO uses the matrix-free form. The
  * materialised form is skipped when its N x M matrix would take more than half
  * of the free device memory. Outputs (may be NULL): the chosen form and the
- * milliseconds per pose update of each form (-1 when not run). No counterpart
- * in the reference, which has one (materialised) form.
+ * milliseconds per pose update of each form (-1 when not run). The
+ * materialised form, which also holds the N x M matrix, is chosen only when it
+ * is at least 10% faster. No counterpart in the reference, which has one
+ * (materialised) form.
  */
 int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
                        float* ms_materialised);
