@@ -1,0 +1,81 @@
+"""Small, fixed workloads for profiling single kernels (each runs its kernel
+twice, so that a profiler can skip the first launch):
+
+    python -m cuda_emicp_softassign_gb300.profile_cases <case>
+
+cases:
+  c2_one      softassign_kernel: one config-2 registration (N = M = 2000, default schedule)
+  c3_short    emicp_kernel: config 3 (N = M = 40097) with sigma_inf = 2e-3 (first 16 sigma steps)
+  batch_mid   batch_kernel: the first 64 config-4 pairs, EM-ICP to sigma_inf = 5e-3,
+              Softassign with JMAX = 1, I0 = 2
+  mat_8000    softassign_mat_kernel: N = M = 8000 (K is 258 MB), one pose update, materialised form
+  adj_20000   emicp_adjoint_kernel: forward + backward, N = M = 20000, sigma_inf = 2e-3 (16 steps)
+"""
+import sys
+
+import numpy as np
+
+
+def c2_one():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
+    for _ in range(2):
+        C.softassign(X, Y)
+
+
+def c3_short():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c3_emicp_40097", seed=0)
+    p = C.Params.default(sigma_inf=2e-3)
+    for _ in range(2):
+        C.emicp(X, Y, param=p)
+
+
+def batch_mid():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    args = []
+    for kind, X, Y, _, _ in W.batch_pairs(count=64, seed=0):
+        if kind == "emicp":
+            args.append((C.ALGO_EMICP, X, Y, C.Params.default(sigma_inf=0.005)))
+        else:
+            args.append((C.ALGO_SOFTASSIGN, X, Y, C.Params.default(JMAX=1, I0=2)))
+    for _ in range(2):
+        C.register_batch(args)
+
+
+def mat_8000():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.surface_pair(n=8000, m=8000, seed=1)
+    p = C.Params.default(JMAX=1, I0=1, sinkhorn_form=C.SINKHORN_MATERIALISED)
+    for _ in range(2):
+        C.softassign(X, Y, param=p)
+
+
+def adj_20000():
+    import torch
+
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    from cuda_emicp_softassign_gb300.autograd import emicp_autograd
+    _, X, Y, _, _ = W.make("c3_emicp_40097", seed=0, n=20000)
+    p = C.Params.default(sigma_inf=2e-3)
+    Xd = torch.tensor(np.asarray(X), dtype=torch.float32, device="cuda", requires_grad=True)
+    Yd = torch.tensor(np.asarray(Y), dtype=torch.float32, device="cuda", requires_grad=True)
+    R0 = torch.eye(3, device="cuda", requires_grad=True)
+    t0 = torch.zeros(3, device="cuda", requires_grad=True)
+    for _ in range(2):
+        R, t = emicp_autograd(Xd, Yd, R0, t0, p)
+        (R.sum() + t.sum()).backward()
+    torch.cuda.synchronize()
+
+
+CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000)}
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2 or sys.argv[1] not in CASES:
+        sys.exit("usage: python -m cuda_emicp_softassign_gb300.profile_cases {%s}" % "|".join(CASES))
+    CASES[sys.argv[1]]()
