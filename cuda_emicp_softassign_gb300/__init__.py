@@ -145,6 +145,12 @@ def lib():
         L.cesa_emicp_forward_device.restype = _i
         L.cesa_emicp_backward_device.argtypes = [_i, _i, _p, _p, _p, _p, _p, _p, _p, _p]
         L.cesa_emicp_backward_device.restype = _i
+        L.cesa_softassign_tape_bytes.argtypes = [_i, _i, _p]
+        L.cesa_softassign_tape_bytes.restype = ctypes.c_size_t
+        L.cesa_softassign_forward_device.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p, _p]
+        L.cesa_softassign_forward_device.restype = _i
+        L.cesa_softassign_backward_device.argtypes = [_i, _i, _p, _p, _p, _p, _p, _p, _p, _p]
+        L.cesa_softassign_backward_device.restype = _i
         L.cesa_tune_sinkhorn.argtypes = [_i, _i, _p, _p, _p, _p]
         L.cesa_tune_sinkhorn.restype = _i
         L.cesa_self_test_waits.argtypes = [_i, _i, _p, _p]

@@ -576,6 +576,29 @@ TapeLayout tape_layout(int N, int M, long nsteps) {
   t.total = off;
   return t;
 }
+// Softassign tape: header, packed clouds, and per pose update the input pose
+// (centred frame, 16 floats) and the input slack s (N) and u (M).
+struct SaTapeLayout {
+  size_t hdr, X, Y, pose, s, u, total;
+};
+SaTapeLayout sa_tape_layout(int N, int M, long nsteps) {
+  SaTapeLayout t;
+  size_t off = 0;
+  t.hdr = off;
+  off += align256(sizeof(CenterHdr));
+  t.X = off;
+  off += align256(sizeof(float4) * (size_t)N);
+  t.Y = off;
+  off += align256(sizeof(float4) * (size_t)M);
+  t.pose = off;
+  off += align256(sizeof(float) * 16 * (size_t)nsteps);
+  t.s = off;
+  off += align256(sizeof(float) * (size_t)N * (size_t)nsteps);
+  t.u = off;
+  off += align256(sizeof(float) * (size_t)M * (size_t)nsteps);
+  t.total = off;
+  return t;
+}
 }  // namespace
 
 extern "C" {
@@ -667,6 +690,126 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
   C.last_kind = 1;
   C.last_trace_steps = 0;
   return map_cuda((cudaError_t)enqueue_emicp_adjoint(L, C.ws.p, C.ws.bytes, st));
+}
+
+size_t cesa_softassign_tape_bytes(int N, int M, const cesa_params* p) {
+  if (N < 1 || M < 1 || check_sa_params(p)) return 0;
+  return sa_tape_layout(N, M, (long)p->JMAX * p->I0).total;
+}
+
+int cesa_softassign_forward_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
+                                   void* tape, int* d_status, cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!dRt || !tape) return CESA_ERR_INVALID_ARGUMENT;
+  rc = check_sa_params(p);
+  if (rc) return rc;
+  const long nsteps = (long)p->JMAX * p->I0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, kFormMatrixFree, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  const SaTapeLayout T = sa_tape_layout(N, M, nsteps);
+  char* tb = static_cast<char*>(tape);
+  SoftassignLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.JMAX = p->JMAX;
+  L.I0 = p->I0;
+  L.I1 = p->I1;
+  L.alpha = p->alpha;
+  L.T_0 = p->T_0;
+  L.TFACTOR = p->TFACTOR;
+  L.moutlier = p->moutlier;
+  L.form = kFormMatrixFree;  // the tape is recorded by the matrix-free kernel
+  L.dRt = dRt;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  L.tape_pose = reinterpret_cast<float*>(tb + T.pose);
+  L.tape_s = reinterpret_cast<float*>(tb + T.s);
+  L.tape_u = reinterpret_cast<float*>(tb + T.u);
+  C.last_kind = 2;
+  C.last_trace_steps = 0;
+  const int k = enqueue_softassign(L, C.ws.p, C.ws.bytes, st, nullptr);
+  if (k) return map_cuda((cudaError_t)k);
+  CenterHdr* hdr = nullptr;
+  float4 *rows = nullptr, *cols = nullptr;
+  softassign_ws_views(C.ws.p, N, M, dev, &hdr, &rows, &cols);
+  e = cudaMemcpyAsync(tb + T.hdr, hdr, sizeof(CenterHdr), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tb + T.X, rows, sizeof(float4) * (size_t)N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tb + T.Y, cols, sizeof(float4) * (size_t)M, cudaMemcpyDeviceToDevice, st);
+  return map_cuda(e);
+}
+
+int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const void* tape, const float* d_gRt,
+                                    float* d_gX, float* d_gY, float* d_gRt0, int* d_status, cesa_stream_t stream) {
+  if (N < 1 || M < 1 || !tape || !d_gRt || !d_gX || !d_gY || !d_gRt0) return CESA_ERR_INVALID_ARGUMENT;
+  int rc = check_sa_params(p);
+  if (rc) return rc;
+  const long nsteps = (long)p->JMAX * p->I0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  const size_t need = softassign_step_adjoint_ws_need(N, M, p->I1);
+  const size_t o_gp = align256(need), o_gs = o_gp + 256, o_gu = o_gs + align256(sizeof(float) * (size_t)N);
+  const size_t total = o_gu + align256(sizeof(float) * (size_t)M);
+  cudaError_t e = C.ws.ensure(total);
+  if (e != cudaSuccess) return map_cuda(e);
+  char* wb = static_cast<char*>(C.ws.p);
+  float* gp = reinterpret_cast<float*>(wb + o_gp);
+  float* gs = reinterpret_cast<float*>(wb + o_gs);
+  float* gu = reinterpret_cast<float*>(wb + o_gu);
+  const SaTapeLayout T = sa_tape_layout(N, M, nsteps);
+  const char* tb = static_cast<const char*>(tape);
+  e = cudaMemcpyAsync(gp, d_gRt, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_gX, 0, sizeof(float) * 3 * (size_t)N, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_gY, 0, sizeof(float) * 3 * (size_t)M, st);
+  if (e != cudaSuccess) return map_cuda(e);
+  // temperatures of the updates, stepped in FP32 as the forward does
+  std::vector<float> Ts;
+  Ts.reserve((size_t)nsteps);
+  float Tk = p->T_0;
+  for (int j = 0; j < p->JMAX; ++j) {
+    for (int i = 0; i < p->I0; ++i) Ts.push_back(Tk);
+    Tk = Tk * p->TFACTOR;
+  }
+  SoftassignStepAdjoint J{};
+  J.X = reinterpret_cast<const float4*>(tb + T.X);
+  J.Y = reinterpret_cast<const float4*>(tb + T.Y);
+  J.hdr = reinterpret_cast<const CenterHdr*>(tb + T.hdr);
+  J.N = N;
+  J.M = M;
+  J.I1 = p->I1;
+  J.alpha = p->alpha;
+  J.gX = d_gX;
+  J.gY = d_gY;
+  J.g_pose_out = gp;
+  J.g_pose_in = gp;
+  J.g_s_in = gs;
+  J.g_u_in = gu;
+  for (long n = nsteps - 1; n >= 0; --n) {
+    J.T = Ts[(size_t)n];
+    J.pose = reinterpret_cast<const float*>(tb + T.pose) + (size_t)n * 16;
+    J.s = reinterpret_cast<const float*>(tb + T.s) + (size_t)n * N;
+    J.u = reinterpret_cast<const float*>(tb + T.u) + (size_t)n * M;
+    J.g_s_out = n == nsteps - 1 ? nullptr : gs;
+    J.g_u_out = n == nsteps - 1 ? nullptr : gu;
+    const int k = enqueue_softassign_step_adjoint(J, C.ws.p, need, st);
+    if (k) return map_cuda((cudaError_t)k);
+  }
+  e = cudaMemcpyAsync(d_gRt0, gp, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  // the backward has no device-side waits: its status is set once all launches are queued
+  if (e == cudaSuccess && d_status) e = cudaMemsetAsync(d_status, 0, sizeof(int), st);
+  C.last_kind = 2;
+  C.last_trace_steps = 0;
+  return map_cuda(e);
 }
 
 int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,

@@ -70,76 +70,12 @@ __device__ void em_step_adjoint(const float* rec, const float (&gRo)[9], const f
   float Xc[3], Yc[3], S[9];
   em_moments_to_S(m, Xc, Yc, S);
   const float L = df_val(m[0]);
-  float q[4];
+  float q[4], V[4][4];
   for (int k = 0; k < 4; ++k) q[k] = rec[64 + k];
-  float R[9], tdummy[3];
-  quat_to_pose<float>(q, Xc, Yc, R, tdummy);
-  // t' = Xc - R Yc
-  float gXc[3], gYc[3], gR[9];
-  for (int i = 0; i < 3; ++i) gXc[i] = gto[i];
-  for (int j = 0; j < 3; ++j) gYc[j] = -(R[j] * gto[0] + R[3 + j] * gto[1] + R[6 + j] * gto[2]);
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) gR[3 * i + j] = gRo[3 * i + j] - gto[i] * Yc[j];
-  // R(q), as in quat_to_pose
-  const float q0 = q[0], qx = q[1], qy = q[2], qz = q[3];
-  const float dR[9][4] = {{q0, qx, -qy, -qz}, {-qz, qy, qx, -q0}, {qy, qz, q0, qx},
-                          {qz, qy, qx, q0},   {q0, -qx, qy, -qz}, {-qx, -q0, qz, qy},
-                          {-qy, qz, -q0, qx}, {qx, q0, qz, qy},   {q0, -qx, -qy, qz}};
-  float gq[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int k = 0; k < 9; ++k)
-    for (int a = 0; a < 4; ++a) gq[a] += 2.f * gR[k] * dR[k][a];
-  // top eigenvector of N(S): eigenbasis from the tape, eigenvalues as
-  // Rayleigh quotients; the column closest to q is the top one
-  float N[4][4];
-  horn_matrix<float>(S, N);
-  float V[4][4], lam[4];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) V[i][j] = rec[48 + 4 * i + j];
-  int top = 0;
-  float best = -1.f;
-  for (int j = 0; j < 4; ++j) {
-    float nv[4], vv = 0.f, vq = 0.f;
-    for (int i = 0; i < 4; ++i) nv[i] = N[i][0] * V[0][j] + N[i][1] * V[1][j] + N[i][2] * V[2][j] + N[i][3] * V[3][j];
-    lam[j] = 0.f;
-    for (int i = 0; i < 4; ++i) {
-      lam[j] += V[i][j] * nv[i];
-      vv += V[i][j] * V[i][j];
-      vq += V[i][j] * q[i];
-    }
-    lam[j] /= vv;
-    const float a = fabsf(vq) * rsqrtf(vv);
-    if (a > best) {
-      best = a;
-      top = j;
-    }
-  }
-  float G[4][4];
-  for (int i = 0; i < 4; ++i)
-    for (int k = 0; k < 4; ++k) G[i][k] = 0.f;
-  for (int j = 0; j < 4; ++j) {
-    if (j == top) continue;
-    float vv = 0.f, vg = 0.f;
-    for (int i = 0; i < 4; ++i) {
-      vv += V[i][j] * V[i][j];
-      vg += V[i][j] * gq[i];
-    }
-    const float c = vg / (vv * (lam[top] - lam[j]));
-    for (int i = 0; i < 4; ++i)
-      for (int k = 0; k < 4; ++k) G[i][k] += c * V[i][j] * q[k];
-  }
-  // N(S) is linear in S (horn_matrix); its adjoint
-  const float a01 = G[0][1] + G[1][0], a02 = G[0][2] + G[2][0], a03 = G[0][3] + G[3][0];
-  const float a12 = G[1][2] + G[2][1], a13 = G[1][3] + G[3][1], a23 = G[2][3] + G[3][2];
-  float gS[9];
-  gS[0] = G[0][0] + G[1][1] - G[2][2] - G[3][3];  // Sxx
-  gS[4] = G[0][0] - G[1][1] + G[2][2] - G[3][3];  // Syy
-  gS[8] = G[0][0] - G[1][1] - G[2][2] + G[3][3];  // Szz
-  gS[5] = a01 + a23;                              // Syz
-  gS[7] = -a01 + a23;                             // Szy
-  gS[6] = a02 + a13;                              // Szx
-  gS[2] = -a02 + a13;                             // Sxz
-  gS[1] = a03 + a12;                              // Sxy
-  gS[3] = -a03 + a12;                             // Syx
+  float gS[9], gXc[3], gYc[3];
+  horn_pose_adjoint(S, Xc, Yc, q, V, gRo, gto, gS, gXc, gYc);
   // S[i + 3j] = Q[i + 3j] - L Xc_i Yc_j, Xc = U / L, Yc = P / L
   float gL = 0.f;
   for (int i = 0; i < 3; ++i)

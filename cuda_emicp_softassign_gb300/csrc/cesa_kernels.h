@@ -66,6 +66,11 @@ struct SoftassignLaunch {
   unsigned long long* timeline;
   int timeline_cap;
   uint64_t timeout_ns;
+  // optional tape of the matrix-free form, per pose update: the input pose in
+  // the centred frame [nsteps][16] and the input slack s [nsteps][N], u [nsteps][M]
+  float* tape_pose;
+  float* tape_s;
+  float* tape_u;
 };
 
 // One pair of a batched launch (device pointers).
@@ -133,6 +138,31 @@ size_t emicp_adjoint_ws_need(int N, int M, int device);
 int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st);
 // The forward workspace's packed clouds and centring header (for the tape).
 void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);
+
+void softassign_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);
+
+// Adjoint of one Softassign inner iteration (recomputing). Device pointers.
+struct SoftassignStepAdjoint {
+  const float4* X;        // X' centred (N), as packed by the forward
+  const float4* Y;        // Y' centred (M)
+  const CenterHdr* hdr;
+  int N, M, I1;
+  float T, alpha;
+  const float* pose;      // [12] input pose, centred frame (R, t')
+  const float* s;         // [N] input slack
+  const float* u;         // [M]
+  const float* g_pose_out;  // [12] dL/dR, dL/dt of the output pose, caller frame
+  const float* g_s_out;   // [N] dL/ds of the output slack (nullptr: zero)
+  const float* g_u_out;   // [M] (nullptr: zero)
+  float* gX;              // SoA [3N], accumulated
+  float* gY;              // SoA [3M], accumulated
+  float* g_pose_in;       // [12] dL/d(R, t) of the input pose, caller frame (written)
+  float* g_s_in;          // [N] (written; may alias g_s_out)
+  float* g_u_in;          // [M] (written; may alias g_u_out)
+  float* pose_out;        // optional [12]: the recomputed output pose, centred frame
+};
+size_t softassign_step_adjoint_ws_need(int N, int M, int I1);
+int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st);
 
 // Control-block status of the last launch that used workspace ws.
 int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written = nullptr);

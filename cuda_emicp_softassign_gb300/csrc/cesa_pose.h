@@ -272,4 +272,79 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
   return 0;
 }
 
+// Adjoint of the pose update (R, t) = (R(q), Xc - R(q) Yc) with q the top
+// eigenvector of Horn's N(S) (horn_matrix, quat_to_pose): from dL/dR (9,
+// row-major) and dL/dt of the output, dL/dS (h_S layout), dL/dXc and dL/dYc.
+// V: the eigenbasis of N(S) (columns; as left by horn_quaternion), q the
+// quaternion used. Eigenvalues are Rayleigh quotients; the column closest to q
+// is the top one; dq = sum over the other eigenvectors of v_j (v_j^T dN q) /
+// (l_top - l_j).
+template <typename T>
+CESA_HD void horn_pose_adjoint(const T S[9], const T Xc[3], const T Yc[3], const T q[4], const T (&V)[4][4],
+                               const T gRo[9], const T gto[3], T gS[9], T gXc[3], T gYc[3]) {
+  T R[9], tdummy[3];
+  quat_to_pose<T>(q, Xc, Yc, R, tdummy);
+  // t = Xc - R Yc
+  T gR[9];
+  for (int i = 0; i < 3; ++i) gXc[i] = gto[i];
+  for (int j = 0; j < 3; ++j) gYc[j] = -(R[j] * gto[0] + R[3 + j] * gto[1] + R[6 + j] * gto[2]);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) gR[3 * i + j] = gRo[3 * i + j] - gto[i] * Yc[j];
+  // R(q): dR_k / dq_a = 2 dR[k][a]
+  const T q0 = q[0], qx = q[1], qy = q[2], qz = q[3];
+  const T dR[9][4] = {{q0, qx, -qy, -qz}, {-qz, qy, qx, -q0}, {qy, qz, q0, qx},
+                      {qz, qy, qx, q0},   {q0, -qx, qy, -qz}, {-qx, -q0, qz, qy},
+                      {-qy, qz, -q0, qx}, {qx, q0, qz, qy},   {q0, -qx, -qy, qz}};
+  T gq[4] = {T(0), T(0), T(0), T(0)};
+  for (int k = 0; k < 9; ++k)
+    for (int a = 0; a < 4; ++a) gq[a] += T(2) * gR[k] * dR[k][a];
+  T N[4][4];
+  horn_matrix<T>(S, N);
+  T lam[4];
+  int top = 0;
+  T best = T(-1);
+  for (int j = 0; j < 4; ++j) {
+    T nv[4], vv = T(0), vq = T(0);
+    for (int i = 0; i < 4; ++i) nv[i] = N[i][0] * V[0][j] + N[i][1] * V[1][j] + N[i][2] * V[2][j] + N[i][3] * V[3][j];
+    lam[j] = T(0);
+    for (int i = 0; i < 4; ++i) {
+      lam[j] += V[i][j] * nv[i];
+      vv += V[i][j] * V[i][j];
+      vq += V[i][j] * q[i];
+    }
+    lam[j] = t_div(lam[j], vv);
+    const T a = t_abs(vq) * t_rsqrt(vv);
+    if (a > best) {
+      best = a;
+      top = j;
+    }
+  }
+  T G[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int k = 0; k < 4; ++k) G[i][k] = T(0);
+  for (int j = 0; j < 4; ++j) {
+    if (j == top) continue;
+    T vv = T(0), vg = T(0);
+    for (int i = 0; i < 4; ++i) {
+      vv += V[i][j] * V[i][j];
+      vg += V[i][j] * gq[i];
+    }
+    const T c = t_div(vg, vv * (lam[top] - lam[j]));
+    for (int i = 0; i < 4; ++i)
+      for (int k = 0; k < 4; ++k) G[i][k] += c * V[i][j] * q[k];
+  }
+  // N(S) is linear in S (horn_matrix); its adjoint
+  const T a01 = G[0][1] + G[1][0], a02 = G[0][2] + G[2][0], a03 = G[0][3] + G[3][0];
+  const T a12 = G[1][2] + G[2][1], a13 = G[1][3] + G[3][1], a23 = G[2][3] + G[3][2];
+  gS[0] = G[0][0] + G[1][1] - G[2][2] - G[3][3];  // Sxx
+  gS[4] = G[0][0] - G[1][1] + G[2][2] - G[3][3];  // Syy
+  gS[8] = G[0][0] - G[1][1] - G[2][2] + G[3][3];  // Szz
+  gS[5] = a01 + a23;                              // Syz
+  gS[7] = -a01 + a23;                             // Szy
+  gS[6] = a02 + a13;                              // Szx
+  gS[2] = -a02 + a13;                             // Sxz
+  gS[1] = a03 + a12;                              // Sxy
+  gS[3] = -a03 + a12;                             // Syx
+}
+
 }  // namespace cesa

@@ -63,6 +63,9 @@ struct SoftArgs {
   unsigned long long* tl;
   int tl_cap;
   uint64_t timeout_ns;
+  float* tape_pose;    // optional [nsteps][16]: input pose of each update (centred frame)
+  float* tape_s;       // optional [nsteps][N]: input slack s of each update
+  float* tape_u;       // optional [nsteps][M]
 };
 
 // Sum of the S slice partials of point i (deferred completion), 8 loads in flight.
@@ -279,6 +282,16 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
 #pragma unroll
       for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
+      if (A.tape_pose) {
+        // the update's inputs for the adjoint: s and u are the current ping-pong
+        // buffers, which are next overwritten two grid barriers from here
+        if (blockIdx.x == 0 && tid < 12) A.tape_pose[(size_t)step * 16 + tid] = s_pose[tid];
+        const int stride = (int)G * kThreads;
+        for (int i = blockIdx.x * kThreads + tid; i < A.N; i += stride)
+          A.tape_s[(size_t)step * A.N + i] = __ldcg(A.sbuf + (size_t)sp * Np + i);
+        for (int i = blockIdx.x * kThreads + tid; i < A.M; i += stride)
+          A.tape_u[(size_t)step * A.M + i] = __ldcg(A.ubuf + (size_t)up * Mp + i);
+      }
       __syncthreads();
       const SinkElem se{nk, c0};
       for (int k = 0; k < A.I1 && ok; ++k) {
@@ -507,6 +520,14 @@ SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
 }
 }  // namespace
 
+void softassign_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols) {
+  const SaPlan P = plan_sa(N, M, device);
+  SaCarved w = carve_sa(ws, P, N, M, nullptr);
+  *hdr = w.hdr;
+  *rows = w.rows;
+  *cols = w.cols;
+}
+
 size_t softassign_ws_need(int N, int M, int form, int device) {
   if (form == kFormMaterialised) return softassign_mat_ws_need(N, M, device);
   const SaPlan P = plan_sa(N, M, device);
@@ -581,6 +602,9 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.tl = L.timeline;
   A.tl_cap = L.timeline_cap;
   A.timeout_ns = L.timeout_ns;
+  A.tape_pose = L.tape_pose;
+  A.tape_s = L.tape_s;
+  A.tape_u = L.tape_u;
   void* args[] = {(void*)&A};
   e = cudaLaunchCooperativeKernel((const void*)softassign_kernel, dim3(P.grid), dim3(kThreads), args,
                                   P.smem, st);

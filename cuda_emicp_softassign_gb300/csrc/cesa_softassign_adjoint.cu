@@ -1,0 +1,831 @@
+// Adjoint of Softassign (src/softassign.cu:486-822) for sm_103a.
+//
+// One inner iteration (src/softassign.cu:494-798) maps (pose, s, u) to
+// (pose', s', u') at temperature T for fixed X, Y. With
+// K_ij = exp((alpha - |x_i - z_j|^2)/T)/sqrt(T), z_j = R y_j + t, a^0 = 1,
+// b^0 = 1, s^0 = s, u^0 = u:
+//   row pass k:    r^k = K b^k,       rs^k = a^k r^k + s^k,  a^{k+1} = a^k/rs^k,  s^{k+1} = s^k/rs^k
+//   column pass k: c^k = K^T a^{k+1}, cs^k = b^k c^k + u^k,  b^{k+1} = b^k/cs^k,  u^{k+1} = u^k/cs^k
+//   final:  rho = K b, w = a rho, sumM = sum w, Xc = sum w x / sumM,
+//           Yc = sum cs y / sumM, p_i = w_i x_i - Xc, h_j = b_j (cs_j y_j - Yc),
+//           V = K h, S = sum_i a_i p_i V_i^T, (R', t') = Horn(S, Xc, Yc)
+// with a = a^{I1}, b = b^{I1}, cs = cs^{I1-1}, all in the caller's frame
+// (the reference's S is not translation invariant). The backward of one
+// iteration recomputes these vectors (K is never stored), then runs the
+// chain rule through Horn's pose (horn_pose_adjoint), the final stage, and
+// the column and row passes in reverse. Each pass's adjoint is one K or K^T
+// product. dL/dK is a sum of 4 + 2 I1 rank-1 terms alpha_m beta_m^T:
+//   (g(V)_d, h_d) d = 0..2,  (g(rho), b^{I1}),  (a^{k+1}, g(c^k)),  (g(r^k), b^k)
+// so dL/dx and dL/dz come from two more recomputing sweeps (own rows, own
+// columns): dL/dx_i = (2/T) sum_j G_ij (z_j - x_i), G = K .* dL/dK, and
+// likewise for z. dL/dy = R^T dL/dz plus the direct terms of Yc and h;
+// dL/dR, dL/dt of the input pose are sum dL/dz y^T and sum dL/dz.
+//
+// Sweeps are plain launches over (owned block, streamed slice) tiles: each
+// thread owns 4 points (two packed FP32 pairs) and the streamed points pass
+// through shared memory. Slice partials are summed in slice order, so every
+// result is deterministic. O(N + M) steps are small kernels; sums over all
+// points use compensated arithmetic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "cesa_kernels.h"
+#include "cesa_ops.cuh"
+#include "cesa_pose.h"
+#include "cesa_prep.cuh"
+
+namespace cesa {
+namespace {
+
+constexpr int kSwT = 128;                 // threads per sweep block
+constexpr int kOwnBlk = kSwT * 4;         // owned points per sweep block (4 per thread)
+constexpr int kTile = kSwT;               // streamed points per shared-memory tile
+constexpr int kMaxTerms = 10;             // rank-1 terms per gradient sweep
+constexpr int kGlue = 256;                // threads of the per-point kernels
+
+struct Pose12 {
+  float R[9], t[3];
+};
+
+__device__ __forceinline__ Pose12 load_pose(const float* p) {
+  Pose12 P;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) P.R[k] = __ldg(p + k);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) P.t[k] = __ldg(p + 9 + k);
+  return P;
+}
+
+__device__ __forceinline__ float4 posed(const Pose12& P, float4 y) {
+  return make_float4(P.R[0] * y.x + P.R[1] * y.y + P.R[2] * y.z + P.t[0],
+                     P.R[3] * y.x + P.R[4] * y.y + P.R[5] * y.z + P.t[1],
+                     P.R[6] * y.x + P.R[7] * y.y + P.R[8] * y.z + P.t[2], 0.f);
+}
+
+// One sweep's geometry: the owned side (n_own points, optionally posed) and the
+// streamed side, cut into S slices of len points.
+struct SweepIO {
+  const float4* own;
+  const float4* str;
+  int n_own, n_str;
+  bool own_posed, str_posed;
+  int S, len;
+};
+
+// Owned point of (thread, pair p, lane l): coalesced per (p, l).
+__device__ __forceinline__ int own_index(int p, int l) {
+  return blockIdx.x * kOwnBlk + (2 * p + l) * kSwT + (int)threadIdx.x;
+}
+
+__device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, float2 (&q)[2][3]) {
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    float v[2][3];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int i = own_index(p, l);
+      float4 o = i < io.n_own ? io.own[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (io.own_posed) o = posed(P, o);
+      v[l][0] = -o.x;
+      v[l][1] = -o.y;
+      v[l][2] = -o.z;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) q[p][d] = make_float2(v[0][d], v[1][d]);
+  }
+}
+
+__device__ __forceinline__ void kernel_consts(float T, float alpha, float& nk, float& c0) {
+  // K = exp((alpha - d^2)/T)/sqrt(T) = 2^(c0 + nk d^2), as the forward kernels form it
+  const float kk = kLog2e / T;
+  nk = -kk;
+  c0 = fmaf(alpha, kk, -0.5f * log2f(T));
+}
+
+// part[sl][m][i] = sum over slice sl of K(own_i, str_j) w_m[j], m < NW.
+template <int NW>
+__global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, float T, float alpha,
+                                                    const float* w, int ldw, float* part) {
+  __shared__ float4 s_pt[kTile];
+  __shared__ float s_w[NW > 1 ? NW - 1 : 1][kTile];
+  float nk, c0;
+  kernel_consts(T, alpha, nk, c0);
+  const Pose12 P = load_pose(pose);
+  float2 q[2][3];
+  load_owned(io, P, q);
+  float2 acc[2][NW];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int m = 0; m < NW; ++m) acc[p][m] = make_float2(0.f, 0.f);
+  const int sl = blockIdx.y;
+  const int jb = sl * io.len, je = min(jb + io.len, io.n_str);
+  for (int j0 = jb; j0 < je; j0 += kTile) {
+    const int n = min(kTile, je - j0);
+    __syncthreads();
+    if ((int)threadIdx.x < n) {
+      const int j = j0 + threadIdx.x;
+      float4 s = io.str[j];
+      if (io.str_posed) s = posed(P, s);
+      s.w = w[j];
+#pragma unroll
+      for (int m = 1; m < NW; ++m) s_w[m - 1][threadIdx.x] = w[(size_t)m * ldw + j];
+      s_pt[threadIdx.x] = s;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int j = 0; j < n; ++j) {
+      const float4 s = s_pt[j];
+      float wm[NW];
+      wm[0] = s.w;
+#pragma unroll
+      for (int m = 1; m < NW; ++m) wm[m] = s_w[m - 1][j];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q[p], s), dup2(nk), dup2(c0)));
+#pragma unroll
+        for (int m = 0; m < NW; ++m) acc[p][m] = __ffma2_rn(e, dup2(wm[m]), acc[p][m]);
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int i = own_index(p, l);
+      if (i < io.n_own)
+#pragma unroll
+        for (int m = 0; m < NW; ++m) part[((size_t)sl * NW + m) * io.n_own + i] = l ? acc[p][m].y : acc[p][m].x;
+    }
+}
+
+// Rank-1 terms of dL/dK: own side alpha, streamed side beta.
+struct Terms {
+  const float* own[kMaxTerms];
+  const float* str[kMaxTerms];
+  int n;
+};
+
+// part[sl][d][i] = (2/T) sum over slice sl of G_ij (s_j - o_i)_d with
+// G_ij = K_ij sum_m own_m[i] str_m[j].
+__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, float T, float alpha,
+                                                     Terms tm, float* part) {
+  __shared__ float4 s_pt[kTile];
+  __shared__ float s_b[kMaxTerms][kTile];
+  float nk, c0;
+  kernel_consts(T, alpha, nk, c0);
+  const Pose12 P = load_pose(pose);
+  float2 q[2][3];
+  load_owned(io, P, q);
+  float2 al[2][kMaxTerms];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int m = 0; m < kMaxTerms; ++m) {
+      const int i0 = own_index(p, 0), i1 = own_index(p, 1);
+      al[p][m] = make_float2(m < tm.n && i0 < io.n_own ? tm.own[m][i0] : 0.f,
+                             m < tm.n && i1 < io.n_own ? tm.own[m][i1] : 0.f);
+    }
+  float2 g[2][3];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[p][d] = make_float2(0.f, 0.f);
+  const int sl = blockIdx.y;
+  const int jb = sl * io.len, je = min(jb + io.len, io.n_str);
+  for (int j0 = jb; j0 < je; j0 += kTile) {
+    const int n = min(kTile, je - j0);
+    __syncthreads();
+    if ((int)threadIdx.x < n) {
+      const int j = j0 + threadIdx.x;
+      float4 s = io.str[j];
+      if (io.str_posed) s = posed(P, s);
+      s_pt[threadIdx.x] = s;
+#pragma unroll
+      for (int m = 0; m < kMaxTerms; ++m) s_b[m][threadIdx.x] = m < tm.n ? tm.str[m][j] : 0.f;
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+      const float4 s = s_pt[j];
+      float b[kMaxTerms];
+#pragma unroll
+      for (int m = 0; m < kMaxTerms; ++m) b[m] = s_b[m][j];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const float2 dx = __fadd2_rn(dup2(s.x), q[p][0]);
+        const float2 dy = __fadd2_rn(dup2(s.y), q[p][1]);
+        const float2 dz = __fadd2_rn(dup2(s.z), q[p][2]);
+        float2 d2 = __fmul2_rn(dx, dx);
+        d2 = __ffma2_rn(dy, dy, d2);
+        d2 = __ffma2_rn(dz, dz, d2);
+        const float2 e = ex2_pair(__ffma2_rn(d2, dup2(nk), dup2(c0)));
+        float2 gs = __fmul2_rn(al[p][0], dup2(b[0]));
+#pragma unroll
+        for (int m = 1; m < kMaxTerms; ++m) gs = __ffma2_rn(al[p][m], dup2(b[m]), gs);
+        const float2 G = __fmul2_rn(e, gs);
+        g[p][0] = __ffma2_rn(G, dx, g[p][0]);
+        g[p][1] = __ffma2_rn(G, dy, g[p][1]);
+        g[p][2] = __ffma2_rn(G, dz, g[p][2]);
+      }
+    }
+  }
+  const float sc = 2.f / T;
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int i = own_index(p, l);
+      if (i < io.n_own)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) part[((size_t)sl * 3 + d) * io.n_own + i] = sc * (l ? g[p][d].y : g[p][d].x);
+    }
+}
+
+// out[m][i] (+)= sum over slices of part[sl][m][i], in slice order.
+__global__ void k_reduce_slices(const float* __restrict__ part, int S, int NW, int n, float* out, int ldo, int acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int k = 0; k < S; ++k) s += part[((size_t)k * NW + m) * n + i];
+  float* o = out + (size_t)m * ldo + i;
+  *o = acc ? *o + s : s;
+}
+
+// ------------------------------------------------------------- O(N + M) steps
+// Scalars of one iteration (double).
+enum : int {
+  kSsum = 0,     // sumM
+  kSXc = 1,      // Xc (caller frame)
+  kSXcp = 4,     // Xc - oX
+  kSYc = 7,      // Yc (caller frame)
+  kSYd = 10,     // Yc - oY
+  kSS = 13,      // S[i + 3 j]
+  kSq = 22,      // q
+  kSV = 26,      // eigenbasis V[4][4]
+  kSgS = 42,     // dL/dS
+  kSgXc = 51,    // dL/dXc
+  kSgYc = 54,    // dL/dYc
+  kSgsum = 57,   // dL/dsumM
+  kScalN = 64
+};
+
+struct Vecs {
+  int N, M, I1;
+  const float4* X;  // X' (centred)
+  const float4* Y;  // Y' (centred, unposed)
+  const CenterHdr* hdr;
+  const float* pose;  // centred-frame input pose (R, t')
+  float *a, *s;       // [I1 + 1][N]
+  float *b, *u;       // [I1 + 1][M]
+  float *r, *rs;      // [I1][N]
+  float *c, *cs;      // [I1][M]
+  float *rho, *w;     // N
+  float* V;           // [3][N]
+  float* h;           // [3][M]
+  double* scal;       // kScalN
+  float* pose_out;    // 12, centred frame
+  float *ga, *gs;     // N
+  float *gb, *gu, *gcs;  // M
+  float* gV;          // [3][N]
+  float* gp;          // [3][N]
+  float* gw;          // N: known part of dL/dw
+  float* grho;        // N
+  float* wt4;         // [4][N]: weights of the K^T sweep (g(V), a gw)
+  float* gh;          // [4][M]: K^T of wt4
+  float* gr;          // [I1][N] g(r^k)
+  float* gc;          // [I1][M] g(c^k)
+  float* gX;          // [3][N]
+  float* gZ;          // [3][M]
+  float* gY;          // [3][M]
+};
+
+__global__ void k_fill(float* p, int n, float v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+
+// Pass completion: t = a r + s, a' = a / t, s' = s / t (row pass; the column
+// pass is the same with b, c, u).
+__global__ void k_pass_done(const float* a, const float* r, const float* s, float* t, float* an, float* sn, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = fmaf(a[i], r[i], s[i]);
+  t[i] = v;
+  an[i] = a[i] / v;
+  sn[i] = s[i] / v;
+}
+
+// One block: w = a rho, sumM, Xc and Yc (compensated), as the forward's moments.
+__global__ void __launch_bounds__(1024) k_centres(Vecs A) {
+  __shared__ df red[8 * 32];
+  const float* aF = A.a + (size_t)A.I1 * A.N;
+  const float* csF = A.cs + (size_t)(A.I1 - 1) * A.M;
+  df v[8];
+  for (int k = 0; k < 8; ++k) v[k] = df_make(0.f);
+  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
+    const float4 x = A.X[i];
+    const float w = aF[i] * A.rho[i];
+    A.w[i] = w;
+    df_add(v[0], w);
+    df_add_prod(v[1], w, x.x);
+    df_add_prod(v[2], w, x.y);
+    df_add_prod(v[3], w, x.z);
+  }
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
+    const float4 y = A.Y[j];
+    df_add(v[4], csF[j]);
+    df_add_prod(v[5], csF[j], y.x);
+    df_add_prod(v[6], csF[j], y.y);
+    df_add_prod(v[7], csF[j], y.z);
+  }
+  block_reduce_df<8>(v, red);
+  if (threadIdx.x == 0) {
+    const double sm = df_dbl(v[0]), scs = df_dbl(v[4]);
+    A.scal[kSsum] = sm;
+    for (int k = 0; k < 3; ++k) {
+      const double xcp = df_dbl(v[1 + k]) / sm;
+      // Yc - oY = sum cs y' / sumM + (sum cs / sumM - 1) oY
+      const double yd = df_dbl(v[5 + k]) / sm + (scs / sm - 1.0) * (double)A.hdr->oY[k];
+      A.scal[kSXcp + k] = xcp;
+      A.scal[kSXc + k] = xcp + (double)A.hdr->oX[k];
+      A.scal[kSYd + k] = yd;
+      A.scal[kSYc + k] = yd + (double)A.hdr->oY[k];
+    }
+  }
+}
+
+// h_j = b_j (cs_j y_j - Yc) = b_j (cs_j y'_j - Yd + (cs_j - 1) oY), [3][M].
+__global__ void k_h(Vecs A) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= A.M) return;
+  const float* bF = A.b + (size_t)A.I1 * A.M;
+  const float cs = A.cs[(size_t)(A.I1 - 1) * A.M + j];
+  const float4 y = A.Y[j];
+  const float yv[3] = {y.x, y.y, y.z};
+  for (int d = 0; d < 3; ++d)
+    A.h[(size_t)d * A.M + j] =
+        bF[j] * (fmaf(cs, yv[d], -(float)A.scal[kSYd + d]) + (cs - 1.f) * A.hdr->oY[d]);
+}
+
+// p_i = w_i x_i - Xc = w_i x'_i - Xc' + (w_i - 1) oX
+__device__ __forceinline__ void p_of(const Vecs& A, int i, float p[3]) {
+  const float4 x = A.X[i];
+  const float xv[3] = {x.x, x.y, x.z};
+  const float w = A.w[i];
+  for (int d = 0; d < 3; ++d) p[d] = fmaf(w, xv[d], -(float)A.scal[kSXcp + d]) + (w - 1.f) * A.hdr->oX[d];
+}
+
+// One block: S = sum_i a_i p_i V_i^T (S[p + 3 q] = sum a p_p V_q), then Horn's
+// pose; the output pose in the centred frame t' = Xc' - R (Yc - oY) as the
+// forward kernel forms it.
+__global__ void __launch_bounds__(1024) k_S_pose(Vecs A) {
+  __shared__ df red[9 * 32];
+  const float* aF = A.a + (size_t)A.I1 * A.N;
+  df v[9];
+  for (int k = 0; k < 9; ++k) v[k] = df_make(0.f);
+  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
+    float p[3];
+    p_of(A, i, p);
+    for (int pp = 0; pp < 3; ++pp) {
+      const float ap = aF[i] * p[pp];
+      for (int qq = 0; qq < 3; ++qq) df_add_prod(v[pp + 3 * qq], ap, A.V[(size_t)qq * A.N + i]);
+    }
+  }
+  block_reduce_df<9>(v, red);
+  if (threadIdx.x == 0) {
+    float S[9], Xcp[3], Yd[3], q[4], gap, lmax, R[9], t[3];
+    for (int k = 0; k < 9; ++k) {
+      S[k] = df_val(v[k]);
+      A.scal[kSS + k] = S[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+      Xcp[k] = (float)A.scal[kSXcp + k];
+      Yd[k] = (float)A.scal[kSYd + k];
+    }
+    HornState<float> st;
+    st.reset();
+    horn_quaternion<float>(S, st, q, &gap, &lmax);
+    quat_to_pose<float>(q, Xcp, Yd, R, t);
+    for (int k = 0; k < 4; ++k) A.scal[kSq + k] = q[k];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) A.scal[kSV + 4 * i + j] = st.V[i][j];
+    for (int k = 0; k < 9; ++k) A.pose_out[k] = R[k];
+    for (int k = 0; k < 3; ++k) A.pose_out[9 + k] = t[k];
+  }
+}
+
+// Horn adjoint (one thread): dL/d(R, t) of the output pose in the caller's
+// frame, where (R, t) = (R(q), Xc - R Yc) -> dL/dS, dL/dXc, dL/dYc.
+__global__ void k_horn_adjoint(Vecs A, const float* g_out) {
+  float gRo[9], gto[3], S[9], Xc[3], Yc[3], q[4], V[4][4], gS[9], gXc[3], gYc[3];
+  for (int k = 0; k < 9; ++k) gRo[k] = g_out[k];
+  for (int k = 0; k < 3; ++k) gto[k] = g_out[9 + k];
+  for (int k = 0; k < 9; ++k) S[k] = (float)A.scal[kSS + k];
+  for (int k = 0; k < 3; ++k) {
+    Xc[k] = (float)A.scal[kSXc + k];
+    Yc[k] = (float)A.scal[kSYc + k];
+  }
+  for (int k = 0; k < 4; ++k) q[k] = (float)A.scal[kSq + k];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) V[i][j] = (float)A.scal[kSV + 4 * i + j];
+  horn_pose_adjoint<float>(S, Xc, Yc, q, V, gRo, gto, gS, gXc, gYc);
+  for (int k = 0; k < 9; ++k) A.scal[kSgS + k] = gS[k];
+  for (int k = 0; k < 3; ++k) {
+    A.scal[kSgXc + k] = gXc[k];
+    A.scal[kSgYc + k] = gYc[k];
+  }
+}
+
+// One block, per row: g(p_i) = a_i gS V_i, g(V_i) = a_i gS^T p_i, dL/da_i from
+// S; dL/dXc -= sum g(p).
+__global__ void __launch_bounds__(1024) k_back_S(Vecs A) {
+  __shared__ df red[3 * 32];
+  const float* aF = A.a + (size_t)A.I1 * A.N;
+  float gS[9];
+  for (int k = 0; k < 9; ++k) gS[k] = (float)A.scal[kSgS + k];
+  df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
+  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
+    float p[3];
+    p_of(A, i, p);
+    const float Vi[3] = {A.V[i], A.V[(size_t)A.N + i], A.V[2 * (size_t)A.N + i]};
+    float ga = 0.f;
+    for (int pp = 0; pp < 3; ++pp) {
+      float gp = 0.f, gv = 0.f;
+      for (int qq = 0; qq < 3; ++qq) {
+        gp = fmaf(gS[pp + 3 * qq], Vi[qq], gp);
+        gv = fmaf(gS[qq + 3 * pp], p[qq], gv);
+      }
+      ga = fmaf(gp, p[pp], ga);
+      A.gp[(size_t)pp * A.N + i] = aF[i] * gp;
+      A.gV[(size_t)pp * A.N + i] = aF[i] * gv;
+      df_add(v[pp], aF[i] * gp);
+    }
+    A.ga[i] = ga;
+  }
+  block_reduce_df<3>(v, red);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) A.scal[kSgXc + k] -= df_dbl(v[k]);
+}
+
+// Per row: the part of dL/dw known before dL/dsumM, gw = x . (g(p) + gXc/sumM);
+// direct dL/dx = w (g(p) + gXc/sumM); the weights of the K^T sweep.
+__global__ void k_back_w(Vecs A, float* wt4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.N) return;
+  const float* aF = A.a + (size_t)A.I1 * A.N;
+  const float inv = (float)(1.0 / A.scal[kSsum]);
+  const float4 x = A.X[i];
+  const float xv[3] = {x.x, x.y, x.z};
+  float gw = 0.f;
+  for (int d = 0; d < 3; ++d) {
+    const float g = fmaf((float)A.scal[kSgXc + d], inv, A.gp[(size_t)d * A.N + i]);
+    gw = fmaf(xv[d] + A.hdr->oX[d], g, gw);
+    A.gX[(size_t)d * A.N + i] = A.w[i] * g;
+    wt4[(size_t)d * A.N + i] = A.gV[(size_t)d * A.N + i];
+  }
+  A.gw[i] = gw;
+  wt4[3 * (size_t)A.N + i] = aF[i] * gw;
+}
+
+// One block after the K^T sweep: dL/dYc -= sum_j b_j g(h_j);
+// dL/dsumM = -(gXc . Xc + gYc . Yc) / sumM.
+__global__ void __launch_bounds__(1024) k_back_Yc(Vecs A, const float* gh) {
+  __shared__ df red[3 * 32];
+  const float* bF = A.b + (size_t)A.I1 * A.M;
+  df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x)
+    for (int d = 0; d < 3; ++d) df_add_prod(v[d], bF[j], gh[(size_t)d * A.M + j]);
+  block_reduce_df<3>(v, red);
+  if (threadIdx.x == 0) {
+    double g = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      A.scal[kSgYc + d] -= df_dbl(v[d]);
+      g -= A.scal[kSgXc + d] * A.scal[kSXc + d] + A.scal[kSgYc + d] * A.scal[kSYc + d];
+    }
+    A.scal[kSgsum] = g / A.scal[kSsum];
+  }
+}
+
+// Per row: g(rho) = a (gw + gsum); dL/da^{I1} += (gw + gsum) rho.
+__global__ void k_back_rho(Vecs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.N) return;
+  const float* aF = A.a + (size_t)A.I1 * A.N;
+  const float gw = A.gw[i] + (float)A.scal[kSgsum];
+  A.grho[i] = aF[i] * gw;
+  A.ga[i] = fmaf(gw, A.rho[i], A.ga[i]);
+}
+
+// Per column, final stage: dL/db^{I1} = (cs y - Yc) . g(h) + K^T g(rho), where
+// K^T g(rho) = K^T (a gw) + gsum c^{I1-1}; dL/dcs^{I1-1} = y . (b g(h) + gYc / sumM);
+// direct dL/dy = cs (b g(h) + gYc / sumM).
+__global__ void k_back_final_cols(Vecs A, const float* gh) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= A.M) return;
+  const int k = A.I1 - 1;
+  const float bF = A.b[(size_t)A.I1 * A.M + j];
+  const float cs = A.cs[(size_t)k * A.M + j];
+  const float c = A.c[(size_t)k * A.M + j];
+  const float inv = (float)(1.0 / A.scal[kSsum]);
+  const float4 y = A.Y[j];
+  const float yv[3] = {y.x, y.y, y.z};
+  float gb = fmaf((float)A.scal[kSgsum], c, gh[3 * (size_t)A.M + j]), gcs = 0.f;
+  for (int d = 0; d < 3; ++d) {
+    const float ghd = gh[(size_t)d * A.M + j];
+    const float gy = fmaf(bF, ghd, (float)A.scal[kSgYc + d] * inv);
+    gb = fmaf(fmaf(cs, yv[d], -(float)A.scal[kSYd + d]) + (cs - 1.f) * A.hdr->oY[d], ghd, gb);
+    gcs = fmaf(yv[d] + A.hdr->oY[d], gy, gcs);
+    A.gY[(size_t)d * A.M + j] = cs * gy;
+  }
+  A.gb[j] = gb;
+  A.gcs[j] = gcs;
+}
+
+// Column pass k backward: from dL/db^{k+1}, dL/du^{k+1} and the direct dL/dcs^k,
+// dL/db^k, dL/du^k and g(c^k) = dL/dcs^k b^k. d(b/cs)/dcs = -b^{k+1}/cs: the
+// new scalings are used instead of b^k/cs^2, whose square overflows FP32 at low
+// temperature (K ~ e^(alpha/T)).
+__global__ void k_back_colpass(Vecs A, int k) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= A.M) return;
+  const size_t o = (size_t)k * A.M + j;
+  const float bk = A.b[o], cs = A.cs[o], c = A.c[o];
+  const float b1 = A.b[o + A.M], u1 = A.u[o + A.M];
+  const float gb1 = A.gb[j], gu1 = A.gu[j];
+  const float gcs = A.gcs[j] - fmaf(gb1, b1, gu1 * u1) / cs;
+  A.gc[o] = gcs * bk;
+  A.gb[j] = fmaf(gcs, c, gb1 / cs);
+  A.gu[j] = gu1 / cs + gcs;
+  A.gcs[j] = 0.f;
+}
+
+// Row pass k backward: from dL/da^{k+1}, dL/ds^{k+1}: dL/da^k, dL/ds^k and
+// g(r^k) = dL/drs^k a^k (with a^{k+1}, s^{k+1} as in the column pass).
+__global__ void k_back_rowpass(Vecs A, int k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.N) return;
+  const size_t o = (size_t)k * A.N + i;
+  const float ak = A.a[o], rs = A.rs[o], r = A.r[o];
+  const float a1 = A.a[o + A.N], s1 = A.s[o + A.N];
+  const float ga1 = A.ga[i], gs1 = A.gs[i];
+  const float grs = -fmaf(ga1, a1, gs1 * s1) / rs;
+  A.gr[o] = grs * ak;
+  A.ga[i] = fmaf(grs, r, ga1 / rs);
+  A.gs[i] = gs1 / rs + grs;
+}
+
+// One block: dL/dR = sum gz y^T, dL/dt = sum gz (caller frame, y = y' + oY);
+// per column dL/dy += R^T gz; writes dL/d(R, t) of the input pose.
+__global__ void __launch_bounds__(1024) k_pose_grad(Vecs A, float* g_in) {
+  __shared__ df red[12 * 32];
+  float R[9];
+  for (int k = 0; k < 9; ++k) R[k] = A.pose[k];
+  df v[12];
+  for (int k = 0; k < 12; ++k) v[k] = df_make(0.f);
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
+    const float4 y = A.Y[j];
+    const float yv[3] = {y.x, y.y, y.z};
+    const float g[3] = {A.gZ[j], A.gZ[(size_t)A.M + j], A.gZ[2 * (size_t)A.M + j]};
+    for (int i = 0; i < 3; ++i) {
+      for (int jj = 0; jj < 3; ++jj) df_add_prod(v[3 * i + jj], g[i], yv[jj]);
+      df_add(v[9 + i], g[i]);
+    }
+    for (int jj = 0; jj < 3; ++jj)
+      A.gY[(size_t)jj * A.M + j] += R[jj] * g[0] + R[3 + jj] * g[1] + R[6 + jj] * g[2];
+  }
+  block_reduce_df<12>(v, red);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 3; ++i) {
+      const float gt = df_val(v[9 + i]);
+      g_in[9 + i] = gt;
+      for (int j = 0; j < 3; ++j) g_in[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
+    }
+}
+
+__global__ void k_add(float* d, const float* s, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] += s[i];
+}
+
+// ------------------------------------------------------------------ host side
+struct Carve {
+  char* p;
+  size_t off = 0;
+  explicit Carve(void* base) : p(static_cast<char*>(base)) {}
+  template <class T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* r = p ? reinterpret_cast<T*>(p + off) : nullptr;
+    off += n * sizeof(T);
+    return r;
+  }
+};
+
+struct Plan {
+  SweepIO rows, cols;  // own X / stream Y; own Y / stream X
+};
+
+// Slices so that a sweep has about 1200 blocks (8 per SM of 152).
+void plan_side(SweepIO& io, int n_own, int n_str) {
+  const int nb = (n_own + kOwnBlk - 1) / kOwnBlk;
+  const int max_s = std::max(1, (n_str + kTile - 1) / kTile);
+  io.S = std::max(1, std::min(max_s, (1200 + nb - 1) / nb));
+  io.len = (n_str + io.S - 1) / io.S;
+  io.S = (n_str + io.len - 1) / io.len;
+  io.n_own = n_own;
+  io.n_str = n_str;
+}
+
+Plan make_plan(int N, int M) {
+  Plan P{};
+  plan_side(P.rows, N, M);
+  plan_side(P.cols, M, N);
+  P.rows.own_posed = false;
+  P.rows.str_posed = true;
+  P.cols.own_posed = true;
+  P.cols.str_posed = false;
+  return P;
+}
+
+struct Layout {
+  Vecs V;
+  float* wt4;   // [4][N]
+  float* gh;    // [4][M]
+  float* part;
+  size_t total;
+};
+
+Layout carve(void* base, int N, int M, int I1, const Plan& P) {
+  Carve c(base);
+  Layout L{};
+  Vecs& A = L.V;
+  A.N = N;
+  A.M = M;
+  A.I1 = I1;
+  A.a = c.take<float>((size_t)(I1 + 1) * N);
+  A.s = c.take<float>((size_t)(I1 + 1) * N);
+  A.b = c.take<float>((size_t)(I1 + 1) * M);
+  A.u = c.take<float>((size_t)(I1 + 1) * M);
+  A.r = c.take<float>((size_t)I1 * N);
+  A.rs = c.take<float>((size_t)I1 * N);
+  A.c = c.take<float>((size_t)I1 * M);
+  A.cs = c.take<float>((size_t)I1 * M);
+  A.rho = c.take<float>(N);
+  A.w = c.take<float>(N);
+  A.V = c.take<float>(3 * (size_t)N);
+  A.h = c.take<float>(3 * (size_t)M);
+  A.scal = c.take<double>(kScalN);
+  A.pose_out = c.take<float>(16);
+  A.ga = c.take<float>(N);
+  A.gs = c.take<float>(N);
+  A.gb = c.take<float>(M);
+  A.gu = c.take<float>(M);
+  A.gcs = c.take<float>(M);
+  A.gV = c.take<float>(3 * (size_t)N);
+  A.gp = c.take<float>(3 * (size_t)N);
+  A.gw = c.take<float>(N);
+  A.grho = c.take<float>(N);
+  A.gr = c.take<float>((size_t)I1 * N);
+  A.gc = c.take<float>((size_t)I1 * M);
+  A.gX = c.take<float>(3 * (size_t)N);
+  A.gZ = c.take<float>(3 * (size_t)M);
+  A.gY = c.take<float>(3 * (size_t)M);
+  L.wt4 = c.take<float>(4 * (size_t)N);
+  L.gh = c.take<float>(4 * (size_t)M);
+  const size_t pr = (size_t)P.rows.S * 4 * N, pc = (size_t)P.cols.S * 4 * M;
+  L.part = c.take<float>(std::max(pr, pc));
+  L.total = c.off;
+  return L;
+}
+
+int blocks(int n) { return (n + kGlue - 1) / kGlue; }
+
+// out[m] (+)= K-products of NW weight vectors (rows: K w, w over columns;
+// columns: K^T w, w over rows).
+template <int NW>
+void sum_sweep(const SweepIO& io, const Layout& L, const float* pose, float T, float alpha, const float* w, int ldw,
+               float* out, int ldo, bool acc, cudaStream_t st) {
+  dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
+  k_sweep_sum<NW><<<g, kSwT, 0, st>>>(io, pose, T, alpha, w, ldw, L.part);
+  k_reduce_slices<<<dim3(blocks(io.n_own), NW), kGlue, 0, st>>>(L.part, io.S, NW, io.n_own, out, ldo, acc ? 1 : 0);
+}
+
+void grad_sweep(const SweepIO& io, const Layout& L, const float* pose, float T, float alpha, const Terms& tm,
+                float* out, bool acc, cudaStream_t st) {
+  dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
+  k_sweep_grad<<<g, kSwT, 0, st>>>(io, pose, T, alpha, tm, L.part);
+  k_reduce_slices<<<dim3(blocks(io.n_own), 3), kGlue, 0, st>>>(L.part, io.S, 3, io.n_own, out, io.n_own, acc ? 1 : 0);
+}
+
+}  // namespace
+
+size_t softassign_step_adjoint_ws_need(int N, int M, int I1) {
+  const Plan P = make_plan(N, M);
+  return carve(nullptr, N, M, I1, P).total;
+}
+
+int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st) {
+  const int N = J.N, M = J.M, I1 = J.I1;
+  if (N < 1 || M < 1 || I1 < 1 || 4 + 2 * I1 > 64 || !(J.T > 0.f)) return (int)cudaErrorInvalidValue;
+  Plan P = make_plan(N, M);
+  P.rows.own = J.X;
+  P.rows.str = J.Y;
+  P.cols.own = J.Y;
+  P.cols.str = J.X;
+  const Layout L = carve(ws, N, M, I1, P);
+  if (!ws || L.total > ws_bytes) return (int)cudaErrorInvalidValue;
+  Vecs A = L.V;
+  A.X = J.X;
+  A.Y = J.Y;
+  A.hdr = J.hdr;
+  A.pose = J.pose;
+  const float T = J.T, al = J.alpha;
+  const float* pose = J.pose;
+  // ---- recompute of the iteration, recording every vector
+  k_fill<<<std::min(blocks(N), 1024), kGlue, 0, st>>>(A.a, N, 1.f);
+  k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(A.b, M, 1.f);
+  cudaError_t e = cudaMemcpyAsync(A.s, J.s, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(A.u, J.u, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return (int)e;
+  for (int k = 0; k < I1; ++k) {
+    float* ak = A.a + (size_t)k * N;
+    float* sk = A.s + (size_t)k * N;
+    float* bk = A.b + (size_t)k * M;
+    float* uk = A.u + (size_t)k * M;
+    float* rk = A.r + (size_t)k * N;
+    float* ck = A.c + (size_t)k * M;
+    sum_sweep<1>(P.rows, L, pose, T, al, bk, M, rk, N, false, st);
+    k_pass_done<<<blocks(N), kGlue, 0, st>>>(ak, rk, sk, A.rs + (size_t)k * N, ak + N, sk + N, N);
+    sum_sweep<1>(P.cols, L, pose, T, al, ak + N, N, ck, M, false, st);
+    k_pass_done<<<blocks(M), kGlue, 0, st>>>(bk, ck, uk, A.cs + (size_t)k * M, bk + M, uk + M, M);
+  }
+  const float* bF = A.b + (size_t)I1 * M;
+  sum_sweep<1>(P.rows, L, pose, T, al, bF, M, A.rho, N, false, st);
+  k_centres<<<1, 1024, 0, st>>>(A);
+  k_h<<<blocks(M), kGlue, 0, st>>>(A);
+  sum_sweep<3>(P.rows, L, pose, T, al, A.h, M, A.V, N, false, st);
+  k_S_pose<<<1, 1024, 0, st>>>(A);
+  // ---- backward
+  k_horn_adjoint<<<1, 1, 0, st>>>(A, J.g_pose_out);
+  k_back_S<<<1, 1024, 0, st>>>(A);
+  k_back_w<<<blocks(N), kGlue, 0, st>>>(A, L.wt4);
+  sum_sweep<4>(P.cols, L, pose, T, al, L.wt4, N, L.gh, M, false, st);
+  k_back_Yc<<<1, 1024, 0, st>>>(A, L.gh);
+  k_back_rho<<<blocks(N), kGlue, 0, st>>>(A);
+  k_back_final_cols<<<blocks(M), kGlue, 0, st>>>(A, L.gh);
+  if (J.g_s_out) e = cudaMemcpyAsync(A.gs, J.g_s_out, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
+  else e = cudaMemsetAsync(A.gs, 0, sizeof(float) * N, st);
+  if (e == cudaSuccess) {
+    if (J.g_u_out) e = cudaMemcpyAsync(A.gu, J.g_u_out, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
+    else e = cudaMemsetAsync(A.gu, 0, sizeof(float) * M, st);
+  }
+  if (e != cudaSuccess) return (int)e;
+  for (int k = I1 - 1; k >= 0; --k) {
+    k_back_colpass<<<blocks(M), kGlue, 0, st>>>(A, k);
+    // dL/da^{k+1} += K g(c^k)
+    sum_sweep<1>(P.rows, L, pose, T, al, A.gc + (size_t)k * M, M, A.ga, N, true, st);
+    k_back_rowpass<<<blocks(N), kGlue, 0, st>>>(A, k);
+    // dL/db^k += K^T g(r^k); b^0 = 1 is a constant
+    if (k >= 1) sum_sweep<1>(P.cols, L, pose, T, al, A.gr + (size_t)k * N, N, A.gb, M, true, st);
+  }
+  // rank-1 terms of dL/dK (rows: alpha, columns: beta)
+  const int nterms = 4 + 2 * I1;
+  const float* ta[64];
+  const float* tb[64];
+  for (int d = 0; d < 3; ++d) {
+    ta[d] = A.gV + (size_t)d * N;
+    tb[d] = A.h + (size_t)d * M;
+  }
+  ta[3] = A.grho;
+  tb[3] = bF;
+  for (int k = 0; k < I1; ++k) {
+    ta[4 + k] = A.a + (size_t)(k + 1) * N;
+    tb[4 + k] = A.gc + (size_t)k * M;
+    ta[4 + I1 + k] = A.gr + (size_t)k * N;
+    tb[4 + I1 + k] = A.b + (size_t)k * M;
+  }
+  for (int t0 = 0; t0 < nterms; t0 += kMaxTerms) {
+    Terms tr{}, tcol{};
+    tr.n = tcol.n = std::min(kMaxTerms, nterms - t0);
+    for (int m = 0; m < tr.n; ++m) {
+      tr.own[m] = ta[t0 + m];
+      tr.str[m] = tb[t0 + m];
+      tcol.own[m] = tb[t0 + m];
+      tcol.str[m] = ta[t0 + m];
+    }
+    grad_sweep(P.rows, L, pose, T, al, tr, A.gX, true, st);
+    grad_sweep(P.cols, L, pose, T, al, tcol, A.gZ, t0 > 0, st);
+  }
+  k_pose_grad<<<1, 1024, 0, st>>>(A, J.g_pose_in);
+  k_add<<<blocks(3 * N), kGlue, 0, st>>>(J.gX, A.gX, 3 * N);
+  k_add<<<blocks(3 * M), kGlue, 0, st>>>(J.gY, A.gY, 3 * M);
+  e = cudaMemcpyAsync(J.g_s_in, A.gs, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(J.g_u_in, A.gu, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && J.pose_out)
+    e = cudaMemcpyAsync(J.pose_out, A.pose_out, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return (int)e;
+}
+
+}  // namespace cesa

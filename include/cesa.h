@@ -269,6 +269,28 @@ int cesa_emicp_forward_device(const float* dX, int N, const float* dY, int M, fl
 int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* tape, const float* d_gRt,
                                float* d_gX, float* d_gY, float* d_gRt0, int* d_status, cesa_stream_t stream);
 
+/*
+ * Adjoint of Softassign (no counterpart in the reference). The forward runs
+ * the matrix-free kernel (whatever p->sinkhorn_form says) and records a tape:
+ * the packed clouds and, per pose update, its input pose and slack vectors s
+ * (N) and u (M), the state carried between updates (checkpoints of the
+ * annealing loop, src/softassign.cu:486-822). The backward walks the updates
+ * in reverse; for each it recomputes the update's Sinkhorn scalings with the
+ * affinities formed on the fly (no N x M matrix is stored) and runs the
+ * adjoint of the row and column passes, of the weighted centres and S, and of
+ * the Horn pose. Given dL/dR (9, row-major) and dL/dt (3) of the returned
+ * pose it writes dL/dX (SoA 3N), dL/dY (SoA 3M) and dL/dR0, dL/dt0 of the
+ * initial pose (12). All pointers are device pointers.
+ * cesa_softassign_forward_device returns the same pose as
+ * cesa_softassign_device with the matrix-free form.
+ */
+size_t cesa_softassign_tape_bytes(int N, int M, const cesa_params* p);
+int cesa_softassign_forward_device(const float* dX, int N, const float* dY, int M, float* dRt,
+                                   const cesa_params* p, void* tape, int* d_status, cesa_stream_t stream);
+int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const void* tape, const float* d_gRt,
+                                    float* d_gX, float* d_gY, float* d_gRt0, int* d_status,
+                                    cesa_stream_t stream);
+
 /* Releases cached device workspaces of the calling process. */
 void cesa_release_workspaces(void);
 

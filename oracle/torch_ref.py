@@ -1,10 +1,10 @@
-"""Dense FP64 restatement of EM-ICP in torch, differentiable by autograd --
-TEST INFRASTRUCTURE ONLY.
+"""Dense FP64 restatements of EM-ICP and Softassign in torch, differentiable
+by autograd -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/ may import this module. It is the FP64 dense reference gradient
-of the EM-ICP adjoint: the whole N x M affinity matrix of every sigma step is
-formed, Horn's quaternion is the top eigenvector from torch.linalg.eigh, and
-autograd differentiates the unrolled schedule. Runs on the CPU in float64.
+of the adjoints: the whole N x M affinity matrix of every step is formed,
+Horn's quaternion is the top eigenvector from torch.linalg.eigh, and autograd
+differentiates the unrolled schedule. Runs on the CPU in float64.
 
 The algorithm is that of emicp_cpu() (src/emicp_cpu.cpp:305-528, identical to
 src/emicp.cu:443-669): per step, A_rc = exp(-|x_c - (R y_r + t)|^2 / sigma_p2),
@@ -105,3 +105,66 @@ def loss_value(X, Y, R0, t0, R_true, t_true, **sched):
         R, t = emicp(torch.tensor(X, dtype=torch.float64), torch.tensor(Y, dtype=torch.float64),
                      torch.tensor(R0, dtype=torch.float64), torch.tensor(t0, dtype=torch.float64), **sched)
         return float(((R - torch.tensor(R_true)) ** 2).sum() + ((t - torch.tensor(t_true)) ** 2).sum())
+
+
+def softassign_moutlier(T_0):
+    """The slack's initial value 1/sqrt(T_0) e^-1 in FP32 (src/softassign.cu:385-390)."""
+    return float(np.float32(1.0 / np.sqrt(np.float32(T_0)) * np.exp(np.float32(-1.0))))
+
+
+def softassign(X, Y, R0, t0, JMAX=100, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR=0.95, moutlier=None):
+    """Annealed Softassign, as oracle_softassign (src/softassign.cu:486-822):
+    per update M = exp(-(|x_r - (R y_c + t)|^2 - alpha)/T)/sqrt(T), I1 slack
+    row/column normalisations with s and u carried across all updates, w = M 1,
+    Xc = sum w x / sum w, Yc = sum cs y / sum w (cs: the last column sums
+    before their normalisation), S = (w x - Xc)^T M (cs y - Yc) and Horn's
+    pose. X (N,3), Y (M,3), R0, t0 float64 tensors -> (R, t)."""
+    N, M = X.shape[0], Y.shape[0]
+    if moutlier is None:
+        moutlier = softassign_moutlier(T_0)
+    s = torch.full((N,), moutlier, dtype=X.dtype)
+    u = torch.full((M,), moutlier, dtype=X.dtype)
+    R, t = R0, t0
+    T = np.float32(T_0)
+    for _ in range(JMAX):
+        Tv = float(T)
+        for _ in range(I0):
+            Z = Y @ R.T + t
+            d2 = ((X[:, None, :] - Z[None, :, :]) ** 2).sum(-1)  # (N, M)
+            Mx = torch.exp(-(d2 - float(np.float32(alpha))) / Tv) / np.sqrt(Tv)
+            for _ in range(I1):
+                rs = Mx.sum(1) + s
+                Mx = Mx / rs[:, None]
+                s = s / rs
+                cs = Mx.sum(0) + u
+                Mx = Mx / cs[None, :]
+                u = u / cs
+            w = Mx.sum(1)
+            sumM = w.sum()
+            Xc = (w[:, None] * X).sum(0) / sumM
+            Yc = (cs[:, None] * Y).sum(0) / sumM
+            Xw = w[:, None] * X - Xc
+            Yw = cs[:, None] * Y - Yc
+            Sm = Xw.T @ (Mx @ Yw)  # S_ij = sum_r xw_ri (M Yw)_rj
+            S = Sm.T.reshape(-1)  # S[i + 3 j]
+            _, V = torch.linalg.eigh(horn_matrix(S))
+            q = V[:, -1]
+            R = quat_to_R(q)
+            t = Xc - R @ Yc
+        T = np.float32(T * np.float32(TFACTOR))
+    return R, t
+
+
+def softassign_loss_grads(X, Y, R0, t0, R_true, t_true, **sched):
+    """As pose_loss_grads, for Softassign."""
+    Xt = torch.tensor(np.asarray(X, np.float64), requires_grad=True)
+    Yt = torch.tensor(np.asarray(Y, np.float64), requires_grad=True)
+    w = torch.zeros(3, dtype=torch.float64, requires_grad=True)
+    v = torch.zeros(3, dtype=torch.float64, requires_grad=True)
+    R0t = torch.tensor(np.asarray(R0, np.float64))
+    t0t = torch.tensor(np.asarray(t0, np.float64))
+    R, t = softassign(Xt, Yt, so3_exp(w) @ R0t, t0t + v, **sched)
+    loss = ((R - torch.tensor(R_true)) ** 2).sum() + ((t - torch.tensor(t_true)) ** 2).sum()
+    loss.backward()
+    return (float(loss.detach()), Xt.grad.numpy(), Yt.grad.numpy(), w.grad.numpy(), v.grad.numpy(),
+            R.detach().numpy(), t.detach().numpy())
