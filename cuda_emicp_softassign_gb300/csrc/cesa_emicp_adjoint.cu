@@ -10,21 +10,25 @@
 //      giving dL/d(L, U, P, Q) for L = sum lambda, U = sum u, P = sum lambda y,
 //      Q = sum u y^T;
 //   2. one sweep that recomputes the affinities e_rc = exp(-|x_c - z_r|^2 / 2 s2)
-//      (z_r = R y_r + t) for (row block, column slice) units and forms, per
-//      element, ge = gA_r + gB_r . x_c + 2 e gC_r (the adjoints of the row sums
-//      A = sum e, B = sum e x, C = sum e^2 + outlier) and w = e ge / s2:
-//        dL/dz_r += w (x_c - z_r)            (per row, in registers)
-//        dL/dx_c += e gB_r - w (x_c - z_r)   (per column, reduced over the
-//                                             block's 128 rows by a warp
-//                                             reduce-scatter, one partial per
-//                                             row block and column);
-//   3. the block that completes a row block (split completion over slices)
-//      adds dL/dy_r = R^T dL/dz_r + lambda_r gP + gQ^T u_r and writes the row
-//      block's record of sum dL/dz_r y_r^T (row-major, as R), sum dL/dz_r and, for rows on the
-//      C_r <= 1e-6 branch (lambda = 1, u = mean X), sum gu_r;
+//      (z_r = R y_r + t) over (column block, row slice) units. A lane owns 6
+//      X columns; Y rows stream through shared memory as records of packed
+//      row pairs (-z, the scaled row-sum adjoints, gB). Per element,
+//      ge = gA_r + gB_r . x_c + 2 e gC_r (the adjoints of the row sums A = sum e,
+//      B = sum e x, C = sum e^2 + outlier) and w = e ge / s2:
+//        dL/dx_c += e gB_r - w (x_c - z_r)   (per column, in registers)
+//        dL/dz_r += w (x_c - z_r)            (per row: summed over the lane's
+//                                             columns, then over the lanes by a
+//                                             transposed shared-memory sum, then
+//                                             over the warps; one partial per
+//                                             column block and row);
+//   3. the block that completes a row slice (split completion over the column
+//      blocks) sums the row partials in column-block order, adds
+//      dL/dy_r = R^T dL/dz_r + lambda_r gP + gQ^T u_r and writes the slice's
+//      record of sum dL/dz_r y_r^T (row-major, as R), sum dL/dz_r and, for rows
+//      on the C_r <= 1e-6 branch (lambda = 1, u = mean X), sum gu_r;
 //   4. after the grid barrier every block reduces the records (the upstream
 //      gradient of the previous step's pose) and adds, for its share of the
-//      columns, the row-block partials of dL/dx_c in a fixed order.
+//      columns, the row-slice partials of dL/dx_c in a fixed order.
 // Per element: 6 (distance) + 1 (exponent) + 4 (ge) + 1 (w, with 1/s2 folded
 // into the row coefficients) + 3 (dz) + 6 (dx) FP32 ops + 1 MUFU, against
 // 12 + 1 in the forward, on packed pairs of rows (FFMA2/FADD2/FMUL2).
@@ -36,14 +40,25 @@
 namespace cesa {
 namespace {
 
-constexpr int kColGroup = 4;  // columns per warp reduce-scatter (4 columns x 4 components)
-constexpr int kPairs2 = 2 * kPairs;  // packed row pairs per lane: 4 rows of each of two row blocks
+constexpr int kAdjCols = 6;                       // owned X columns per lane
+constexpr int kAdjColBlk = kThreads * kAdjCols;   // owned columns per unit
+constexpr int kAdjRows = kThreads;                // streamed Y rows per chunk (one record per thread)
+constexpr int kAdjRP = kAdjRows / 2;              // row pairs per chunk
+constexpr int kAdjBatch = 4;                      // row pairs per warp transpose-sum
+constexpr int kAdjVals = kAdjBatch * 6;           // values per transpose-sum (2 rows x 3 axes per pair)
+constexpr int kScrStride = 36;                    // floats per transpose row (32 lanes + pad)
+constexpr float kFar = 1e15f;                     // padding coordinate: its affinities are exactly 0
+
+// Units: nb column blocks x S row slices of len rows (even), slice-major.
+struct AdjGeom {
+  int nb, S, len, units;
+};
 
 struct EmAdjArgs {
   const float4* rows;  // Y' centred (M)
   const float4* cols;  // X' centred (N)
   int M, N;
-  SweepGeom geo;  // own rows (M), stream columns (N)
+  AdjGeom geo;
   int nsteps;
   const float* tape;      // [nsteps][kEmTape]
   const float* row_tape;  // [nsteps][M][5]
@@ -52,10 +67,10 @@ struct EmAdjArgs {
   float4* gX;             // [N] accumulated (centred = caller frame)
   float4* gY;             // [M]
   float* g_in;            // [12] dL/d(R, t) of the initial pose, caller frame
-  float* part;            // split partials [units][3][128]
-  unsigned* cnt;          // [nblk]
-  df* rec;                // [2][nblk][16]
-  float4* part_x;         // [2][ceil(nblk / 2)][N]: one partial per pair of row blocks
+  float4* part_z;         // [nb][M]: dL/dz per column block
+  unsigned* cnt;          // [S] slice completion counters (monotonic)
+  df* rec;                // [2][S][16]
+  float4* part_x;         // [2][S][N]: dL/dx per row slice
   Ctl* ctl;
   int* d_status;
   uint64_t timeout_ns;
@@ -94,34 +109,15 @@ __device__ void em_step_adjoint(const float* rec, const float (&gRo)[9], const f
   coef[0] = gL;
 }
 
-// Sum over the 32 lanes of v[k] for k = 0..15; lane l receives the sum for
-// k = l & 15 (a fold of the two half-warps, then a reduce-scatter).
-__device__ __forceinline__ float reduce_scatter16(float (&v)[16]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], 16);
-#pragma unroll
-  for (int m = 8, n = 8; m >= 1; m >>= 1, n >>= 1) {
-    const bool up = lane & m;
-#pragma unroll
-    for (int i = 0; i < n; ++i) {
-      const float send = up ? v[i] : v[i + n];
-      const float keep = up ? v[i + n] : v[i];
-      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
-    }
-  }
-  return v[0];
-}
-
-// Per owned row: z (posed), and the row-sum adjoints gA, gB[3], gC (zero for
+// Per row: z (posed), and the row-sum adjoints gA, gB[3], gC (zero for
 // rows on the C <= 1e-6 branch and for rows past M).
 struct RowCoef {
   float z[3];
   float gA, gB[3], gC2;  // gC2 = 2 gC
 };
 
-__device__ __forceinline__ RowCoef row_coef(const float4 y, bool valid, const float* rt, const float (&R)[9],
-                                            const float (&t)[3], const float (&coef)[16]) {
+__device__ __forceinline__ RowCoef row_coef(const float4 y, bool valid, const float* rt, const float* R,
+                                            const float* t, const float* coef) {
   RowCoef c;
   c.z[0] = R[0] * y.x + R[1] * y.y + R[2] * y.z + t[0];
   c.z[1] = R[3] * y.x + R[4] * y.y + R[5] * y.z + t[1];
@@ -148,14 +144,42 @@ __device__ __forceinline__ RowCoef row_coef(const float4 y, bool valid, const fl
 }
 
 struct AdjSmem {
-  float4 raw[2][kChunk];
-  float4 prep[kChunk];
-  float red[kMaxAcc][kWarps][kBlockPts];
-  uint64_t full[2];
-  int flag;
+  float2 rec[kAdjRP][12];                     // row-pair records (11 float2 used)
+  float scr[kWarps][kAdjVals][kScrStride];    // per-warp transpose of the row partials
+  float wsum[3][kWarps][kAdjRows];            // per-warp row totals of a chunk
+  df red[16 * kWarps];
+  unsigned flag;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjArgs A) {
+// The record of one streamed row (one thread per row): -z, -gA/s2, -gB/s2,
+// -2gC/s2 and gB, interleaved with the other row of its pair.
+__device__ __forceinline__ void build_row_record(AdjSmem& sm, int i, bool valid, float4 y, const float (&rt)[5],
+                                                 const float* R, const float* t, const float* coef, float inv_s2) {
+  float v[11];
+  if (valid) {
+    const RowCoef c = row_coef(y, true, rt, R, t, coef);
+    v[0] = -c.z[0];
+    v[1] = -c.z[1];
+    v[2] = -c.z[2];
+    v[3] = -c.gA * inv_s2;
+    v[4] = -c.gB[0] * inv_s2;
+    v[5] = -c.gB[1] * inv_s2;
+    v[6] = -c.gB[2] * inv_s2;
+    v[7] = -c.gC2 * inv_s2;
+    v[8] = c.gB[0];
+    v[9] = c.gB[1];
+    v[10] = c.gB[2];
+  } else {  // far away, no coefficients: every term it feeds is 0
+    v[0] = v[1] = v[2] = kFar;
+#pragma unroll
+    for (int k = 3; k < 11; ++k) v[k] = 0.f;
+  }
+  float* dst = reinterpret_cast<float*>(&sm.rec[i >> 1][0]) + (i & 1);
+#pragma unroll
+  for (int k = 0; k < 11; ++k) dst[2 * k] = v[k];
+}
+
+__global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   AdjSmem& sm = *reinterpret_cast<AdjSmem*>(smem_raw);
   __shared__ float s_g[12];     // dL/d(R, t') of the current step's output pose
@@ -166,10 +190,8 @@ __global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjA
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned G = gridDim.x;
-  const SweepGeom& g = A.geo;
+  const AdjGeom& g = A.geo;
   if (tid == 0) {
-    for (int s = 0; s < 2; ++s) mbar_init(&sm.full[s], 1);
-    mbar_init_fence();
     // caller frame -> centred frame: t = t' + oX - R oY, so dL/dt' = dL/dt and
     // dL/dR' = dL/dR - dL/dt oY^T
     for (int i = 0; i < 3; ++i) {
@@ -178,11 +200,11 @@ __global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjA
     }
   }
   __syncthreads();
-  unsigned uses[2] = {0u, 0u};
   unsigned epoch = 0;
   bool ok = true;
   for (int k = A.nsteps - 1; k >= 0 && ok; --k) {
     const int par = k & 1;
+    const unsigned round = (unsigned)(A.nsteps - 1 - k);
     const float* rec = A.tape + (size_t)k * kEmTape;
     if (tid == 0) {
       float gRo[9], gto[3], coef[16];
@@ -193,170 +215,187 @@ __global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjA
       for (int i = 0; i < 13; ++i) s_pose[i] = rec[i];
     }
     __syncthreads();
-    float R[9], t[3], coef[16];
-    for (int i = 0; i < 9; ++i) R[i] = s_pose[i];
-    for (int i = 0; i < 3; ++i) t[i] = s_pose[9 + i];
-    for (int i = 0; i < 16; ++i) coef[i] = s_coef[i];
+    // the step's pose and coefficients stay in shared memory (read per row record)
+    const float* R = s_pose;
+    const float* t = s_pose + 9;
+    const float* coef = s_coef;
     const float s2 = s_pose[12];
     const float nk = -kLog2e / (2.f * s2), inv_s2 = 1.f / s2;
+    const float2 nk2 = dup2(nk);
     const float* rtape = A.row_tape + (size_t)k * A.M * 5;
-    df* recs = A.rec + (size_t)par * g.nblk * 16;
-    float4* px = A.part_x + (size_t)par * ((g.nblk + 1) / 2) * A.N;
+    df* recs = A.rec + (size_t)par * g.S * 16;
+    float4* px = A.part_x + (size_t)par * g.S * A.N;
 
-    // units: (pair of row blocks, slice); a lane holds 4 rows of each row block
-    const int nb2 = (g.nblk + 1) / 2;
-    for (int u = blockIdx.x; u < g.units && ok; u += G) {
-      const int b2 = u / g.slices, sl = u - b2 * g.slices;
-      const int cb = sl * g.slice_len, ce = min(cb + g.slice_len, g.n_stream);
-      // rows in packed pairs: pair P = 2 h + k holds rows (2k, 2k + 1) of row
-      // block 2 b2 + h: -z, gA, gB, 2 gC (all scaled by 1/s2), and dL/dz
-      float2 nz[kPairs2][3], pgA[kPairs2], pgB[kPairs2][3], pgC[kPairs2], gz2[kPairs2][3];
+    for (int u = blockIdx.x; u < g.units; u += G) {
+      const int sl = u / g.nb, cb = u - sl * g.nb;
+      const int rb = sl * g.len, re = min(rb + g.len, A.M);
+      // owned columns, duplicated into both halves of a packed pair
+      float2 xd[kAdjCols][3], gx[kAdjCols][3];
 #pragma unroll
-      for (int P = 0; P < kPairs2; ++P) {
-        RowCoef c2[2];
+      for (int j = 0; j < kAdjCols; ++j) {
+        const int c = cb * kAdjColBlk + j * kThreads + tid;
+        const float4 x = c < A.N ? ld_cg(A.cols + c) : make_float4(kFar, kFar, kFar, 0.f);
+        xd[j][0] = dup2(x.x);
+        xd[j][1] = dup2(x.y);
+        xd[j][2] = dup2(x.z);
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          const int r = (2 * b2 + (P >> 1)) * kBlockPts + lane + 32 * (2 * (P & 1) + hh);
-          const bool valid = r < A.M;
-          const float4 y = valid ? ld_cg(A.rows + r) : make_float4(0.f, 0.f, 0.f, 0.f);
-          c2[hh] = row_coef(y, valid, rtape + (size_t)(valid ? r : 0) * 5, R, t, coef);
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          nz[P][a] = make_float2(-c2[0].z[a], -c2[1].z[a]);
-          pgB[P][a] = make_float2(c2[0].gB[a] * inv_s2, c2[1].gB[a] * inv_s2);
-          gz2[P][a] = make_float2(0.f, 0.f);
-        }
-        pgA[P] = make_float2(c2[0].gA * inv_s2, c2[1].gA * inv_s2);
-        pgC[P] = make_float2(c2[0].gC2 * inv_s2, c2[1].gC2 * inv_s2);
+        for (int a = 0; a < 3; ++a) gx[j][a] = make_float2(0.f, 0.f);
       }
-      int st = 0;
-      uses[0] += 1;
+      // the first chunk's row, loaded by its thread
+      float4 yn = make_float4(0.f, 0.f, 0.f, 0.f);
+      float rtn[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (rb + tid < re) {
+        yn = ld_cg(A.rows + rb + tid);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) rtn[q] = __ldcg(rtape + (size_t)(rb + tid) * 5 + q);
+      }
+      for (int r0 = rb; r0 < re; r0 += kAdjRows) {
+        __syncthreads();  // the previous chunk's records and sums are consumed
+        build_row_record(sm, tid, r0 + tid < re, yn, rtn, R, t, coef, inv_s2);
+        __syncthreads();
+        // the next chunk's row, in flight during this chunk's sweep
+        const int rn = r0 + kAdjRows + tid;
+        if (rn < re) {
+          yn = ld_cg(A.rows + rn);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) rtn[q] = __ldcg(rtape + (size_t)rn * 5 + q);
+        }
+        const int npairs = min(kAdjRP, (re - r0 + 1) >> 1);
+        for (int pb = 0; pb < npairs; pb += kAdjBatch) {
+#pragma unroll
+          for (int q = 0; q < kAdjBatch; ++q) {
+            const float4* rp = reinterpret_cast<const float4*>(&sm.rec[pb + q][0]);
+            const float4 a0 = rp[0], a1 = rp[1], a2 = rp[2], a3 = rp[3], a4 = rp[4], a5 = rp[5];
+            const float2 nz0 = make_float2(a0.x, a0.y), nz1 = make_float2(a0.z, a0.w);
+            const float2 nz2 = make_float2(a1.x, a1.y), ngA = make_float2(a1.z, a1.w);
+            const float2 ngB0 = make_float2(a2.x, a2.y), ngB1 = make_float2(a2.z, a2.w);
+            const float2 ngB2 = make_float2(a3.x, a3.y), ngC = make_float2(a3.z, a3.w);
+            const float2 gB0 = make_float2(a4.x, a4.y), gB1 = make_float2(a4.z, a4.w);
+            const float2 gB2 = make_float2(a5.x, a5.y);
+            float2 gz0 = make_float2(0.f, 0.f), gz1 = gz0, gz2 = gz0;  // sum of -w (x - z)
+#pragma unroll
+            for (int j = 0; j < kAdjCols; ++j) {
+              const float2 dx = __fadd2_rn(xd[j][0], nz0);
+              const float2 dy = __fadd2_rn(xd[j][1], nz1);
+              const float2 dz = __fadd2_rn(xd[j][2], nz2);
+              float2 d2 = __fmul2_rn(dx, dx);
+              d2 = __ffma2_rn(dy, dy, d2);
+              d2 = __ffma2_rn(dz, dz, d2);
+              const float2 e = ex2_pair(__fmul2_rn(d2, nk2));
+              float2 nge = __ffma2_rn(ngB0, xd[j][0], ngA);
+              nge = __ffma2_rn(ngB1, xd[j][1], nge);
+              nge = __ffma2_rn(ngB2, xd[j][2], nge);
+              nge = __ffma2_rn(ngC, e, nge);
+              const float2 nw = __fmul2_rn(e, nge);  // -w
+              gz0 = __ffma2_rn(nw, dx, gz0);
+              gz1 = __ffma2_rn(nw, dy, gz1);
+              gz2 = __ffma2_rn(nw, dz, gz2);
+              gx[j][0] = __ffma2_rn(e, gB0, gx[j][0]);
+              gx[j][1] = __ffma2_rn(e, gB1, gx[j][1]);
+              gx[j][2] = __ffma2_rn(e, gB2, gx[j][2]);
+              gx[j][0] = __ffma2_rn(nw, dx, gx[j][0]);
+              gx[j][1] = __ffma2_rn(nw, dy, gx[j][1]);
+              gx[j][2] = __ffma2_rn(nw, dz, gx[j][2]);
+            }
+            float* col = &sm.scr[warp][6 * q][lane];
+            col[0 * kScrStride] = gz0.x;
+            col[1 * kScrStride] = gz1.x;
+            col[2 * kScrStride] = gz2.x;
+            col[3 * kScrStride] = gz0.y;
+            col[4 * kScrStride] = gz1.y;
+            col[5 * kScrStride] = gz2.y;
+          }
+          __syncwarp();
+          // lane v < kAdjVals: the sum over the 32 lanes of value v, in lane order
+          if (lane < kAdjVals) {
+            const float4* src = reinterpret_cast<const float4*>(&sm.scr[warp][lane][0]);
+            float sum = 0.f;
+#pragma unroll
+            for (int qq = 0; qq < 8; ++qq) {
+              const float4 v4 = src[qq];
+              sum += v4.x;
+              sum += v4.y;
+              sum += v4.z;
+              sum += v4.w;
+            }
+            const int q = lane / 6, comp = lane - 6 * q;
+            const int row = 2 * (pb + q) + (comp >= 3 ? 1 : 0);
+            sm.wsum[comp % 3][warp][row] = sum;
+          }
+          __syncwarp();
+        }
+        __syncthreads();
+        // this column block's dL/dz of the chunk's rows: the warps in order
+        if (r0 + tid < re) {
+          float gz[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            float v = sm.wsum[a][0][tid];
+#pragma unroll
+            for (int w = 1; w < kWarps; ++w) v += sm.wsum[a][w][tid];
+            gz[a] = -v;
+          }
+          __stcg(A.part_z + (size_t)cb * A.M + r0 + tid, make_float4(gz[0], gz[1], gz[2], 0.f));
+        }
+      }
+      // this row slice's dL/dx of the owned columns
+#pragma unroll
+      for (int j = 0; j < kAdjCols; ++j) {
+        const int c = cb * kAdjColBlk + j * kThreads + tid;
+        if (c < A.N)
+          __stcg(px + (size_t)sl * A.N + c,
+                 make_float4(gx[j][0].x + gx[j][0].y, gx[j][1].x + gx[j][1].y, gx[j][2].x + gx[j][2].y, 0.f));
+      }
+      // split completion of the row slice: the last of its nb units
+      __threadfence();
+      __syncthreads();
       if (tid == 0) {
-        const int len = min(kChunk, ce - cb);
-        mbar_arrive_expect_tx(&sm.full[0], (unsigned)len * 16u);
-        bulk_g2s(&sm.raw[0][0], A.cols + cb, (unsigned)len * 16u, &sm.full[0]);
+        const unsigned old = atom_acq_rel_add(A.cnt + sl, 1u);
+        sm.flag = (old == (round + 1u) * (unsigned)g.nb - 1u) ? 1u : 0u;
       }
-      for (int first = cb; first < ce; first += kChunk) {
-        const int len = min(kChunk, ce - first);
-        const int nst = st ^ 1;
-        const bool more = first + kChunk < ce;
-        if (more) {
-          uses[nst] += 1;
-          if (tid == 0) {
-            const int nlen = min(kChunk, ce - first - kChunk);
-            mbar_arrive_expect_tx(&sm.full[nst], (unsigned)nlen * 16u);
-            bulk_g2s(&sm.raw[nst][0], A.cols + first + kChunk, (unsigned)nlen * 16u, &sm.full[nst]);
+      __syncthreads();
+      if (sm.flag) {
+        __threadfence();
+        df vv[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) vv[q] = df_make(0.f);
+        for (int r = rb + tid; r < re; r += kThreads) {
+          float totz[3] = {0.f, 0.f, 0.f};
+          for (int b = 0; b < g.nb; ++b) {
+            const float4 p = __ldcg(A.part_z + (size_t)b * A.M + r);
+            totz[0] += p.x;
+            totz[1] += p.y;
+            totz[2] += p.z;
+          }
+          const float4 y = ld_cg(A.rows + r);
+          const float* rt = rtape + (size_t)r * 5;
+          const float C = rt[0], lam = rt[1];
+          const float uu[3] = {rt[2], rt[3], rt[4]};
+          const float yy[3] = {y.x, y.y, y.z};
+          // dL/dy = R^T dL/dz + lambda gP + gQ^T u
+          float gy[3];
+          for (int jj = 0; jj < 3; ++jj)
+            gy[jj] = R[jj] * totz[0] + R[3 + jj] * totz[1] + R[6 + jj] * totz[2] + lam * coef[4 + jj] +
+                     coef[7 + 3 * jj] * uu[0] + coef[8 + 3 * jj] * uu[1] + coef[9 + 3 * jj] * uu[2];
+          float4 o = A.gY[r];
+          o.x += gy[0];
+          o.y += gy[1];
+          o.z += gy[2];
+          A.gY[r] = o;
+          for (int i = 0; i < 3; ++i) {
+            for (int jj = 0; jj < 3; ++jj) df_add_prod(vv[3 * i + jj], totz[i], yy[jj]);  // dL/dR_ij, row-major
+            df_add(vv[9 + i], totz[i]);
+          }
+          if (!(C > 10e-7f)) {  // branch rows: u = mean X
+            for (int i = 0; i < 3; ++i)
+              df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
           }
         }
-        const bool bad = !mbar_wait(&sm.full[st], (uses[st] - 1u) & 1u, A.ctl, A.timeout_ns, 100);
-        if (__syncthreads_or(bad)) {
-          if (more) mbar_wait(&sm.full[nst], (uses[nst] - 1u) & 1u, A.ctl, A.timeout_ns, 101);
-          ok = false;
-          break;
-        }
-        // columns past the chunk's end in the last group: points so far away that
-        // their affinity is exactly 0, so every term they feed is 0
-        if (tid < kColGroup - 1 && len + tid < kChunk)
-          sm.raw[st][len + tid] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        block_reduce_df<16>(vv, sm.red);
+        if (tid == 0)
+          for (int q = 0; q < 16; ++q)
+            __stcg(reinterpret_cast<float2*>(recs + (size_t)sl * 16 + q), make_float2(vv[q].hi, vv[q].lo));
         __syncthreads();
-        const float4* xs = sm.raw[st];
-        // groups of 4 columns per warp: per column, 8 rows per lane, then the
-        // 4 x 4 column partials (x, y, z, pad) reduce-scattered over the lanes
-        for (int c0 = warp * kColGroup; c0 < len; c0 += kWarps * kColGroup) {
-          float v[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] = 0.f;
-#pragma unroll
-          for (int cc = 0; cc < kColGroup; ++cc) {
-            {
-              const float4 x = xs[c0 + cc];
-              const float2 xx = dup2(x.x), xy = dup2(x.y), xz = dup2(x.z);
-              float2 vx = make_float2(0.f, 0.f), vy = vx, vz = vx;  // sum e gB'
-              float2 ux = vx, uy = vx, uz = vx;                       // sum w (x - z)
-#pragma unroll
-              for (int P = 0; P < kPairs2; ++P) {
-                const float2 dx = __fadd2_rn(xx, nz[P][0]);
-                const float2 dy = __fadd2_rn(xy, nz[P][1]);
-                const float2 dz = __fadd2_rn(xz, nz[P][2]);
-                float2 d2 = __fmul2_rn(dx, dx);
-                d2 = __ffma2_rn(dy, dy, d2);
-                d2 = __ffma2_rn(dz, dz, d2);
-                const float2 e = ex2_pair(__fmul2_rn(d2, dup2(nk)));
-                float2 ge = __ffma2_rn(pgB[P][0], xx, pgA[P]);
-                ge = __ffma2_rn(pgB[P][1], xy, ge);
-                ge = __ffma2_rn(pgB[P][2], xz, ge);
-                ge = __ffma2_rn(e, pgC[P], ge);
-                const float2 w = __fmul2_rn(e, ge);
-                gz2[P][0] = __ffma2_rn(w, dx, gz2[P][0]);
-                gz2[P][1] = __ffma2_rn(w, dy, gz2[P][1]);
-                gz2[P][2] = __ffma2_rn(w, dz, gz2[P][2]);
-                ux = __ffma2_rn(w, dx, ux);
-                uy = __ffma2_rn(w, dy, uy);
-                uz = __ffma2_rn(w, dz, uz);
-                vx = __ffma2_rn(e, pgB[P][0], vx);
-                vy = __ffma2_rn(e, pgB[P][1], vy);
-                vz = __ffma2_rn(e, pgB[P][2], vz);
-              }
-              // dL/dx_c partial: sum e gB - sum w (x - z), gB = s2 gB'
-              v[4 * cc + 0] = fmaf(vx.x + vx.y, s2, -(ux.x + ux.y));
-              v[4 * cc + 1] = fmaf(vy.x + vy.y, s2, -(uy.x + uy.y));
-              v[4 * cc + 2] = fmaf(vz.x + vz.y, s2, -(uz.x + uz.y));
-            }
-          }
-          const float tot = reduce_scatter16(v);
-          const int cc = (lane & 15) >> 2, comp = lane & 3;
-          if (lane < 16 && c0 + cc < len)
-            reinterpret_cast<float*>(px + (size_t)b2 * A.N + first + c0 + cc)[comp] = comp < 3 ? tot : 0.f;
-        }
-        __syncthreads();
-        st = nst;
-      }
-      if (!ok) break;
-      // dL/dz per row: sum over the warps, then over the slices, per row block
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int rb = 2 * b2 + hh;
-        if (rb >= g.nblk) break;  // uniform
-        float2 acc[kPairs][3];
-#pragma unroll
-        for (int kk = 0; kk < kPairs; ++kk)
-#pragma unroll
-          for (int a = 0; a < 3; ++a) acc[kk][a] = gz2[2 * hh + kk][a];
-        float totz[3];
-        reduce_warps<3>(sm, acc, totz);
-        if (split_complete<3>(sm, g, rb, sl, (unsigned)(A.nsteps - 1 - k), A.part, A.cnt, totz)) {
-          df vv[16];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) vv[q] = df_make(0.f);
-          const int r = rb * kBlockPts + tid;
-          if (tid < kBlockPts && r < A.M) {
-            const float4 y = ld_cg(A.rows + r);
-            const float* rt = rtape + (size_t)r * 5;
-            const float C = rt[0], lam = rt[1];
-            const float uu[3] = {rt[2], rt[3], rt[4]};
-            const float yy[3] = {y.x, y.y, y.z};
-            // dL/dy = R^T dL/dz + lambda gP + gQ^T u
-            float gy[3];
-            for (int jj = 0; jj < 3; ++jj)
-              gy[jj] = R[jj] * totz[0] + R[3 + jj] * totz[1] + R[6 + jj] * totz[2] + lam * coef[4 + jj] +
-                       coef[7 + 3 * jj] * uu[0] + coef[8 + 3 * jj] * uu[1] + coef[9 + 3 * jj] * uu[2];
-            float4 o = A.gY[r];
-            o.x += gy[0];
-            o.y += gy[1];
-            o.z += gy[2];
-            A.gY[r] = o;
-            for (int i = 0; i < 3; ++i) {
-              for (int jj = 0; jj < 3; ++jj) df_add_prod(vv[3 * i + jj], totz[i], yy[jj]);  // dL/dR_ij, row-major
-              df_add(vv[9 + i], totz[i]);
-            }
-            if (!(C > 10e-7f)) {  // branch rows: u = mean X
-              for (int i = 0; i < 3; ++i)
-                df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
-            }
-          }
-          owned_block_sum<16>(vv, reinterpret_cast<df*>(sm.prep), recs + (size_t)rb * 16);
-        }
       }
     }
     if (!ok || !grid_sync(A.ctl, epoch, G, A.timeout_ns, 102)) {
@@ -364,17 +403,16 @@ __global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjA
       break;
     }
     // upstream gradient of the previous step's output pose, identical in every block
-    reduce_block_partials<16>(recs, g.nblk, s_red, s_tot);
+    reduce_block_partials<16>(recs, g.S, s_red, s_tot);
     if (tid < 12) s_g[tid] = df_val(s_tot[tid]);
     __syncthreads();
     const float gxb[3] = {df_val(s_tot[12]) / (float)A.N, df_val(s_tot[13]) / (float)A.N,
                           df_val(s_tot[14]) / (float)A.N};
-    // dL/dx_c: this block's share of the columns, row-block partials in order
+    // dL/dx_c: this block's share of the columns, row-slice partials in order
     for (int c = blockIdx.x * kThreads + tid; c < A.N; c += G * kThreads) {
       float sx = gxb[0], sy = gxb[1], sz = gxb[2];
       int b = 0;
-      const int nb2 = (g.nblk + 1) / 2;
-      for (; b + 16 <= nb2; b += 16) {  // 16 loads in flight, summed in order
+      for (; b + 16 <= g.S; b += 16) {  // 16 loads in flight, summed in order
         float4 p[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) p[j] = __ldcg(px + (size_t)(b + j) * A.N + c);
@@ -385,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1) emicp_adjoint_kernel(const EmAdjA
           sz += p[j].z;
         }
       }
-      for (; b < nb2; ++b) {
+      for (; b < g.S; ++b) {
         const float4 p = __ldcg(px + (size_t)b * A.N + c);
         sx += p.x;
         sy += p.y;
@@ -443,20 +481,40 @@ struct Carve {
 
 struct AdjPlan {
   int grid;
-  SweepGeom geo;
+  AdjGeom geo;
   size_t smem;
 };
 
+// Column blocks of kAdjColBlk columns and row slices of an even number of rows,
+// as many slices as fill whole waves of the co-resident grid best (up to 4 waves;
+// at least 64 rows per slice).
 AdjPlan plan_adj(int N, int M, int device) {
   AdjPlan P;
   P.smem = sizeof(AdjSmem);
   const int limit = persistent_grid_limit(device, (const void*)emicp_adjoint_kernel, P.smem);
-  // units own pairs of row blocks: plan the slices for ceil(nblk / 2) owned blocks
-  const int nblk = (M + kBlockPts - 1) / kBlockPts;
-  const int nb2 = (nblk + 1) / 2;
-  const SweepGeomH h = plan_sweep(nb2 * kBlockPts, N, limit);
-  P.geo = SweepGeom{M, N, nblk, h.slices, h.slice_len, nb2 * h.slices};
-  P.grid = P.geo.units < limit ? P.geo.units : limit;
+  AdjGeom g;
+  g.nb = (N + kAdjColBlk - 1) / kAdjColBlk;
+  const int max_s = (M + 63) / 64;  // at least 64 rows per slice
+  int bestS = 1;
+  double best = -1.0;
+  for (int w = 1; w <= 4; ++w) {
+    int S = (w * limit) / g.nb;
+    if (S < 1) S = 1;
+    if (S > max_s) S = max_s;
+    const int units = g.nb * S;
+    const int waves = (units + limit - 1) / limit;
+    const double eff = (double)units / ((double)waves * limit);
+    if (eff > best + 0.02) {
+      best = eff;
+      bestS = S;
+    }
+  }
+  g.len = (M + bestS - 1) / bestS;
+  g.len += g.len & 1;
+  g.S = (M + g.len - 1) / g.len;
+  g.units = g.nb * g.S;
+  P.geo = g;
+  P.grid = g.units < limit ? g.units : limit;
   return P;
 }
 
@@ -468,13 +526,13 @@ size_t emicp_adjoint_ws_need(int N, int M, int device) {
   const AdjPlan P = plan_adj(N, M, device);
   Carve c(nullptr);
   c.take<Ctl>(1);
-  c.take<unsigned>((size_t)P.geo.nblk);
+  c.take<unsigned>((size_t)P.geo.S);
   c.take<float4>((size_t)N);
   c.take<float4>((size_t)M);
   c.take<float>(12);
-  c.take<float>((size_t)P.geo.nblk * P.geo.slices * 3 * kBlockPts);
-  c.take<df>((size_t)2 * P.geo.nblk * 16);
-  c.take<float4>((size_t)2 * ((P.geo.nblk + 1) / 2) * N);
+  c.take<float4>((size_t)P.geo.nb * M);
+  c.take<df>((size_t)2 * P.geo.S * 16);
+  c.take<float4>((size_t)2 * P.geo.S * N);
   return c.off;
 }
 
@@ -485,14 +543,14 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   const AdjPlan P = plan_adj(L.N, L.M, device);
   Carve c(ws);
   Ctl* ctl = c.take<Ctl>(1);
-  unsigned* cnt = c.take<unsigned>((size_t)P.geo.nblk);
+  unsigned* cnt = c.take<unsigned>((size_t)P.geo.S);
   float4* gX = c.take<float4>((size_t)L.N);
   float4* gY = c.take<float4>((size_t)L.M);
   float* g_in = c.take<float>(12);
   const size_t zero_bytes = c.off;
-  float* part = c.take<float>((size_t)P.geo.nblk * P.geo.slices * 3 * kBlockPts);
-  df* rec = c.take<df>((size_t)2 * P.geo.nblk * 16);
-  float4* part_x = c.take<float4>((size_t)2 * ((P.geo.nblk + 1) / 2) * L.N);
+  float4* part_z = c.take<float4>((size_t)P.geo.nb * L.M);
+  df* rec = c.take<df>((size_t)2 * P.geo.S * 16);
+  float4* part_x = c.take<float4>((size_t)2 * P.geo.S * L.N);
   if (c.off > ws_bytes) return (int)cudaErrorInvalidValue;
   e = cudaMemsetAsync(ws, 0, zero_bytes, st);
   if (e != cudaSuccess) return (int)e;
@@ -510,7 +568,7 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   A.gX = gX;
   A.gY = gY;
   A.g_in = g_in;
-  A.part = part;
+  A.part_z = part_z;
   A.cnt = cnt;
   A.rec = rec;
   A.part_x = part_x;

@@ -112,13 +112,43 @@ def softassign_moutlier(T_0):
     return float(np.float32(1.0 / np.sqrt(np.float32(T_0)) * np.exp(np.float32(-1.0))))
 
 
-def softassign(X, Y, R0, t0, JMAX=100, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR=0.95, moutlier=None):
+def _softassign_updates(X, Y, R, t, s, u, Tv, I0, I1, alpha):
+    for _ in range(I0):
+        Z = Y @ R.T + t
+        d2 = ((X[:, None, :] - Z[None, :, :]) ** 2).sum(-1)  # (N, M)
+        Mx = torch.exp(-(d2 - float(np.float32(alpha))) / Tv) / np.sqrt(Tv)
+        for _ in range(I1):
+            rs = Mx.sum(1) + s
+            Mx = Mx / rs[:, None]
+            s = s / rs
+            cs = Mx.sum(0) + u
+            Mx = Mx / cs[None, :]
+            u = u / cs
+        w = Mx.sum(1)
+        sumM = w.sum()
+        Xc = (w[:, None] * X).sum(0) / sumM
+        Yc = (cs[:, None] * Y).sum(0) / sumM
+        Xw = w[:, None] * X - Xc
+        Yw = cs[:, None] * Y - Yc
+        Sm = Xw.T @ (Mx @ Yw)  # S_ij = sum_r xw_ri (M Yw)_rj
+        S = Sm.T.reshape(-1)  # S[i + 3 j]
+        _, V = torch.linalg.eigh(horn_matrix(S))
+        q = V[:, -1]
+        R = quat_to_R(q)
+        t = Xc - R @ Yc
+    return R, t, s, u
+
+
+def softassign(X, Y, R0, t0, JMAX=100, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR=0.95, moutlier=None,
+               checkpoint=False):
     """Annealed Softassign, as oracle_softassign (src/softassign.cu:486-822):
     per update M = exp(-(|x_r - (R y_c + t)|^2 - alpha)/T)/sqrt(T), I1 slack
     row/column normalisations with s and u carried across all updates, w = M 1,
     Xc = sum w x / sum w, Yc = sum cs y / sum w (cs: the last column sums
     before their normalisation), S = (w x - Xc)^T M (cs y - Yc) and Horn's
-    pose. X (N,3), Y (M,3), R0, t0 float64 tensors -> (R, t)."""
+    pose. X (N,3), Y (M,3), R0, t0 float64 tensors -> (R, t). checkpoint:
+    keep only (R, t, s, u) per T step for autograd and recompute the T step's
+    updates in the backward (bounded memory for long schedules)."""
     N, M = X.shape[0], Y.shape[0]
     if moutlier is None:
         moutlier = softassign_moutlier(T_0)
@@ -127,30 +157,11 @@ def softassign(X, Y, R0, t0, JMAX=100, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR
     R, t = R0, t0
     T = np.float32(T_0)
     for _ in range(JMAX):
-        Tv = float(T)
-        for _ in range(I0):
-            Z = Y @ R.T + t
-            d2 = ((X[:, None, :] - Z[None, :, :]) ** 2).sum(-1)  # (N, M)
-            Mx = torch.exp(-(d2 - float(np.float32(alpha))) / Tv) / np.sqrt(Tv)
-            for _ in range(I1):
-                rs = Mx.sum(1) + s
-                Mx = Mx / rs[:, None]
-                s = s / rs
-                cs = Mx.sum(0) + u
-                Mx = Mx / cs[None, :]
-                u = u / cs
-            w = Mx.sum(1)
-            sumM = w.sum()
-            Xc = (w[:, None] * X).sum(0) / sumM
-            Yc = (cs[:, None] * Y).sum(0) / sumM
-            Xw = w[:, None] * X - Xc
-            Yw = cs[:, None] * Y - Yc
-            Sm = Xw.T @ (Mx @ Yw)  # S_ij = sum_r xw_ri (M Yw)_rj
-            S = Sm.T.reshape(-1)  # S[i + 3 j]
-            _, V = torch.linalg.eigh(horn_matrix(S))
-            q = V[:, -1]
-            R = quat_to_R(q)
-            t = Xc - R @ Yc
+        if checkpoint:
+            from torch.utils.checkpoint import checkpoint as ckpt
+            R, t, s, u = ckpt(_softassign_updates, X, Y, R, t, s, u, float(T), I0, I1, alpha, use_reentrant=False)
+        else:
+            R, t, s, u = _softassign_updates(X, Y, R, t, s, u, float(T), I0, I1, alpha)
         T = np.float32(T * np.float32(TFACTOR))
     return R, t
 

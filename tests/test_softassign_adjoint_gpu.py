@@ -133,3 +133,34 @@ def test_ragged_sizes_and_inner_counts(cesa, torch_cuda, n, m, I1, seed):
     assert _rel(gXd, gX) < TOL, _rel(gXd, gX)
     assert _rel(gYd, gY) < TOL, _rel(gYd, gY)
     assert _rel(g6, np.r_[gw, gv]) < TOL, (g6, np.r_[gw, gv])
+
+
+def test_c5_copy_full_schedule(cesa, torch_cuda):
+    """The Softassign adjoint workload's check: its generator at N = M = 300 and
+    the default schedule (JMAX = 100, I0 = 5, I1 = 3: 500 updates from T = 100).
+    The reference (checkpointed per T step) is pinned by central differences of
+    its forward at two X and two Y coordinates. Annealing from T = 100 erases
+    the initial pose (|dL/d se(3)| ~ 1e-8), so that block is checked in
+    absolute terms, within 5e-3 of the largest |dL/dY|."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    from oracle import torch_ref as T
+    _, X, Y, Rt, tt = W.make("c5_softassign_20000", seed=0, n=300)
+    X = X.astype(np.float32).astype(np.float64)
+    Y = Y.astype(np.float32).astype(np.float64)
+    _, gX, gY, gw, gv, _, _ = T.softassign_loss_grads(X, Y, np.eye(3), np.zeros(3), Rt, tt, checkpoint=True)
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    for name, P, G in (("X", X, gX), ("Y", Y, gY)):
+        for _ in range(2):
+            i, k = int(rng.integers(len(P))), int(rng.integers(3))
+            Pp, Pm = P.copy(), P.copy()
+            Pp[i, k] += h
+            Pm[i, k] -= h
+            a = (Pp, Y) if name == "X" else (X, Pp)
+            b = (Pm, Y) if name == "X" else (X, Pm)
+            fd = (_loss_t(*a, np.eye(3), np.zeros(3), Rt, tt) - _loss_t(*b, np.eye(3), np.zeros(3), Rt, tt)) / (2 * h)
+            assert abs(fd - G[i, k]) <= 1e-6 * np.abs(G).max(), (name, i, k, fd, G[i, k])
+    _, _, gXd, gYd, g6 = _gpu_grads(cesa, torch_cuda, X, Y, np.eye(3), np.zeros(3), Rt, tt)
+    assert _rel(gXd, gX) < TOL, _rel(gXd, gX)
+    assert _rel(gYd, gY) < TOL, _rel(gYd, gY)
+    assert np.abs(g6 - np.r_[gw, gv]).max() <= TOL * np.abs(gY).max(), (g6, np.r_[gw, gv])
