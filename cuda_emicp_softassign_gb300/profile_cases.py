@@ -10,6 +10,8 @@ cases:
               Softassign with JMAX = 1, I0 = 2
   mat_8000    softassign_mat_kernel: N = M = 8000 (K is 258 MB), one pose update, materialised form
   adj_20000   emicp_adjoint_kernel: forward + backward, N = M = 20000, sigma_inf = 2e-3 (16 steps)
+  sa_adj_20000  Softassign adjoint sweeps (k_sweep_sum, k_sweep_grad): forward + backward,
+              N = M = 20000 (config-5 generator), JMAX = 1, I0 = 2 (two pose updates)
 """
 import sys
 
@@ -73,7 +75,25 @@ def adj_20000():
     torch.cuda.synchronize()
 
 
-CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000)}
+def sa_adj_20000():
+    import torch
+
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    from cuda_emicp_softassign_gb300.autograd import softassign_autograd
+    _, X, Y, _, _ = W.make("c5_softassign_20000", seed=0)
+    p = C.Params.default(JMAX=1, I0=2)
+    Xd = torch.tensor(np.asarray(X), dtype=torch.float32, device="cuda", requires_grad=True)
+    Yd = torch.tensor(np.asarray(Y), dtype=torch.float32, device="cuda", requires_grad=True)
+    R0 = torch.eye(3, device="cuda", requires_grad=True)
+    t0 = torch.zeros(3, device="cuda", requires_grad=True)
+    for _ in range(2):
+        R, t = softassign_autograd(Xd, Yd, R0, t0, p)
+        (R.sum() + t.sum()).backward()
+    torch.cuda.synchronize()
+
+
+CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000)}
 
 if __name__ == "__main__":
     if len(sys.argv) != 2 or sys.argv[1] not in CASES:
