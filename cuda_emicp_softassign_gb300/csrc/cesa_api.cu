@@ -576,26 +576,31 @@ TapeLayout tape_layout(int N, int M, long nsteps) {
   t.total = off;
   return t;
 }
-// Softassign tape: header, packed clouds, and per pose update the input pose
-// (centred frame, 16 floats) and the input slack s (N) and u (M).
+// Softassign tape: header, packed clouds, and per pose update its record
+// (kSaTape floats: input pose, sumM, centres, S, Horn's solve), the input slack
+// s (N) and u (M), the row- and column-pass vectors ([I1][4][N], [I1][4][M])
+// and the final sweep's row sums ([5][N]).
 struct SaTapeLayout {
-  size_t hdr, X, Y, pose, s, u, total;
+  size_t hdr, X, Y, pose, s, u, rows, cols, fin, total;
 };
-SaTapeLayout sa_tape_layout(int N, int M, long nsteps) {
+SaTapeLayout sa_tape_layout(int N, int M, int I1, long nsteps) {
   SaTapeLayout t;
   size_t off = 0;
-  t.hdr = off;
-  off += align256(sizeof(CenterHdr));
-  t.X = off;
-  off += align256(sizeof(float4) * (size_t)N);
-  t.Y = off;
-  off += align256(sizeof(float4) * (size_t)M);
-  t.pose = off;
-  off += align256(sizeof(float) * 16 * (size_t)nsteps);
-  t.s = off;
-  off += align256(sizeof(float) * (size_t)N * (size_t)nsteps);
-  t.u = off;
-  off += align256(sizeof(float) * (size_t)M * (size_t)nsteps);
+  auto put = [&off](size_t bytes) {
+    const size_t at = off;
+    off += align256(bytes);
+    return at;
+  };
+  const size_t n = (size_t)nsteps;
+  t.hdr = put(sizeof(CenterHdr));
+  t.X = put(sizeof(float4) * (size_t)N);
+  t.Y = put(sizeof(float4) * (size_t)M);
+  t.pose = put(sizeof(float) * kSaTape * n);
+  t.s = put(sizeof(float) * (size_t)N * n);
+  t.u = put(sizeof(float) * (size_t)M * n);
+  t.rows = put(sizeof(float) * (size_t)I1 * 4 * N * n);
+  t.cols = put(sizeof(float) * (size_t)I1 * 4 * M * n);
+  t.fin = put(sizeof(float) * 5 * (size_t)N * n);
   t.total = off;
   return t;
 }
@@ -694,7 +699,7 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
 
 size_t cesa_softassign_tape_bytes(int N, int M, const cesa_params* p) {
   if (N < 1 || M < 1 || check_sa_params(p)) return 0;
-  return sa_tape_layout(N, M, (long)p->JMAX * p->I0).total;
+  return sa_tape_layout(N, M, p->I1, (long)p->JMAX * p->I0).total;
 }
 
 int cesa_softassign_forward_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
@@ -712,7 +717,7 @@ int cesa_softassign_forward_device(const float* dX, int N, const float* dY, int 
   StreamCtx& C = ctx_for(dev, st);
   cudaError_t e = C.ws.ensure(softassign_ws_need(N, M, kFormMatrixFree, dev));
   if (e != cudaSuccess) return map_cuda(e);
-  const SaTapeLayout T = sa_tape_layout(N, M, nsteps);
+  const SaTapeLayout T = sa_tape_layout(N, M, p->I1, nsteps);
   char* tb = static_cast<char*>(tape);
   SoftassignLaunch L{};
   L.dX = dX;
@@ -733,6 +738,9 @@ int cesa_softassign_forward_device(const float* dX, int N, const float* dY, int 
   L.tape_pose = reinterpret_cast<float*>(tb + T.pose);
   L.tape_s = reinterpret_cast<float*>(tb + T.s);
   L.tape_u = reinterpret_cast<float*>(tb + T.u);
+  L.tape_rows = reinterpret_cast<float*>(tb + T.rows);
+  L.tape_cols = reinterpret_cast<float*>(tb + T.cols);
+  L.tape_fin = reinterpret_cast<float*>(tb + T.fin);
   C.last_kind = 2;
   C.last_trace_steps = 0;
   const int k = enqueue_softassign(L, C.ws.p, C.ws.bytes, st, nullptr);
@@ -766,7 +774,7 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
   float* gp = reinterpret_cast<float*>(wb + o_gp);
   float* gs = reinterpret_cast<float*>(wb + o_gs);
   float* gu = reinterpret_cast<float*>(wb + o_gu);
-  const SaTapeLayout T = sa_tape_layout(N, M, nsteps);
+  const SaTapeLayout T = sa_tape_layout(N, M, p->I1, nsteps);
   const char* tb = static_cast<const char*>(tape);
   e = cudaMemcpyAsync(gp, d_gRt, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_gX, 0, sizeof(float) * 3 * (size_t)N, st);
@@ -780,6 +788,7 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
     for (int i = 0; i < p->I0; ++i) Ts.push_back(Tk);
     Tk = Tk * p->TFACTOR;
   }
+  const size_t I1 = (size_t)p->I1;
   SoftassignStepAdjoint J{};
   J.X = reinterpret_cast<const float4*>(tb + T.X);
   J.Y = reinterpret_cast<const float4*>(tb + T.Y);
@@ -790,19 +799,21 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
   J.alpha = p->alpha;
   J.gX = d_gX;
   J.gY = d_gY;
-  J.g_pose_out = gp;
-  J.g_pose_in = gp;
-  J.g_s_in = gs;
-  J.g_u_in = gu;
+  J.g_pose = gp;
+  J.g_s = gs;
+  J.g_u = gu;
   for (long n = nsteps - 1; n >= 0; --n) {
-    J.T = Ts[(size_t)n];
-    J.pose = reinterpret_cast<const float*>(tb + T.pose) + (size_t)n * 16;
-    J.s = reinterpret_cast<const float*>(tb + T.s) + (size_t)n * N;
-    J.u = reinterpret_cast<const float*>(tb + T.u) + (size_t)n * M;
-    J.g_s_out = n == nsteps - 1 ? nullptr : gs;
-    J.g_u_out = n == nsteps - 1 ? nullptr : gu;
-    const int k = enqueue_softassign_step_adjoint(J, C.ws.p, need, st);
-    if (k) return map_cuda((cudaError_t)k);
+    const size_t k = (size_t)n;
+    J.T = Ts[k];
+    J.rec = reinterpret_cast<const float*>(tb + T.pose) + k * kSaTape;
+    J.s0 = reinterpret_cast<const float*>(tb + T.s) + k * N;
+    J.u0 = reinterpret_cast<const float*>(tb + T.u) + k * M;
+    J.rows = reinterpret_cast<const float*>(tb + T.rows) + k * I1 * 4 * N;
+    J.cols = reinterpret_cast<const float*>(tb + T.cols) + k * I1 * 4 * M;
+    J.fin = reinterpret_cast<const float*>(tb + T.fin) + k * 5 * N;
+    J.first = n == nsteps - 1 ? 1 : 0;
+    const int r = enqueue_softassign_step_adjoint(J, C.ws.p, need, st);
+    if (r) return map_cuda((cudaError_t)r);
   }
   e = cudaMemcpyAsync(d_gRt0, gp, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
   // the backward has no device-side waits: its status is set once all launches are queued

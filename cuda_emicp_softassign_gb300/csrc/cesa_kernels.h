@@ -66,12 +66,23 @@ struct SoftassignLaunch {
   unsigned long long* timeline;
   int timeline_cap;
   uint64_t timeout_ns;
-  // optional tape of the matrix-free form, per pose update: the input pose in
-  // the centred frame [nsteps][16] and the input slack s [nsteps][N], u [nsteps][M]
+  // optional tape of the matrix-free form, per pose update n:
+  //   tape_pose [n][kSaTape]: input pose (centred), sumM, centres, S, q, eigenbasis
+  //   tape_s [n][N], tape_u [n][M]: the input slack
+  //   tape_rows [n][I1][4][N]: per row pass k: a^(k+1), s^(k+1), rs^k, r^k
+  //   tape_cols [n][I1][4][M]: per column pass k: b^(k+1), u^(k+1), cs^k, c^k
+  //   tape_fin [n][5][N]: the final sweep's row sums K b, K (b (cs - 1)), K (b cs (y' - Yhat))
   float* tape_pose;
   float* tape_s;
   float* tape_u;
+  float* tape_rows;
+  float* tape_cols;
+  float* tape_fin;
 };
+// Softassign tape record of one pose update (floats):
+//   0-11 input pose (R, t', centred)  12-13 sumM (hi, lo)  14-16 Xc  17-19 Yc (caller frame)
+//   20-22 Xc - oX  23-25 Yc - oY  26-34 S  35-38 q  39-54 Horn eigenbasis V[4][4]
+constexpr int kSaTape = 64;
 
 // One pair of a batched launch (device pointers).
 constexpr int kMaxBatchPairs = 1024;
@@ -141,25 +152,25 @@ void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4*
 
 void softassign_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);
 
-// Adjoint of one Softassign inner iteration (recomputing). Device pointers.
+// Adjoint of one Softassign pose update from its tape. Device pointers.
 struct SoftassignStepAdjoint {
   const float4* X;        // X' centred (N), as packed by the forward
   const float4* Y;        // Y' centred (M)
   const CenterHdr* hdr;
   int N, M, I1;
   float T, alpha;
-  const float* pose;      // [12] input pose, centred frame (R, t')
-  const float* s;         // [N] input slack
-  const float* u;         // [M]
-  const float* g_pose_out;  // [12] dL/dR, dL/dt of the output pose, caller frame
-  const float* g_s_out;   // [N] dL/ds of the output slack (nullptr: zero)
-  const float* g_u_out;   // [M] (nullptr: zero)
+  const float* rec;       // [kSaTape] the update's record
+  const float* s0;        // [N] input slack
+  const float* u0;        // [M]
+  const float* rows;      // [I1][4][N]
+  const float* cols;      // [I1][4][M]
+  const float* fin;       // [5][N]
+  float* g_pose;          // [12] in: dL/d(R, t) of the output pose; out: of the input pose (caller frame)
+  float* g_s;             // [N] in: dL/ds of the output slack (ignored when first); out: of the input slack
+  float* g_u;             // [M]
+  int first;              // the last update of the schedule: the output slack does not feed the loss
   float* gX;              // SoA [3N], accumulated
   float* gY;              // SoA [3M], accumulated
-  float* g_pose_in;       // [12] dL/d(R, t) of the input pose, caller frame (written)
-  float* g_s_in;          // [N] (written; may alias g_s_out)
-  float* g_u_in;          // [M] (written; may alias g_u_out)
-  float* pose_out;        // optional [12]: the recomputed output pose, centred frame
 };
 size_t softassign_step_adjoint_ws_need(int N, int M, int I1);
 int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st);

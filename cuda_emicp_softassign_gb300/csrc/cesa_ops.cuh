@@ -160,6 +160,7 @@ struct FinalFin {
   int N;
   df* scratch;     // shared, >= 33 * 128 dfs
   df* rbpart;      // this update's row-block records [nblk_r][32] (slots 0..27 used)
+  float* tape_fin = nullptr;  // optional [5][N]: the raw row sums tot[]
   __device__ void operator()(int blk, const float (&tot)[5]) const {
     df v[32];
 #pragma unroll
@@ -172,6 +173,10 @@ struct FinalFin {
       const float V[3] = {ar * tot[2], ar * tot[3], ar * tot[4]};
       const float xp[3] = {x.x, x.y, x.z};
       if (w_out) w_out[r] = w;
+      if (tape_fin) {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) __stcg(tape_fin + (size_t)m * N + r, tot[m]);
+      }
       const float w2 = w * w, wmu = w * mu;
       df_add(v[0], w);
 #pragma unroll

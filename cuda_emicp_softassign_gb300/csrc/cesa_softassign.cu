@@ -63,9 +63,12 @@ struct SoftArgs {
   unsigned long long* tl;
   int tl_cap;
   uint64_t timeout_ns;
-  float* tape_pose;    // optional [nsteps][16]: input pose of each update (centred frame)
+  float* tape_pose;    // optional [nsteps][kSaTape] (see SoftassignLaunch)
   float* tape_s;       // optional [nsteps][N]: input slack s of each update
   float* tape_u;       // optional [nsteps][M]
+  float* tape_rows;    // optional [nsteps][I1][4][N]
+  float* tape_cols;    // optional [nsteps][I1][4][M]
+  float* tape_fin;     // optional [nsteps][5][N]
 };
 
 // Sum of the S slice partials of point i (deferred completion), 8 loads in flight.
@@ -95,6 +98,8 @@ struct ColDone {
   float* b_new;
   float* u_new;
   float* cs_out;
+  float* tape = nullptr;  // optional [4][M]: b_new, u_new, cs, column sum
+  int M = 0;
   __device__ __forceinline__ void operator()(int c, bool store, float& bn, float& csv) const {
     const float sum = slice_sum(pc, S, ld, c);
     const float bo = b_old ? __ldcg(b_old + c) : 1.f;
@@ -102,9 +107,16 @@ struct ColDone {
     csv = fmaf(bo, sum, uo);
     bn = bo / csv;
     if (store) {
+      const float un = uo / csv;
       __stcg(b_new + c, bn);
-      __stcg(u_new + c, uo / csv);
+      __stcg(u_new + c, un);
       __stcg(cs_out + c, csv);
+      if (tape) {
+        __stcg(tape + c, bn);
+        __stcg(tape + (size_t)M + c, un);
+        __stcg(tape + 2 * (size_t)M + c, csv);
+        __stcg(tape + 3 * (size_t)M + c, sum);
+      }
     }
   }
 };
@@ -142,6 +154,8 @@ struct ColPrep {
   float* a_new;
   float* s_new;
   float* rs_out;
+  float* tape = nullptr;  // optional [4][N]: a_new, s_new, rs, row sum
+  int N = 0;
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
     for (int c = threadIdx.x; c < len; c += kThreads) {
@@ -153,9 +167,16 @@ struct ColPrep {
       const float rsv = fmaf(ao, sum, so);
       const float an = ao / rsv;
       if (blk == 0) {
+        const float sn = so / rsv;
         __stcg(a_new + r, an);
-        __stcg(s_new + r, so / rsv);
+        __stcg(s_new + r, sn);
         __stcg(rs_out + r, rsv);
+        if (tape) {
+          __stcg(tape + r, an);
+          __stcg(tape + (size_t)N + r, sn);
+          __stcg(tape + 2 * (size_t)N + r, rsv);
+          __stcg(tape + 3 * (size_t)N + r, sum);
+        }
       }
       sm.prep[c] = make_float4(x.x, x.y, x.z, an);
     }
@@ -219,6 +240,9 @@ struct FinalPrep {
   }
 };
 
+// kTape: the variant that records the adjoint's tape (the plain variant
+// carries none of its pointers, so its register allocation is unaffected).
+template <bool kTape>
 __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem& sm = *reinterpret_cast<SweepSmem*>(smem_raw);
@@ -282,10 +306,10 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
 #pragma unroll
       for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
-      if (A.tape_pose) {
+      if (kTape) {
         // the update's inputs for the adjoint: s and u are the current ping-pong
         // buffers, which are next overwritten two grid barriers from here
-        if (blockIdx.x == 0 && tid < 12) A.tape_pose[(size_t)step * 16 + tid] = s_pose[tid];
+        if (blockIdx.x == 0 && tid < 12) A.tape_pose[(size_t)step * kSaTape + tid] = s_pose[tid];
         const int stride = (int)G * kThreads;
         for (int i = blockIdx.x * kThreads + tid; i < A.N; i += stride)
           A.tape_s[(size_t)step * A.N + i] = __ldcg(A.sbuf + (size_t)sp * Np + i);
@@ -294,6 +318,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       }
       __syncthreads();
       const SinkElem se{nk, c0};
+      float* trow = kTape ? A.tape_rows + (size_t)step * A.I1 * 4 * A.N : nullptr;
+      float* tcol = kTape ? A.tape_cols + (size_t)step * A.I1 * 4 * A.M : nullptr;
       for (int k = 0; k < A.I1 && ok; ++k) {
         // row pass k: own X rows, stream Y columns weighted by b^(k); row partials -> pr
         RowPrep rp;
@@ -310,6 +336,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.bbuf + (size_t)(k & 1) * Mp,
                         A.ubuf + (size_t)(up ^ 1) * Mp,
                         A.cs};
+        rp.cd.tape = (tcol && k >= 1) ? tcol + (size_t)(k - 1) * 4 * A.M : nullptr;  // column pass k-1
+        rp.cd.M = A.M;
         ok = sweep_units<1, SinkElem, RowPrep, NoFin, true>(sm, pipe, A.gr, src_cols, A.rows, false, R,
                                                             tc, 0u, A.pr, nullptr, se, rp, NoFin{},
                                                             A.ctl, A.timeout_ns, 30, tl, Np, &oc_rows);
@@ -319,14 +347,16 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         if (!ok) break;
         if (k >= 1) up ^= 1;  // the row pass completed column pass k-1
         // column pass k: own Y columns, stream X rows weighted by a^(k+1)
-        const ColPrep cp{A.pr,
-                         A.gr.slices,
-                         Np,
-                         k >= 1 ? A.abuf + (size_t)(k & 1) * Np : nullptr,
-                         A.sbuf + (size_t)sp * Np,
-                         A.abuf + (size_t)((k + 1) & 1) * Np,
-                         A.sbuf + (size_t)(sp ^ 1) * Np,
-                         A.rs};
+        ColPrep cp{A.pr,
+                   A.gr.slices,
+                   Np,
+                   k >= 1 ? A.abuf + (size_t)(k & 1) * Np : nullptr,
+                   A.sbuf + (size_t)sp * Np,
+                   A.abuf + (size_t)((k + 1) & 1) * Np,
+                   A.sbuf + (size_t)(sp ^ 1) * Np,
+                   A.rs};
+        cp.tape = trow ? trow + (size_t)k * 4 * A.N : nullptr;  // row pass k
+        cp.N = A.N;
         ok = sweep_units<1, SinkElem, ColPrep, NoFin, true>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
                                                            0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
                                                            A.timeout_ns, 40, tl, Mp, &oc_cols);
@@ -355,6 +385,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.bbuf + (size_t)(A.I1 & 1) * Mp,
                         A.ubuf + (size_t)(up ^ 1) * Mp,
                         A.cs};
+        fp.cd.tape = tcol ? tcol + (size_t)kl * 4 * A.M : nullptr;  // the last column pass
+        fp.cd.M = A.M;
         df* mom = A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32;
         fp.colacc = s_colacc;
         fp.red = s_red;
@@ -364,8 +396,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         // owned_block_sum<32> scratch (32 * (128 + 8) dfs) spans prep, prep2 and red
         static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >= 32 * (kBlockPts + 8) * sizeof(df),
                       "moment scratch does not fit");
-        const FinalFin ff{A.rows, A.abuf + (size_t)(A.I1 & 1) * Np, A.w_out, A.N,
-                          reinterpret_cast<df*>(sm.prep), mom};
+        FinalFin ff{A.rows, A.abuf + (size_t)(A.I1 & 1) * Np, A.w_out, A.N,
+                    reinterpret_cast<df*>(sm.prep), mom};
+        ff.tape_fin = kTape ? A.tape_fin + (size_t)step * 5 * A.N : nullptr;
         const StreamSrc src_final{A.cols, nullptr, false};
         ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_f++, A.part_f,
                             A.cnt_f, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl, 0, &oc_rows);
@@ -401,6 +434,21 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];
         for (int k = 0; k < 3; ++k) s_pose[9 + k] = tn[k];
         if (blockIdx.x == 0) {
+          if (kTape) {  // the update's solve, for the adjoint
+            float* rec = A.tape_pose + (size_t)step * kSaTape;
+            rec[12] = s_tot[0].hi;
+            rec[13] = s_tot[0].lo;
+            for (int i = 0; i < 3; ++i) {
+              rec[14 + i] = Xc[i];
+              rec[17 + i] = Yc[i];
+              rec[20 + i] = Xcp[i];
+              rec[23 + i] = Yd[i];
+            }
+            for (int i = 0; i < 9; ++i) rec[26 + i] = S[i];
+            for (int i = 0; i < 4; ++i) rec[35 + i] = q[i];
+            for (int i = 0; i < 4; ++i)
+              for (int j = 0; j < 4; ++j) rec[39 + 4 * i + j] = horn.V[i][j];
+          }
           if (A.trace && step < A.trace_cap) {
             double* rec = A.trace + (size_t)step * 32;
             float to[3];
@@ -471,7 +519,10 @@ struct SaPlan {
 SaPlan plan_sa(int N, int M, int device) {
   SaPlan P;
   P.smem = sizeof(SweepSmem);
-  const int limit = persistent_grid_limit(device, (const void*)softassign_kernel, P.smem);
+  // both variants: the call also sets each one's dynamic shared-memory limit
+  const int lim0 = persistent_grid_limit(device, (const void*)softassign_kernel<false>, P.smem);
+  const int lim1 = persistent_grid_limit(device, (const void*)softassign_kernel<true>, P.smem);
+  const int limit = lim0 < lim1 ? lim0 : lim1;
   const SweepGeomH r = plan_sweep(N, M, limit);
   const SweepGeomH c = plan_sweep(M, N, limit);
   P.gr = SweepGeom{r.n_own, r.n_stream, r.nblk, r.slices, r.slice_len, r.units};
@@ -605,8 +656,12 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.tape_pose = L.tape_pose;
   A.tape_s = L.tape_s;
   A.tape_u = L.tape_u;
+  A.tape_rows = L.tape_rows;
+  A.tape_cols = L.tape_cols;
+  A.tape_fin = L.tape_fin;
   void* args[] = {(void*)&A};
-  e = cudaLaunchCooperativeKernel((const void*)softassign_kernel, dim3(P.grid), dim3(kThreads), args,
+  const void* kern = L.tape_pose ? (const void*)softassign_kernel<true> : (const void*)softassign_kernel<false>;
+  e = cudaLaunchCooperativeKernel(kern, dim3(P.grid), dim3(kThreads), args,
                                   P.smem, st);
   if (e != cudaSuccess) return (int)e;
   // the slack buffers toggle once per row / column pass completion

@@ -10,16 +10,21 @@
 //           Yc = sum cs y / sumM, p_i = w_i x_i - Xc, h_j = b_j (cs_j y_j - Yc),
 //           V = K h, S = sum_i a_i p_i V_i^T, (R', t') = Horn(S, Xc, Yc)
 // with a = a^{I1}, b = b^{I1}, cs = cs^{I1-1}, all in the caller's frame
-// (the reference's S is not translation invariant). The backward of one
-// iteration recomputes these vectors (K is never stored), then runs the
-// chain rule through Horn's pose (horn_pose_adjoint), the final stage, and
-// the column and row passes in reverse. Each pass's adjoint is one K or K^T
-// product. dL/dK is a sum of 4 + 2 I1 rank-1 terms alpha_m beta_m^T:
+// (the reference's S is not translation invariant). The forward kernel tapes
+// every one of these vectors (the scalings and sums of each pass, the final
+// sweep's row sums and Horn's solve; O(N + M) per pass), so the backward of
+// an update runs no forward sweep: it applies the chain rule through Horn's
+// pose (horn_pose_adjoint), the final stage, and the column and row passes in
+// reverse. Each pass's adjoint is one K or K^T product (K recomputed, never
+// stored). dL/dK is a sum of 4 + 2 I1 rank-1 terms alpha_m beta_m^T:
 //   (g(V)_d, h_d) d = 0..2,  (g(rho), b^{I1}),  (a^{k+1}, g(c^k)),  (g(r^k), b^k)
 // so dL/dx and dL/dz come from two more recomputing sweeps (own rows, own
 // columns): dL/dx_i = (2/T) sum_j G_ij (z_j - x_i), G = K .* dL/dK, and
 // likewise for z. dL/dy = R^T dL/dz plus the direct terms of Yc and h;
 // dL/dR, dL/dt of the input pose are sum dL/dz y^T and sum dL/dz.
+// V_i = sum_j K_ij h_j comes from the final sweep's sums rho = K b,
+// m = K (b (cs - 1)) and v = K (b cs (y' - Yhat)):
+//   V = v + (Yhat - (Yc - oY)) rho + (Yhat + oY) m.
 //
 // Sweeps are plain launches over (owned block, streamed slice) tiles: each
 // thread owns 4 points (two packed FP32 pairs) and the streamed points pass
@@ -254,21 +259,13 @@ __global__ void k_reduce_slices(const float* __restrict__ part, int S, int NW, i
 }
 
 // ------------------------------------------------------------- O(N + M) steps
-// Scalars of one iteration (double).
+// Scalars of the backward of one update (double).
 enum : int {
-  kSsum = 0,     // sumM
-  kSXc = 1,      // Xc (caller frame)
-  kSXcp = 4,     // Xc - oX
-  kSYc = 7,      // Yc (caller frame)
-  kSYd = 10,     // Yc - oY
-  kSS = 13,      // S[i + 3 j]
-  kSq = 22,      // q
-  kSV = 26,      // eigenbasis V[4][4]
-  kSgS = 42,     // dL/dS
-  kSgXc = 51,    // dL/dXc
-  kSgYc = 54,    // dL/dYc
-  kSgsum = 57,   // dL/dsumM
-  kScalN = 64
+  kSgS = 0,     // dL/dS
+  kSgXc = 9,    // dL/dXc
+  kSgYc = 12,   // dL/dYc
+  kSgsum = 15,  // dL/dsumM
+  kScalN = 16
 };
 
 struct Vecs {
@@ -276,159 +273,92 @@ struct Vecs {
   const float4* X;  // X' (centred)
   const float4* Y;  // Y' (centred, unposed)
   const CenterHdr* hdr;
-  const float* pose;  // centred-frame input pose (R, t')
-  float *a, *s;       // [I1 + 1][N]
-  float *b, *u;       // [I1 + 1][M]
-  float *r, *rs;      // [I1][N]
-  float *c, *cs;      // [I1][M]
-  float *rho, *w;     // N
-  float* V;           // [3][N]
+  const float* rec;   // the update's record (kSaTape)
+  const float* s0;    // [N] input slack
+  const float* u0;    // [M]
+  const float* rows;  // [I1][4][N]: a^{k+1}, s^{k+1}, rs^k, r^k
+  const float* cols;  // [I1][4][M]: b^{k+1}, u^{k+1}, cs^k, c^k
+  const float* fin;   // [5][N]: K b, K (b (cs - 1)), K (b cs (y' - Yhat))
+  float* ones;        // [M]: b^0
   float* h;           // [3][M]
   double* scal;       // kScalN
-  float* pose_out;    // 12, centred frame
-  float *ga, *gs;     // N
-  float *gb, *gu, *gcs;  // M
+  float* g_pose;      // [12]
+  float *gs, *gu;     // [N], [M]: slack adjoints (in place)
+  float* ga;          // [N]
+  float *gb, *gcs;    // [M]
   float* gV;          // [3][N]
   float* gp;          // [3][N]
-  float* gw;          // N: known part of dL/dw
-  float* grho;        // N
+  float* gw;          // [N]: known part of dL/dw
+  float* grho;        // [N]
   float* wt4;         // [4][N]: weights of the K^T sweep (g(V), a gw)
   float* gh;          // [4][M]: K^T of wt4
   float* gr;          // [I1][N] g(r^k)
   float* gc;          // [I1][M] g(c^k)
-  float* gX;          // [3][N]
   float* gZ;          // [3][M]
-  float* gY;          // [3][M]
+  float* gX;          // [3][N] accumulated
+  float* gY;          // [3][M] accumulated
 };
+
+__device__ __forceinline__ const float* a_of(const Vecs& A, int k) { return A.rows + (size_t)(k - 1) * 4 * A.N; }
+__device__ __forceinline__ float a_at(const Vecs& A, int k, int i) { return k == 0 ? 1.f : a_of(A, k)[i]; }
+__device__ __forceinline__ float s_at(const Vecs& A, int k, int i) {
+  return k == 0 ? A.s0[i] : A.rows[((size_t)(k - 1) * 4 + 1) * A.N + i];
+}
+__device__ __forceinline__ float rs_at(const Vecs& A, int k, int i) { return A.rows[((size_t)k * 4 + 2) * A.N + i]; }
+__device__ __forceinline__ float r_at(const Vecs& A, int k, int i) { return A.rows[((size_t)k * 4 + 3) * A.N + i]; }
+__device__ __forceinline__ float b_at(const Vecs& A, int k, int j) {
+  return k == 0 ? 1.f : A.cols[((size_t)(k - 1) * 4) * A.M + j];
+}
+__device__ __forceinline__ float u_at(const Vecs& A, int k, int j) {
+  return k == 0 ? A.u0[j] : A.cols[((size_t)(k - 1) * 4 + 1) * A.M + j];
+}
+__device__ __forceinline__ float cs_at(const Vecs& A, int k, int j) { return A.cols[((size_t)k * 4 + 2) * A.M + j]; }
+__device__ __forceinline__ float c_at(const Vecs& A, int k, int j) { return A.cols[((size_t)k * 4 + 3) * A.M + j]; }
+__device__ __forceinline__ double sumM_of(const Vecs& A) { return (double)A.rec[12] + (double)A.rec[13]; }
 
 __global__ void k_fill(float* p, int n, float v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
 
-// Pass completion: t = a r + s, a' = a / t, s' = s / t (row pass; the column
-// pass is the same with b, c, u).
-__global__ void k_pass_done(const float* a, const float* r, const float* s, float* t, float* an, float* sn, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float v = fmaf(a[i], r[i], s[i]);
-  t[i] = v;
-  an[i] = a[i] / v;
-  sn[i] = s[i] / v;
-}
-
-// One block: w = a rho, sumM, Xc and Yc (compensated), as the forward's moments.
-__global__ void __launch_bounds__(1024) k_centres(Vecs A) {
-  __shared__ df red[8 * 32];
-  const float* aF = A.a + (size_t)A.I1 * A.N;
-  const float* csF = A.cs + (size_t)(A.I1 - 1) * A.M;
-  df v[8];
-  for (int k = 0; k < 8; ++k) v[k] = df_make(0.f);
-  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
-    const float4 x = A.X[i];
-    const float w = aF[i] * A.rho[i];
-    A.w[i] = w;
-    df_add(v[0], w);
-    df_add_prod(v[1], w, x.x);
-    df_add_prod(v[2], w, x.y);
-    df_add_prod(v[3], w, x.z);
-  }
-  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
-    const float4 y = A.Y[j];
-    df_add(v[4], csF[j]);
-    df_add_prod(v[5], csF[j], y.x);
-    df_add_prod(v[6], csF[j], y.y);
-    df_add_prod(v[7], csF[j], y.z);
-  }
-  block_reduce_df<8>(v, red);
-  if (threadIdx.x == 0) {
-    const double sm = df_dbl(v[0]), scs = df_dbl(v[4]);
-    A.scal[kSsum] = sm;
-    for (int k = 0; k < 3; ++k) {
-      const double xcp = df_dbl(v[1 + k]) / sm;
-      // Yc - oY = sum cs y' / sumM + (sum cs / sumM - 1) oY
-      const double yd = df_dbl(v[5 + k]) / sm + (scs / sm - 1.0) * (double)A.hdr->oY[k];
-      A.scal[kSXcp + k] = xcp;
-      A.scal[kSXc + k] = xcp + (double)A.hdr->oX[k];
-      A.scal[kSYd + k] = yd;
-      A.scal[kSYc + k] = yd + (double)A.hdr->oY[k];
-    }
-  }
-}
-
-// h_j = b_j (cs_j y_j - Yc) = b_j (cs_j y'_j - Yd + (cs_j - 1) oY), [3][M].
+// h_j = b_j (cs_j y_j - Yc) = b_j (cs_j y'_j - Yd + (cs_j - 1) oY), [3][M]
+// (b = b^{I1}, cs = cs^{I1-1}, Yd = Yc - oY).
 __global__ void k_h(Vecs A) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= A.M) return;
-  const float* bF = A.b + (size_t)A.I1 * A.M;
-  const float cs = A.cs[(size_t)(A.I1 - 1) * A.M + j];
+  const float b = b_at(A, A.I1, j), cs = cs_at(A, A.I1 - 1, j);
   const float4 y = A.Y[j];
   const float yv[3] = {y.x, y.y, y.z};
   for (int d = 0; d < 3; ++d)
-    A.h[(size_t)d * A.M + j] =
-        bF[j] * (fmaf(cs, yv[d], -(float)A.scal[kSYd + d]) + (cs - 1.f) * A.hdr->oY[d]);
+    A.h[(size_t)d * A.M + j] = b * (fmaf(cs, yv[d], -A.rec[23 + d]) + (cs - 1.f) * A.hdr->oY[d]);
 }
 
-// p_i = w_i x_i - Xc = w_i x'_i - Xc' + (w_i - 1) oX
-__device__ __forceinline__ void p_of(const Vecs& A, int i, float p[3]) {
+// p_i = w_i x_i - Xc = w_i x'_i - Xc' + (w_i - 1) oX, and V_i from the final sweep's sums.
+__device__ __forceinline__ void pv_of(const Vecs& A, int i, float& w, float p[3], float V[3]) {
   const float4 x = A.X[i];
   const float xv[3] = {x.x, x.y, x.z};
-  const float w = A.w[i];
-  for (int d = 0; d < 3; ++d) p[d] = fmaf(w, xv[d], -(float)A.scal[kSXcp + d]) + (w - 1.f) * A.hdr->oX[d];
-}
-
-// One block: S = sum_i a_i p_i V_i^T (S[p + 3 q] = sum a p_p V_q), then Horn's
-// pose; the output pose in the centred frame t' = Xc' - R (Yc - oY) as the
-// forward kernel forms it.
-__global__ void __launch_bounds__(1024) k_S_pose(Vecs A) {
-  __shared__ df red[9 * 32];
-  const float* aF = A.a + (size_t)A.I1 * A.N;
-  df v[9];
-  for (int k = 0; k < 9; ++k) v[k] = df_make(0.f);
-  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
-    float p[3];
-    p_of(A, i, p);
-    for (int pp = 0; pp < 3; ++pp) {
-      const float ap = aF[i] * p[pp];
-      for (int qq = 0; qq < 3; ++qq) df_add_prod(v[pp + 3 * qq], ap, A.V[(size_t)qq * A.N + i]);
-    }
-  }
-  block_reduce_df<9>(v, red);
-  if (threadIdx.x == 0) {
-    float S[9], Xcp[3], Yd[3], q[4], gap, lmax, R[9], t[3];
-    for (int k = 0; k < 9; ++k) {
-      S[k] = df_val(v[k]);
-      A.scal[kSS + k] = S[k];
-    }
-    for (int k = 0; k < 3; ++k) {
-      Xcp[k] = (float)A.scal[kSXcp + k];
-      Yd[k] = (float)A.scal[kSYd + k];
-    }
-    HornState<float> st;
-    st.reset();
-    horn_quaternion<float>(S, st, q, &gap, &lmax);
-    quat_to_pose<float>(q, Xcp, Yd, R, t);
-    for (int k = 0; k < 4; ++k) A.scal[kSq + k] = q[k];
-    for (int i = 0; i < 4; ++i)
-      for (int j = 0; j < 4; ++j) A.scal[kSV + 4 * i + j] = st.V[i][j];
-    for (int k = 0; k < 9; ++k) A.pose_out[k] = R[k];
-    for (int k = 0; k < 3; ++k) A.pose_out[9 + k] = t[k];
+  const float rho = A.fin[i], m = A.fin[(size_t)A.N + i];
+  w = a_of(A, A.I1)[i] * rho;
+  for (int d = 0; d < 3; ++d) {
+    p[d] = fmaf(w, xv[d], -A.rec[20 + d]) + (w - 1.f) * A.hdr->oX[d];
+    const float yh = A.hdr->ymean[d];
+    V[d] = A.fin[(size_t)(2 + d) * A.N + i] + (yh - A.rec[23 + d]) * rho + (yh + A.hdr->oY[d]) * m;
   }
 }
 
 // Horn adjoint (one thread): dL/d(R, t) of the output pose in the caller's
 // frame, where (R, t) = (R(q), Xc - R Yc) -> dL/dS, dL/dXc, dL/dYc.
-__global__ void k_horn_adjoint(Vecs A, const float* g_out) {
+__global__ void k_horn_adjoint(Vecs A) {
   float gRo[9], gto[3], S[9], Xc[3], Yc[3], q[4], V[4][4], gS[9], gXc[3], gYc[3];
-  for (int k = 0; k < 9; ++k) gRo[k] = g_out[k];
-  for (int k = 0; k < 3; ++k) gto[k] = g_out[9 + k];
-  for (int k = 0; k < 9; ++k) S[k] = (float)A.scal[kSS + k];
+  for (int k = 0; k < 9; ++k) gRo[k] = A.g_pose[k];
+  for (int k = 0; k < 3; ++k) gto[k] = A.g_pose[9 + k];
+  for (int k = 0; k < 9; ++k) S[k] = A.rec[26 + k];
   for (int k = 0; k < 3; ++k) {
-    Xc[k] = (float)A.scal[kSXc + k];
-    Yc[k] = (float)A.scal[kSYc + k];
+    Xc[k] = A.rec[14 + k];
+    Yc[k] = A.rec[17 + k];
   }
-  for (int k = 0; k < 4; ++k) q[k] = (float)A.scal[kSq + k];
+  for (int k = 0; k < 4; ++k) q[k] = A.rec[35 + k];
   for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) V[i][j] = (float)A.scal[kSV + 4 * i + j];
+    for (int j = 0; j < 4; ++j) V[i][j] = A.rec[39 + 4 * i + j];
   horn_pose_adjoint<float>(S, Xc, Yc, q, V, gRo, gto, gS, gXc, gYc);
   for (int k = 0; k < 9; ++k) A.scal[kSgS + k] = gS[k];
   for (int k = 0; k < 3; ++k) {
@@ -438,17 +368,16 @@ __global__ void k_horn_adjoint(Vecs A, const float* g_out) {
 }
 
 // One block, per row: g(p_i) = a_i gS V_i, g(V_i) = a_i gS^T p_i, dL/da_i from
-// S; dL/dXc -= sum g(p).
+// S (S[p + 3 q] = sum a p_p V_q); dL/dXc -= sum g(p).
 __global__ void __launch_bounds__(1024) k_back_S(Vecs A) {
   __shared__ df red[3 * 32];
-  const float* aF = A.a + (size_t)A.I1 * A.N;
+  const float* aF = a_of(A, A.I1);
   float gS[9];
   for (int k = 0; k < 9; ++k) gS[k] = (float)A.scal[kSgS + k];
   df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
   for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
-    float p[3];
-    p_of(A, i, p);
-    const float Vi[3] = {A.V[i], A.V[(size_t)A.N + i], A.V[2 * (size_t)A.N + i]};
+    float w, p[3], Vi[3];
+    pv_of(A, i, w, p, Vi);
     float ga = 0.f;
     for (int pp = 0; pp < 3; ++pp) {
       float gp = 0.f, gv = 0.f;
@@ -469,118 +398,127 @@ __global__ void __launch_bounds__(1024) k_back_S(Vecs A) {
 }
 
 // Per row: the part of dL/dw known before dL/dsumM, gw = x . (g(p) + gXc/sumM);
-// direct dL/dx = w (g(p) + gXc/sumM); the weights of the K^T sweep.
-__global__ void k_back_w(Vecs A, float* wt4) {
+// direct dL/dx += w (g(p) + gXc/sumM); the weights of the K^T sweep.
+__global__ void k_back_w(Vecs A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.N) return;
-  const float* aF = A.a + (size_t)A.I1 * A.N;
-  const float inv = (float)(1.0 / A.scal[kSsum]);
+  const float a = a_of(A, A.I1)[i];
+  const float w = a * A.fin[i];
+  const float inv = (float)(1.0 / sumM_of(A));
   const float4 x = A.X[i];
   const float xv[3] = {x.x, x.y, x.z};
   float gw = 0.f;
   for (int d = 0; d < 3; ++d) {
     const float g = fmaf((float)A.scal[kSgXc + d], inv, A.gp[(size_t)d * A.N + i]);
     gw = fmaf(xv[d] + A.hdr->oX[d], g, gw);
-    A.gX[(size_t)d * A.N + i] = A.w[i] * g;
-    wt4[(size_t)d * A.N + i] = A.gV[(size_t)d * A.N + i];
+    A.gX[(size_t)d * A.N + i] += w * g;
+    A.wt4[(size_t)d * A.N + i] = A.gV[(size_t)d * A.N + i];
   }
   A.gw[i] = gw;
-  wt4[3 * (size_t)A.N + i] = aF[i] * gw;
+  A.wt4[3 * (size_t)A.N + i] = a * gw;
 }
 
 // One block after the K^T sweep: dL/dYc -= sum_j b_j g(h_j);
 // dL/dsumM = -(gXc . Xc + gYc . Yc) / sumM.
-__global__ void __launch_bounds__(1024) k_back_Yc(Vecs A, const float* gh) {
+__global__ void __launch_bounds__(1024) k_back_Yc(Vecs A) {
   __shared__ df red[3 * 32];
-  const float* bF = A.b + (size_t)A.I1 * A.M;
   df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
-  for (int j = threadIdx.x; j < A.M; j += blockDim.x)
-    for (int d = 0; d < 3; ++d) df_add_prod(v[d], bF[j], gh[(size_t)d * A.M + j]);
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
+    const float b = b_at(A, A.I1, j);
+    for (int d = 0; d < 3; ++d) df_add_prod(v[d], b, A.gh[(size_t)d * A.M + j]);
+  }
   block_reduce_df<3>(v, red);
   if (threadIdx.x == 0) {
     double g = 0.0;
     for (int d = 0; d < 3; ++d) {
       A.scal[kSgYc + d] -= df_dbl(v[d]);
-      g -= A.scal[kSgXc + d] * A.scal[kSXc + d] + A.scal[kSgYc + d] * A.scal[kSYc + d];
+      g -= A.scal[kSgXc + d] * (double)A.rec[14 + d] + A.scal[kSgYc + d] * (double)A.rec[17 + d];
     }
-    A.scal[kSgsum] = g / A.scal[kSsum];
+    A.scal[kSgsum] = g / sumM_of(A);
   }
 }
 
-// Per row: g(rho) = a (gw + gsum); dL/da^{I1} += (gw + gsum) rho.
-__global__ void k_back_rho(Vecs A) {
+// Rows (i < N): g(rho) = a (gw + gsum); dL/da^{I1} += (gw + gsum) rho.
+// Columns (j = i - N < M), final stage: dL/db^{I1} = (cs y - Yc) . g(h) + K^T g(rho),
+// where K^T g(rho) = K^T (a gw) + gsum c^{I1-1}; dL/dcs^{I1-1} = y . (b g(h) + gYc / sumM);
+// direct dL/dy += cs (b g(h) + gYc / sumM).
+__global__ void k_back_final(Vecs A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= A.N) return;
-  const float* aF = A.a + (size_t)A.I1 * A.N;
-  const float gw = A.gw[i] + (float)A.scal[kSgsum];
-  A.grho[i] = aF[i] * gw;
-  A.ga[i] = fmaf(gw, A.rho[i], A.ga[i]);
-}
-
-// Per column, final stage: dL/db^{I1} = (cs y - Yc) . g(h) + K^T g(rho), where
-// K^T g(rho) = K^T (a gw) + gsum c^{I1-1}; dL/dcs^{I1-1} = y . (b g(h) + gYc / sumM);
-// direct dL/dy = cs (b g(h) + gYc / sumM).
-__global__ void k_back_final_cols(Vecs A, const float* gh) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const float gsum = (float)A.scal[kSgsum];
+  if (i < A.N) {
+    const float a = a_of(A, A.I1)[i];
+    const float gw = A.gw[i] + gsum;
+    A.grho[i] = a * gw;
+    A.ga[i] = fmaf(gw, A.fin[i], A.ga[i]);
+    return;
+  }
+  const int j = i - A.N;
   if (j >= A.M) return;
   const int k = A.I1 - 1;
-  const float bF = A.b[(size_t)A.I1 * A.M + j];
-  const float cs = A.cs[(size_t)k * A.M + j];
-  const float c = A.c[(size_t)k * A.M + j];
-  const float inv = (float)(1.0 / A.scal[kSsum]);
+  const float b = b_at(A, A.I1, j), cs = cs_at(A, k, j), c = c_at(A, k, j);
+  const float inv = (float)(1.0 / sumM_of(A));
   const float4 y = A.Y[j];
   const float yv[3] = {y.x, y.y, y.z};
-  float gb = fmaf((float)A.scal[kSgsum], c, gh[3 * (size_t)A.M + j]), gcs = 0.f;
+  float gb = fmaf(gsum, c, A.gh[3 * (size_t)A.M + j]), gcs = 0.f;
   for (int d = 0; d < 3; ++d) {
-    const float ghd = gh[(size_t)d * A.M + j];
-    const float gy = fmaf(bF, ghd, (float)A.scal[kSgYc + d] * inv);
-    gb = fmaf(fmaf(cs, yv[d], -(float)A.scal[kSYd + d]) + (cs - 1.f) * A.hdr->oY[d], ghd, gb);
+    const float ghd = A.gh[(size_t)d * A.M + j];
+    const float gy = fmaf(b, ghd, (float)A.scal[kSgYc + d] * inv);
+    gb = fmaf(fmaf(cs, yv[d], -A.rec[23 + d]) + (cs - 1.f) * A.hdr->oY[d], ghd, gb);
     gcs = fmaf(yv[d] + A.hdr->oY[d], gy, gcs);
-    A.gY[(size_t)d * A.M + j] = cs * gy;
+    A.gY[(size_t)d * A.M + j] += cs * gy;
   }
   A.gb[j] = gb;
   A.gcs[j] = gcs;
 }
 
-// Column pass k backward: from dL/db^{k+1}, dL/du^{k+1} and the direct dL/dcs^k,
-// dL/db^k, dL/du^k and g(c^k) = dL/dcs^k b^k. d(b/cs)/dcs = -b^{k+1}/cs: the
-// new scalings are used instead of b^k/cs^2, whose square overflows FP32 at low
-// temperature (K ~ e^(alpha/T)).
-__global__ void k_back_colpass(Vecs A, int k) {
+// Slice partials of a K or K^T product: the sum over slices, in order.
+__device__ __forceinline__ float slices_sum(const float* part, int S, int n, int i) {
+  float s = 0.f;
+  for (int k = 0; k < S; ++k) s += __ldcg(part + (size_t)k * n + i);
+  return s;
+}
+
+// Column pass k backward: from dL/db^{k+1} (+ the pending K^T g(r^{k+1}) slice
+// partials), dL/du^{k+1} and the direct dL/dcs^k: dL/db^k, dL/du^k and
+// g(c^k) = dL/dcs^k b^k. d(b/cs)/dcs = -b^{k+1}/cs: the new scalings are used
+// instead of b^k/cs^2, whose square overflows FP32 at low temperature
+// (K ~ e^(alpha/T)).
+__global__ void k_back_colpass(Vecs A, int k, const float* part, int S) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= A.M) return;
-  const size_t o = (size_t)k * A.M + j;
-  const float bk = A.b[o], cs = A.cs[o], c = A.c[o];
-  const float b1 = A.b[o + A.M], u1 = A.u[o + A.M];
-  const float gb1 = A.gb[j], gu1 = A.gu[j];
+  const float bk = b_at(A, k, j), cs = cs_at(A, k, j), c = c_at(A, k, j);
+  const float b1 = b_at(A, k + 1, j), u1 = u_at(A, k + 1, j);
+  float gb1 = A.gb[j];
+  if (part) gb1 += slices_sum(part, S, A.M, j);
+  const float gu1 = A.gu[j];
   const float gcs = A.gcs[j] - fmaf(gb1, b1, gu1 * u1) / cs;
-  A.gc[o] = gcs * bk;
+  A.gc[(size_t)k * A.M + j] = gcs * bk;
   A.gb[j] = fmaf(gcs, c, gb1 / cs);
   A.gu[j] = gu1 / cs + gcs;
   A.gcs[j] = 0.f;
 }
 
-// Row pass k backward: from dL/da^{k+1}, dL/ds^{k+1}: dL/da^k, dL/ds^k and
-// g(r^k) = dL/drs^k a^k (with a^{k+1}, s^{k+1} as in the column pass).
-__global__ void k_back_rowpass(Vecs A, int k) {
+// Row pass k backward: from dL/da^{k+1} (+ the pending K g(c^k) slice partials)
+// and dL/ds^{k+1}: dL/da^k, dL/ds^k and g(r^k) = dL/drs^k a^k.
+__global__ void k_back_rowpass(Vecs A, int k, const float* part, int S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.N) return;
-  const size_t o = (size_t)k * A.N + i;
-  const float ak = A.a[o], rs = A.rs[o], r = A.r[o];
-  const float a1 = A.a[o + A.N], s1 = A.s[o + A.N];
-  const float ga1 = A.ga[i], gs1 = A.gs[i];
+  const float ak = a_at(A, k, i), rs = rs_at(A, k, i), r = r_at(A, k, i);
+  const float a1 = a_at(A, k + 1, i), s1 = s_at(A, k + 1, i);
+  const float ga1 = A.ga[i] + slices_sum(part, S, A.N, i);
+  const float gs1 = A.gs[i];
   const float grs = -fmaf(ga1, a1, gs1 * s1) / rs;
-  A.gr[o] = grs * ak;
+  A.gr[(size_t)k * A.N + i] = grs * ak;
   A.ga[i] = fmaf(grs, r, ga1 / rs);
   A.gs[i] = gs1 / rs + grs;
 }
 
 // One block: dL/dR = sum gz y^T, dL/dt = sum gz (caller frame, y = y' + oY);
 // per column dL/dy += R^T gz; writes dL/d(R, t) of the input pose.
-__global__ void __launch_bounds__(1024) k_pose_grad(Vecs A, float* g_in) {
+__global__ void __launch_bounds__(1024) k_pose_grad(Vecs A) {
   __shared__ df red[12 * 32];
   float R[9];
-  for (int k = 0; k < 9; ++k) R[k] = A.pose[k];
+  for (int k = 0; k < 9; ++k) R[k] = A.rec[k];
   df v[12];
   for (int k = 0; k < 12; ++k) v[k] = df_make(0.f);
   for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
@@ -598,14 +536,9 @@ __global__ void __launch_bounds__(1024) k_pose_grad(Vecs A, float* g_in) {
   if (threadIdx.x == 0)
     for (int i = 0; i < 3; ++i) {
       const float gt = df_val(v[9 + i]);
-      g_in[9 + i] = gt;
-      for (int j = 0; j < 3; ++j) g_in[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
+      A.g_pose[9 + i] = gt;
+      for (int j = 0; j < 3; ++j) A.g_pose[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
     }
-}
-
-__global__ void k_add(float* d, const float* s, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) d[i] += s[i];
 }
 
 // ------------------------------------------------------------------ host side
@@ -650,8 +583,6 @@ Plan make_plan(int N, int M) {
 
 struct Layout {
   Vecs V;
-  float* wt4;   // [4][N]
-  float* gh;    // [4][M]
   float* part;
   size_t total;
 };
@@ -663,36 +594,21 @@ Layout carve(void* base, int N, int M, int I1, const Plan& P) {
   A.N = N;
   A.M = M;
   A.I1 = I1;
-  A.a = c.take<float>((size_t)(I1 + 1) * N);
-  A.s = c.take<float>((size_t)(I1 + 1) * N);
-  A.b = c.take<float>((size_t)(I1 + 1) * M);
-  A.u = c.take<float>((size_t)(I1 + 1) * M);
-  A.r = c.take<float>((size_t)I1 * N);
-  A.rs = c.take<float>((size_t)I1 * N);
-  A.c = c.take<float>((size_t)I1 * M);
-  A.cs = c.take<float>((size_t)I1 * M);
-  A.rho = c.take<float>(N);
-  A.w = c.take<float>(N);
-  A.V = c.take<float>(3 * (size_t)N);
+  A.ones = c.take<float>(M);
   A.h = c.take<float>(3 * (size_t)M);
   A.scal = c.take<double>(kScalN);
-  A.pose_out = c.take<float>(16);
   A.ga = c.take<float>(N);
-  A.gs = c.take<float>(N);
   A.gb = c.take<float>(M);
-  A.gu = c.take<float>(M);
   A.gcs = c.take<float>(M);
   A.gV = c.take<float>(3 * (size_t)N);
   A.gp = c.take<float>(3 * (size_t)N);
   A.gw = c.take<float>(N);
   A.grho = c.take<float>(N);
+  A.wt4 = c.take<float>(4 * (size_t)N);
+  A.gh = c.take<float>(4 * (size_t)M);
   A.gr = c.take<float>((size_t)I1 * N);
   A.gc = c.take<float>((size_t)I1 * M);
-  A.gX = c.take<float>(3 * (size_t)N);
   A.gZ = c.take<float>(3 * (size_t)M);
-  A.gY = c.take<float>(3 * (size_t)M);
-  L.wt4 = c.take<float>(4 * (size_t)N);
-  L.gh = c.take<float>(4 * (size_t)M);
   const size_t pr = (size_t)P.rows.S * 4 * N, pc = (size_t)P.cols.S * 4 * M;
   L.part = c.take<float>(std::max(pr, pc));
   L.total = c.off;
@@ -701,13 +617,20 @@ Layout carve(void* base, int N, int M, int I1, const Plan& P) {
 
 int blocks(int n) { return (n + kGlue - 1) / kGlue; }
 
-// out[m] (+)= K-products of NW weight vectors (rows: K w, w over columns;
-// columns: K^T w, w over rows).
+// Slice partials of NW K-products of weight vectors into part (rows: K w, w
+// over columns; columns: K^T w, w over rows).
+template <int NW>
+void sweep_partials(const SweepIO& io, float* part, const float* pose, float T, float alpha, const float* w, int ldw,
+                    cudaStream_t st) {
+  dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
+  k_sweep_sum<NW><<<g, kSwT, 0, st>>>(io, pose, T, alpha, w, ldw, part);
+}
+
+// out[m] (+)= the slice-ordered sums of a sweep's partials.
 template <int NW>
 void sum_sweep(const SweepIO& io, const Layout& L, const float* pose, float T, float alpha, const float* w, int ldw,
                float* out, int ldo, bool acc, cudaStream_t st) {
-  dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
-  k_sweep_sum<NW><<<g, kSwT, 0, st>>>(io, pose, T, alpha, w, ldw, L.part);
+  sweep_partials<NW>(io, L.part, pose, T, alpha, w, ldw, st);
   k_reduce_slices<<<dim3(blocks(io.n_own), NW), kGlue, 0, st>>>(L.part, io.S, NW, io.n_own, out, ldo, acc ? 1 : 0);
 }
 
@@ -739,57 +662,50 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
   A.X = J.X;
   A.Y = J.Y;
   A.hdr = J.hdr;
-  A.pose = J.pose;
+  A.rec = J.rec;
+  A.s0 = J.s0;
+  A.u0 = J.u0;
+  A.rows = J.rows;
+  A.cols = J.cols;
+  A.fin = J.fin;
+  A.g_pose = J.g_pose;
+  A.gs = J.g_s;
+  A.gu = J.g_u;
+  A.gX = J.gX;
+  A.gY = J.gY;
   const float T = J.T, al = J.alpha;
-  const float* pose = J.pose;
-  // ---- recompute of the iteration, recording every vector
-  k_fill<<<std::min(blocks(N), 1024), kGlue, 0, st>>>(A.a, N, 1.f);
-  k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(A.b, M, 1.f);
-  cudaError_t e = cudaMemcpyAsync(A.s, J.s, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(A.u, J.u, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
-  if (e != cudaSuccess) return (int)e;
-  for (int k = 0; k < I1; ++k) {
-    float* ak = A.a + (size_t)k * N;
-    float* sk = A.s + (size_t)k * N;
-    float* bk = A.b + (size_t)k * M;
-    float* uk = A.u + (size_t)k * M;
-    float* rk = A.r + (size_t)k * N;
-    float* ck = A.c + (size_t)k * M;
-    sum_sweep<1>(P.rows, L, pose, T, al, bk, M, rk, N, false, st);
-    k_pass_done<<<blocks(N), kGlue, 0, st>>>(ak, rk, sk, A.rs + (size_t)k * N, ak + N, sk + N, N);
-    sum_sweep<1>(P.cols, L, pose, T, al, ak + N, N, ck, M, false, st);
-    k_pass_done<<<blocks(M), kGlue, 0, st>>>(bk, ck, uk, A.cs + (size_t)k * M, bk + M, uk + M, M);
+  const float* pose = J.rec;  // the update's input pose (centred) leads its record
+  cudaError_t e = cudaSuccess;
+  if (J.first) {
+    k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(A.ones, M, 1.f);
+    e = cudaMemsetAsync(A.gs, 0, sizeof(float) * N, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.gu, 0, sizeof(float) * M, st);
+    if (e != cudaSuccess) return (int)e;
   }
-  const float* bF = A.b + (size_t)I1 * M;
-  sum_sweep<1>(P.rows, L, pose, T, al, bF, M, A.rho, N, false, st);
-  k_centres<<<1, 1024, 0, st>>>(A);
+  // ---- final stage and Horn
   k_h<<<blocks(M), kGlue, 0, st>>>(A);
-  sum_sweep<3>(P.rows, L, pose, T, al, A.h, M, A.V, N, false, st);
-  k_S_pose<<<1, 1024, 0, st>>>(A);
-  // ---- backward
-  k_horn_adjoint<<<1, 1, 0, st>>>(A, J.g_pose_out);
+  k_horn_adjoint<<<1, 1, 0, st>>>(A);
   k_back_S<<<1, 1024, 0, st>>>(A);
-  k_back_w<<<blocks(N), kGlue, 0, st>>>(A, L.wt4);
-  sum_sweep<4>(P.cols, L, pose, T, al, L.wt4, N, L.gh, M, false, st);
-  k_back_Yc<<<1, 1024, 0, st>>>(A, L.gh);
-  k_back_rho<<<blocks(N), kGlue, 0, st>>>(A);
-  k_back_final_cols<<<blocks(M), kGlue, 0, st>>>(A, L.gh);
-  if (J.g_s_out) e = cudaMemcpyAsync(A.gs, J.g_s_out, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
-  else e = cudaMemsetAsync(A.gs, 0, sizeof(float) * N, st);
-  if (e == cudaSuccess) {
-    if (J.g_u_out) e = cudaMemcpyAsync(A.gu, J.g_u_out, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
-    else e = cudaMemsetAsync(A.gu, 0, sizeof(float) * M, st);
-  }
-  if (e != cudaSuccess) return (int)e;
+  k_back_w<<<blocks(N), kGlue, 0, st>>>(A);
+  sum_sweep<4>(P.cols, L, pose, T, al, A.wt4, N, A.gh, M, false, st);
+  k_back_Yc<<<1, 1024, 0, st>>>(A);
+  k_back_final<<<blocks(N + M), kGlue, 0, st>>>(A);
+  // ---- the column and row passes in reverse; each K / K^T product's slice
+  // partials are summed by the kernel that consumes them
+  const float* pending = nullptr;
   for (int k = I1 - 1; k >= 0; --k) {
-    k_back_colpass<<<blocks(M), kGlue, 0, st>>>(A, k);
+    k_back_colpass<<<blocks(M), kGlue, 0, st>>>(A, k, pending, P.cols.S);
     // dL/da^{k+1} += K g(c^k)
-    sum_sweep<1>(P.rows, L, pose, T, al, A.gc + (size_t)k * M, M, A.ga, N, true, st);
-    k_back_rowpass<<<blocks(N), kGlue, 0, st>>>(A, k);
+    sweep_partials<1>(P.rows, L.part, pose, T, al, A.gc + (size_t)k * M, M, st);
+    k_back_rowpass<<<blocks(N), kGlue, 0, st>>>(A, k, L.part, P.rows.S);
     // dL/db^k += K^T g(r^k); b^0 = 1 is a constant
-    if (k >= 1) sum_sweep<1>(P.cols, L, pose, T, al, A.gr + (size_t)k * N, N, A.gb, M, true, st);
+    pending = nullptr;
+    if (k >= 1) {
+      sweep_partials<1>(P.cols, L.part, pose, T, al, A.gr + (size_t)k * N, N, st);
+      pending = L.part;
+    }
   }
-  // rank-1 terms of dL/dK (rows: alpha, columns: beta)
+  // ---- rank-1 terms of dL/dK (rows: alpha, columns: beta)
   const int nterms = 4 + 2 * I1;
   const float* ta[64];
   const float* tb[64];
@@ -798,12 +714,12 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
     tb[d] = A.h + (size_t)d * M;
   }
   ta[3] = A.grho;
-  tb[3] = bF;
+  tb[3] = J.cols + (size_t)(I1 - 1) * 4 * M;  // b^{I1}
   for (int k = 0; k < I1; ++k) {
-    ta[4 + k] = A.a + (size_t)(k + 1) * N;
+    ta[4 + k] = J.rows + (size_t)k * 4 * N;  // a^{k+1}
     tb[4 + k] = A.gc + (size_t)k * M;
     ta[4 + I1 + k] = A.gr + (size_t)k * N;
-    tb[4 + I1 + k] = A.b + (size_t)k * M;
+    tb[4 + I1 + k] = k == 0 ? A.ones : J.cols + (size_t)(k - 1) * 4 * M;  // b^k
   }
   for (int t0 = 0; t0 < nterms; t0 += kMaxTerms) {
     Terms tr{}, tcol{};
@@ -817,15 +733,8 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
     grad_sweep(P.rows, L, pose, T, al, tr, A.gX, true, st);
     grad_sweep(P.cols, L, pose, T, al, tcol, A.gZ, t0 > 0, st);
   }
-  k_pose_grad<<<1, 1024, 0, st>>>(A, J.g_pose_in);
-  k_add<<<blocks(3 * N), kGlue, 0, st>>>(J.gX, A.gX, 3 * N);
-  k_add<<<blocks(3 * M), kGlue, 0, st>>>(J.gY, A.gY, 3 * M);
-  e = cudaMemcpyAsync(J.g_s_in, A.gs, sizeof(float) * N, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(J.g_u_in, A.gu, sizeof(float) * M, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess && J.pose_out)
-    e = cudaMemcpyAsync(J.pose_out, A.pose_out, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess) e = cudaGetLastError();
-  return (int)e;
+  k_pose_grad<<<1, 1024, 0, st>>>(A);
+  return (int)cudaGetLastError();
 }
 
 }  // namespace cesa
