@@ -2,7 +2,7 @@
 """Benchmark of the soft-correspondence registration path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000|
+                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000|icp_40097|
                                 c4_batch_256]
 
 One step is one complete registration (the whole annealing schedule) of the
@@ -82,6 +82,7 @@ class RefDefaults:
     JMAX, I0, I1, alpha, T_0, TFACTOR = 100, 5, 3, 3.0, 100.0, 0.95
     moutlier = float(np.float32(np.exp(np.float32(-1.0)) / np.sqrt(np.float32(100.0))))
     sigma_p2, sigma_inf, sigma_factor, d_02 = 0.01, 1e-5, 0.9, 0.01
+    maxIteration = 30
 
 
 FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2}
@@ -100,6 +101,8 @@ def materialised_bytes(N, M, p):
 def pose_updates(kind, p):
     if kind == "softassign":
         return p.JMAX * p.I0
+    if kind == "icp":
+        return p.maxIteration
     n, s = 0, np.float32(p.sigma_p2)
     while s > np.float32(p.sigma_inf):
         n += 1
@@ -112,6 +115,8 @@ def algorithmic_work(kind, N, M, p):
 
     EM-ICP: per element 12 FP32-pipe ops + 1 ex2 (3 FADD, FMUL + 2 FFMA for
     d^2, FMUL scale, FFMA + FADD + 3 FFMA accumulators).
+    ICP: per element and iteration 6 FP32-pipe ops (the squared distance) and a
+    compare-select of (distance, index) on the ALU pipe, no ex2.
     Softassign: per pose update 2*I1 Sinkhorn sweeps of 8 FP32 ops + 1 ex2
     (3 FADD, FMUL + 2 FFMA, FFMA exponent, FFMA weighted sum) and one final
     sweep of 12 FP32 ops + 1 ex2 (the same with 5 weighted sums).
@@ -120,13 +125,15 @@ def algorithmic_work(kind, N, M, p):
     e = float(N) * float(M)
     if kind == "emicp":
         return 12.0 * e * n, e * n, e * n
+    if kind == "icp":  # 3 FADD, FMUL + 2 FFMA per element; the compare-select runs on the ALU pipe
+        return 6.0 * e * n, 0.0, e * n
     sweeps = 2 * p.I1
     return e * n * (8.0 * sweeps + 12.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
 
 
 def kernels_per_registration(kind):
     # prep_center + 2 x prep_pack (+ 2 x fill for the slack vectors) + the persistent kernel
-    return 4 if kind == "emicp" else 6
+    return 6 if kind == "softassign" else 4
 
 
 class ClockSampler:
@@ -204,6 +211,14 @@ def cpu_baseline(kind, X, Y, p, target_s, threads=None):
         O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=float(sig), sigma_factor=p.sigma_factor,
                 d_02=p.d_02, precision="f32", trace=False)
         dt = time.perf_counter() - t0
+    elif kind == "icp":
+        t0 = time.perf_counter()
+        O.icp(X, Y, maxIteration=1, precision="f32", trace=False)
+        one = time.perf_counter() - t0
+        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
+        t0 = time.perf_counter()
+        O.icp(X, Y, maxIteration=k, precision="f32", trace=False)
+        dt = time.perf_counter() - t0
     else:
         t0 = time.perf_counter()
         O.softassign(X, Y, JMAX=1, I0=1, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
@@ -218,6 +233,8 @@ def cpu_baseline(kind, X, Y, p, target_s, threads=None):
     regs_per_s = 1.0 / (per_update * n_full)
     desc = ("first %d of %d pose updates of one registration (FP32 port of the reference algorithm, "
             "OpenMP), scaled to a full registration" % (k, n_full))
+    if kind == "icp":
+        desc += "; ICP's port searches exhaustively (the reference's FLANN kd-tree is not available)"
     return regs_per_s, desc, threads
 
 
@@ -268,6 +285,8 @@ def config_of(args, kind, X, Y, p):
          "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
     if kind == "softassign":
         c.update(JMAX=p.JMAX, I0=p.I0, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR)
+    elif kind == "icp":
+        c.update(maxIteration=p.maxIteration, search="exhaustive nearest neighbour")
     else:
         c.update(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_inf, sigma_factor=p.sigma_factor, d_02=p.d_02)
     return c
@@ -557,8 +576,7 @@ def run_ours(args, rank, world, local):
         f, ms_free, ms_mat = cesa.tune_sinkhorn(N, M, p)  # records the choice used by "auto"
         tuned = {"chosen": "materialised" if f == 2 else "matrix_free",
                  "ms_per_update_matrix_free": ms_free, "ms_per_update_materialised": ms_mat}
-    dev_call = cesa.emicp_device if kind == "emicp" else cesa.softassign_device
-    host_call = cesa.emicp if kind == "emicp" else cesa.softassign
+    dev_call = {"emicp": cesa.emicp_device, "softassign": cesa.softassign_device, "icp": cesa.icp_device}[kind]
 
     dX = torch.from_numpy(cesa.cloud2data(X)).cuda()
     dY = torch.from_numpy(cesa.cloud2data(Y)).cuda()
@@ -609,7 +627,7 @@ def run_ours(args, rank, world, local):
     lib = cesa.lib()
     Rh = np.eye(3, dtype=np.float32).reshape(-1).copy()
     th = np.zeros(3, np.float32)
-    fn = lib.cesa_emicp if kind == "emicp" else lib.cesa_softassign
+    fn = {"emicp": lib.cesa_emicp, "softassign": lib.cesa_softassign, "icp": lib.cesa_icp}[kind]
     ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
     for _ in range(max(1, args.warmup)):
         Rh[:] = np.eye(3, dtype=np.float32).reshape(-1)
@@ -695,7 +713,10 @@ def run_ours(args, rank, world, local):
     if kind == "softassign":
         line["config"]["sinkhorn_form"] = form_used
         line["config"]["sinkhorn_tuner"] = tuned
-    if not args.no_adjoint:
+    if kind == "icp":
+        roofline["note"] += ("; ICP: 6 FP32-pipe ops per element (squared distance) counted, the "
+                             "compare-select of (distance, index) runs on the ALU pipe")
+    if not args.no_adjoint and kind != "icp":
         line["adjoint"] = measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0)
     print(json.dumps(line), flush=True)
 

@@ -111,10 +111,12 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.cesa_params_default.argtypes = [_p]
         L.cesa_params_default.restype = None
-        for name in ("cesa_emicp", "cesa_softassign"):
+        for name in ("cesa_emicp", "cesa_softassign", "cesa_icp"):
             fn = getattr(L, name)
             fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
             fn.restype = _i
+        L.cesa_icp_device.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p, _p]
+        L.cesa_icp_device.restype = _i
         for name in ("cesa_emicp_device", "cesa_softassign_device"):
             fn = getattr(L, name)
             fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
@@ -271,6 +273,24 @@ def _stream_handle(stream):
 
 def _dptr(t):
     return ctypes.c_void_p(t.data_ptr())
+
+
+def icp(X, Y, R=None, t=None, param=None, trace=False):
+    """ICP on the GPU, maxIteration iterations of exhaustive nearest-neighbour
+    matching and Horn's pose (replaces icp(), src/icp.cpp:122-290, whose FLANN
+    search is approximate). Returns (R, t), or (R, t, trace, report)."""
+    return _host_call("cesa_icp", X, Y, R, t, param or Params.default(), trace)
+
+
+def icp_device(dX, dY, dRt, param=None, d_nn=None, d_status=None, stream=None):
+    """Enqueue ICP on device SoA tensors; dRt (12 floats) is in/out; d_nn
+    (optional int32 tensor of M) receives the last iteration's matches."""
+    p = param or Params.default()
+    rc = lib().cesa_icp_device(_dptr(dX), dX.numel() // 3, _dptr(dY), dY.numel() // 3, _dptr(dRt), ctypes.byref(p),
+                               _dptr(d_nn) if d_nn is not None else None,
+                               _dptr(d_status) if d_status is not None else None,
+                               ctypes.c_void_p(_stream_handle(stream)))
+    _check(rc, "icp_device")
 
 
 def emicp_device(dX, dY, dRt, param=None, d_status=None, stream=None):

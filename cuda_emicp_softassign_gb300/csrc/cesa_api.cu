@@ -110,6 +110,12 @@ int check_sa_params(const cesa_params* p) {
   return CESA_OK;
 }
 
+int check_icp_params(const cesa_params* p) {
+  if (!p) return CESA_ERR_INVALID_ARGUMENT;
+  if (p->maxIteration < 0 || p->maxIteration > 100000000) return CESA_ERR_INVALID_ARGUMENT;
+  return CESA_OK;
+}
+
 int select_device(const cesa_params* p, int* dev) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return CESA_ERR_NO_DEVICE;
@@ -173,10 +179,11 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   int rc = check_points(X, N, Y, M);
   if (rc) return rc;
   if (!R || !t) return CESA_ERR_INVALID_ARGUMENT;
-  rc = kind == 1 ? check_emicp_params(p) : check_sa_params(p);
+  rc = kind == 1 ? check_emicp_params(p) : kind == 2 ? check_sa_params(p) : check_icp_params(p);
   if (rc) return rc;
-  long nsteps = kind == 1 ? emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor)
-                          : (long)p->JMAX * (long)p->I0;
+  long nsteps = kind == 1   ? emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor)
+                : kind == 2 ? (long)p->JMAX * (long)p->I0
+                            : (long)p->maxIteration;
   if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
   int dev = 0;
   rc = select_device(p, &dev);
@@ -191,8 +198,10 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   float* dX = static_cast<float*>(C.io.p);
   float* dY = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx);
   float* dRt = reinterpret_cast<float*>(static_cast<char*>(C.io.p) + bx + by);
-  const int form = kind == 1 ? 0 : resolve_form(p->sinkhorn_form, N, M, dev);
-  const size_t need = kind == 1 ? emicp_ws_need(N, M, dev) : softassign_ws_need(N, M, form, dev);
+  const int form = kind == 2 ? resolve_form(p->sinkhorn_form, N, M, dev) : 0;
+  const size_t need = kind == 1   ? emicp_ws_need(N, M, dev)
+                      : kind == 2 ? softassign_ws_need(N, M, form, dev)
+                                  : icp_ws_need(N, M, dev);
   e = C.ws.ensure(need);
   if (e != cudaSuccess) return map_cuda(e);
   const int cap = (rep && rep->trace && rep->trace_capacity > 0) ? rep->trace_capacity : 0;
@@ -240,6 +249,18 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
       L.timeline_cap = tl_cap;
       L.timeout_ns = timeout_ns_of(p);
       kerr = enqueue_emicp(L, C.ws.p, C.ws.bytes, st, &grid);
+    } else if (kind == 3) {
+      IcpLaunch L{};
+      L.dX = dX;
+      L.dY = dY;
+      L.N = N;
+      L.M = M;
+      L.iters = (int)nsteps;
+      L.dRt = dRt;
+      L.trace = dtrace;
+      L.trace_cap = cap;
+      L.timeout_ns = timeout_ns_of(p);
+      kerr = enqueue_icp(L, C.ws.p, C.ws.bytes, st, &grid);
     } else {
       SoftassignLaunch L{};
       L.dX = dX;
@@ -389,6 +410,40 @@ int cesa_emicp(const float* X, int N, const float* Y, int M, float R[9], float t
 int cesa_softassign(const float* X, int N, const float* Y, int M, float R[9], float t[3],
                     const cesa_params* p, cesa_report* rep) {
   return run_host(2, X, N, Y, M, R, t, p, rep);
+}
+
+int cesa_icp(const float* X, int N, const float* Y, int M, float R[9], float t[3], const cesa_params* p,
+             cesa_report* rep) {
+  return run_host(3, X, N, Y, M, R, t, p, rep);
+}
+
+int cesa_icp_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
+                    int* d_nn, int* d_status, cesa_stream_t stream) {
+  int rc = check_points(dX, N, dY, M);
+  if (rc) return rc;
+  if (!dRt) return CESA_ERR_INVALID_ARGUMENT;
+  rc = check_icp_params(p);
+  if (rc) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_mu);
+  StreamCtx& C = ctx_for(dev, st);
+  cudaError_t e = C.ws.ensure(icp_ws_need(N, M, dev));
+  if (e != cudaSuccess) return map_cuda(e);
+  IcpLaunch L{};
+  L.dX = dX;
+  L.dY = dY;
+  L.N = N;
+  L.M = M;
+  L.iters = p->maxIteration;
+  L.dRt = dRt;
+  L.nn_out = d_nn;
+  L.d_status = d_status;
+  L.timeout_ns = timeout_ns_of(p);
+  C.last_kind = 3;
+  C.last_trace_steps = 0;
+  return map_cuda((cudaError_t)enqueue_icp(L, C.ws.p, C.ws.bytes, st, nullptr));
 }
 
 int cesa_emicp_device(const float* dX, int N, const float* dY, int M, float* dRt,

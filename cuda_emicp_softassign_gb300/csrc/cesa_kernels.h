@@ -175,6 +175,21 @@ struct SoftassignStepAdjoint {
 size_t softassign_step_adjoint_ws_need(int N, int M, int I1);
 int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st);
 
+// ICP (exhaustive nearest neighbours): maxIteration iterations in one launch.
+struct IcpLaunch {
+  const float* dX;  // SoA, N (searched)
+  const float* dY;  // SoA, M (moved)
+  int N, M, iters;
+  float* dRt;       // PoseIO in/out (device)
+  int* nn_out;      // optional [M]: the last iteration's matches
+  double* trace;
+  int trace_cap;
+  int* d_status;
+  uint64_t timeout_ns;
+};
+size_t icp_ws_need(int N, int M, int device);
+int enqueue_icp(const IcpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
+
 // Control-block status of the last launch that used workspace ws.
 int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_written = nullptr);
 

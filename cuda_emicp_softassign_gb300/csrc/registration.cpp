@@ -1,4 +1,4 @@
-// C++ drop-in layer: emicp(), softassign(), findRTfromS() and cloud2data()
+// C++ drop-in layer: emicp(), softassign(), icp(), findRTfromS() and cloud2data()
 // with the reference's signatures (src/3dregistration.h:82-116), implemented
 // over the C ABI of libcesa.so. Compile this file into the program (as the
 // reference README asks for emicp.cu / softassign.cu) and link -lcesa.
@@ -60,6 +60,12 @@ void emicp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
            const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float* h_R, float* h_t,
            const registrationParameters& param) {
   run("emicp", cesa_emicp, cloud_target, cloud_source, h_R, h_t, param);
+}
+
+void icp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
+         const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float* h_R, float* h_t,
+         const registrationParameters& param) {
+  run("icp", cesa_icp, cloud_target, cloud_source, h_R, h_t, param);
 }
 
 void softassign(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,

@@ -115,6 +115,8 @@ CONFIGS = {
     "c2_softassign_2000": dict(kind="softassign", gen="surface", n=2000),
     "c3_emicp_40097": dict(kind="emicp", gen="surface", n=40097, max_deg=20.0, outlier_frac=0.05),
     "c5_softassign_20000": dict(kind="softassign", gen="surface", n=20000),
+    # ICP on config 3's clouds (no benchmark config of the reference names ICP)
+    "icp_40097": dict(kind="icp", gen="surface", n=40097, max_deg=20.0, outlier_frac=0.05),
 }
 
 

@@ -1,7 +1,7 @@
 /*
  * Drop-in replacement for the reference's public header
  * (src/3dregistration.h): the same registrationParameters fields, in the same
- * order, and the same entry points emicp(), softassign(), findRTfromS() and
+ * order, and the same entry points emicp(), softassign(), icp(), findRTfromS() and
  * cloud2data(). Their implementation (registration.cpp in the package's csrc/
  * directory) runs the GB300 kernels of libcesa.so through the C ABI in cesa.h.
  *
@@ -77,6 +77,10 @@ void softassign(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
 void emicp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
            const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float *h_R, float *h_t,
            const registrationParameters &param);
+
+void icp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
+         const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float *h_R, float *h_t,
+         const registrationParameters &param);
 
 void findRTfromS(const float *h_Xc, const float *h_Yc, const float *h_S, float *h_R, float *h_t);
 

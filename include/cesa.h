@@ -1,6 +1,7 @@
 /*
  * cesa.h -- C ABI of the GB300-native soft-correspondence registration library
- * (libcesa.so): annealed EM-ICP and Softassign rigid registration on one GPU.
+ * (libcesa.so): annealed EM-ICP and Softassign (and plain ICP) rigid
+ * registration on one GPU.
  *
  * Every entry point takes plain pointers and sizes. Point sets are SoA float
  * arrays [x0..xn-1, y0..yn-1, z0..zn-1], the layout the reference builds with
@@ -61,8 +62,8 @@ typedef struct cesa_params {
   float sigma_inf;    /* stop value of sigma_p2 */
   float sigma_factor; /* factor for sigma_p2 */
   float d_02;         /* outlier distance^2 */
-  /* ICP (kept for layout parity; not used by these entry points) */
-  int maxIteration;
+  /* ICP */
+  int maxIteration;   /* iterations of cesa_icp (no convergence test, as the reference) */
   /* GPU path controls */
   int sinkhorn_form; /* CESA_SINKHORN_* */
   int timeout_ms;    /* limit of any device-side wait; 0 selects 10000 ms */
@@ -193,6 +194,20 @@ int cesa_emicp_device_noalloc(const float* dX, int N, const float* dY, int M, fl
 
 /* Status of the last registration enqueued on `stream` (synchronises it). */
 int cesa_stream_status(cesa_stream_t stream);
+
+/*
+ * ICP: maxIteration iterations of nearest-neighbour matching of the moved
+ * source Y to the target X, then Horn's pose (replaces icp(),
+ * src/icp.cpp:122-290, declared at src/3dregistration.h:96-99). The
+ * reference's FLANN kd-tree search is approximate; this one is exhaustive
+ * (exact nearest neighbour; the first of equal distances in X order). Same
+ * argument conventions as cesa_emicp; the device variant optionally writes
+ * the last iteration's matches (d_nn: M ints, may be NULL).
+ */
+int cesa_icp(const float* X, int N, const float* Y, int M, float R[9], float t[3], const cesa_params* p,
+             cesa_report* report);
+int cesa_icp_device(const float* dX, int N, const float* dY, int M, float* dRt, const cesa_params* p,
+                    int* d_nn, int* d_status, cesa_stream_t stream);
 
 /*
  * One EM-ICP sigma step (E-step + weighted moments) from pose (R, t): the

@@ -55,6 +55,9 @@ def lib():
             fn = getattr(L, "oracle_softassign_step" + sfx)
             fn.restype = ctypes.c_double
             fn.argtypes = [_p, _i, _p, _i, _p, _p, _f, _f, _i, _p, _p, _p, _p, _p, _p, _p, _p]
+            fn = getattr(L, "oracle_icp" + sfx)
+            fn.restype = _i
+            fn.argtypes = [_p, _i, _p, _i, _p, _p, _i, _p, _p, _i]
         L.oracle_set_threads.argtypes = [_i]
         L.oracle_max_threads.restype = _i
     return _lib
@@ -188,6 +191,23 @@ def softassign_step(X, Y, R, t, T, alpha, I1, s, u, precision="f64"):
                                                        alpha, I1, _ptr(s), _ptr(u), _ptr(rs), _ptr(cs),
                                                        _ptr(w), _ptr(Xc), _ptr(Yc), _ptr(S))
     return dict(s=s, u=u, rs=rs, cs=cs, w=w, Xc=Xc, Yc=Yc, S=S, sum=sm)
+
+
+def icp(X, Y, R0=None, t0=None, maxIteration=30, precision="f64", trace=True):
+    """ICP with exhaustive nearest neighbours (src/icp.cpp:122-290; the
+    reference's FLANN search is approximate). Returns (R, t, trace, nn) with
+    nn the matches of the last iteration."""
+    dt, sfx = _dt(precision)
+    Xs, Ys = soa(X), soa(Y)
+    R = np.ascontiguousarray(np.eye(3) if R0 is None else R0, dtype=dt).reshape(-1).copy()
+    t = np.ascontiguousarray(np.zeros(3) if t0 is None else t0, dtype=dt).reshape(-1).copy()
+    tr = np.zeros((max(maxIteration, 1) if trace else 0, TRACE_STRIDE))
+    nn = np.zeros(len(Y), np.int32)
+    n = getattr(lib(), "oracle_icp" + sfx)(_ptr(Xs), len(X), _ptr(Ys), len(Y), _ptr(R), _ptr(t), maxIteration,
+                                          _ptr(nn), _ptr(tr) if trace else None, tr.shape[0])
+    if n < 0:
+        raise ValueError("oracle_icp: invalid arguments")
+    return R.reshape(3, 3).astype(np.float64), t.astype(np.float64), tr[: min(n, tr.shape[0])], nn
 
 
 def ref_emicp_cpu(X, Y, R0=None, t0=None, sigma_p2=0.01, sigma_inf=1e-5, sigma_factor=0.9, d_02=0.01):

@@ -377,6 +377,88 @@ double FN(oracle_softassign_step)(const float* X, int N, const float* Y, int M, 
   return r;
 }
 
+/*
+ * ICP, src/icp.cpp:122-290: Yc = mean(Y) once; per iteration every y is moved
+ * by the current pose and matched to its nearest X point; Xc = mean of the
+ * matches, S = sum (x_nn - Xc)(y - Yc)^T (h_S layout, src/icp.cpp:251-262),
+ * pose = findRTfromS(Xc, Yc, S); maxIteration iterations, no convergence test.
+ * The reference searches with FLANN's randomised kd-trees and default search
+ * checks (src/icp.cpp:170-175,211-216), which is approximate; this
+ * restatement searches exhaustively and keeps the first of equal distances
+ * (lowest X index). nn_out (optional, M): the matches of the last iteration.
+ * Trace [2] holds the sum of squared match distances of the iteration.
+ */
+int FN(oracle_icp)(const float* X, int N, const float* Y, int M, REAL R[9], REAL t[3], int maxIteration,
+                   int* nn_out, double* trace, int trace_cap) {
+  if (N <= 0 || M <= 0 || maxIteration < 0) return -1;
+  const float* Xx = X;
+  const float* Xy = X + N;
+  const float* Xz = X + 2 * N;
+  const float* Yx = Y;
+  const float* Yy = Y + M;
+  const float* Yz = Y + 2 * M;
+  int* nn = (int*)malloc(sizeof(int) * (size_t)M);
+  REAL* d2min = (REAL*)malloc(sizeof(REAL) * (size_t)M);
+  if (!nn || !d2min) {
+    free(nn);
+    free(d2min);
+    return -2;
+  }
+  /* findCenter(Y), src/icp.cpp:88-100 */
+  REAL Yc[3] = {0, 0, 0};
+  for (int i = 0; i < M; ++i) {
+    Yc[0] += Yx[i];
+    Yc[1] += Yy[i];
+    Yc[2] += Yz[i];
+  }
+  for (int k = 0; k < 3; ++k) Yc[k] /= (REAL)M;
+  double q_prev[4] = {1, 0, 0, 0};
+  for (int iter = 0; iter < maxIteration; ++iter) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < M; ++i) {
+      const REAL zx = R[0] * Yx[i] + R[1] * Yy[i] + R[2] * Yz[i] + t[0];
+      const REAL zy = R[3] * Yx[i] + R[4] * Yy[i] + R[5] * Yz[i] + t[1];
+      const REAL zz = R[6] * Yx[i] + R[7] * Yy[i] + R[8] * Yz[i] + t[2];
+      REAL best = 0;
+      int bi = -1;
+      for (int c = 0; c < N; ++c) {
+        const REAL dx = (REAL)Xx[c] - zx, dy = (REAL)Xy[c] - zy, dz = (REAL)Xz[c] - zz;
+        const REAL d2 = dx * dx + dy * dy + dz * dz;
+        if (bi < 0 || d2 < best) {
+          best = d2;
+          bi = c;
+        }
+      }
+      nn[i] = bi;
+      d2min[i] = best;
+    }
+    REAL Xc[3] = {0, 0, 0}, S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double cost = 0;
+    for (int i = 0; i < M; ++i) {
+      Xc[0] += Xx[nn[i]];
+      Xc[1] += Xy[nn[i]];
+      Xc[2] += Xz[nn[i]];
+      cost += (double)d2min[i];
+    }
+    for (int k = 0; k < 3; ++k) Xc[k] /= (REAL)M;
+    for (int i = 0; i < M; ++i) {
+      const REAL xw[3] = {Xx[nn[i]] - Xc[0], Xy[nn[i]] - Xc[1], Xz[nn[i]] - Xc[2]};
+      const REAL yw[3] = {Yx[i] - Yc[0], Yy[i] - Yc[1], Yz[i] - Yc[2]};
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) S[k + 3 * j] += xw[k] * yw[j];
+    }
+    double gap = 0, lmax = 0;
+    FN(pose_update)(Xc, Yc, S, R, t, q_prev, &gap, &lmax);
+    if (trace && iter < trace_cap)
+      FN(trace_put)(trace + (size_t)ORACLE_TRACE_STRIDE * iter, iter, (double)iter, cost, Xc, Yc, S, R, t, gap,
+                    lmax);
+  }
+  if (nn_out) memcpy(nn_out, nn, sizeof(int) * (size_t)M);
+  free(nn);
+  free(d2min);
+  return maxIteration;
+}
+
 #undef FN
 #undef CAT
 #undef CAT_

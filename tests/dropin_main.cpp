@@ -1,5 +1,5 @@
 // A user program written against the reference API (src/3dregistration.h):
-// reads SoA clouds from argv files, runs emicp() or softassign() with the
+// reads SoA clouds from argv files, runs emicp(), softassign() or icp() with the
 // reference defaults, prints R (row-major) and t.
 #include <cmath>
 #include <cstdio>
@@ -35,6 +35,8 @@ int main(int argc, char** argv) {
   pcl::PointCloud<pcl::PointXYZ>::Ptr X = load(argv[2]), Y = load(argv[3]);
   if (std::strcmp(argv[1], "emicp") == 0)
     emicp(X, Y, h_R, h_t, param);
+  else if (std::strcmp(argv[1], "icp") == 0)
+    icp(X, Y, h_R, h_t, param);
   else
     softassign(X, Y, h_R, h_t, param);
   // cloud2data and findRTfromS are part of the same API

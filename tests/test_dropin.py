@@ -61,3 +61,13 @@ def test_dropin_emicp_and_softassign_match_oracle(dropin_exe, oracle):
     R, t, ok, err = _run(dropin_exe, "softassign", X, Y)
     Ro, to, _ = oracle.softassign(X, Y)
     assert rot_err_deg(R, Ro) < 1e-3
+
+
+@pytest.mark.gpu
+def test_dropin_icp_matches_oracle(dropin_exe, oracle):
+    from cuda_emicp_softassign_gb300 import workloads as W
+    X, Y, _, _ = W.uniform_pair(n=800, seed=33, max_deg=15.0, t_range=0.05)
+    R, t, ok, err = _run(dropin_exe, "icp", X, Y)
+    Ro, to, _, _ = oracle.icp(X, Y)
+    assert ok == 1 and err == ""
+    assert rot_err_deg(R, Ro) < 1e-3 and np.abs(t - to).max() < 1e-5
