@@ -117,6 +117,19 @@ def lib():
             fn.restype = _i
         L.cesa_icp_device.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p, _p]
         L.cesa_icp_device.restype = _i
+        L.cesa_load_points.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
+                                       ctypes.POINTER(_i)]
+        L.cesa_load_points.restype = _i
+        L.cesa_free.argtypes = [_p]
+        L.cesa_free.restype = None
+        L.cesa_points_reduction.argtypes = [_p, ctypes.POINTER(_i), ctypes.c_float, ctypes.c_ulonglong]
+        L.cesa_points_reduction.restype = _i
+        L.cesa_align_scale_once.argtypes = [_p, _i, _p, _i]
+        L.cesa_align_scale_once.restype = _i
+        L.cesa_save_rt.argtypes = [ctypes.c_char_p, _p, _p]
+        L.cesa_save_rt.restype = _i
+        L.cesa_load_rt.argtypes = [ctypes.c_char_p, _p, _p]
+        L.cesa_load_rt.restype = _i
         for name in ("cesa_emicp_device", "cesa_softassign_device"):
             fn = getattr(L, name)
             fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
@@ -291,6 +304,49 @@ def icp_device(dX, dY, dRt, param=None, d_nn=None, d_status=None, stream=None):
                                _dptr(d_status) if d_status is not None else None,
                                ctypes.c_void_p(_stream_handle(stream)))
     _check(rc, "icp_device")
+
+
+def load_points(path):
+    """Points of a PLY (ASCII / binary) or text file as an (n, 3) float32
+    array, non-finite points dropped (the reference CLI's loadFile)."""
+    L = lib()
+    buf = ctypes.POINTER(ctypes.c_float)()
+    n = _i(0)
+    _check(L.cesa_load_points(os.fsencode(path), ctypes.byref(buf), ctypes.byref(n)), "load_points")
+    try:
+        out = np.ctypeslib.as_array(buf, shape=(n.value * 3,)).reshape(-1, 3).copy() if n.value else \
+            np.zeros((0, 3), np.float32)
+    finally:
+        L.cesa_free(ctypes.cast(buf, _p))
+    return out
+
+
+def points_reduction(P, percent, seed=0):
+    """Keeps each point with probability percent / 100, in order (seeded)."""
+    a = np.ascontiguousarray(P, dtype=np.float32).copy()
+    n = _i(len(a))
+    _check(lib().cesa_points_reduction(_ptr(a), ctypes.byref(n), float(percent), int(seed)), "points_reduction")
+    return a[: n.value]
+
+
+def align_scale_once(X, Y):
+    """Both clouds scaled about the origin to a covariance trace of 0.003."""
+    a = np.ascontiguousarray(X, dtype=np.float32).copy()
+    b = np.ascontiguousarray(Y, dtype=np.float32).copy()
+    _check(lib().cesa_align_scale_once(_ptr(a), len(a), _ptr(b), len(b)), "align_scale_once")
+    return a, b
+
+
+def save_rt(path, R, t):
+    Rh, th = _pose_in(R, t)
+    _check(lib().cesa_save_rt(os.fsencode(path), _ptr(Rh), _ptr(th)), "save_rt")
+
+
+def load_rt(path):
+    Rh = np.zeros(9, np.float32)
+    th = np.zeros(3, np.float32)
+    _check(lib().cesa_load_rt(os.fsencode(path), _ptr(Rh), _ptr(th)), "load_rt")
+    return Rh.reshape(3, 3).astype(np.float64), th.astype(np.float64)
 
 
 def emicp_device(dX, dY, dRt, param=None, d_status=None, stream=None):

@@ -18,13 +18,14 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcesa.so")
 PEAKS_LIB = os.path.join(HERE, "libcesa_peaks.so")
+CLI = os.path.join(HERE, "cesa_register")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 SOURCES = ["cesa_api.cu", "cesa_emicp.cu", "cesa_softassign.cu", "cesa_noalloc.cu", "cesa_selftest.cu",
            "cesa_batch.cu", "cesa_softassign_mat.cu", "cesa_emicp_adjoint.cu",
-           "cesa_softassign_adjoint.cu", "cesa_icp.cu"]
+           "cesa_softassign_adjoint.cu", "cesa_icp.cu", "cesa_io.cpp"]
 HEADERS = ["cesa_common.cuh", "cesa_sweep.cuh", "cesa_pose.h", "cesa_kernels.h", "cesa_prep.cuh", "cesa_ops.cuh"]
 
 
@@ -87,6 +88,22 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def build_cli(force=False):
+    """Compiles the cesa_register command line (host C++ over libcesa.so)."""
+    lib = build()
+    src = os.path.join(CSRC, "cesa_cli.cpp")
+    if not force and _mtime(CLI) >= max(_mtime(src), _mtime(lib), _mtime(os.path.join(INCLUDE, "cesa.h"))):
+        return CLI
+    tmp = CLI + ".tmp"
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-I", INCLUDE, src, "-L", HERE, "-lcesa", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for cesa_cli.cpp:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build_peaks(force=False):
     """Compiles libcesa_peaks.so (FP32 / MUFU throughput probes for bench.py)."""
     os.makedirs(BUILD, exist_ok=True)
@@ -104,4 +121,5 @@ def build_peaks(force=False):
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_cli(force="--force" in sys.argv))
     print(build_peaks(force="--force" in sys.argv))

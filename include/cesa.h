@@ -306,6 +306,28 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
                                     float* d_gX, float* d_gY, float* d_gRt0, int* d_status,
                                     cesa_stream_t stream);
 
+/*
+ * Point-cloud front end of the registration CLI (host only; restates the
+ * reference CLI's loadFile, pointsReduction, alignScaleOnce, saveRTtoFile and
+ * loadRTfromFile, src/main.cpp:41-228, without PCL). Points are AoS xyz.
+ *   cesa_load_points: PLY (ASCII / binary, vertex x, y, z of any scalar type)
+ *     or text ("x y z" per line); points with a non-finite coordinate are
+ *     dropped (as pcl::removeNaNFromPointCloud). *xyz is malloc'ed: release it
+ *     with cesa_free.
+ *   cesa_points_reduction: keeps each point with probability percent/100, in
+ *     order; the reference seeds rand() with the clock, this takes a seed.
+ *   cesa_align_scale_once: scales both clouds about the origin so that the
+ *     trace of each one's covariance (normalised by n) becomes 0.003.
+ *   cesa_save_rt / cesa_load_rt: the reference's R, t text file ("%f " per
+ *     entry, three per line, then t).
+ */
+int cesa_load_points(const char* path, float** xyz, int* n);
+void cesa_free(void* p);
+int cesa_points_reduction(float* xyz, int* n, float percent, unsigned long long seed);
+int cesa_align_scale_once(float* xyz1, int n1, float* xyz2, int n2);
+int cesa_save_rt(const char* path, const float R[9], const float t[3]);
+int cesa_load_rt(const char* path, float R[9], float t[3]);
+
 /* Releases cached device workspaces of the calling process. */
 void cesa_release_workspaces(void);
 
