@@ -48,6 +48,11 @@ constexpr int kOwnBlk = kSwT * 4;         // owned points per sweep block (4 per
 constexpr int kTile = kSwT;               // streamed points per shared-memory tile
 constexpr int kMaxTerms = 10;             // rank-1 terms per gradient sweep
 constexpr int kGlue = 256;                // threads of the per-point kernels
+// Threads of the one-block reductions (sums over all points): the block
+// reduction's last step is serial over the warps, so small clouds use 8 warps
+// and large ones 32 (where the per-thread point loop dominates).
+constexpr int kOneBlock = 1024;
+int one_block_threads(int n) { return n > 4096 ? 1024 : 256; }
 
 struct Pose12 {
   float R[9], t[3];
@@ -369,8 +374,8 @@ __global__ void k_horn_adjoint(Vecs A) {
 
 // One block, per row: g(p_i) = a_i gS V_i, g(V_i) = a_i gS^T p_i, dL/da_i from
 // S (S[p + 3 q] = sum a p_p V_q); dL/dXc -= sum g(p).
-__global__ void __launch_bounds__(1024) k_back_S(Vecs A) {
-  __shared__ df red[3 * 32];
+__global__ void __launch_bounds__(kOneBlock) k_back_S(Vecs A) {
+  __shared__ df red[3 * (kOneBlock / 32)];
   const float* aF = a_of(A, A.I1);
   float gS[9];
   for (int k = 0; k < 9; ++k) gS[k] = (float)A.scal[kSgS + k];
@@ -420,8 +425,8 @@ __global__ void k_back_w(Vecs A) {
 
 // One block after the K^T sweep: dL/dYc -= sum_j b_j g(h_j);
 // dL/dsumM = -(gXc . Xc + gYc . Yc) / sumM.
-__global__ void __launch_bounds__(1024) k_back_Yc(Vecs A) {
-  __shared__ df red[3 * 32];
+__global__ void __launch_bounds__(kOneBlock) k_back_Yc(Vecs A) {
+  __shared__ df red[3 * (kOneBlock / 32)];
   df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
   for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
     const float b = b_at(A, A.I1, j);
@@ -515,8 +520,8 @@ __global__ void k_back_rowpass(Vecs A, int k, const float* part, int S) {
 
 // One block: dL/dR = sum gz y^T, dL/dt = sum gz (caller frame, y = y' + oY);
 // per column dL/dy += R^T gz; writes dL/d(R, t) of the input pose.
-__global__ void __launch_bounds__(1024) k_pose_grad(Vecs A) {
-  __shared__ df red[12 * 32];
+__global__ void __launch_bounds__(kOneBlock) k_pose_grad(Vecs A) {
+  __shared__ df red[12 * (kOneBlock / 32)];
   float R[9];
   for (int k = 0; k < 9; ++k) R[k] = A.rec[k];
   df v[12];
@@ -559,10 +564,12 @@ struct Plan {
   SweepIO rows, cols;  // own X / stream Y; own Y / stream X
 };
 
-// Slices so that a sweep has about 1200 blocks (8 per SM of 152).
+// Slices so that a sweep has about 1200 blocks (8 per SM of 152), each slice
+// at least 32 streamed points (small clouds get short slices rather than an
+// under-filled grid).
 void plan_side(SweepIO& io, int n_own, int n_str) {
   const int nb = (n_own + kOwnBlk - 1) / kOwnBlk;
-  const int max_s = std::max(1, (n_str + kTile - 1) / kTile);
+  const int max_s = std::max(1, (n_str + 31) / 32);
   io.S = std::max(1, std::min(max_s, (1200 + nb - 1) / nb));
   io.len = (n_str + io.S - 1) / io.S;
   io.S = (n_str + io.len - 1) / io.len;
@@ -675,6 +682,7 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
   A.gY = J.gY;
   const float T = J.T, al = J.alpha;
   const float* pose = J.rec;  // the update's input pose (centred) leads its record
+  const int ob = one_block_threads(std::max(N, M));
   cudaError_t e = cudaSuccess;
   if (J.first) {
     k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(A.ones, M, 1.f);
@@ -685,10 +693,10 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
   // ---- final stage and Horn
   k_h<<<blocks(M), kGlue, 0, st>>>(A);
   k_horn_adjoint<<<1, 1, 0, st>>>(A);
-  k_back_S<<<1, 1024, 0, st>>>(A);
+  k_back_S<<<1, ob, 0, st>>>(A);
   k_back_w<<<blocks(N), kGlue, 0, st>>>(A);
   sum_sweep<4>(P.cols, L, pose, T, al, A.wt4, N, A.gh, M, false, st);
-  k_back_Yc<<<1, 1024, 0, st>>>(A);
+  k_back_Yc<<<1, ob, 0, st>>>(A);
   k_back_final<<<blocks(N + M), kGlue, 0, st>>>(A);
   // ---- the column and row passes in reverse; each K / K^T product's slice
   // partials are summed by the kernel that consumes them
@@ -733,7 +741,7 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
     grad_sweep(P.rows, L, pose, T, al, tr, A.gX, true, st);
     grad_sweep(P.cols, L, pose, T, al, tcol, A.gZ, t0 > 0, st);
   }
-  k_pose_grad<<<1, 1024, 0, st>>>(A);
+  k_pose_grad<<<1, ob, 0, st>>>(A);
   return (int)cudaGetLastError();
 }
 
