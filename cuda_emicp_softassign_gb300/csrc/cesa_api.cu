@@ -45,11 +45,33 @@ struct DevBuf {
   }
 };
 
+// The Softassign backward's per-update launches, captured as a CUDA graph for
+// one workspace layout and replayed once per update (on a stream of its own,
+// ordered after and before the caller's stream by events).
+struct SaBwdGraph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  void* ws = nullptr;
+  size_t bytes = 0;
+  int N = 0, M = 0, I1 = 0;
+  float alpha = 0.f;
+  void release() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (stream) cudaStreamDestroy(stream);
+    *this = SaBwdGraph{};
+  }
+};
+
 struct StreamCtx {
   DevBuf ws;     // kernel workspace (control block first)
   DevBuf io;     // point copies + pose + outputs for host-pointer calls
   DevBuf trace;  // device trace records
   DevBuf tl;     // device phase timeline
+  SaBwdGraph sa_bwd;
   int last_trace_steps = 0;
   int last_kind = 0;  // 1 emicp, 2 softassign
 };
@@ -820,59 +842,97 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  const size_t need = softassign_step_adjoint_ws_need(N, M, p->I1);
-  const size_t o_gp = align256(need), o_gs = o_gp + 256, o_gu = o_gs + align256(sizeof(float) * (size_t)N);
-  const size_t total = o_gu + align256(sizeof(float) * (size_t)M);
-  cudaError_t e = C.ws.ensure(total);
+  const size_t need = softassign_bwd_ws_need(N, M, p->I1, nsteps);
+  if (C.ws.bytes < need) C.sa_bwd.release();  // its graph refers to the old workspace
+  cudaError_t e = C.ws.ensure(need);
   if (e != cudaSuccess) return map_cuda(e);
-  char* wb = static_cast<char*>(C.ws.p);
-  float* gp = reinterpret_cast<float*>(wb + o_gp);
-  float* gs = reinterpret_cast<float*>(wb + o_gs);
-  float* gu = reinterpret_cast<float*>(wb + o_gu);
   const SaTapeLayout T = sa_tape_layout(N, M, p->I1, nsteps);
   const char* tb = static_cast<const char*>(tape);
-  e = cudaMemcpyAsync(gp, d_gRt, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_gX, 0, sizeof(float) * 3 * (size_t)N, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_gY, 0, sizeof(float) * 3 * (size_t)M, st);
-  if (e != cudaSuccess) return map_cuda(e);
-  // temperatures of the updates, stepped in FP32 as the forward does
-  std::vector<float> Ts;
-  Ts.reserve((size_t)nsteps);
-  float Tk = p->T_0;
-  for (int j = 0; j < p->JMAX; ++j) {
-    for (int i = 0; i < p->I0; ++i) Ts.push_back(Tk);
-    Tk = Tk * p->TFACTOR;
+  SoftassignBackward B{};
+  B.X = reinterpret_cast<const float4*>(tb + T.X);
+  B.Y = reinterpret_cast<const float4*>(tb + T.Y);
+  B.hdr = reinterpret_cast<const CenterHdr*>(tb + T.hdr);
+  B.N = N;
+  B.M = M;
+  B.I1 = p->I1;
+  B.nsteps = nsteps;
+  B.alpha = p->alpha;
+  B.g_out = d_gRt;
+  B.gX = d_gX;
+  B.gY = d_gY;
+  B.g_in = d_gRt0;
+  // the updates' tape slices and temperatures (T stepped in FP32 as the forward does)
+  std::vector<SaUpdate> tab((size_t)nsteps);
+  {
+    const size_t I1 = (size_t)p->I1;
+    float Tk = p->T_0;
+    size_t k = 0;
+    for (int j = 0; j < p->JMAX; ++j) {
+      for (int i = 0; i < p->I0; ++i, ++k) {
+        SaUpdate& U = tab[k];
+        U.rec = reinterpret_cast<const float*>(tb + T.pose) + k * kSaTape;
+        U.s0 = reinterpret_cast<const float*>(tb + T.s) + k * N;
+        U.u0 = reinterpret_cast<const float*>(tb + T.u) + k * M;
+        U.rows = reinterpret_cast<const float*>(tb + T.rows) + k * I1 * 4 * N;
+        U.cols = reinterpret_cast<const float*>(tb + T.cols) + k * I1 * 4 * M;
+        U.fin = reinterpret_cast<const float*>(tb + T.fin) + k * 5 * N;
+        U.T = Tk;
+      }
+      Tk = Tk * p->TFACTOR;
+    }
   }
-  const size_t I1 = (size_t)p->I1;
-  SoftassignStepAdjoint J{};
-  J.X = reinterpret_cast<const float4*>(tb + T.X);
-  J.Y = reinterpret_cast<const float4*>(tb + T.Y);
-  J.hdr = reinterpret_cast<const CenterHdr*>(tb + T.hdr);
-  J.N = N;
-  J.M = M;
-  J.I1 = p->I1;
-  J.alpha = p->alpha;
-  J.gX = d_gX;
-  J.gY = d_gY;
-  J.g_pose = gp;
-  J.g_s = gs;
-  J.g_u = gu;
-  for (long n = nsteps - 1; n >= 0; --n) {
-    const size_t k = (size_t)n;
-    J.T = Ts[k];
-    J.rec = reinterpret_cast<const float*>(tb + T.pose) + k * kSaTape;
-    J.s0 = reinterpret_cast<const float*>(tb + T.s) + k * N;
-    J.u0 = reinterpret_cast<const float*>(tb + T.u) + k * M;
-    J.rows = reinterpret_cast<const float*>(tb + T.rows) + k * I1 * 4 * N;
-    J.cols = reinterpret_cast<const float*>(tb + T.cols) + k * I1 * 4 * M;
-    J.fin = reinterpret_cast<const float*>(tb + T.fin) + k * 5 * N;
-    J.first = n == nsteps - 1 ? 1 : 0;
-    const int r = enqueue_softassign_step_adjoint(J, C.ws.p, need, st);
-    if (r) return map_cuda((cudaError_t)r);
+  int r = softassign_bwd_prepare(B, tab.data(), C.ws.p, C.ws.bytes, st);
+  if (r) return map_cuda((cudaError_t)r);
+  // one update's launches as a graph (captured once per workspace layout), replayed per update
+  SaBwdGraph& G = C.sa_bwd;
+  bool graphed = false;
+  if (nsteps > 0) {
+    const bool same = G.exec && G.ws == C.ws.p && G.bytes == C.ws.bytes && G.N == N && G.M == M && G.I1 == p->I1 &&
+                      G.alpha == p->alpha;
+    if (!same) {
+      G.release();
+      if (cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking) == cudaSuccess &&
+          cudaEventCreateWithFlags(&G.fork, cudaEventDisableTiming) == cudaSuccess &&
+          cudaEventCreateWithFlags(&G.join, cudaEventDisableTiming) == cudaSuccess &&
+          cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int ur = softassign_bwd_update(B, C.ws.p, C.ws.bytes, G.stream);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(G.stream, &graph);
+        if (ur == 0 && ce == cudaSuccess && graph &&
+            cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
+          G.ws = C.ws.p;
+          G.bytes = C.ws.bytes;
+          G.N = N;
+          G.M = M;
+          G.I1 = p->I1;
+          G.alpha = p->alpha;
+        } else {
+          G.exec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();  // a failed capture leaves the direct launches below
+      if (!G.exec) G.release();
+    }
+    if (G.exec) {
+      e = cudaEventRecord(G.fork, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(G.stream, G.fork, 0);
+      for (long n = 0; n < nsteps && e == cudaSuccess; ++n) e = cudaGraphLaunch(G.exec, G.stream);
+      if (e == cudaSuccess) e = cudaEventRecord(G.join, G.stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, G.join, 0);
+      if (e != cudaSuccess) return map_cuda(e);
+      graphed = true;
+    }
   }
-  e = cudaMemcpyAsync(d_gRt0, gp, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  if (!graphed)
+    for (long n = 0; n < nsteps; ++n) {
+      r = softassign_bwd_update(B, C.ws.p, C.ws.bytes, st);
+      if (r) return map_cuda((cudaError_t)r);
+    }
+  r = softassign_bwd_finish(B, C.ws.p, C.ws.bytes, st);
+  if (r) return map_cuda((cudaError_t)r);
   // the backward has no device-side waits: its status is set once all launches are queued
-  if (e == cudaSuccess && d_status) e = cudaMemsetAsync(d_status, 0, sizeof(int), st);
+  if (d_status) e = cudaMemsetAsync(d_status, 0, sizeof(int), st);
   C.last_kind = 2;
   C.last_trace_steps = 0;
   return map_cuda(e);
@@ -1141,6 +1201,7 @@ void cesa_release_workspaces(void) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(kv.first.first);
+    kv.second.sa_bwd.release();
     kv.second.ws.release();
     kv.second.io.release();
     kv.second.trace.release();

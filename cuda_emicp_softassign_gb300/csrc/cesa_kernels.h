@@ -152,28 +152,38 @@ void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4*
 
 void softassign_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);
 
-// Adjoint of one Softassign pose update from its tape. Device pointers.
-struct SoftassignStepAdjoint {
-  const float4* X;        // X' centred (N), as packed by the forward
-  const float4* Y;        // Y' centred (M)
+// Softassign adjoint over a recorded tape (device pointers). One update's
+// backward is the same launch sequence for every update: a device counter
+// selects the update's tape slices from a table, which a first kernel copies
+// into fixed workspace buffers, and the last kernel steps the counter. The
+// sequence can therefore be captured once as a CUDA graph and replayed.
+struct SaUpdate {
+  const float* rec;   // [kSaTape]
+  const float* s0;    // [N]
+  const float* u0;    // [M]
+  const float* rows;  // [I1][4][N]
+  const float* cols;  // [I1][4][M]
+  const float* fin;   // [5][N]
+  float T;
+  int pad;
+};
+struct SoftassignBackward {
+  const float4* X;    // X' centred (N), as packed by the forward
+  const float4* Y;    // Y' centred (M)
   const CenterHdr* hdr;
   int N, M, I1;
-  float T, alpha;
-  const float* rec;       // [kSaTape] the update's record
-  const float* s0;        // [N] input slack
-  const float* u0;        // [M]
-  const float* rows;      // [I1][4][N]
-  const float* cols;      // [I1][4][M]
-  const float* fin;       // [5][N]
-  float* g_pose;          // [12] in: dL/d(R, t) of the output pose; out: of the input pose (caller frame)
-  float* g_s;             // [N] in: dL/ds of the output slack (ignored when first); out: of the input slack
-  float* g_u;             // [M]
-  int first;              // the last update of the schedule: the output slack does not feed the loss
-  float* gX;              // SoA [3N], accumulated
-  float* gY;              // SoA [3M], accumulated
+  long nsteps;
+  float alpha;
+  const float* g_out; // [12] dL/dR, dL/dt of the final pose (caller frame)
+  float* gX;          // SoA [3N] (written by finish)
+  float* gY;          // SoA [3M]
+  float* g_in;        // [12] dL/d(R, t) of the initial pose
 };
-size_t softassign_step_adjoint_ws_need(int N, int M, int I1);
-int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st);
+size_t softassign_bwd_ws_need(int N, int M, int I1, long nsteps);
+int softassign_bwd_prepare(const SoftassignBackward& B, const SaUpdate* host_tab, void* ws, size_t ws_bytes,
+                           cudaStream_t st);
+int softassign_bwd_update(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st);
+int softassign_bwd_finish(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st);
 
 // ICP (exhaustive nearest neighbours): maxIteration iterations in one launch.
 struct IcpLaunch {

@@ -106,6 +106,9 @@ __device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, f
   }
 }
 
+// The per-update record copy carries T and alpha in otherwise unused slots.
+constexpr int kRecT = 60, kRecAlpha = 61;
+
 __device__ __forceinline__ void kernel_consts(float T, float alpha, float& nk, float& c0) {
   // K = exp((alpha - d^2)/T)/sqrt(T) = 2^(c0 + nk d^2), as the forward kernels form it
   const float kk = kLog2e / T;
@@ -115,8 +118,9 @@ __device__ __forceinline__ void kernel_consts(float T, float alpha, float& nk, f
 
 // part[sl][m][i] = sum over slice sl of K(own_i, str_j) w_m[j], m < NW.
 template <int NW>
-__global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, float T, float alpha,
-                                                    const float* w, int ldw, float* part) {
+__global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, const float* w, int ldw,
+                                                    float* part) {
+  const float T = pose[kRecT], alpha = pose[kRecAlpha];
   __shared__ float4 s_pt[kTile];
   __shared__ float s_w[NW > 1 ? NW - 1 : 1][kTile];
   float nk, c0;
@@ -179,8 +183,8 @@ struct Terms {
 
 // part[sl][d][i] = (2/T) sum over slice sl of G_ij (s_j - o_i)_d with
 // G_ij = K_ij sum_m own_m[i] str_m[j].
-__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, float T, float alpha,
-                                                     Terms tm, float* part) {
+__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
+  const float T = pose[kRecT], alpha = pose[kRecAlpha];
   __shared__ float4 s_pt[kTile];
   __shared__ float s_b[kMaxTerms][kTile];
   float nk, c0;
@@ -302,6 +306,7 @@ struct Vecs {
   float* gZ;          // [3][M]
   float* gX;          // [3][N] accumulated
   float* gY;          // [3][M] accumulated
+  int* cur;           // the update being differentiated (device counter, stepped down by k_pose_grad)
 };
 
 __device__ __forceinline__ const float* a_of(const Vecs& A, int k) { return A.rows + (size_t)(k - 1) * 4 * A.N; }
@@ -538,12 +543,34 @@ __global__ void __launch_bounds__(kOneBlock) k_pose_grad(Vecs A) {
       A.gY[(size_t)jj * A.M + j] += R[jj] * g[0] + R[3 + jj] * g[1] + R[6 + jj] * g[2];
   }
   block_reduce_df<12>(v, red);
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     for (int i = 0; i < 3; ++i) {
       const float gt = df_val(v[9 + i]);
       A.g_pose[9 + i] = gt;
       for (int j = 0; j < 3; ++j) A.g_pose[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
     }
+    *A.cur -= 1;  // the next update back
+  }
+}
+
+// The current update's tape slices into the fixed copies every other kernel of
+// the update reads (so one update's launches are the same for every update).
+__global__ void k_load_update(const SaUpdate* tab, const int* cur, float* rec, float* s0, float* u0, float* rows,
+                              float* cols, float* fin, int N, int M, int I1, float alpha) {
+  const SaUpdate U = tab[*cur];
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = tid; i < kSaTape; i += stride) rec[i] = i == kRecT ? U.T : i == kRecAlpha ? alpha : U.rec[i];
+  for (int i = tid; i < N; i += stride) s0[i] = U.s0[i];
+  for (int i = tid; i < M; i += stride) u0[i] = U.u0[i];
+  const int nr = I1 * 4 * N, nc = I1 * 4 * M;
+  for (int i = tid; i < nr; i += stride) rows[i] = U.rows[i];
+  for (int i = tid; i < nc; i += stride) cols[i] = U.cols[i];
+  for (int i = tid; i < 5 * N; i += stride) fin[i] = U.fin[i];
+}
+
+// SoA outputs and the input pose's gradient out of the accumulators.
+__global__ void k_copy(float* dst, const float* src, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
 }
 
 // ------------------------------------------------------------------ host side
@@ -591,16 +618,26 @@ Plan make_plan(int N, int M) {
 struct Layout {
   Vecs V;
   float* part;
+  float *rec, *s0, *u0, *rows, *cols, *fin;  // the current update's tape slices (copies)
+  float4 *X, *Y;                             // the packed clouds (copies)
+  CenterHdr* hdr;
+  SaUpdate* tab;                             // [nsteps]
   size_t total;
 };
 
-Layout carve(void* base, int N, int M, int I1, const Plan& P) {
+Layout carve(void* base, int N, int M, int I1, long nsteps, const Plan& P) {
   Carve c(base);
   Layout L{};
   Vecs& A = L.V;
   A.N = N;
   A.M = M;
   A.I1 = I1;
+  A.cur = c.take<int>(1);
+  A.g_pose = c.take<float>(16);
+  A.gs = c.take<float>(N);
+  A.gu = c.take<float>(M);
+  A.gX = c.take<float>(3 * (size_t)N);
+  A.gY = c.take<float>(3 * (size_t)M);
   A.ones = c.take<float>(M);
   A.h = c.take<float>(3 * (size_t)M);
   A.scal = c.take<double>(kScalN);
@@ -616,8 +653,25 @@ Layout carve(void* base, int N, int M, int I1, const Plan& P) {
   A.gr = c.take<float>((size_t)I1 * N);
   A.gc = c.take<float>((size_t)I1 * M);
   A.gZ = c.take<float>(3 * (size_t)M);
+  L.rec = c.take<float>(kSaTape);
+  L.s0 = c.take<float>(N);
+  L.u0 = c.take<float>(M);
+  L.rows = c.take<float>((size_t)I1 * 4 * N);
+  L.cols = c.take<float>((size_t)I1 * 4 * M);
+  L.fin = c.take<float>(5 * (size_t)N);
+  L.X = c.take<float4>(N);
+  L.Y = c.take<float4>(M);
+  L.hdr = c.take<CenterHdr>(1);
+  A.rec = L.rec;
+  A.s0 = L.s0;
+  A.u0 = L.u0;
+  A.rows = L.rows;
+  A.cols = L.cols;
+  A.fin = L.fin;
   const size_t pr = (size_t)P.rows.S * 4 * N, pc = (size_t)P.cols.S * 4 * M;
   L.part = c.take<float>(std::max(pr, pc));
+  // last, so that every other offset is the same whatever the schedule's length
+  L.tab = c.take<SaUpdate>((size_t)(nsteps > 0 ? nsteps : 1));
   L.total = c.off;
   return L;
 }
@@ -627,75 +681,104 @@ int blocks(int n) { return (n + kGlue - 1) / kGlue; }
 // Slice partials of NW K-products of weight vectors into part (rows: K w, w
 // over columns; columns: K^T w, w over rows).
 template <int NW>
-void sweep_partials(const SweepIO& io, float* part, const float* pose, float T, float alpha, const float* w, int ldw,
-                    cudaStream_t st) {
+void sweep_partials(const SweepIO& io, float* part, const float* rec, const float* w, int ldw, cudaStream_t st) {
   dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
-  k_sweep_sum<NW><<<g, kSwT, 0, st>>>(io, pose, T, alpha, w, ldw, part);
+  k_sweep_sum<NW><<<g, kSwT, 0, st>>>(io, rec, w, ldw, part);
 }
 
 // out[m] (+)= the slice-ordered sums of a sweep's partials.
 template <int NW>
-void sum_sweep(const SweepIO& io, const Layout& L, const float* pose, float T, float alpha, const float* w, int ldw,
-               float* out, int ldo, bool acc, cudaStream_t st) {
-  sweep_partials<NW>(io, L.part, pose, T, alpha, w, ldw, st);
+void sum_sweep(const SweepIO& io, const Layout& L, const float* w, int ldw, float* out, int ldo, bool acc,
+               cudaStream_t st) {
+  sweep_partials<NW>(io, L.part, L.rec, w, ldw, st);
   k_reduce_slices<<<dim3(blocks(io.n_own), NW), kGlue, 0, st>>>(L.part, io.S, NW, io.n_own, out, ldo, acc ? 1 : 0);
 }
 
-void grad_sweep(const SweepIO& io, const Layout& L, const float* pose, float T, float alpha, const Terms& tm,
-                float* out, bool acc, cudaStream_t st) {
+void grad_sweep(const SweepIO& io, const Layout& L, const Terms& tm, float* out, bool acc, cudaStream_t st) {
   dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
-  k_sweep_grad<<<g, kSwT, 0, st>>>(io, pose, T, alpha, tm, L.part);
+  k_sweep_grad<<<g, kSwT, 0, st>>>(io, L.rec, tm, L.part);
   k_reduce_slices<<<dim3(blocks(io.n_own), 3), kGlue, 0, st>>>(L.part, io.S, 3, io.n_own, out, io.n_own, acc ? 1 : 0);
+}
+
+struct Ctx {
+  Plan P;
+  Layout L;
+  Vecs A;
+};
+
+int make_ctx(const SoftassignBackward& B, void* ws, size_t ws_bytes, Ctx& c) {
+  const int N = B.N, M = B.M, I1 = B.I1;
+  if (N < 1 || M < 1 || I1 < 1 || 4 + 2 * I1 > 64 || B.nsteps < 0) return (int)cudaErrorInvalidValue;
+  c.P = make_plan(N, M);
+  c.L = carve(ws, N, M, I1, B.nsteps, c.P);
+  if (!ws || c.L.total > ws_bytes) return (int)cudaErrorInvalidValue;
+  // every launch reads the workspace copies of the clouds, so that one
+  // update's launches do not depend on where the tape lives
+  c.P.rows.own = c.L.X;
+  c.P.rows.str = c.L.Y;
+  c.P.cols.own = c.L.Y;
+  c.P.cols.str = c.L.X;
+  c.A = c.L.V;
+  c.A.X = c.L.X;
+  c.A.Y = c.L.Y;
+  c.A.hdr = c.L.hdr;
+  return 0;
 }
 
 }  // namespace
 
-size_t softassign_step_adjoint_ws_need(int N, int M, int I1) {
+size_t softassign_bwd_ws_need(int N, int M, int I1, long nsteps) {
   const Plan P = make_plan(N, M);
-  return carve(nullptr, N, M, I1, P).total;
+  return carve(nullptr, N, M, I1, nsteps, P).total;
 }
 
-int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, size_t ws_bytes, cudaStream_t st) {
-  const int N = J.N, M = J.M, I1 = J.I1;
-  if (N < 1 || M < 1 || I1 < 1 || 4 + 2 * I1 > 64 || !(J.T > 0.f)) return (int)cudaErrorInvalidValue;
-  Plan P = make_plan(N, M);
-  P.rows.own = J.X;
-  P.rows.str = J.Y;
-  P.cols.own = J.Y;
-  P.cols.str = J.X;
-  const Layout L = carve(ws, N, M, I1, P);
-  if (!ws || L.total > ws_bytes) return (int)cudaErrorInvalidValue;
-  Vecs A = L.V;
-  A.X = J.X;
-  A.Y = J.Y;
-  A.hdr = J.hdr;
-  A.rec = J.rec;
-  A.s0 = J.s0;
-  A.u0 = J.u0;
-  A.rows = J.rows;
-  A.cols = J.cols;
-  A.fin = J.fin;
-  A.g_pose = J.g_pose;
-  A.gs = J.g_s;
-  A.gu = J.g_u;
-  A.gX = J.gX;
-  A.gY = J.gY;
-  const float T = J.T, al = J.alpha;
-  const float* pose = J.rec;  // the update's input pose (centred) leads its record
-  const int ob = one_block_threads(std::max(N, M));
+int softassign_bwd_prepare(const SoftassignBackward& B, const SaUpdate* host_tab, void* ws, size_t ws_bytes,
+                           cudaStream_t st) {
+  Ctx c;
+  int r = make_ctx(B, ws, ws_bytes, c);
+  if (r) return r;
+  const int N = B.N, M = B.M;
+  const int last = (int)B.nsteps - 1;
   cudaError_t e = cudaSuccess;
-  if (J.first) {
-    k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(A.ones, M, 1.f);
-    e = cudaMemsetAsync(A.gs, 0, sizeof(float) * N, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(A.gu, 0, sizeof(float) * M, st);
-    if (e != cudaSuccess) return (int)e;
+  if (B.nsteps > 0)
+    e = cudaMemcpyAsync(c.L.tab, host_tab, sizeof(SaUpdate) * (size_t)B.nsteps, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.A.cur, &last, sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.L.X, B.X, sizeof(float4) * (size_t)N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.L.Y, B.Y, sizeof(float4) * (size_t)M, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.L.hdr, B.hdr, sizeof(CenterHdr), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.A.g_pose, B.g_out, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  // the output slack of the last update does not feed the loss
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gs, 0, sizeof(float) * N, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gu, 0, sizeof(float) * M, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gX, 0, sizeof(float) * 3 * (size_t)N, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gY, 0, sizeof(float) * 3 * (size_t)M, st);
+  if (e != cudaSuccess) return (int)e;
+  k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(c.A.ones, M, 1.f);
+  return (int)cudaGetLastError();
+}
+
+// The launches of one update's backward, the update chosen on the device (the
+// same launches, with the same arguments, for every update).
+int softassign_bwd_update(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st) {
+  Ctx c;
+  int r = make_ctx(B, ws, ws_bytes, c);
+  if (r) return r;
+  const Plan& P = c.P;
+  const Layout& L = c.L;
+  Vecs& A = c.A;
+  const int N = B.N, M = B.M, I1 = B.I1;
+  const int ob = one_block_threads(std::max(N, M));
+  {
+    const int total = 4 * I1 * (N + M) + 6 * N + M;
+    const int g = std::min(std::max(1, (total + 4 * kGlue - 1) / (4 * kGlue)), 1024);
+    k_load_update<<<g, kGlue, 0, st>>>(L.tab, A.cur, L.rec, L.s0, L.u0, L.rows, L.cols, L.fin, N, M, I1, B.alpha);
   }
   // ---- final stage and Horn
   k_h<<<blocks(M), kGlue, 0, st>>>(A);
   k_horn_adjoint<<<1, 1, 0, st>>>(A);
   k_back_S<<<1, ob, 0, st>>>(A);
   k_back_w<<<blocks(N), kGlue, 0, st>>>(A);
-  sum_sweep<4>(P.cols, L, pose, T, al, A.wt4, N, A.gh, M, false, st);
+  sum_sweep<4>(P.cols, L, A.wt4, N, A.gh, M, false, st);
   k_back_Yc<<<1, ob, 0, st>>>(A);
   k_back_final<<<blocks(N + M), kGlue, 0, st>>>(A);
   // ---- the column and row passes in reverse; each K / K^T product's slice
@@ -704,12 +787,12 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
   for (int k = I1 - 1; k >= 0; --k) {
     k_back_colpass<<<blocks(M), kGlue, 0, st>>>(A, k, pending, P.cols.S);
     // dL/da^{k+1} += K g(c^k)
-    sweep_partials<1>(P.rows, L.part, pose, T, al, A.gc + (size_t)k * M, M, st);
+    sweep_partials<1>(P.rows, L.part, L.rec, A.gc + (size_t)k * M, M, st);
     k_back_rowpass<<<blocks(N), kGlue, 0, st>>>(A, k, L.part, P.rows.S);
     // dL/db^k += K^T g(r^k); b^0 = 1 is a constant
     pending = nullptr;
     if (k >= 1) {
-      sweep_partials<1>(P.cols, L.part, pose, T, al, A.gr + (size_t)k * N, N, st);
+      sweep_partials<1>(P.cols, L.part, L.rec, A.gr + (size_t)k * N, N, st);
       pending = L.part;
     }
   }
@@ -722,12 +805,12 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
     tb[d] = A.h + (size_t)d * M;
   }
   ta[3] = A.grho;
-  tb[3] = J.cols + (size_t)(I1 - 1) * 4 * M;  // b^{I1}
+  tb[3] = L.cols + (size_t)(I1 - 1) * 4 * M;  // b^{I1}
   for (int k = 0; k < I1; ++k) {
-    ta[4 + k] = J.rows + (size_t)k * 4 * N;  // a^{k+1}
+    ta[4 + k] = L.rows + (size_t)k * 4 * N;  // a^{k+1}
     tb[4 + k] = A.gc + (size_t)k * M;
     ta[4 + I1 + k] = A.gr + (size_t)k * N;
-    tb[4 + I1 + k] = k == 0 ? A.ones : J.cols + (size_t)(k - 1) * 4 * M;  // b^k
+    tb[4 + I1 + k] = k == 0 ? A.ones : L.cols + (size_t)(k - 1) * 4 * M;  // b^k
   }
   for (int t0 = 0; t0 < nterms; t0 += kMaxTerms) {
     Terms tr{}, tcol{};
@@ -738,10 +821,21 @@ int enqueue_softassign_step_adjoint(const SoftassignStepAdjoint& J, void* ws, si
       tcol.own[m] = tb[t0 + m];
       tcol.str[m] = ta[t0 + m];
     }
-    grad_sweep(P.rows, L, pose, T, al, tr, A.gX, true, st);
-    grad_sweep(P.cols, L, pose, T, al, tcol, A.gZ, t0 > 0, st);
+    grad_sweep(P.rows, L, tr, A.gX, true, st);
+    grad_sweep(P.cols, L, tcol, A.gZ, t0 > 0, st);
   }
   k_pose_grad<<<1, ob, 0, st>>>(A);
+  return (int)cudaGetLastError();
+}
+
+int softassign_bwd_finish(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st) {
+  Ctx c;
+  int r = make_ctx(B, ws, ws_bytes, c);
+  if (r) return r;
+  const int N = B.N, M = B.M;
+  k_copy<<<std::min(blocks(3 * N), 1024), kGlue, 0, st>>>(B.gX, c.A.gX, 3 * N);
+  k_copy<<<std::min(blocks(3 * M), 1024), kGlue, 0, st>>>(B.gY, c.A.gY, 3 * M);
+  k_copy<<<1, 32, 0, st>>>(B.g_in, c.A.g_pose, 12);
   return (int)cudaGetLastError();
 }
 
