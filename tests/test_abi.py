@@ -136,6 +136,31 @@ def test_invalid_arguments_are_rejected(cesa):
     bad = cesa.Params.default(I1=0)  # the reference would read uninitialised column sums
     assert L.cesa_softassign(ptr(X), 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(bad), None) == cesa.CESA_ERR_INVALID_ARGUMENT
     assert cesa.status_string(cesa.CESA_ERR_TIMEOUT) == "device-side wait timed out"
+    # ICP and the adjoints validate before touching a device
+    assert L.cesa_icp(ptr(X), 2, ptr(X), 0, ptr(R), ptr(t), ctypes.byref(p), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    bad = cesa.Params.default(maxIteration=-1)
+    assert L.cesa_icp(ptr(X), 2, ptr(X), 2, ptr(R), ptr(t), ctypes.byref(bad), None) == cesa.CESA_ERR_INVALID_ARGUMENT
+    assert L.cesa_softassign_tape_bytes(0, 5, ctypes.byref(p)) == 0
+    assert L.cesa_softassign_tape_bytes(5, 5, ctypes.byref(cesa.Params.default(I1=0))) == 0
+    assert L.cesa_emicp_tape_bytes(5, 0, ctypes.byref(p)) == 0
+    assert L.cesa_softassign_backward_device(5, 5, ctypes.byref(p), None, None, None, None, None, None, None) == \
+        cesa.CESA_ERR_INVALID_ARGUMENT
+    assert L.cesa_emicp_backward_device(0, 5, ctypes.byref(p), None, None, None, None, None, None, None) == \
+        cesa.CESA_ERR_INVALID_ARGUMENT
+
+
+def test_tape_sizes_grow_with_the_schedule(cesa):
+    """The Softassign tape holds, per pose update, the record, the slack and
+    4 (N + M) floats per Sinkhorn pass plus 5 N; EM-ICP's, per sigma step, the
+    record and 5 M floats."""
+    L = cesa.lib()
+    p = cesa.Params.default(JMAX=10, I0=5, I1=3)
+    n = L.cesa_softassign_tape_bytes(1000, 800, ctypes.byref(p))
+    per_update = 4 * (64 + 1000 + 800 + 3 * 4 * (1000 + 800) + 5 * 1000)
+    assert per_update * 50 <= n <= per_update * 50 + 4 * 256 * 12 + 16 * (1000 + 800) + 256
+    q = cesa.Params.default(JMAX=20, I0=5, I1=3)
+    # 50 more updates: the same per-update bytes again, up to the sections' 256-byte alignment
+    assert abs(L.cesa_softassign_tape_bytes(1000, 800, ctypes.byref(q)) - n - per_update * 50) <= 6 * 256
 
 
 def test_invalid_batches_are_rejected(cesa):
