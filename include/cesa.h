@@ -287,15 +287,17 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
 /*
  * Adjoint of Softassign (no counterpart in the reference). The forward runs
  * the matrix-free kernel (whatever p->sinkhorn_form says) and records a tape:
- * the packed clouds and, per pose update, its input pose and slack vectors s
- * (N) and u (M), the state carried between updates (checkpoints of the
- * annealing loop, src/softassign.cu:486-822). The backward walks the updates
- * in reverse; for each it recomputes the update's Sinkhorn scalings with the
- * affinities formed on the fly (no N x M matrix is stored) and runs the
- * adjoint of the row and column passes, of the weighted centres and S, and of
- * the Horn pose. Given dL/dR (9, row-major) and dL/dt (3) of the returned
- * pose it writes dL/dX (SoA 3N), dL/dY (SoA 3M) and dL/dR0, dL/dt0 of the
- * initial pose (12). All pointers are device pointers.
+ * the packed clouds and, per pose update (src/softassign.cu:494-798), its
+ * input pose and slack vectors s (N) and u (M), every Sinkhorn pass's
+ * scalings, slack and sums (4 (N + M) floats per row and column pass), the
+ * final sweep's row sums (5 N) and the Horn solve. The tape is O(N + M) per
+ * pass; no N x M matrix is stored. The backward walks the updates in reverse
+ * and runs the adjoint of the Horn pose, of the weighted centres and S, and of
+ * the column and row passes, forming the affinities on the fly in each K or
+ * K^T product and in the two gradient sweeps. One update's launches are
+ * replayed as a CUDA graph. Given dL/dR (9, row-major) and dL/dt (3) of the
+ * returned pose it writes dL/dX (SoA 3N), dL/dY (SoA 3M) and dL/dR0, dL/dt0 of
+ * the initial pose (12). All pointers are device pointers.
  * cesa_softassign_forward_device returns the same pose as
  * cesa_softassign_device with the matrix-free form.
  */
