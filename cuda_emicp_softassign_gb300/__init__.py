@@ -29,6 +29,9 @@ CESA_ERR_NOALLOC_LIMIT = 7
 SINKHORN_AUTO = 0
 SINKHORN_MATRIX_FREE = 1
 SINKHORN_MATERIALISED = 2
+ICP_SEARCH_AUTO = 0
+ICP_SEARCH_EXHAUSTIVE = 1
+ICP_SEARCH_GRID = 2
 
 TRACE_STRIDE = 32
 # trace record fields
@@ -53,7 +56,7 @@ class Params(ctypes.Structure):
         ("sigma_factor", ctypes.c_float), ("d_02", ctypes.c_float),
         ("maxIteration", ctypes.c_int),
         ("sinkhorn_form", ctypes.c_int), ("timeout_ms", ctypes.c_int), ("device", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("icp_search", ctypes.c_int), ("reserved", ctypes.c_int * 4),
     ]
 
     @classmethod

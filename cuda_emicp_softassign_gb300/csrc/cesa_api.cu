@@ -135,6 +135,7 @@ int check_sa_params(const cesa_params* p) {
 int check_icp_params(const cesa_params* p) {
   if (!p) return CESA_ERR_INVALID_ARGUMENT;
   if (p->maxIteration < 0 || p->maxIteration > 100000000) return CESA_ERR_INVALID_ARGUMENT;
+  if (p->icp_search < CESA_ICP_SEARCH_AUTO || p->icp_search > CESA_ICP_SEARCH_GRID) return CESA_ERR_INVALID_ARGUMENT;
   return CESA_OK;
 }
 
@@ -223,7 +224,7 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
   const int form = kind == 2 ? resolve_form(p->sinkhorn_form, N, M, dev) : 0;
   const size_t need = kind == 1   ? emicp_ws_need(N, M, dev)
                       : kind == 2 ? softassign_ws_need(N, M, form, dev)
-                                  : icp_ws_need(N, M, dev);
+                                  : icp_ws_need(N, M, dev, p->icp_search);
   e = C.ws.ensure(need);
   if (e != cudaSuccess) return map_cuda(e);
   const int cap = (rep && rep->trace && rep->trace_capacity > 0) ? rep->trace_capacity : 0;
@@ -278,6 +279,7 @@ int run_host(int kind, const float* X, int N, const float* Y, int M, float R[9],
       L.N = N;
       L.M = M;
       L.iters = (int)nsteps;
+      L.search = p->icp_search;
       L.dRt = dRt;
       L.trace = dtrace;
       L.trace_cap = cap;
@@ -451,7 +453,7 @@ int cesa_icp_device(const float* dX, int N, const float* dY, int M, float* dRt, 
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  cudaError_t e = C.ws.ensure(icp_ws_need(N, M, dev));
+  cudaError_t e = C.ws.ensure(icp_ws_need(N, M, dev, p->icp_search));
   if (e != cudaSuccess) return map_cuda(e);
   IcpLaunch L{};
   L.dX = dX;
@@ -459,6 +461,7 @@ int cesa_icp_device(const float* dX, int N, const float* dY, int M, float* dRt, 
   L.N = N;
   L.M = M;
   L.iters = p->maxIteration;
+  L.search = p->icp_search;
   L.dRt = dRt;
   L.nn_out = d_nn;
   L.d_status = d_status;

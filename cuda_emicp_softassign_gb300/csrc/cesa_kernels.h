@@ -192,12 +192,13 @@ struct IcpLaunch {
   int N, M, iters;
   float* dRt;       // PoseIO in/out (device)
   int* nn_out;      // optional [M]: the last iteration's matches
+  int search;       // CESA_ICP_SEARCH_*
   double* trace;
   int trace_cap;
   int* d_status;
   uint64_t timeout_ns;
 };
-size_t icp_ws_need(int N, int M, int device);
+size_t icp_ws_need(int N, int M, int device, int search);
 int enqueue_icp(const IcpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
 
 // Control-block status of the last launch that used workspace ws.

@@ -12,7 +12,8 @@ cases:
   adj_20000   emicp_adjoint_kernel: forward + backward, N = M = 20000, sigma_inf = 2e-3 (16 steps)
   sa_adj_20000  Softassign adjoint sweeps (k_sweep_sum, k_sweep_grad): forward + backward,
               N = M = 20000 (config-5 generator), JMAX = 1, I0 = 2 (two pose updates)
-  icp_20000   icp_kernel: ICP on config 3's generator at N = M = 20000, 5 iterations
+  icp_20000   icp_kernel: ICP on config 3's generator at N = M = 20000, 5 iterations, exhaustive search
+  icp_grid_20000  icp_kernel: the same with the uniform-grid search
 """
 import sys
 
@@ -94,16 +95,25 @@ def sa_adj_20000():
     torch.cuda.synchronize()
 
 
-def icp_20000():
+def _icp(search):
     import cuda_emicp_softassign_gb300 as C
     from cuda_emicp_softassign_gb300 import workloads as W
     _, X, Y, _, _ = W.make("icp_40097", seed=0, n=20000)
-    p = C.Params.default(maxIteration=5)
+    p = C.Params.default(maxIteration=5, icp_search=search)
     for _ in range(2):
         C.icp(X, Y, param=p)
 
 
-CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000)}
+def icp_20000():
+    _icp(1)  # CESA_ICP_SEARCH_EXHAUSTIVE
+
+
+def icp_grid_20000():
+    _icp(2)  # CESA_ICP_SEARCH_GRID
+
+
+CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+                                  icp_grid_20000)}
 
 if __name__ == "__main__":
     if len(sys.argv) != 2 or sys.argv[1] not in CASES:

@@ -68,8 +68,15 @@ typedef struct cesa_params {
   int sinkhorn_form; /* CESA_SINKHORN_* */
   int timeout_ms;    /* limit of any device-side wait; 0 selects 10000 ms */
   int device;        /* CUDA device ordinal for the host-pointer entry points; -1 = current */
-  int reserved[5];
+  int icp_search;    /* CESA_ICP_SEARCH_*: nearest-neighbour search of cesa_icp */
+  int reserved[4];
 } cesa_params;
+
+/* ICP nearest-neighbour search (cesa_params.icp_search). Both are exact and
+ * give the same matches (the first of equal distances in X order). */
+#define CESA_ICP_SEARCH_AUTO 0       /* uniform grid from 4096 target points on, else exhaustive */
+#define CESA_ICP_SEARCH_EXHAUSTIVE 1 /* every target point, tiled through shared memory */
+#define CESA_ICP_SEARCH_GRID 2       /* uniform grid over the target, rings of cells around each query */
 
 /*
  * Optional per-call report (may be NULL). trace, when non-NULL, receives one

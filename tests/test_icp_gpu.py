@@ -90,3 +90,37 @@ def test_icp_deterministic_and_zero_iterations(cesa):
     R0 = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
     R, t = cesa.icp(X, Y, R0, np.array([0.1, 0.2, 0.3]), param=cesa.Params.default(maxIteration=0))
     assert np.allclose(R, R0) and np.allclose(t, [0.1, 0.2, 0.3], atol=1e-6)
+
+
+@pytest.mark.parametrize("n,m,seed", [(5000, 4000, 21), (20000, 3000, 22), (300, 2000, 23)])
+def test_grid_search_equals_exhaustive_bitwise(cesa, torch_cuda, n, m, seed):
+    """The grid search returns the same matches as the exhaustive search (both
+    take the first of equal distances), so the registrations are bitwise equal;
+    surface views (a 2-D manifold in a 3-D grid) and a uniform cube."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    if seed == 21:
+        X, Y, _, _ = W.uniform_pair(n=n, m=m, seed=seed, max_deg=20.0, t_range=0.05)
+    else:
+        X, Y, _, _ = W.surface_pair(n=n, m=m, seed=seed)
+    out = []
+    for mode in (cesa.ICP_SEARCH_EXHAUSTIVE, cesa.ICP_SEARCH_GRID):
+        p = cesa.Params.default(maxIteration=12, icp_search=mode)
+        out.append(_device_nn(cesa, torch_cuda, X, Y, p))
+    (R1, t1, nn1), (R2, t2, nn2) = out
+    assert np.array_equal(nn1, nn2)
+    assert np.array_equal(R1, R2) and np.array_equal(t1, t2)
+
+
+def test_grid_search_far_points_and_duplicates(cesa, torch_cuda):
+    """Queries far outside the target's grid, duplicate targets (equal
+    distances: the lowest index) and a flat target (one-cell-thick grid)."""
+    rng = np.random.default_rng(4)
+    base = rng.uniform(0, 1, (2500, 3))
+    base[:, 2] = 0.0  # flat
+    X = np.concatenate([base, base])
+    Y = np.concatenate([base[rng.permutation(2500)][:2000], rng.uniform(-50, 50, (300, 3))])
+    res = []
+    for mode in (cesa.ICP_SEARCH_EXHAUSTIVE, cesa.ICP_SEARCH_GRID):
+        res.append(_device_nn(cesa, torch_cuda, X, Y, cesa.Params.default(maxIteration=1, icp_search=mode)))
+    assert np.array_equal(res[0][2], res[1][2])
+    assert res[1][2][:2000].max() < 2500
