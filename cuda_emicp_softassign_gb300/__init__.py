@@ -32,6 +32,10 @@ SINKHORN_MATERIALISED = 2
 ICP_SEARCH_AUTO = 0
 ICP_SEARCH_EXHAUSTIVE = 1
 ICP_SEARCH_GRID = 2
+POINTS_BY_NAME = 0
+POINTS_PCD = 1
+POINTS_PLY = 2
+POINTS_TEXT = 3
 
 TRACE_STRIDE = 32
 # trace record fields
@@ -133,6 +137,10 @@ def lib():
         L.cesa_save_rt.restype = _i
         L.cesa_load_rt.argtypes = [ctypes.c_char_p, _p, _p]
         L.cesa_load_rt.restype = _i
+        L.cesa_save_points.argtypes = [ctypes.c_char_p, _p, _i, _i]
+        L.cesa_save_points.restype = _i
+        L.cesa_transform_points.argtypes = [_p, _i, _p, _p]
+        L.cesa_transform_points.restype = _i
         for name in ("cesa_emicp_device", "cesa_softassign_device"):
             fn = getattr(L, name)
             fn.argtypes = [_p, _i, _p, _i, _p, _p, _p, _p]
@@ -310,8 +318,9 @@ def icp_device(dX, dY, dRt, param=None, d_nn=None, d_status=None, stream=None):
 
 
 def load_points(path):
-    """Points of a PLY (ASCII / binary) or text file as an (n, 3) float32
-    array, non-finite points dropped (the reference CLI's loadFile)."""
+    """Points of a PLY (ASCII / binary), PCD (ascii / binary /
+    binary_compressed) or text file as an (n, 3) float32 array, non-finite
+    points dropped (the reference CLI's loadFile)."""
     L = lib()
     buf = ctypes.POINTER(ctypes.c_float)()
     n = _i(0)
@@ -338,6 +347,21 @@ def align_scale_once(X, Y):
     b = np.ascontiguousarray(Y, dtype=np.float32).copy()
     _check(lib().cesa_align_scale_once(_ptr(a), len(a), _ptr(b), len(b)), "align_scale_once")
     return a, b
+
+
+def save_points(path, P, fmt=POINTS_BY_NAME):
+    """Writes (n, 3) points as ASCII PCD (PCL's savePCDFileASCII layout), ASCII
+    PLY or text; POINTS_BY_NAME picks by the extension."""
+    a = np.ascontiguousarray(P, dtype=np.float32).reshape(-1, 3)
+    _check(lib().cesa_save_points(os.fsencode(path), _ptr(a), len(a), int(fmt)), "save_points")
+
+
+def transform_points(P, R, t):
+    """R P + t per point in FP32 (the reference tools' pcl::transformPointCloud)."""
+    a = np.ascontiguousarray(P, dtype=np.float32).reshape(-1, 3).copy()
+    Rh, th = _pose_in(R, t)
+    _check(lib().cesa_transform_points(_ptr(a), len(a), _ptr(Rh), _ptr(th)), "transform_points")
+    return a
 
 
 def save_rt(path, R, t):

@@ -19,10 +19,14 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcesa.so")
 PEAKS_LIB = os.path.join(HERE, "libcesa_peaks.so")
 CLI = os.path.join(HERE, "cesa_register")
+TOOLS = os.path.join(HERE, "cesa_tools")
+TOOL_NAMES = ("add_rigid_transform", "merge", "pcd2ply")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE]
+# host code: no contraction into fused multiply-adds, so that it rounds the
+# same on x86_64 and aarch64 (gcc contracts by default on aarch64)
+NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE]
 SOURCES = ["cesa_api.cu", "cesa_emicp.cu", "cesa_softassign.cu", "cesa_noalloc.cu", "cesa_selftest.cu",
            "cesa_batch.cu", "cesa_softassign_mat.cu", "cesa_emicp_adjoint.cu",
            "cesa_softassign_adjoint.cu", "cesa_icp.cu", "cesa_io.cpp"]
@@ -88,20 +92,43 @@ def build(force=False, verbose=False):
     return LIB
 
 
-def build_cli(force=False):
-    """Compiles the cesa_register command line (host C++ over libcesa.so)."""
+def _build_exe(src_name, out, force):
+    """Compiles one host C++ executable over libcesa.so (found beside it)."""
     lib = build()
-    src = os.path.join(CSRC, "cesa_cli.cpp")
-    if not force and _mtime(CLI) >= max(_mtime(src), _mtime(lib), _mtime(os.path.join(INCLUDE, "cesa.h"))):
-        return CLI
-    tmp = CLI + ".tmp"
+    src = os.path.join(CSRC, src_name)
+    if not force and _mtime(out) >= max(_mtime(src), _mtime(lib), _mtime(os.path.join(INCLUDE, "cesa.h"))):
+        return out
+    tmp = out + ".tmp"
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-std=c++17", "-O2", "-I", INCLUDE, src, "-L", HERE, "-lcesa", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I", INCLUDE, src, "-L", HERE, "-lcesa",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError("g++ failed for cesa_cli.cpp:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, CLI)
-    return CLI
+        raise RuntimeError("g++ failed for %s:\n%s\n%s" % (src_name, r.stdout, r.stderr))
+    os.replace(tmp, out)
+    return out
+
+
+def build_cli(force=False):
+    """Compiles the cesa_register command line; returns its path."""
+    return _build_exe("cesa_cli.cpp", CLI, force)
+
+
+def build_tools(force=False):
+    """Compiles the point-cloud tools (one executable, cesa_tools) and links
+    the names it answers to beside it; returns {tool name: path}."""
+    exe = _build_exe("cesa_tools.cpp", TOOLS, force)
+    out = {}
+    for name in TOOL_NAMES:
+        path = os.path.join(HERE, name)
+        if os.path.islink(path) or os.path.exists(path):
+            if os.path.islink(path) and os.readlink(path) == os.path.basename(exe):
+                out[name] = path
+                continue
+            os.remove(path)
+        os.symlink(os.path.basename(exe), path)
+        out[name] = path
+    return out
 
 
 def build_peaks(force=False):
@@ -122,4 +149,5 @@ def build_peaks(force=False):
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
     print(build_cli(force="--force" in sys.argv))
+    print(build_tools(force="--force" in sys.argv))
     print(build_peaks(force="--force" in sys.argv))

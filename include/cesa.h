@@ -329,13 +329,32 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
  *     trace of each one's covariance (normalised by n) becomes 0.003.
  *   cesa_save_rt / cesa_load_rt: the reference's R, t text file ("%f " per
  *     entry, three per line, then t).
+ * cesa_load_points also reads PCD (PCL's format: DATA ascii, binary or
+ * binary_compressed), which the reference's loader reads through PCL.
+ *
+ * Writers and the rigid transform of the reference's point-cloud tools
+ * (src/add_rigid_transform.cpp, src/merge.cpp, src/pcd2ply.cpp):
+ *   cesa_save_points: format CESA_POINTS_PCD writes ASCII PCD as PCL's
+ *     savePCDFileASCII does (v0.7 header, FIELDS x y z, 8 significant
+ *     digits); CESA_POINTS_PLY ASCII PLY (vertex x, y, z float, 8 digits);
+ *     CESA_POINTS_TEXT "x y z" lines with 9 digits (exact for FP32);
+ *     CESA_POINTS_BY_NAME picks by the extension (.pcd, .ply, else text).
+ *   cesa_transform_points: p <- R p + t in place, R row-major; each product
+ *     and sum rounded in FP32, left to right, as pcl::transformPointCloud
+ *     with an Affine3f.
  */
+#define CESA_POINTS_BY_NAME 0
+#define CESA_POINTS_PCD 1
+#define CESA_POINTS_PLY 2
+#define CESA_POINTS_TEXT 3
 int cesa_load_points(const char* path, float** xyz, int* n);
 void cesa_free(void* p);
 int cesa_points_reduction(float* xyz, int* n, float percent, unsigned long long seed);
 int cesa_align_scale_once(float* xyz1, int n1, float* xyz2, int n2);
 int cesa_save_rt(const char* path, const float R[9], const float t[3]);
 int cesa_load_rt(const char* path, float R[9], float t[3]);
+int cesa_save_points(const char* path, const float* xyz, int n, int format);
+int cesa_transform_points(float* xyz, int n, const float R[9], const float t[3]);
 
 /* Releases cached device workspaces of the calling process. */
 void cesa_release_workspaces(void);
