@@ -29,6 +29,7 @@ CESA_ERR_NOALLOC_LIMIT = 7
 SINKHORN_AUTO = 0
 SINKHORN_MATRIX_FREE = 1
 SINKHORN_MATERIALISED = 2
+SINKHORN_BANDED = 3
 ICP_SEARCH_AUTO = 0
 ICP_SEARCH_EXHAUSTIVE = 1
 ICP_SEARCH_GRID = 2

@@ -29,8 +29,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE]
 SOURCES = ["cesa_api.cu", "cesa_emicp.cu", "cesa_softassign.cu", "cesa_noalloc.cu", "cesa_selftest.cu",
            "cesa_batch.cu", "cesa_softassign_mat.cu", "cesa_emicp_adjoint.cu",
-           "cesa_softassign_adjoint.cu", "cesa_icp.cu", "cesa_io.cpp"]
-HEADERS = ["cesa_common.cuh", "cesa_sweep.cuh", "cesa_pose.h", "cesa_kernels.h", "cesa_prep.cuh", "cesa_ops.cuh"]
+           "cesa_softassign_adjoint.cu", "cesa_icp.cu", "cesa_io.cpp", "cesa_softassign_band.cu"]
+HEADERS = ["cesa_common.cuh", "cesa_sweep.cuh", "cesa_pose.h", "cesa_kernels.h", "cesa_prep.cuh", "cesa_ops.cuh",
+           "cesa_sa_pose.cuh"]
 
 
 def nvcc():

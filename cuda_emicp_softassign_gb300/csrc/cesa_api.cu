@@ -161,7 +161,8 @@ cudaStream_t own_stream(int dev) {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-static_assert(kFormMatrixFree == CESA_SINKHORN_MATRIX_FREE && kFormMaterialised == CESA_SINKHORN_MATERIALISED,
+static_assert(kFormMatrixFree == CESA_SINKHORN_MATRIX_FREE && kFormMaterialised == CESA_SINKHORN_MATERIALISED &&
+                  kFormBanded == CESA_SINKHORN_BANDED,
               "Sinkhorn form values");
 
 // Sinkhorn form chosen per size by the tuner (cesa_tune_sinkhorn): measured
@@ -185,15 +186,20 @@ bool materialised_fits(int N, int M) {
   return k_bytes < 0.5 * (double)free_b;
 }
 
-// Form for a request; AUTO takes the tuner's decision for the size bucket,
-// else the matrix-free form (measured faster wherever the tuner has run on
-// GB300; the materialised form streams 28 bytes per element per update).
+// Form for a request. BANDED falls back to the matrix-free form where the
+// clouds do not fit it. AUTO takes the tuner's decision for the size bucket;
+// without one, the banded form where it fits and fills the GPU, else the
+// matrix-free form (the materialised form streams 28 bytes per element per
+// update and has not been faster on GB300).
 int resolve_form(int requested, int N, int M, int dev) {
   if (requested == CESA_SINKHORN_MATRIX_FREE) return kFormMatrixFree;
   if (requested == CESA_SINKHORN_MATERIALISED) return kFormMaterialised;
+  if (requested == CESA_SINKHORN_BANDED) return softassign_band_fits(N, M, dev) ? kFormBanded : kFormMatrixFree;
   auto it = g_tuned.find(TuneKey{dev, size_bucket(N), size_bucket(M)});
-  if (it != g_tuned.end() && (it->second != kFormMaterialised || materialised_fits(N, M))) return it->second;
-  return kFormMatrixFree;
+  if (it != g_tuned.end() && (it->second != kFormMaterialised || materialised_fits(N, M)) &&
+      (it->second != kFormBanded || softassign_band_fits(N, M, dev)))
+    return it->second;
+  return softassign_band_preferred(N, M, dev) ? kFormBanded : kFormMatrixFree;
 }
 
 // Shared body of the two host-pointer entry points.
@@ -967,9 +973,12 @@ int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float*
   for (auto& v : hx) v = next();
   for (auto& v : hy) v = next();
   const bool try_mat = materialised_fits(N, M);
+  const bool try_band = softassign_band_fits(N, M, dev);
   const size_t need_f = softassign_ws_need(N, M, kFormMatrixFree, dev);
   const size_t need_m = try_mat ? softassign_ws_need(N, M, kFormMaterialised, dev) : 0;
-  const size_t need = need_f > need_m ? need_f : need_m;
+  const size_t need_b = try_band ? softassign_ws_need(N, M, kFormBanded, dev) : 0;
+  size_t need = need_f > need_m ? need_f : need_m;
+  if (need_b > need) need = need_b;
   void* mem = nullptr;
   const size_t bx = align256(sizeof(float) * hx.size()), by = align256(sizeof(float) * hy.size());
   cudaError_t e = cudaMalloc(&mem, bx + by + 256 + need);
@@ -985,10 +994,10 @@ int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float*
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  float ms[2] = {-1.f, -1.f};
-  for (int f = 0; f < 2 && e == cudaSuccess; ++f) {
-    const int form = f == 0 ? kFormMatrixFree : kFormMaterialised;
-    if (form == kFormMaterialised && !try_mat) break;
+  float ms[3] = {-1.f, -1.f, -1.f};  // matrix-free, materialised, banded
+  for (int f = 0; f < 3 && e == cudaSuccess; ++f) {
+    const int form = f == 0 ? kFormMatrixFree : f == 1 ? kFormMaterialised : kFormBanded;
+    if ((form == kFormMaterialised && !try_mat) || (form == kFormBanded && !try_band)) continue;
     SoftassignLaunch L{};
     L.dX = dX;
     L.dY = dY;
@@ -1026,11 +1035,16 @@ int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float*
   cudaFree(mem);
   if (e != cudaSuccess) return map_cuda(e);
   if (rc) return rc;
-  // the materialised form also holds N x M floats: it must win by 10%
-  const int form = (ms[1] >= 0.f && ms[1] < 0.9f * ms[0]) ? kFormMaterialised : kFormMatrixFree;
+  // matrix-free arithmetic: the faster of its two decompositions; the
+  // materialised form also holds N x M floats: it must win by 10%
+  const bool band_wins = ms[2] >= 0.f && ms[2] < ms[0];
+  const float ms_free = band_wins ? ms[2] : ms[0];
+  const int form = (ms[1] >= 0.f && ms[1] < 0.9f * ms_free) ? kFormMaterialised
+                   : band_wins                               ? kFormBanded
+                                                             : kFormMatrixFree;
   g_tuned[TuneKey{dev, size_bucket(N), size_bucket(M)}] = form;
   if (form_out) *form_out = form;
-  if (ms_matrix_free) *ms_matrix_free = ms[0] * 0.5f;  // per pose update
+  if (ms_matrix_free) *ms_matrix_free = ms_free * 0.5f;  // per pose update
   if (ms_materialised) *ms_materialised = ms[1] >= 0.f ? ms[1] * 0.5f : -1.f;
   return CESA_OK;
 }

@@ -10,7 +10,7 @@
 //
 // Solves min ||X - (R Y + t)||. Additions (no counterpart in the reference):
 // -seed= (pointsReduction's seed; the reference seeds with the clock) and
-// -sinkhorn_form=auto|matrix_free|materialised. There is no viewer: the
+// -sinkhorn_form=auto|matrix_free|materialised|banded. There is no viewer: the
 // viewer flags are accepted and have no effect. -emicpcpu runs the GPU EM-ICP
 // (this build has no CPU registration path) and says so on stderr.
 #include <chrono>
@@ -120,6 +120,7 @@ int main(int argc, char** argv) {
   if (str_arg(argc, argv, "sinkhorn_form", form)) {
     if (form == "matrix_free") p.sinkhorn_form = CESA_SINKHORN_MATRIX_FREE;
     else if (form == "materialised") p.sinkhorn_form = CESA_SINKHORN_MATERIALISED;
+    else if (form == "banded") p.sinkhorn_form = CESA_SINKHORN_BANDED;
     else p.sinkhorn_form = CESA_SINKHORN_AUTO;
   }
   const unsigned long long seed = (unsigned long long)int_arg(argc, argv, "seed");

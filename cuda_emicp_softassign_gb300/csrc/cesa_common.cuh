@@ -192,6 +192,42 @@ __device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nb
   return s_ok != 0;
 }
 
+// ---------------------------------------------------------------- clusters
+// Barrier over all threads of every CTA of the thread-block cluster (every
+// thread must call it, convergently): release of this CTA's prior writes,
+// acquire of the peers'. It has no time limit, so a kernel calls it the same
+// number of times in every CTA of a cluster, whatever happens elsewhere.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Shared-memory address of `p` (a variable of this CTA's shared memory) in the
+// CTA of cluster rank `rank`.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, unsigned rank) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+  uint32_t b;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(b) : "r"(a), "r"(rank));
+  return b;
+}
+
+__device__ __forceinline__ float ld_dsmem(const float* p, unsigned rank) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(dsmem_addr(p, rank)) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ df ld_dsmem(const df* p, unsigned rank) {
+  df v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.hi), "=f"(v.lo) : "r"(dsmem_addr(p, rank)) : "memory");
+  return v;
+}
+
 // ---------------------------------------------------------------- TMA bulk copy
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));

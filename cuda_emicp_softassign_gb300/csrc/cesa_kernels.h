@@ -101,6 +101,7 @@ struct BatchLaunchPair {
 // Sinkhorn forms of SoftassignLaunch.form (the CESA_SINKHORN_* values).
 constexpr int kFormMatrixFree = 1;
 constexpr int kFormMaterialised = 2;
+constexpr int kFormBanded = 3;  // matrix-free arithmetic, one thread-block cluster per band of rows
 
 // Device workspace carved from one allocation (see api.cu).
 struct Workspace {
@@ -124,6 +125,13 @@ size_t emicp_ws_need(int N, int M, int device);
 size_t softassign_ws_need(int N, int M, int form, int device);
 size_t softassign_mat_ws_need(int N, int M, int device);
 int enqueue_softassign_mat(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
+// Banded form: fits when M <= 2048 and all nb = ceil(N / 64) clusters can be
+// resident at once; preferred (AUTO without a tuned decision) when it also
+// occupies at least half of the SMs and nb <= 48.
+bool softassign_band_fits(int N, int M, int device);
+bool softassign_band_preferred(int N, int M, int device);
+size_t softassign_band_ws_need(int N, int M, int device);
+int enqueue_softassign_band(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st, int* grid_used);
 
 // Batched registration: all pairs in one persistent launch.
 size_t batch_ws_need(const BatchLaunchPair* pairs, int npairs, int device);

@@ -153,6 +153,29 @@ struct FinalElem {
 //  0: sum w            1-3: sum w x'         4-12: sum w x'_i Vhat_j (i + 3j)
 // 13-15: sum Vhat       16-18: sum w mu x'    19: sum mu
 // 20-22: sum w^2 x'     23: sum w^2           24-26: sum w Vhat      27: sum w mu
+// One row's contribution to the 28 row-side moments (slots as listed above).
+template <int NV>
+__device__ __forceinline__ void sa_row_moments(df (&v)[NV], float w, float mu, const float (&V)[3],
+                                               const float (&xp)[3]) {
+  static_assert(NV >= 28, "28 row moments");
+  const float w2 = w * w, wmu = w * mu;
+  df_add(v[0], w);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    df_add_prod(v[1 + i], w, xp[i]);
+    const float wx = w * xp[i];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) df_add_prod(v[4 + i + 3 * j], wx, V[j]);
+    df_add(v[13 + i], V[i]);
+    df_add_prod(v[16 + i], wmu, xp[i]);
+    df_add_prod(v[20 + i], w2, xp[i]);
+    df_add_prod(v[24 + i], w, V[i]);
+  }
+  df_add(v[19], mu);
+  df_add_prod(v[23], w, w);
+  df_add_prod(v[27], w, mu);
+}
+
 struct FinalFin {
   const float4* rows;
   const float* a;  // a^(I1)
@@ -177,22 +200,7 @@ struct FinalFin {
 #pragma unroll
         for (int m = 0; m < 5; ++m) __stcg(tape_fin + (size_t)m * N + r, tot[m]);
       }
-      const float w2 = w * w, wmu = w * mu;
-      df_add(v[0], w);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        df_add_prod(v[1 + i], w, xp[i]);
-        const float wx = w * xp[i];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) df_add_prod(v[4 + i + 3 * j], wx, V[j]);
-        df_add(v[13 + i], V[i]);
-        df_add_prod(v[16 + i], wmu, xp[i]);
-        df_add_prod(v[20 + i], w2, xp[i]);
-        df_add_prod(v[24 + i], w, V[i]);
-      }
-      df_add(v[19], mu);
-      df_add_prod(v[23], w, w);
-      df_add_prod(v[27], w, mu);
+      sa_row_moments(v, w, mu, V, xp);
     }
     owned_block_sum<32>(v, scratch, rbpart + (size_t)blk * 32);
   }

@@ -32,6 +32,7 @@
 #include "cesa_ops.cuh"
 #include "cesa_pose.h"
 #include "cesa_prep.cuh"
+#include "cesa_sa_pose.cuh"
 
 namespace cesa {
 
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   __shared__ df s_tmp4[4];
   __shared__ OwnCache oc_rows, oc_cols;
   __shared__ float s_hdr[12];
-  __shared__ float s_S[9], s_xcp[3], s_yd[3], s_xc[3], s_yc[3];
+  __shared__ SaPoseScratch ps;
 
   const int tid = threadIdx.x;
   const unsigned G = gridDim.x;
@@ -412,66 +413,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       reduce_block_partials<32>(A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32,
                                 A.gr.nblk + A.gr.slices, s_red, s_tot);
       tl.mark(6);
-      // S_ij by threads 0..8, centres by threads 9..11, then the pose by thread 0.
-      if (tid < 12)
-        sa_moments_to_S(tid, s_tot, &s_hdr[0], &s_hdr[3], &s_hdr[6], s_S, s_xcp, s_yd, s_xc, s_yc);
-      __syncthreads();
-      if (tid == 0) {
-        const float* oX = &s_hdr[0];
-        const float* oY = &s_hdr[3];
-        float S[9], Xc[3], Yc[3], Xcp[3], Yd[3];
-        for (int k = 0; k < 9; ++k) S[k] = s_S[k];
-        for (int i = 0; i < 3; ++i) {
-          Xc[i] = s_xc[i];
-          Yc[i] = s_yc[i];
-          Xcp[i] = s_xcp[i];
-          Yd[i] = s_yd[i];
-        }
-        float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
-        horn_quaternion<float>(S, horn, q, &gap, &lmax);
-        // centred-frame translation t' = Xc' - R (Yc - oY)
-        quat_to_pose<float>(q, Xcp, Yd, Rn, tn);
-        for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];
-        for (int k = 0; k < 3; ++k) s_pose[9 + k] = tn[k];
-        if (blockIdx.x == 0) {
-          if (kTape) {  // the update's solve, for the adjoint
-            float* rec = A.tape_pose + (size_t)step * kSaTape;
-            rec[12] = s_tot[0].hi;
-            rec[13] = s_tot[0].lo;
-            for (int i = 0; i < 3; ++i) {
-              rec[14 + i] = Xc[i];
-              rec[17 + i] = Yc[i];
-              rec[20 + i] = Xcp[i];
-              rec[23 + i] = Yd[i];
-            }
-            for (int i = 0; i < 9; ++i) rec[26 + i] = S[i];
-            for (int i = 0; i < 4; ++i) rec[35 + i] = q[i];
-            for (int i = 0; i < 4; ++i)
-              for (int j = 0; j < 4; ++j) rec[39 + 4 * i + j] = horn.V[i][j];
-          }
-          if (A.trace && step < A.trace_cap) {
-            double* rec = A.trace + (size_t)step * 32;
-            float to[3];
-            pose_from_centred(Rn, tn, oX, oY, to);
-            rec[0] = step;
-            rec[1] = T;
-            rec[2] = df_dbl(s_tot[0]);
-            for (int i = 0; i < 3; ++i) {
-              rec[3 + i] = Xc[i];
-              rec[6 + i] = Yc[i];
-              rec[27 + i] = to[i];
-            }
-            for (int k = 0; k < 9; ++k) {
-              rec[9 + k] = S[k];
-              rec[18 + k] = Rn[k];
-            }
-            rec[30] = gap;
-            rec[31] = lmax;
-          }
-          A.ctl->steps_done = step + 1;
-        }
-      }
-      __syncthreads();
+      float* tape_rec = kTape ? A.tape_pose + (size_t)step * kSaTape : nullptr;
+      double* trace_rec = (A.trace && step < A.trace_cap) ? A.trace + (size_t)step * 32 : nullptr;
+      sa_pose_update(s_tot, s_hdr, ps, horn, s_pose, blockIdx.x == 0, tape_rec, trace_rec, step, T, A.ctl);
       tl.mark(7);
     }
     T = T * A.TFACTOR;  // FP32, src/softassign.cu:820
@@ -581,6 +525,7 @@ void softassign_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, fl
 
 size_t softassign_ws_need(int N, int M, int form, int device) {
   if (form == kFormMaterialised) return softassign_mat_ws_need(N, M, device);
+  if (form == kFormBanded) return softassign_band_ws_need(N, M, device);
   const SaPlan P = plan_sa(N, M, device);
   size_t total = 0;
   carve_sa(nullptr, P, N, M, &total);
@@ -590,6 +535,7 @@ size_t softassign_ws_need(int N, int M, int form, int device) {
 int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st,
                        int* grid_used) {
   if (L.form == kFormMaterialised) return enqueue_softassign_mat(L, ws, ws_bytes, st, grid_used);
+  if (L.form == kFormBanded) return enqueue_softassign_band(L, ws, ws_bytes, st, grid_used);
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return (int)e;

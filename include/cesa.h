@@ -40,6 +40,8 @@ typedef struct CUstream_st* cesa_stream_t;
 #define CESA_SINKHORN_AUTO 0         /* per-size choice by the built-in tuner */
 #define CESA_SINKHORN_MATRIX_FREE 1  /* scaling vectors, affinities recomputed per sweep */
 #define CESA_SINKHORN_MATERIALISED 2 /* affinity matrix stored once per inner iteration */
+#define CESA_SINKHORN_BANDED 3       /* matrix-free, one thread-block cluster per band of 64 rows
+                                        (M <= 2048 and all bands resident; else the matrix-free form) */
 
 /*
  * Registration parameters. The first twelve fields mirror
@@ -257,18 +259,21 @@ int cesa_find_rt_from_s(const float Xc[3], const float Yc[3], const float S[9], 
 int cesa_cloud2data(const float* points, int n, int stride_floats, float* soa_out);
 
 /*
- * Autotuner of the Softassign Sinkhorn form. Times both forms (two pose
+ * Autotuner of the Softassign Sinkhorn form. Times the forms (two pose
  * updates each, after a warm-up) on synthetic clouds of N and M points with
  * the schedule parameters of *p (NULL: defaults) on the current device, and
- * records the faster one for the size bucket (half-octaves of N and M).
- * Later calls with sinkhorn_form = CESA_SINKHORN_AUTO and sizes in that bucket
- * use it; without a recorded decision AUTO uses the matrix-free form. The
- * materialised form is skipped when its N x M matrix would take more than half
- * of the free device memory. Outputs (may be NULL): the chosen form and the
- * milliseconds per pose update of each form (-1 when not run). The
- * materialised form, which also holds the N x M matrix, is chosen only when it
- * is at least 10% faster. No counterpart in the reference, which has one
- * (materialised) form.
+ * records the fastest for the size bucket (half-octaves of N and M). Later
+ * calls with sinkhorn_form = CESA_SINKHORN_AUTO and sizes in that bucket use
+ * it. Without a recorded decision AUTO uses the banded form where it fits and
+ * its grid covers at least half of the SMs with at most 48 bands, else the
+ * matrix-free form. The materialised form is skipped when its N x M matrix
+ * would take more than half of the free device memory, the banded form where
+ * it does not fit. Outputs (may be NULL): the chosen form, the milliseconds
+ * per pose update of the matrix-free arithmetic (the faster of the
+ * matrix-free and banded decompositions) and of the materialised form (-1
+ * when not run). The materialised form, which also holds the N x M matrix, is
+ * chosen only when it is at least 10% faster. No counterpart in the
+ * reference, which has one (materialised) form.
  */
 int cesa_tune_sinkhorn(int N, int M, const cesa_params* p, int* form_out, float* ms_matrix_free,
                        float* ms_materialised);

@@ -101,9 +101,10 @@ def test_device_entry_point_and_determinism(cesa, torch_cuda):
 def test_tuner_records_a_decision_used_by_auto(cesa):
     from cuda_emicp_softassign_gb300 import workloads as W
     form, ms_free, ms_mat = cesa.tune_sinkhorn(1500, 1400)
-    assert form in (cesa.SINKHORN_MATRIX_FREE, cesa.SINKHORN_MATERIALISED)
+    # ms_free: the faster decomposition of the matrix-free arithmetic (grid or banded)
+    assert form in (cesa.SINKHORN_MATRIX_FREE, cesa.SINKHORN_MATERIALISED, cesa.SINKHORN_BANDED)
     assert ms_free > 0 and ms_mat > 0
-    assert form == (cesa.SINKHORN_MATERIALISED if ms_mat < 0.9 * ms_free else cesa.SINKHORN_MATRIX_FREE)
+    assert (form == cesa.SINKHORN_MATERIALISED) == (ms_mat < 0.9 * ms_free)
     X, Y, _, _ = W.surface_pair(n=1500, m=1400, seed=9)
     _, _, _, rep = cesa.softassign(X, Y, param=cesa.Params.default(JMAX=2), trace=True)
     assert rep.sinkhorn_form == form
