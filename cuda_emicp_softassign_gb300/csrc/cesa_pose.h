@@ -64,7 +64,7 @@ struct HornState {
 // One Jacobi rotation of the symmetric B in the (p,q) plane: computes (c, s)
 // that zero B[p][q] (Numerical-Recipes convention theta = (bqq-bpp)/(2 bpq)).
 template <typename T>
-CESA_HD bool jacobi_angle(T bpp, T bqq, T bpq, T tol, T& c, T& s) {
+CESA_HD bool jacobi_angle(T bpp, T bqq, T bpq, T tol, T& c, T& s, T& tmax) {
   if (t_abs(bpq) <= tol) {
     c = T(1);
     s = T(0);
@@ -77,6 +77,7 @@ CESA_HD bool jacobi_angle(T bpp, T bqq, T bpq, T tol, T& c, T& s) {
   const T den = t_abs(d) + r;
   T t = t_div(T(2) * bpq, den);
   if (d < T(0)) t = -t;
+  tmax = t_abs(t) > tmax ? t_abs(t) : tmax;
   c = t_rsqrt(T(1) + t * t);
   s = t * c;
   return true;
@@ -107,10 +108,10 @@ CESA_HD void jacobi_apply(T (&B)[4][4], T (&W)[4][4], T c, T s) {
 
 // Two disjoint rotations per round: {(0,1),(2,3)}, {(0,2),(1,3)}, {(0,3),(1,2)}.
 template <typename T, int P1, int Q1, int P2, int Q2>
-CESA_HD bool jacobi_round(T (&B)[4][4], T (&W)[4][4], T tol) {
+CESA_HD bool jacobi_round(T (&B)[4][4], T (&W)[4][4], T tol, T& tmax) {
   T c1, s1, c2, s2;
-  const bool r1 = jacobi_angle<T>(B[P1][P1], B[Q1][Q1], B[P1][Q1], tol, c1, s1);
-  const bool r2 = jacobi_angle<T>(B[P2][P2], B[Q2][Q2], B[P2][Q2], tol, c2, s2);
+  const bool r1 = jacobi_angle<T>(B[P1][P1], B[Q1][Q1], B[P1][Q1], tol, c1, s1, tmax);
+  const bool r2 = jacobi_angle<T>(B[P2][P2], B[Q2][Q2], B[P2][Q2], tol, c2, s2, tmax);
   if (r1) jacobi_apply<T, P1, Q1>(B, W, c1, s1);
   if (r2) jacobi_apply<T, P2, Q2>(B, W, c2, s2);
   return r1 || r2;
@@ -204,11 +205,16 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
     for (int j = 0; j < 4; ++j) scale = t_abs(N[i][j]) > scale ? t_abs(N[i][j]) : scale;
   const T eps = sizeof(T) == 4 ? T(1.2e-7) : T(2.3e-16);
   const T tol = T(4) * eps * scale + T(1e-37);
+  // A sweep whose rotations all have |tan| < sqrt(eps) leaves off-diagonal
+  // entries of order tan^2 (relative): the next sweep would change nothing
+  // above round-off, so it is not run.
+  const T tquad = sizeof(T) == 4 ? T(3.4e-4) : T(1.5e-8);
   for (int sweep = 0; sweep < 16; ++sweep) {
-    bool rot = jacobi_round<T, 0, 1, 2, 3>(B, W, tol);
-    rot = jacobi_round<T, 0, 2, 1, 3>(B, W, tol) || rot;
-    rot = jacobi_round<T, 0, 3, 1, 2>(B, W, tol) || rot;
-    if (!rot) break;
+    T tmax = T(0);
+    bool rot = jacobi_round<T, 0, 1, 2, 3>(B, W, tol, tmax);
+    rot = jacobi_round<T, 0, 2, 1, 3>(B, W, tol, tmax) || rot;
+    rot = jacobi_round<T, 0, 3, 1, 2>(B, W, tol, tmax) || rot;
+    if (!rot || tmax < tquad) break;
   }
   // V <- V W, then one Newton-Schulz step V <- V (3I - V^T V)/2
   T V2[4][4], G[4][4];

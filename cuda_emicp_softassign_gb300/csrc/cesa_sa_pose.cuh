@@ -22,10 +22,11 @@ struct SaPoseScratch {
 __device__ __forceinline__ void sa_pose_update(const df* s_tot, const float* s_hdr, SaPoseScratch& ps,
                                                HornState<float>& horn, float* s_pose, bool leads,
                                                float* tape_rec, double* trace_rec, int step, float T,
-                                               Ctl* ctl) {
+                                               Ctl* ctl, Timeline* tl = nullptr) {
   const int tid = threadIdx.x;
   if (tid < 12) sa_moments_to_S(tid, s_tot, &s_hdr[0], &s_hdr[3], &s_hdr[6], ps.S, ps.xcp, ps.yd, ps.xc, ps.yc);
   __syncthreads();
+  if (tl) tl->mark(13);
   if (tid == 0) {
     const float* oX = &s_hdr[0];
     const float* oY = &s_hdr[3];

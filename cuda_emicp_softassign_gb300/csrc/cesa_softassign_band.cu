@@ -21,8 +21,9 @@
 //    completes the pass (cs, b, u) itself.
 //  - Final row sweep: w, mu and Vhat over the tile, added across the cluster;
 //    the band's rows are finalised by the cluster's CTAs in 64 / CS row
-//    shares; their 28 row moments (and in band 0 the 4 column moments of the
-//    tiles) are added across the cluster by rank 0 into one record per band.
+//    shares and the tiles' columns in shares c = band (mod nb); their 28 row
+//    and 4 column moments are added across the cluster by rank 0 into one
+//    record per band.
 //    One grid barrier, then every CTA reduces the nb records and solves the
 //    pose.
 // Per pose update: I1 + 1 grid barriers and I1 + 2 cluster barriers, against
@@ -60,7 +61,7 @@ struct BandArgs {
   float* cs_out;
   float* w_out;
   float* pc;           // column-pass partials [2][nb][Mp] (by pass parity)
-  df* mom;             // [2][nb][32] moment records per band (band 0 also holds the column moments)
+  df* mom;             // [2][nb][32] moment records per band
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -80,6 +81,13 @@ constexpr int kRowPairs = kBandRows / 64;
 constexpr int kColPairs = kTileCols / 64;
 constexpr int kMaxCluster = 8;
 constexpr int kBandRed = kMaxAcc * kBandRows > kTileCols ? kMaxAcc * kBandRows : kTileCols;
+// The tile's affinities K[c][r], computed by the first row pass of every
+// inner iteration and read by its other 2 I1 sweeps (K depends on the pose and
+// T only). Column stride 65: the row sweeps read 32 consecutive rows of a
+// column, the column sweeps one row of 32 columns 65 apart, both without bank
+// conflicts.
+constexpr int kKld = kBandRows + 1;
+static_assert(kWarps * kBandRed * sizeof(float) >= (32 * 32 + 32 * kWarps) * 8, "moment scratch");
 
 struct __align__(16) BandSmem {
   float4 xr[kBandRows];   // the band's rows x' (fixed)
@@ -91,21 +99,53 @@ struct __align__(16) BandSmem {
   float b[kTileCols], u[kTileCols], cs[kTileCols];  // tile columns
   float xpart[2][kMaxAcc][kBandRows];               // this CTA's row partials, read by the cluster
   df mrec[32];                                      // this CTA's moments, read by rank 0
-  float red[kWarps * kBandRed];                     // cross-warp reduction scratch
+  float red[kWarps * kBandRed];                     // cross-warp reduction scratch (also 32 x 40 dfs)
+  float K[kTileCols * kKld];                        // the tile's affinities, column-major
 };
 
-// acc += elem over the streamed points [0, len) of sa (and sb); the 8 warps
-// split the points and every lane evaluates its P owned pairs.
-template <int NACC, int P, class Elem>
-__device__ __forceinline__ void band_sweep(const Elem& e, const float2 (&q)[P][3], const float4* sa,
-                                           const float4* sb, int len, float2 (&acc)[P][NACC]) {
-  const int warp = threadIdx.x >> 5;
+// Row sweeps over the cached K: acc (rows lane, lane + 32) += K[c][r] w_c over
+// the streamed columns c < len (w_c: the .w of sw[c], and for NACC = 5 also
+// the second stream h[c]). With `store`, K is computed (e = 2^(cK + nk d^2),
+// as in SinkElem) and written to the cache instead of read.
+template <int NACC, bool kStore>
+__device__ __forceinline__ void band_row_sweep(float* K, const float2 (&q)[3], float nk, float cK, const float4* sw,
+                                               const float4* h, int len, float2 (&acc)[NACC]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll 2
   for (int c = warp; c < len; c += kWarps) {
-    const float4 a = sa[c];
-    const float4 b = sb ? sb[c] : a;
+    const float4 y = sw[c];
+    float2 e;
+    if (kStore) {
+      e = ex2_pair(__ffma2_rn(dist2_pair(q, y), dup2(nk), dup2(cK)));
+      K[c * kKld + lane] = e.x;
+      K[c * kKld + lane + 32] = e.y;
+    } else {
+      e = make_float2(K[c * kKld + lane], K[c * kKld + lane + 32]);
+    }
+    acc[0] = __ffma2_rn(e, dup2(y.w), acc[0]);
+    if (NACC == 5) {
+      const float4 g = h[c];
+      acc[1] = __ffma2_rn(e, dup2(g.w), acc[1]);
+      acc[2] = __ffma2_rn(e, dup2(g.x), acc[2]);
+      acc[3] = __ffma2_rn(e, dup2(g.y), acc[3]);
+      acc[4] = __ffma2_rn(e, dup2(g.z), acc[4]);
+    }
+  }
+}
+
+// Column sweep over the cached K: acc (columns lane + 64 k, lane + 64 k + 32)
+// += K[c][r] a_r over the streamed rows r < len (a_r: the .w of sx[r]).
+__device__ __forceinline__ void band_col_sweep(const float* K, const float4* sx, int len,
+                                               float2 (&acc)[kColPairs][1]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 2
+  for (int r = warp; r < len; r += kWarps) {
+    const float a = sx[r].w;
 #pragma unroll
-    for (int k = 0; k < P; ++k) e(acc[k], q[k], a, b);
+    for (int k = 0; k < kColPairs; ++k) {
+      const float2 e = make_float2(K[(lane + 64 * k) * kKld + r], K[(lane + 64 * k + 32) * kKld + r]);
+      acc[k][0] = __ffma2_rn(e, dup2(a), acc[k][0]);
+    }
   }
 }
 
@@ -161,16 +201,15 @@ __device__ __forceinline__ void band_complete_columns(const BandArgs& A, BandSme
   const int tid = threadIdx.x;
   if (tid < Wt) {
     const float* P = pc_pass + c0 + tid;
+    // the first 32 band partials all in flight before the first add (adding
+    // the zeros of absent bands leaves the sum unchanged), then the rest
+    float v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = j < A.nb ? __ldcg(P + (size_t)j * A.Mp) : 0.f;
     float sum = 0.f;
-    int i = 0;
-    for (; i + 8 <= A.nb; i += 8) {
-      float v[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = __ldcg(P + (size_t)(i + j) * A.Mp);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) sum += v[j];
-    }
-    for (; i < A.nb; ++i) sum += __ldcg(P + (size_t)i * A.Mp);
+    for (int j = 0; j < 32; ++j) sum += v[j];
+    for (int i = 32; i < A.nb; ++i) sum += __ldcg(P + (size_t)i * A.Mp);
     const float bo = kk >= 1 ? sm.b[tid] : 1.f, uo = sm.u[tid];
     const float csv = fmaf(bo, sum, uo);
     const float bn = bo / csv;
@@ -188,49 +227,55 @@ __device__ __forceinline__ void band_complete_columns(const BandArgs& A, BandSme
 }
 
 // Sum over the CTA of the final moments, into dst[32] (shared), in a fixed
-// order: v[0..27] are non-zero only in threads 0..rows-1 (the CTA's row
-// share), v[28..31] only when cols is set (band 0: every thread may hold a
-// column). Shuffle levels are spent only where values are: log2(rows) levels
-// in the first rows / 32 warps for the row moments, a full tree of all warps
-// for the 4 column moments. Synchronises the block.
-__device__ __forceinline__ void band_moment_sum(df (&v)[32], int rows, bool cols, df* red, df* dst) {
+// order. v[] is non-zero only in threads 0..active-1 (the CTA's share of the
+// band's rows and of the tiles' columns). Up to 32 active threads (every
+// cluster of 2 or more CTAs with nb >= 8), through shared memory; else only the
+// first active / 32 warps reduce by shuffles, level-major in groups of values.
+// Synchronises the block.
+__device__ __forceinline__ void band_moment_sum(df (&v)[32], int active, df* red, df* scratch, df* dst) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int row_warps = (rows + 31) >> 5;
-  int top = 1;  // the smallest power of two >= min(rows, 32)
-  while (top < rows && top < 32) top <<= 1;
-  if (warp < row_warps) {
-    // level-major within groups of 7 values: a level's shuffles are
-    // independent and overlap, and few values are in flight at once
+  if (active <= 32) {
+    // through shared memory: value k of entry i at scratch[k * 32 + i]; thread
+    // (k, g) = (tid % 32, tid / 32) adds entries g, g + 8, ... in order, then
+    // thread k adds the 8 group sums in order
+    df* part = scratch + 32 * 32;
+    if ((int)threadIdx.x < active)
 #pragma unroll
-    for (int g = 0; g < 28; g += 7)
+      for (int k = 0; k < 32; ++k) scratch[k * 32 + threadIdx.x] = v[k];
+    __syncthreads();
+    df sg = df_make(0.f);
+    for (int i = warp; i < active; i += kWarps) df_add(sg, scratch[lane * 32 + i]);
+    part[lane * kWarps + warp] = sg;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      df s = part[threadIdx.x * kWarps];
+#pragma unroll
+      for (int w = 1; w < kWarps; ++w) df_add(s, part[threadIdx.x * kWarps + w]);
+      dst[threadIdx.x] = s;
+    }
+    __syncthreads();
+    return;
+  }
+  const int nw = (active + 31) >> 5;
+  int top = 1;  // the smallest power of two >= min(active, 32)
+  while (top < active && top < 32) top <<= 1;
+  if (warp < nw) {
+#pragma unroll
+    for (int g = 0; g < 32; g += 8)
       for (int off = top >> 1; off > 0; off >>= 1) {
 #pragma unroll
-        for (int k = g; k < g + 7; ++k) {
+        for (int k = g; k < g + 8; ++k) {
           const df o = df_shfl_down(v[k], off);
           df_add(v[k], o);
         }
       }
     if (lane == 0)
 #pragma unroll
-      for (int k = 0; k < 28; ++k) red[k * kWarps + warp] = v[k];
-  }
-  if (cols) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-      for (int k = 28; k < 32; ++k) {
-        const df o = df_shfl_down(v[k], off);
-        df_add(v[k], o);
-      }
-    }
-    if (lane == 0)
-#pragma unroll
-      for (int k = 28; k < 32; ++k) red[k * kWarps + warp] = v[k];
+      for (int k = 0; k < 32; ++k) red[k * kWarps + warp] = v[k];
   }
   __syncthreads();
   if (threadIdx.x < 32) {
     const int k = threadIdx.x;
-    const int nw = k < 28 ? row_warps : (cols ? kWarps : 0);
     df s = df_make(0.f);
     for (int w = 0; w < nw; ++w) df_add(s, red[k * kWarps + w]);
     dst[k] = s;
@@ -301,7 +346,6 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
     const float kk2 = kLog2e / T;
     const float nk = -kk2;
     const float cK = fmaf(A.alpha, kk2, -0.5f * log2f(T));
-    const SinkElem se{nk, cK};
     for (int iter0 = 0; iter0 < A.I0; ++iter0, ++step) {
       tl.mark(1);
       float R[9], tc[3];
@@ -317,20 +361,26 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
                               : zero4;
       }
       __syncthreads();
-      float2 qy[kColPairs][3];  // the tile's transformed columns, owned in column sweeps
-      own_pairs(sm.ys, qy);
       for (int k = 0; k < A.I1; ++k) {
-        if (k >= 1)
+        if (k >= 1) {
           band_complete_columns(A, sm, A.pc + (size_t)((cpass - 1u) & 1u) * pc_stride, k - 1, c0, Wt, false,
                                 nullptr);
+          tl.mark(14);
+        }
         // row pass k: sum over the tile of K b, added across the cluster
         float2 acc[kRowPairs][1];
 #pragma unroll
         for (int q = 0; q < kRowPairs; ++q) acc[q][0] = make_float2(0.f, 0.f);
-        if (ok) band_sweep<1>(se, qx, sm.ys, nullptr, Wt, acc);
+        if (ok) {
+          if (k == 0)  // K for this inner iteration, into the cache
+            band_row_sweep<1, true>(sm.K, qx[0], nk, cK, sm.ys, nullptr, Wt, acc[0]);
+          else
+            band_row_sweep<1, false>(sm.K, qx[0], nk, cK, sm.ys, nullptr, Wt, acc[0]);
+        }
         float tot[1];
         band_reduce<1>(sm.red, acc, tot);
         if (tid < kBandRows) sm.xpart[xpar][0][tid] = tot[0];
+        tl.mark(15);
         cluster_sync_all();
         tl.mark(8);
         // completion (normalizeMbySinkhorn_row + Saxpy, src/softassign.cu:538-561):
@@ -360,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
         float2 acc2[kColPairs][1];
 #pragma unroll
         for (int q = 0; q < kColPairs; ++q) acc2[q][0] = make_float2(0.f, 0.f);
-        if (ok) band_sweep<1>(se, qy, sm.xs, nullptr, Hb, acc2);
+        if (ok) band_col_sweep(sm.K, sm.xs, Hb, acc2);
         band_reduce<1>(sm.red, acc2, tot);
         if (tid < Wt) __stcg(A.pc + (size_t)(cpass & 1u) * pc_stride + (size_t)band * A.Mp + c0 + tid, tot[0]);
         ++cpass;
@@ -372,13 +422,12 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
       band_complete_columns(A, sm, A.pc + (size_t)((cpass - 1u) & 1u) * pc_stride, A.I1 - 1, c0, Wt, true,
                             &s_hdr[6]);
       tl.mark(2);
-      const FinalElem fe{nk, cK};
       float2 acc5[kRowPairs][5];
 #pragma unroll
       for (int q = 0; q < kRowPairs; ++q)
 #pragma unroll
         for (int m = 0; m < 5; ++m) acc5[q][m] = make_float2(0.f, 0.f);
-      if (ok) band_sweep<5>(fe, qx, sm.ys, sm.ys2, Wt, acc5);
+      if (ok) band_row_sweep<5, false>(sm.K, qx[0], nk, cK, sm.ys, sm.ys2, Wt, acc5[0]);
       float tot5[5];
       band_reduce<5>(sm.red, acc5, tot5);
       if (tid < kBandRows) {
@@ -420,9 +469,13 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
           sa_row_moments(v, w, mu, V, xp);
         }
       }
-      if (col_rec && tid < Wt) {  // band 0: the column moments sum cs, sum cs y' of the tile
-        const float csv = sm.cs[tid];
-        const float4 y = sm.yc[tid];
+      // the column moments sum cs, sum cs y' of the tile's columns c = band
+      // (mod nb), so that every band takes a share of them
+      const int ncols = Wt > band ? (Wt - band + A.nb - 1) / A.nb : 0;
+      if (tid < ncols) {
+        const int c = band + tid * A.nb;
+        const float csv = sm.cs[c];
+        const float4 y = sm.yc[c];
         df_add(v[28], csv);
         df_add_prod(v[29], csv, y.x);
         df_add_prod(v[30], csv, y.y);
@@ -430,8 +483,11 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
       }
       xpar ^= 1;
       tl.mark(11);
-      band_moment_sum(v, max(0, min((kBandRows + CS - 1) / CS, Hb - (int)rank * ((kBandRows + CS - 1) / CS))),
-                      col_rec, s_red, sm.mrec);
+      {
+        const int share = (kBandRows + CS - 1) / CS;
+        const int nrows = max(0, min(share, Hb - (int)rank * share));
+        band_moment_sum(v, max(nrows, ncols), s_red, reinterpret_cast<df*>(sm.red), sm.mrec);
+      }
       tl.mark(12);
       cluster_sync_all();
       tl.mark(10);
@@ -453,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
         reduce_block_partials<32>(rec, A.nb, s_red, s_tot);
         tl.mark(6);
         double* trace_rec = (A.trace && step < A.trace_cap) ? A.trace + (size_t)step * 32 : nullptr;
-        sa_pose_update(s_tot, s_hdr, ps, horn, s_pose, blockIdx.x == 0, nullptr, trace_rec, step, T, A.ctl);
+        sa_pose_update(s_tot, s_hdr, ps, horn, s_pose, blockIdx.x == 0, nullptr, trace_rec, step, T, A.ctl, &tl);
       }
       tl.mark(7);
     }
