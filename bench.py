@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0,
                     help="target seconds of CPU work for the CPU-baseline sample")
-    ap.add_argument("--sinkhorn-form", default="auto", choices=["auto", "matrix_free", "materialised"],
+    ap.add_argument("--sinkhorn-form", default="auto", choices=["auto", "matrix_free", "materialised", "banded"],
                     help="Softassign Sinkhorn form (auto: the library's recorded choice for the size, "
                          "matrix-free when none)")
     ap.add_argument("--tune", action="store_true",
@@ -85,7 +85,8 @@ class RefDefaults:
     maxIteration = 30
 
 
-FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2}
+FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2, "banded": 3}
+FORM_NAMES = {1: "matrix_free", 2: "materialised", 3: "banded"}
 
 
 def params_for(cesa, kind, form="auto"):
@@ -131,9 +132,12 @@ def algorithmic_work(kind, N, M, p):
     return e * n * (8.0 * sweeps + 12.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
 
 
-def kernels_per_registration(kind):
-    # prep_center + 2 x prep_pack (+ 2 x fill for the slack vectors) + the persistent kernel
-    return 6 if kind == "softassign" else 4
+def kernels_per_registration(kind, form=None):
+    # prep_center + 2 x prep_pack (+ 2 x fill for the slack vectors) + the persistent kernel;
+    # the banded Softassign kernel initialises the slack itself
+    if kind == "softassign" and form != "banded":
+        return 6
+    return 4
 
 
 class ClockSampler:
@@ -574,7 +578,7 @@ def run_ours(args, rank, world, local):
     tuned = None
     if kind == "softassign" and args.tune:
         f, ms_free, ms_mat = cesa.tune_sinkhorn(N, M, p)  # records the choice used by "auto"
-        tuned = {"chosen": "materialised" if f == 2 else "matrix_free",
+        tuned = {"chosen": FORM_NAMES.get(f, "matrix_free"),
                  "ms_per_update_matrix_free": ms_free, "ms_per_update_materialised": ms_mat}
     dev_call = {"emicp": cesa.emicp_device, "softassign": cesa.softassign_device, "icp": cesa.icp_device}[kind]
 
@@ -669,10 +673,21 @@ def run_ours(args, rank, world, local):
                         "sequence (prep kernels included)"}
     form_used = None
     if kind == "softassign":
-        if args.sinkhorn_form != "auto":
-            form_used = args.sinkhorn_form
-        else:
-            form_used = tuned["chosen"] if tuned else "matrix_free"
+        # the form the library resolved for this request (AUTO: tuned or by size), as it reports it
+        import copy
+        q = copy.copy(p)
+        q.JMAX = 1
+        rep = cesa.softassign(X, Y, param=q, trace=True)[3]
+        form_used = FORM_NAMES.get(rep.sinkhorn_form, str(rep.sinkhorn_form))
+    if form_used == "banded":
+        roofline["note"] += (". The banded form computes each affinity once per inner iteration and "
+                             "keeps the tile in shared memory for the other 2*I1 sweeps, so it executes "
+                             "fewer operations than this per-sweep count: per element and pose update 1 ex2 "
+                             "and %d FP32 ops (the first row sweep 8, each later Sinkhorn sweep 1, the final "
+                             "sweep 5)" % (8 + (2 * p.I1 - 1) + 5))
+        roofline["kernel"] = "softassign_band_kernel"
+        roofline["executed_fp32_ops_per_registration"] = float(N) * float(M) * pose_updates(kind, p) * (
+            8 + (2 * p.I1 - 1) + 5)
     if form_used == "materialised":
         hbm_peak = None
         try:
@@ -689,7 +704,7 @@ def run_ours(args, rank, world, local):
                             "each of the 2*I1 later passes, per pose update) / event time"}
     traffic_file = os.path.join(HERE, "profiles", "ncu_traffic.json")
     if os.path.exists(traffic_file):
-        key = args.workload + (":materialised" if form_used == "materialised" else "")
+        key = args.workload + (":" + form_used if form_used in ("materialised", "banded") else "")
         entry = json.load(open(traffic_file)).get(key)
         if entry:
             roofline["traffic"] = entry["bytes_per_launch"]
@@ -708,7 +723,7 @@ def run_ours(args, rank, world, local):
             "e2e": {"value": whole_job_rate(args.steps, world, e2e_s), "unit": "registrations/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * 4},
             "clocks": clocks,
-            "gpu_launches": kernels_per_registration(kind) * args.steps,
+            "gpu_launches": kernels_per_registration(kind, form_used) * args.steps,
             "wall_s_timed_region": t_wall}
     if kind == "softassign":
         line["config"]["sinkhorn_form"] = form_used
@@ -741,7 +756,14 @@ def run_ours(args, rank, world, local):
                               "ms_per_step": total_ms / args.steps, "exhaustive_ms_per_step": exh_s * 1e3,
                               "note": "both searches are exact and return the same matches"}
     if not args.no_adjoint and kind != "icp":
-        line["adjoint"] = measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0)
+        adj = measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0)
+        if kind == "softassign" and form_used != "matrix_free":
+            # the tape comes from the matrix-free kernel; against the forward this
+            # request actually runs (value's form) the ratio is higher
+            fwd_auto = total_ms / args.steps
+            adj["fwd_%s_ms" % form_used] = fwd_auto
+            adj["fwd_plus_bwd_over_fwd_%s" % form_used] = (adj["fwd_taped_ms"] + adj["bwd_ms"]) / fwd_auto
+        line["adjoint"] = adj
     print(json.dumps(line), flush=True)
 
 

@@ -18,7 +18,8 @@
 namespace cesa {
 
 constexpr int kStatusOk = 0;
-constexpr int kStatusTimeout = 3;  // == CESA_ERR_TIMEOUT
+constexpr int kStatusTimeout = 3;      // == CESA_ERR_TIMEOUT
+constexpr int kStatusUnsupported = 6;  // == CESA_ERR_UNSUPPORTED (a launch shape the kernel cannot run)
 
 constexpr float kLog2e = 1.4426950408889634f;
 
@@ -204,6 +205,18 @@ __device__ __forceinline__ void cluster_sync_all() {
 __device__ __forceinline__ unsigned cluster_ctarank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned cluster_id_x() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
   return r;
 }
 

@@ -295,8 +295,16 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
 
   const int tid = threadIdx.x;
   const int CS = A.CS;
+  // The kernel reads its peers' shared memory at ranks 0..CS-1: a launch whose
+  // clusters do not hold CS CTAs (the same answer in every CTA of a cluster)
+  // records an error and leaves before any cluster barrier or remote access.
+  if (cluster_nctarank() != (unsigned)CS || cluster_id_x() >= (unsigned)A.nb) {
+    if (tid == 0) set_status(A.ctl, kStatusUnsupported, 70);
+    if (tid == 0 && blockIdx.x == 0 && A.d_status) *A.d_status = kStatusUnsupported;
+    return;
+  }
   const unsigned rank = cluster_ctarank();
-  const int band = (int)blockIdx.x / CS;
+  const int band = (int)cluster_id_x();
   const int r0 = band * kBandRows, c0 = (int)rank * A.W;
   const int Hb = min(kBandRows, A.N - r0);
   const int Wt = max(0, min(A.W, A.M - c0));

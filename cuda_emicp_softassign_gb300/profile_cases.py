@@ -4,7 +4,9 @@ twice, so that a profiler can skip the first launch):
     python -m cuda_emicp_softassign_gb300.profile_cases <case>
 
 cases:
-  c2_one      softassign_kernel: one config-2 registration (N = M = 2000, default schedule)
+  c2_one      softassign_band_kernel: one config-2 registration (N = M = 2000, default schedule,
+              the form AUTO picks: banded)
+  c2_one_mf   softassign_kernel: the same with the grid-wide matrix-free form
   c3_short    emicp_kernel: config 3 (N = M = 40097) with sigma_inf = 2e-3 (first 16 sigma steps)
   batch_mid   batch_kernel: the first 64 config-4 pairs, EM-ICP to sigma_inf = 5e-3,
               Softassign with JMAX = 1, I0 = 2
@@ -26,6 +28,15 @@ def c2_one():
     _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
     for _ in range(2):
         C.softassign(X, Y)
+
+
+def c2_one_mf():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
+    p = C.Params.default(sinkhorn_form=C.SINKHORN_MATRIX_FREE)
+    for _ in range(2):
+        C.softassign(X, Y, param=p)
 
 
 def c3_short():
@@ -112,7 +123,7 @@ def icp_grid_20000():
     _icp(2)  # CESA_ICP_SEARCH_GRID
 
 
-CASES = {f.__name__: f for f in (c2_one, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
                                   icp_grid_20000)}
 
 if __name__ == "__main__":
