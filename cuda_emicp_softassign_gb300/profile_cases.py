@@ -7,6 +7,9 @@ cases:
   c2_one      softassign_band_kernel: one config-2 registration (N = M = 2000, default schedule,
               the form AUTO picks: banded)
   c2_one_mf   softassign_kernel: the same with the grid-wide matrix-free form
+  c2_timeline softassign_band_kernel's in-kernel phase timeline on config 2 (JMAX = 4, 20 pose
+              updates): prints the mean duration of each phase of a pose update in block 0 and the
+              spread over blocks (no profiler; %globaltimer marks written by thread 0 of every block)
   c3_short    emicp_kernel: config 3 (N = M = 40097) with sigma_inf = 2e-3 (first 16 sigma steps)
   batch_mid   batch_kernel: the first 64 config-4 pairs, EM-ICP to sigma_inf = 5e-3,
               Softassign with JMAX = 1, I0 = 2
@@ -37,6 +40,29 @@ def c2_one_mf():
     p = C.Params.default(sinkhorn_form=C.SINKHORN_MATRIX_FREE)
     for _ in range(2):
         C.softassign(X, Y, param=p)
+
+
+def c2_timeline():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
+    p = C.Params.default(JMAX=4, sinkhorn_form=C.SINKHORN_BANDED)
+    C.softassign(X, Y, param=p)
+    _, _, tl, rep = C.softassign(X, Y, param=p, timeline=256 * 800)
+    rows = C.timeline_table(tl, rep.grid_blocks)
+    names = {1: "start", 2: "final: last column pass completed", 3: "row pass completed (cluster)",
+             4: "column sweep + partial store (final: record store)", 5: "grid barrier", 6: "moment records reduced",
+             7: "Horn solve", 8: "cluster barrier (final sweep included after 2)", 10: "moments: cluster barrier",
+             11: "final rows finalised", 12: "moments summed", 13: "S formed",
+             14: "column pass completed (band partials)", 15: "row sweep + warp reduction"}
+    b0 = rows[rows[:, 0] == 0][:, 1:]
+    starts = np.where(b0[:, 0] == 1)[0]
+    segs = [b0[a:b + 1] for a, b in zip(starts[1:-1], starts[2:])]
+    print("form %d, grid %d, pose update (block 0, mean of %d): %.0f ns"
+          % (rep.sinkhorn_form, rep.grid_blocks, len(segs), np.mean([s[-1, 1] - s[0, 1] for s in segs])))
+    for i in range(1, len(segs[0])):
+        d = np.mean([s[i, 1] - s[i - 1, 1] for s in segs])
+        print("  %2d  %-42s %6.0f ns" % (i, names.get(int(segs[0][i, 0]), "next update"), d))
 
 
 def c3_short():
@@ -123,7 +149,7 @@ def icp_grid_20000():
     _icp(2)  # CESA_ICP_SEARCH_GRID
 
 
-CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
                                   icp_grid_20000)}
 
 if __name__ == "__main__":
