@@ -9,7 +9,10 @@
 // (host C ABI). The device path keeps the previous step's eigenbasis V and
 // starts each solve from B = V^T N V. Consecutive annealing steps change N
 // only slightly, so one or two sweeps reach FP32 round-off. Each solve
-// re-orthonormalises V with one Newton-Schulz step.
+// re-orthonormalises V with one Newton-Schulz step. Kernels that need no
+// eigenbasis (no adjoint tape) first try a certified shifted inverse
+// iteration from the previous quaternion (horn_quaternion_fast), several
+// times cheaper, and fall back to the Jacobi solve.
 #pragma once
 #include <math.h>
 
@@ -276,6 +279,163 @@ CESA_HD int horn_quaternion(const T S[9], HornState<T>& st, T q[4], T* gap, T* l
   if (gap) *gap = t_div(l1 - l2, t_abs(l1) > T(1e-30) ? t_abs(l1) : T(1e-30));
   if (lmax) *lmax = l1;
   return 0;
+}
+
+// Cholesky factor L (lower) of a symmetric 4x4 A, with the reciprocals of its
+// diagonal in rd. False when a pivot is not positive and finite, i.e. when A
+// is not (numerically) positive definite.
+template <typename T>
+CESA_HD bool chol4(const T (&A)[4][4], T (&L)[4][4], T (&rd)[4]) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    T d = A[j][j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= L[j][k] * L[j][k];
+    if (!(d > T(0)) || !t_finite(d)) return false;
+    const T r = t_rsqrt(d);
+    rd[j] = r;
+    L[j][j] = d * r;
+#pragma unroll
+    for (int i = j + 1; i < 4; ++i) {
+      T v = A[i][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) v -= L[i][k] * L[j][k];
+      L[i][j] = v * r;
+    }
+  }
+  return true;
+}
+
+// x = (L L^T)^-1 b, normalised to unit length.
+template <typename T>
+CESA_HD void chol4_solve_unit(const T (&L)[4][4], const T (&rd)[4], const T (&b)[4], T (&x)[4]) {
+  T y[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    T v = b[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) v -= L[i][k] * y[k];
+    y[i] = v * rd[i];
+  }
+#pragma unroll
+  for (int i = 3; i >= 0; --i) {
+    T v = y[i];
+#pragma unroll
+    for (int k = i + 1; k < 4; ++k) v -= L[k][i] * x[k];
+    x[i] = v * rd[i];
+  }
+  const T inv = t_rsqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x[i] *= inv;
+}
+
+// Shifted A = sigma I - N - c v v^T (c < 0 deflates v out of N's spectrum).
+template <typename T>
+CESA_HD void shifted4(const T (&N)[4][4], T sigma, T c, const T (&v)[4], T (&A)[4][4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) A[i][j] = (i == j ? sigma : T(0)) - N[i][j] - c * v[i] * v[j];
+}
+
+// Top eigenvector of the symmetric N by shifted inverse iteration from q0, a
+// unit vector near it (the previous pose update's quaternion). The shift
+// lambda(q0) + 2e-5 max|N| is tried first (a warm q0 is close enough that it
+// lies above the top eigenvalue); where that matrix does not factor, one step
+// with lambda(q0) + 1e-3 max|N| comes first. A shift that factors (sigma I - N
+// positive definite) lies above the largest eigenvalue, so the iteration
+// converges to its eigenvector: one solve, a second when the residual is not
+// yet at round-off. The result is certified, else refused (false): with r the
+// residual N v - lambda v, the Davis-Kahan bound sin(angle to the true
+// eigenvector) <= |r| / gap holds, and the gap is certified by factoring
+// (lambda - g) I - (N - (lambda + max|N|) v v^T), N with v deflated out of its
+// spectrum: positive definite exactly when every other eigenvalue is below
+// lambda - g. g is set so that the bound is 4e-6 (and at
+// least 2% of max|N|). Typically two 4x4 Cholesky factorisations and one
+// solve.
+template <typename T>
+CESA_HD bool horn_top_inverse(const T (&N)[4][4], const T (&q0)[4], T (&q)[4], T* lmax) {
+  T scale = T(0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) scale = t_abs(N[i][j]) > scale ? t_abs(N[i][j]) : scale;
+  if (!(scale > T(1e-30)) || !t_finite(scale)) return false;
+  T v[4], x[4], Nv[4], A[4][4], L[4][4], rd[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = q0[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) Nv[i] = N[i][0] * v[0] + N[i][1] * v[1] + N[i][2] * v[2] + N[i][3] * v[3];
+  T lam = v[0] * Nv[0] + v[1] * Nv[1] + v[2] * Nv[2] + v[3] * Nv[3];
+  shifted4<T>(N, lam + T(2e-5) * scale, T(0), v, A);
+  if (!chol4<T>(A, L, rd)) {
+    shifted4<T>(N, lam + T(1e-3) * scale, T(0), v, A);
+    if (!chol4<T>(A, L, rd)) return false;
+    chol4_solve_unit<T>(L, rd, v, x);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Nv[i] = N[i][0] * x[0] + N[i][1] * x[1] + N[i][2] * x[2] + N[i][3] * x[3];
+    lam = x[0] * Nv[0] + x[1] * Nv[1] + x[2] * Nv[2] + x[3] * Nv[3];
+    shifted4<T>(N, lam + T(2e-5) * scale, T(0), x, A);
+    if (!chol4<T>(A, L, rd)) return false;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = x[i];
+  }
+  T rn = T(0);
+  for (int it = 0; it < 2; ++it) {
+    chol4_solve_unit<T>(L, rd, v, x);
+    // residual and Rayleigh quotient of x
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Nv[i] = N[i][0] * x[0] + N[i][1] * x[1] + N[i][2] * x[2] + N[i][3] * x[3];
+    lam = x[0] * Nv[0] + x[1] * Nv[1] + x[2] * Nv[2] + x[3] * Nv[3];
+    T r2 = T(0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const T ri = Nv[i] - lam * x[i];
+      r2 += ri * ri;
+    }
+    rn = r2 * t_rsqrt(r2 > T(0) ? r2 : T(1e-37));
+    if (rn <= T(4e-6) * T(0.02) * scale) break;  // already within the bound at the smallest gap
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = x[i];
+  }
+  T g = rn / T(4e-6);
+  if (g < T(0.02) * scale) g = T(0.02) * scale;
+  shifted4<T>(N, lam - g, -(lam + scale), x, A);
+  if (!chol4<T>(A, L, rd) || !t_finite(lam)) return false;
+  // the sign that continues the previous quaternion
+  const T s = x[0] * q0[0] + x[1] * q0[1] + x[2] * q0[2] + x[3] * q0[3] < T(0) ? T(-1) : T(1);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = s * x[i];
+  if (lmax) *lmax = lam;
+  return true;
+}
+
+// Horn's top eigenvector for the plain forward kernels: the certified inverse
+// iteration from the previous quaternion (st.q), else the warm-started Jacobi
+// of horn_quaternion (whose basis st.V it then refreshes). gap is reported
+// only by the Jacobi path; the inverse iteration writes -1 (its certificate
+// is gap >= 2% of max|N|). Returns 1 when N is not finite (st.q kept).
+template <typename T>
+CESA_HD int horn_quaternion_fast(const T S[9], HornState<T>& st, T q[4], T* gap, T* lmax) {
+  T N[4][4];
+  horn_matrix<T>(S, N);
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) finite = finite && t_finite(N[i][j]);
+  if (finite) {
+    T q0[4], qq[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q0[i] = st.q[i];
+    if (horn_top_inverse<T>(N, q0, qq, lmax)) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) q[i] = st.q[i] = qq[i];
+      if (gap) *gap = T(-1);
+      return 0;
+    }
+  }
+  return horn_quaternion<T>(S, st, q, gap, lmax);
 }
 
 // Adjoint of the pose update (R, t) = (R(q), Xc - R(q) Yc) with q the top

@@ -12,17 +12,27 @@ struct SaPoseScratch {
   float S[9], xcp[3], yd[3], xc[3], yc[3];
 };
 
+// The certified solve as a call of its own: one thread runs it while the
+// block waits, and outside the kernel's inlined code it gets its own register
+// allocation instead of the sweeps' spills.
+static __device__ __noinline__ void horn_fast_call(const float* S, HornState<float>* st, float* q, float* gap,
+                                                   float* lmax) {
+  horn_quaternion_fast<float>(S, *st, q, gap, lmax);
+}
+
 // Block-wide (every thread calls it). s_tot: the 32 moments; s_hdr: oX, oY,
 // mean(Y') (centring header). Threads 0..8 form S and threads 9..11 the
 // centres; thread 0 then solves Horn's problem (warm-started eigenbasis in
 // `horn`) and writes the next centred pose to s_pose. In the block that
 // `leads`, it also writes the adjoint's record (tape_rec, kSaTape floats, when
 // given), the trace record (trace_rec, 32 doubles, when given) and the step
-// count.
+// count. `fast` selects the certified inverse iteration (horn_quaternion_fast,
+// no eigenbasis for an adjoint; the trace's gap is then -1) over the Jacobi
+// solve that the taped kernels need.
 __device__ __forceinline__ void sa_pose_update(const df* s_tot, const float* s_hdr, SaPoseScratch& ps,
                                                HornState<float>& horn, float* s_pose, bool leads,
                                                float* tape_rec, double* trace_rec, int step, float T,
-                                               Ctl* ctl, Timeline* tl = nullptr) {
+                                               Ctl* ctl, Timeline* tl = nullptr, bool fast = false) {
   const int tid = threadIdx.x;
   if (tid < 12) sa_moments_to_S(tid, s_tot, &s_hdr[0], &s_hdr[3], &s_hdr[6], ps.S, ps.xcp, ps.yd, ps.xc, ps.yc);
   __syncthreads();
@@ -39,7 +49,10 @@ __device__ __forceinline__ void sa_pose_update(const df* s_tot, const float* s_h
       Yd[i] = ps.yd[i];
     }
     float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
-    horn_quaternion<float>(S, horn, q, &gap, &lmax);
+    if (fast)
+      horn_fast_call(S, &horn, q, &gap, &lmax);
+    else
+      horn_quaternion<float>(S, horn, q, &gap, &lmax);
     // centred-frame translation t' = Xc' - R (Yc - oY)
     quat_to_pose<float>(q, Xcp, Yd, Rn, tn);
     for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];

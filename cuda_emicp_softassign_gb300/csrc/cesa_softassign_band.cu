@@ -517,7 +517,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
         reduce_block_partials<32>(rec, A.nb, s_red, s_tot);
         tl.mark(6);
         double* trace_rec = (A.trace && step < A.trace_cap) ? A.trace + (size_t)step * 32 : nullptr;
-        sa_pose_update(s_tot, s_hdr, ps, horn, s_pose, blockIdx.x == 0, nullptr, trace_rec, step, T, A.ctl, &tl);
+        sa_pose_update(s_tot, s_hdr, ps, horn, s_pose, blockIdx.x == 0, nullptr, trace_rec, step, T, A.ctl, &tl,
+                       true);
       }
       tl.mark(7);
     }

@@ -16,6 +16,21 @@ int pose_sequence_f32(const float* S, int K, float* q_out, float* gap_out) {
   }
   return fallbacks;
 }
+// The same with the plain kernels' solver (certified inverse iteration, Jacobi
+// fallback); returns the number of solves that fell back to Jacobi.
+int pose_sequence_fast_f32(const float* S, int K, float* q_out, float* lmax_out) {
+  cesa::HornState<float> st;
+  st.reset();
+  int jacobi = 0;
+  for (int k = 0; k < K; ++k) {
+    float q[4], gap = 0.f, lmax = 0.f;
+    cesa::horn_quaternion_fast<float>(S + 9 * k, st, q, &gap, &lmax);
+    jacobi += gap >= 0.f;
+    for (int i = 0; i < 4; ++i) q_out[4 * k + i] = q[i];
+    lmax_out[k] = lmax;
+  }
+  return jacobi;
+}
 int pose_sequence_f64(const double* S, int K, double* q_out, double* gap_out) {
   cesa::HornState<double> st;
   st.reset();

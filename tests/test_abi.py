@@ -245,6 +245,58 @@ def test_device_pose_solver_fp32_warm_start(pose_harness, oracle):
     assert worst < 1e-4, worst
 
 
+def _fast_sequence(pose_harness, S32):
+    K = len(S32)
+    q = np.zeros((K, 4), np.float32)
+    lmax = np.zeros(K, np.float32)
+    jac = pose_harness.pose_sequence_fast_f32(np.ascontiguousarray(S32).ctypes.data_as(ctypes.c_void_p), K,
+                                              q.ctypes.data_as(ctypes.c_void_p), lmax.ctypes.data_as(ctypes.c_void_p))
+    return q, lmax, jac
+
+
+def test_fast_pose_solver_warm_sequence(pose_harness, oracle):
+    """The plain kernels' solver (certified shifted inverse iteration from the
+    previous quaternion, Jacobi fallback) over the same annealing-like
+    sequence: as accurate as the Jacobi path, and it falls back only where the
+    previous quaternion is far (the first solve)."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    rng = np.random.default_rng(9)
+    K = 200
+    base = rng.standard_normal((3, 3)) * 0.05
+    S32 = np.array([(W._rot([1.0, 2.0, 0.5], np.radians(40.0 * k / K)) * (1.0 + 0.3 * np.sin(k / 7.0)) + base)
+                    .reshape(-1, order="F") for k in range(K)], np.float32)
+    q, lmax, jac = _fast_sequence(pose_harness, S32)
+    assert jac <= 2, jac
+    worst = 0.0
+    for k in range(K):
+        Ro, _, info = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), S32[k].astype(np.float64))
+        worst = max(worst, rot_err_deg(_quat_R(q[k].astype(np.float64)), Ro))
+    assert worst < 1e-4, worst
+
+
+def test_fast_pose_solver_refuses_what_it_cannot_certify(pose_harness, oracle):
+    """Jumps of 90 degrees between solves and near-degenerate top eigenvalues
+    (S = diag(1, 0.2, -0.2): N = diag(1, 1, -0.6, -1.4), plus 1e-7 noise) are
+    refused by the inverse iteration and solved by the Jacobi fallback, still
+    matching the FP64 oracle wherever its own gap is resolvable."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    rng = np.random.default_rng(11)
+    jumps = np.array([W._rot(rng.standard_normal(3), np.radians(90.0 * (k % 2))).reshape(-1, order="F")
+                      for k in range(20)], np.float32)
+    q, _, jac = _fast_sequence(pose_harness, jumps)
+    assert jac >= 10, jac
+    for k in range(20):
+        Ro, _, _ = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), jumps[k].astype(np.float64))
+        assert rot_err_deg(_quat_R(q[k].astype(np.float64)), Ro) < 1e-3
+    near = []
+    for k in range(20):
+        A = np.diag([1.0, 0.2, -0.2]) + 1e-7 * rng.standard_normal((3, 3))
+        near.append(A.reshape(-1, order="F"))
+    near = np.array(near, np.float32)
+    q, _, jac = _fast_sequence(pose_harness, near)
+    assert jac == 20, jac
+
+
 def test_device_pose_solver_random_cold(pose_harness, oracle):
     rng = np.random.default_rng(10)
     for _ in range(100):
