@@ -81,8 +81,12 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   }
   __syncthreads();
 
-  __shared__ HornState<float> horn;  // carried eigenbasis (thread 0)
-  if (tid == 0) horn.reset();
+  __shared__ HornState<float> horn;       // the pose's solver state (thread 0)
+  __shared__ HornState<float> horn_tape;  // block 0 with a tape: the eigenbasis for the adjoint
+  if (tid == 0) {
+    horn.reset();
+    horn_tape.reset();
+  }
   Pipe pipe;
   pipe_init(pipe);
   unsigned epoch = 0;
@@ -121,9 +125,15 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
       float Xc[3], Yc[3], S[9];
       em_moments_to_S(s_tot, Xc, Yc, S);
       float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
-      horn_quaternion<float>(S, horn, q, &gap, &lmax);
+      // the pose: certified inverse iteration (Jacobi fallback); the same with
+      // and without a tape, so that both forwards agree bitwise
+      horn_quaternion_fast<float>(S, horn, q, &gap, &lmax);
       quat_to_pose<float>(q, Xc, Yc, Rn, tn);
       if (A.tape && blockIdx.x == 0) {  // the step's inputs and solve for the adjoint
+        // the adjoint's eigenbasis, from a Jacobi solve of the same S on its own
+        // state (it does not feed back into the pose)
+        float qj[4], gj = 0.f, lj = 0.f;
+        horn_quaternion<float>(S, horn_tape, qj, &gj, &lj);
         float* rec = A.tape + (size_t)step * kEmTape;
         for (int k = 0; k < 12; ++k) rec[k] = s_pose[k];
         rec[12] = s2;
@@ -132,7 +142,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
           rec[17 + 2 * k] = s_tot[k].lo;
         }
         for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 4; ++j) rec[48 + 4 * i + j] = horn.V[i][j];
+          for (int j = 0; j < 4; ++j) rec[48 + 4 * i + j] = horn_tape.V[i][j];
         for (int k = 0; k < 4; ++k) rec[64 + k] = q[k];
       }
       for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];

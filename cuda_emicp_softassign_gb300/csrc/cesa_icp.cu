@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, 2) icp_kernel(const IcpArgs A) {
           S[i + 3 * j] = df_val(a);
         }
       float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
-      horn_quaternion<float>(S, horn, q, &gap, &lmax);
+      horn_quaternion_fast<float>(S, horn, q, &gap, &lmax);
       quat_to_pose<float>(q, Xc, Ym, Rn, tn);  // centred frame: t' = Xc' - R Ym
       for (int k = 0; k < 9; ++k) s_pose[k] = Rn[k];
       for (int k = 0; k < 3; ++k) s_pose[9 + k] = tn[k];
