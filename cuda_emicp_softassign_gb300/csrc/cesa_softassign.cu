@@ -72,20 +72,37 @@ struct SoftArgs {
   float* tape_fin;     // optional [nsteps][5][N]
 };
 
-// Sum of the S slice partials of point i (deferred completion), 8 loads in flight.
-__device__ __forceinline__ float slice_sum(const float* part, int S, int ld, int i) {
-  float s = 0.f;
+// Sums of the S slice partials of points i0 and i1 (i1 only when has1), the
+// deferred completion: each point's partials are added in slice order, and a
+// batch's loads for both points (8 each) are in flight before the first add.
+__device__ __forceinline__ void slice_sum2(const float* part, int S, int ld, int i0, int i1, bool has1, float& s0,
+                                           float& s1) {
+  s0 = 0.f;
+  s1 = 0.f;
   int k = 0;
   for (; k + 8 <= S; k += 8) {
-    float v[8];
+    float v0[8], v1[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = __ldcg(part + (size_t)(k + j) * ld + i);
+    for (int j = 0; j < 8; ++j) v0[j] = __ldcg(part + (size_t)(k + j) * ld + i0);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) s += v[j];
+    for (int j = 0; j < 8; ++j) v1[j] = has1 ? __ldcg(part + (size_t)(k + j) * ld + i1) : 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s0 += v0[j];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s1 += v1[j];
   }
-  for (; k < S; ++k) s += __ldcg(part + (size_t)k * ld + i);
-  return s;
+  for (; k < S; ++k) {
+    const float a = __ldcg(part + (size_t)k * ld + i0);
+    const float b = has1 ? __ldcg(part + (size_t)k * ld + i1) : 0.f;
+    s0 += a;
+    s1 += b;
+  }
 }
+
+// Each thread of a prep step takes points threadIdx.x and threadIdx.x +
+// kThreads of the chunk: their loads are issued together (one L2 round trip
+// per chunk instead of two).
+static_assert(kChunk == 2 * kThreads, "two streamed points per thread in a prep step");
 
 // Completion of a column pass for column c, done by whoever streams c next
 // (normalizeMbySinkhorn_col + Saxpy, src/softassign.cu:579-597):
@@ -101,10 +118,8 @@ struct ColDone {
   float* cs_out;
   float* tape = nullptr;  // optional [4][M]: b_new, u_new, cs, column sum
   int M = 0;
-  __device__ __forceinline__ void operator()(int c, bool store, float& bn, float& csv) const {
-    const float sum = slice_sum(pc, S, ld, c);
-    const float bo = b_old ? __ldcg(b_old + c) : 1.f;
-    const float uo = __ldcg(u_old + c);
+  __device__ __forceinline__ void finish(int c, bool store, float sum, float bo, float uo, float& bn,
+                                         float& csv) const {
     csv = fmaf(bo, sum, uo);
     bn = bo / csv;
     if (store) {
@@ -120,6 +135,18 @@ struct ColDone {
       }
     }
   }
+  // columns c0 and c1 (when has1), all loads issued before either is finished
+  __device__ __forceinline__ void pair(int c0, int c1, bool has1, bool store, float& bn0, float& csv0, float& bn1,
+                                       float& csv1) const {
+    float sum0, sum1;
+    slice_sum2(pc, S, ld, c0, c1, has1, sum0, sum1);
+    const float bo0 = b_old ? __ldcg(b_old + c0) : 1.f;
+    const float uo0 = __ldcg(u_old + c0);
+    const float bo1 = has1 ? (b_old ? __ldcg(b_old + c1) : 1.f) : 1.f;
+    const float uo1 = has1 ? __ldcg(u_old + c1) : 1.f;
+    finish(c0, store, sum0, bo0, uo0, bn0, csv0);
+    if (has1) finish(c1, store, sum1, bo1, uo1, bn1, csv1);
+  }
 };
 
 // Streamed Y columns for Sinkhorn row sweeps: (R y' + t', b_c). b_c := 1 in
@@ -130,16 +157,22 @@ struct RowPrep {
   ColDone cd;
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const float4 y = sm.raw[stage][c];
-      float w = 1.f, csv;
-      if (!fresh) cd(first + c, blk == 0, w, csv);
-      sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
-                               R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w);
+    const int c0 = threadIdx.x, c1 = threadIdx.x + kThreads;
+    if (c0 < len) {
+      const bool h1 = c1 < len;
+      float w0 = 1.f, w1 = 1.f, cs0, cs1;
+      if (!fresh) cd.pair(first + c0, first + c1, h1, blk == 0, w0, cs0, w1, cs1);
+      put(sm, stage, c0, w0);
+      if (h1) put(sm, stage, c1, w1);
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.raw2[stage]};
+  }
+  __device__ __forceinline__ void put(SweepSmem& sm, int stage, int c, float w) const {
+    const float4 y = sm.raw[stage][c];
+    sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
+                             R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
+                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w);
   }
   __device__ __forceinline__ void unit_end(int, int) const {}
 };
@@ -159,30 +192,40 @@ struct ColPrep {
   int N = 0;
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const int r = first + c;
-      const float4 x = sm.raw[stage][c];
-      const float sum = slice_sum(pr, S, ld, r);
-      const float ao = a_old ? __ldcg(a_old + r) : 1.f;
-      const float so = __ldcg(s_old + r);
-      const float rsv = fmaf(ao, sum, so);
-      const float an = ao / rsv;
-      if (blk == 0) {
-        const float sn = so / rsv;
-        __stcg(a_new + r, an);
-        __stcg(s_new + r, sn);
-        __stcg(rs_out + r, rsv);
-        if (tape) {
-          __stcg(tape + r, an);
-          __stcg(tape + (size_t)N + r, sn);
-          __stcg(tape + 2 * (size_t)N + r, rsv);
-          __stcg(tape + 3 * (size_t)N + r, sum);
-        }
-      }
-      sm.prep[c] = make_float4(x.x, x.y, x.z, an);
+    const int c0 = threadIdx.x, c1 = threadIdx.x + kThreads;
+    if (c0 < len) {
+      const bool h1 = c1 < len;
+      const int r0 = first + c0, r1 = first + c1;
+      float sum0, sum1;
+      slice_sum2(pr, S, ld, r0, r1, h1, sum0, sum1);
+      const float ao0 = a_old ? __ldcg(a_old + r0) : 1.f;
+      const float so0 = __ldcg(s_old + r0);
+      const float ao1 = h1 ? (a_old ? __ldcg(a_old + r1) : 1.f) : 1.f;
+      const float so1 = h1 ? __ldcg(s_old + r1) : 1.f;
+      row_done(sm, stage, c0, r0, sum0, ao0, so0, blk);
+      if (h1) row_done(sm, stage, c1, r1, sum1, ao1, so1, blk);
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.raw2[stage]};
+  }
+  __device__ __forceinline__ void row_done(SweepSmem& sm, int stage, int c, int r, float sum, float ao, float so,
+                                           int blk) const {
+    const float4 x = sm.raw[stage][c];
+    const float rsv = fmaf(ao, sum, so);
+    const float an = ao / rsv;
+    if (blk == 0) {
+      const float sn = so / rsv;
+      __stcg(a_new + r, an);
+      __stcg(s_new + r, sn);
+      __stcg(rs_out + r, rsv);
+      if (tape) {
+        __stcg(tape + r, an);
+        __stcg(tape + (size_t)N + r, sn);
+        __stcg(tape + 2 * (size_t)N + r, rsv);
+        __stcg(tape + 3 * (size_t)N + r, sum);
+      }
+    }
+    sm.prep[c] = make_float4(x.x, x.y, x.z, an);
   }
   __device__ __forceinline__ void unit_end(int, int) const {}
 };
@@ -202,26 +245,31 @@ struct FinalPrep {
   df* colrec;   // this update's column records [S_c][32] (slots 28..31 used)
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
-    for (int c = threadIdx.x; c < len; c += kThreads) {
-      const float4 y = sm.raw[stage][c];
-      float bn, csv;
-      cd(first + c, blk == 0, bn, csv);
-      const float g = bn * csv;
-      sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
-                               R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                               R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn);
-      sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]),
-                                bn * (csv - 1.f));
-      if (blk == 0) {
-        df* a = colacc + threadIdx.x * 4;
-        df_add(a[0], csv);
-        df_add_prod(a[1], csv, y.x);
-        df_add_prod(a[2], csv, y.y);
-        df_add_prod(a[3], csv, y.z);
-      }
+    const int c0 = threadIdx.x, c1 = threadIdx.x + kThreads;
+    if (c0 < len) {
+      const bool h1 = c1 < len;
+      float bn0, cs0, bn1, cs1;
+      cd.pair(first + c0, first + c1, h1, blk == 0, bn0, cs0, bn1, cs1);
+      put(sm, stage, c0, bn0, cs0, blk);  // c0 before c1: the running sums' order
+      if (h1) put(sm, stage, c1, bn1, cs1, blk);
     }
     __syncthreads();
     return PrepOut{sm.prep, sm.prep2};
+  }
+  __device__ __forceinline__ void put(SweepSmem& sm, int stage, int c, float bn, float csv, int blk) const {
+    const float4 y = sm.raw[stage][c];
+    const float g = bn * csv;
+    sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
+                             R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
+                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn);
+    sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]), bn * (csv - 1.f));
+    if (blk == 0) {
+      df* a = colacc + threadIdx.x * 4;
+      df_add(a[0], csv);
+      df_add_prod(a[1], csv, y.x);
+      df_add_prod(a[2], csv, y.y);
+      df_add_prod(a[3], csv, y.z);
+    }
   }
   __device__ __forceinline__ void unit_end(int blk, int sl) const {
     if (blk != 0) return;  // uniform per unit

@@ -10,6 +10,7 @@ cases:
   c2_timeline softassign_band_kernel's in-kernel phase timeline on config 2 (JMAX = 4, 20 pose
               updates): prints the mean duration of each phase of a pose update in block 0 and the
               spread over blocks (no profiler; %globaltimer marks written by thread 0 of every block)
+  c5_update   softassign_kernel: config 5 (N = M = 20000), matrix-free form, one pose update
   c3_short    emicp_kernel: config 3 (N = M = 40097) with sigma_inf = 2e-3 (first 16 sigma steps)
   batch_mid   batch_kernel: the first 64 config-4 pairs, EM-ICP to sigma_inf = 5e-3,
               Softassign with JMAX = 1, I0 = 2
@@ -63,6 +64,15 @@ def c2_timeline():
     for i in range(1, len(segs[0])):
         d = np.mean([s[i, 1] - s[i - 1, 1] for s in segs])
         print("  %2d  %-42s %6.0f ns" % (i, names.get(int(segs[0][i, 0]), "next update"), d))
+
+
+def c5_update():
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c5_softassign_20000", seed=0)
+    p = C.Params.default(JMAX=1, I0=1, sinkhorn_form=C.SINKHORN_MATRIX_FREE)
+    for _ in range(2):
+        C.softassign(X, Y, param=p)
 
 
 def c3_short():
@@ -149,7 +159,7 @@ def icp_grid_20000():
     _icp(2)  # CESA_ICP_SEARCH_GRID
 
 
-CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c5_update, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
                                   icp_grid_20000)}
 
 if __name__ == "__main__":
