@@ -17,9 +17,11 @@ from conftest import rel_err, rot_err_deg, soa_tensor
 pytestmark = pytest.mark.gpu
 
 
-# every cluster size (1, 2, 4, 8 column tiles), ragged bands and tiles
+# every cluster size (1, 2, 4, 8 column tiles), ragged bands and tiles; 4100 x 60:
+# 65 bands of one CTA (more than 32 band partials per column, 64 active rows in
+# the moment sum)
 @pytest.mark.parametrize("n,m", [(300, 300), (257, 129), (77, 500), (1000, 31), (130, 100), (600, 2048),
-                                 (2000, 1100), (2000, 2000)])
+                                 (2000, 1100), (2000, 2000), (4100, 60)])
 @pytest.mark.parametrize("T", [100.0, 0.7])
 def test_inner_iteration_matches_oracle(cesa, oracle, torch_cuda, n, m, T):
     from cuda_emicp_softassign_gb300 import workloads as W
@@ -106,7 +108,8 @@ def test_ragged_sizes_are_orthonormal_and_finite_where_the_oracle_is(cesa, oracl
     decays to zero): t is NaN in the FP64 oracle too, and must be here."""
     from cuda_emicp_softassign_gb300 import workloads as W
     p = cesa.Params.default(JMAX=3, sinkhorn_form=cesa.SINKHORN_BANDED)
-    for n, m in ((1, 1), (2, 3), (129, 33), (33, 129), (64, 256), (65, 257), (513, 1), (1, 2048), (2200, 1900)):
+    for n, m in ((1, 1), (2, 3), (129, 33), (33, 129), (64, 256), (65, 257), (513, 1), (1, 2048), (2200, 1900),
+                 (4100, 60)):
         X, Y, _, _ = W.uniform_pair(n=n, m=m, seed=n + m, max_deg=10.0, t_range=0.03)
         R, t, _, rep = cesa.softassign(X, Y, param=p, trace=True)
         assert rep.sinkhorn_form == cesa.SINKHORN_BANDED, (n, m)
