@@ -301,9 +301,10 @@ def _dptr(t):
 
 
 def icp(X, Y, R=None, t=None, param=None, trace=False):
-    """ICP on the GPU, maxIteration iterations of exhaustive nearest-neighbour
-    matching and Horn's pose (replaces icp(), src/icp.cpp:122-290, whose FLANN
-    search is approximate). Returns (R, t), or (R, t, trace, report)."""
+    """ICP on the GPU, maxIteration iterations of exact nearest-neighbour
+    matching (a uniform grid over the target, or exhaustive: param.icp_search)
+    and Horn's pose (replaces icp(), src/icp.cpp:122-290, whose FLANN search is
+    approximate). Returns (R, t), or (R, t, trace, report)."""
     return _host_call("cesa_icp", X, Y, R, t, param or Params.default(), trace)
 
 
