@@ -36,9 +36,9 @@ struct EmicpArgs {
   int nsteps;
   const CenterHdr* hdr;
   float* dRt;           // PoseIO in/out, caller frame
-  float* part;          // split partials [nblk*S][5][128]
-  unsigned* cnt;        // [nblk]
-  df* rbpart;           // [2][nblk][kEmNV] moments per owned block (step parity)
+  float* part;          // row partials [5][S][Mp] (accumulator, column slice, row)
+  int Mp;
+  df* rbpart;           // [2][grid][kEmNV] moments per block (step parity)
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -104,22 +104,75 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
     __syncthreads();
 
-    // e = exp(-d2 / (2 s2)) = 2^(nk d2)
+    // e = exp(-d2 / (2 s2)) = 2^(nk d2). Every unit stores its rows' partial
+    // sums over its column slice (deferred: no completion counter).
     const EmicpElem elem{-kLog2e / (2.f * s2)};
-    df* rb = A.rbpart + (size_t)(step & 1) * A.geo.nblk * kEmNV;
-    const EmicpFin fin{A.rows,    A.M,
-                       outlier,   {s_hdr[6], s_hdr[7], s_hdr[8]},
-                       A.row_out, {s_hdr[0], s_hdr[1], s_hdr[2]},
-                       reinterpret_cast<df*>(sm.prep), rb,
-                       A.row_tape ? A.row_tape + (size_t)step * A.M * 5 : nullptr};
-    if (!sweep_units<5>(sm, pipe, A.geo, src, A.rows, true, R, tc, (unsigned)step, A.part, A.cnt,
-                        elem, NoPrep{}, fin, A.ctl, A.timeout_ns, 10, tl, 0, &oc_rows))
+    if (!sweep_units<5, EmicpElem, NoPrep, NoFin, true>(sm, pipe, A.geo, src, A.rows, true, R, tc, 0u, A.part,
+                                                         nullptr, elem, NoPrep{}, NoFin{}, A.ctl, A.timeout_ns, 10,
+                                                         tl, A.Mp, &oc_rows))
       break;
-
-    // ---- grid-wide moments -> pose (every block computes the same pose)
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
     tl.mark(5);
-    reduce_block_partials<kEmNV>(rb, A.geo.nblk, s_red, s_tot);
+
+    // ---- rows completed, each block a contiguous share of them; its 16
+    // moments are one record. Thread t first sums the slice partials of
+    // (row, accumulator) pairs t, t + kThreads, ... (loads in flight together),
+    // then row threads finish their rows (emicp_row_finish).
+    df* rb = A.rbpart + (size_t)(step & 1) * G * kEmNV;
+    {
+      const int S = A.geo.slices;
+      const int rpc = (A.M + (int)G - 1) / (int)G;
+      const int r0 = (int)blockIdx.x * rpc;
+      const int nrows = max(0, min(rpc, A.M - r0));
+      float* stot = reinterpret_cast<float*>(&sm.raw2[0][0]);  // [kThreads][5]; raw2 carries no stream here
+      static_assert(sizeof(sm.raw2) >= sizeof(float) * 5 * kThreads, "row sums scratch");
+      static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >= sizeof(df) * (kEmNV + 1) * kThreads,
+                    "moment scratch");
+      const float xm[3] = {s_hdr[6], s_hdr[7], s_hdr[8]};
+      const float oX[3] = {s_hdr[0], s_hdr[1], s_hdr[2]};
+      float* row_tape = A.row_tape ? A.row_tape + (size_t)step * A.M * 5 : nullptr;
+      df v[kEmNV];
+#pragma unroll
+      for (int k = 0; k < kEmNV; ++k) v[k] = df_make(0.f);
+      for (int c0 = 0; c0 < nrows; c0 += kThreads) {  // rows [c0, c0 + kThreads) of the share
+        const int nr = min(kThreads, nrows - c0);
+        for (int pq = tid; pq < 5 * nr; pq += kThreads) {
+          const int a = pq % 5, rr = pq / 5;
+          const float* P = A.part + (size_t)a * S * A.Mp + r0 + c0 + rr;
+          float sum = 0.f;
+          int k = 0;
+          for (; k + 16 <= S; k += 16) {
+            float w[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) w[j] = __ldcg(P + (size_t)(k + j) * A.Mp);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sum += w[j];
+          }
+          if (k < S) {
+            float w[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) w[j] = k + j < S ? __ldcg(P + (size_t)(k + j) * A.Mp) : 0.f;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sum += w[j];  // adding the zeros leaves the sum unchanged
+          }
+          stot[rr * 5 + a] = sum;
+        }
+        __syncthreads();
+        if (tid < nr) {
+          const int r = r0 + c0 + tid;
+          const float tot[5] = {stot[tid * 5], stot[tid * 5 + 1], stot[tid * 5 + 2], stot[tid * 5 + 3],
+                                stot[tid * 5 + 4]};
+          emicp_row_finish(r, tot, ld_cg(A.rows + r), outlier, xm, A.row_out, oX, row_tape, v);
+        }
+        __syncthreads();
+      }
+      em_block_moments(v, min(nrows, kThreads), reinterpret_cast<df*>(sm.prep), rb + (size_t)blockIdx.x * kEmNV);
+    }
+    if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 21)) break;
+    tl.mark(8);
+
+    // ---- grid-wide moments -> pose (every block computes the same pose)
+    reduce_block_partials<kEmNV>(rb, (int)G, s_red, s_tot);
     tl.mark(6);
     if (tid == 0) {
       float Xc[3], Yc[3], S[9];
@@ -230,23 +283,21 @@ struct EmicpCarved {
   float4* rows;
   float4* cols;
   float* part;
-  unsigned* cnt;
   df* rbpart;
+  int Mp;
 };
 
 EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* total) {
   Carve c(base);
   EmicpCarved w;
+  w.Mp = (M + 3) & ~3;
   w.ctl = c.take<Ctl>(1);
-  w.cnt = c.take<unsigned>((size_t)P.geo.nblk);
-  const size_t zero_end = c.off;  // ctl + counters are cleared per launch
   w.hdr = c.take<CenterHdr>(1);
   w.rows = c.take<float4>((size_t)M);
   w.cols = c.take<float4>((size_t)N);
-  w.part = c.take<float>((size_t)P.geo.units * 5 * kBlockPts);
-  w.rbpart = c.take<df>((size_t)2 * P.geo.nblk * kEmNV);
+  w.part = c.take<float>((size_t)5 * P.geo.slices * w.Mp);
+  w.rbpart = c.take<df>((size_t)2 * P.grid * kEmNV);
   if (total) *total = c.off;
-  (void)zero_end;
   return w;
 }
 }  // namespace
@@ -275,9 +326,8 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   EmicpCarved w = carve_emicp(ws, P, L.N, L.M, &total);
   if (total > ws_bytes) return (int)cudaErrorInvalidValue;
   if (grid_used) *grid_used = P.grid;
-  // control block + split counters start at zero every launch
+  // the control block starts at zero every launch
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt, 0, sizeof(unsigned) * (size_t)P.geo.nblk, st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
@@ -300,7 +350,7 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.hdr = w.hdr;
   A.dRt = L.dRt;
   A.part = w.part;
-  A.cnt = w.cnt;
+  A.Mp = w.Mp;
   A.rbpart = w.rbpart;
   A.ctl = w.ctl;
   A.trace = L.trace;

@@ -361,7 +361,19 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
         for (int q = 0; q < 16; ++q) vv[q] = df_make(0.f);
         for (int r = rb + tid; r < re; r += kThreads) {
           float totz[3] = {0.f, 0.f, 0.f};
-          for (int b = 0; b < g.nb; ++b) {
+          int b = 0;
+          for (; b + 8 <= g.nb; b += 8) {  // 8 loads in flight, added in column-block order
+            float4 p[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) p[j] = __ldcg(A.part_z + (size_t)(b + j) * A.M + r);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              totz[0] += p[j].x;
+              totz[1] += p[j].y;
+              totz[2] += p[j].z;
+            }
+          }
+          for (; b < g.nb; ++b) {
             const float4 p = __ldcg(A.part_z + (size_t)b * A.M + r);
             totz[0] += p.x;
             totz[1] += p.y;
@@ -391,11 +403,10 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
               df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
           }
         }
-        block_reduce_df<16>(vv, sm.red);
-        if (tid == 0)
-          for (int q = 0; q < 16; ++q)
-            __stcg(reinterpret_cast<float2*>(recs + (size_t)sl * 16 + q), make_float2(vv[q].hi, vv[q].lo));
-        __syncthreads();
+        // the slice's 16 sums, through shared memory (scr and wsum are free here)
+        static_assert(sizeof(sm.scr) + sizeof(sm.wsum) >= sizeof(df) * 17 * kThreads, "moment scratch");
+        em_block_moments(vv, min(kThreads, re - rb), reinterpret_cast<df*>(&sm.scr[0][0][0]),
+                         recs + (size_t)sl * 16);
       }
     }
     if (!ok || !grid_sync(A.ctl, epoch, G, A.timeout_ns, 102)) {

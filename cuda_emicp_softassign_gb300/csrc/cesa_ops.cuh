@@ -42,8 +42,59 @@ struct EmicpElem {
   }
 };
 
-// Row finalize: C_r, lambda_r, u_r = lambda_r X'_r, and the row's share of the
-// 16 moments (block accumulator, compensated).
+// One row's finalize: from its sums tot = (sum e^2, sum e, sum e x) to C_r,
+// lambda_r, u_r = lambda_r X'_r (src/emicp.cu:489-549: C_r <= 1e-6 gives
+// A = 1/N, lambda = 1, X' = mean(X)), the optional row records, and the row's
+// contribution to the 16 moments (added to v).
+__device__ __forceinline__ void emicp_row_finish(int r, const float (&tot)[5], float4 y, float outlier,
+                                                 const float (&xm)[3], float* row_out, const float (&oX)[3],
+                                                 float* row_tape, df (&v)[kEmNV]) {
+  const float C = tot[0] + outlier;
+  float lam, uu[3];
+  if (C > 10e-7f) {  // src/emicp.cu:155
+    const float inv = __frsqrt_rn(C);
+    lam = tot[1] * inv;
+    uu[0] = tot[2] * inv;
+    uu[1] = tot[3] * inv;
+    uu[2] = tot[4] * inv;
+  } else {  // A <- 1/N (src/emicp.cu:159): lambda = 1, lambda X' = mean(X)
+    lam = 1.f;
+    uu[0] = xm[0];
+    uu[1] = xm[1];
+    uu[2] = xm[2];
+  }
+  if (row_tape) {
+    float* o = row_tape + (size_t)r * 5;
+    o[0] = C;
+    o[1] = lam;
+    o[2] = uu[0];
+    o[3] = uu[1];
+    o[4] = uu[2];
+  }
+  if (row_out) {
+    float* o = row_out + (size_t)r * 5;
+    o[0] = C;
+    o[1] = lam;
+    o[2] = fmaf(lam, oX[0], uu[0]);
+    o[3] = fmaf(lam, oX[1], uu[1]);
+    o[4] = fmaf(lam, oX[2], uu[2]);
+  }
+  const float yy[3] = {y.x, y.y, y.z};
+  df_add(v[0], lam);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    df_add(v[1 + i], uu[i]);
+    df_add_prod(v[4 + i], lam, yy[i]);
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
+}
+
+// Row finalize of a split-completed owned block (the batched kernel): every
+// row's emicp_row_finish, then the block's 16 moments (block accumulator,
+// compensated).
 struct EmicpFin {
   const float4* rows;
   int M;
@@ -59,53 +110,39 @@ struct EmicpFin {
 #pragma unroll
     for (int k = 0; k < kEmNV; ++k) v[k] = df_make(0.f);
     const int r = blk * kBlockPts + (int)threadIdx.x;
-    if (threadIdx.x < kBlockPts && r < M) {
-      const float4 y = ld_cg(rows + r);
-      const float C = tot[0] + outlier;
-      float lam, uu[3];
-      if (C > 10e-7f) {  // src/emicp.cu:155
-        const float inv = __frsqrt_rn(C);
-        lam = tot[1] * inv;
-        uu[0] = tot[2] * inv;
-        uu[1] = tot[3] * inv;
-        uu[2] = tot[4] * inv;
-      } else {  // A <- 1/N (src/emicp.cu:159): lambda = 1, lambda X' = mean(X)
-        lam = 1.f;
-        uu[0] = xm[0];
-        uu[1] = xm[1];
-        uu[2] = xm[2];
-      }
-      if (row_tape) {
-        float* o = row_tape + (size_t)r * 5;
-        o[0] = C;
-        o[1] = lam;
-        o[2] = uu[0];
-        o[3] = uu[1];
-        o[4] = uu[2];
-      }
-      if (row_out) {
-        float* o = row_out + (size_t)r * 5;
-        o[0] = C;
-        o[1] = lam;
-        o[2] = fmaf(lam, oX[0], uu[0]);
-        o[3] = fmaf(lam, oX[1], uu[1]);
-        o[4] = fmaf(lam, oX[2], uu[2]);
-      }
-      const float yy[3] = {y.x, y.y, y.z};
-      df_add(v[0], lam);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        df_add(v[1 + i], uu[i]);
-        df_add_prod(v[4 + i], lam, yy[i]);
-      }
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) df_add_prod(v[7 + i + 3 * j], uu[i], yy[j]);
-    }
+    if (threadIdx.x < kBlockPts && r < M)
+      emicp_row_finish(r, tot, ld_cg(rows + r), outlier, xm, row_out, oX, row_tape, v);
     owned_block_sum<kEmNV>(v, scratch, rbpart + (size_t)blk * kEmNV);
   }
 };
+
+// Sum over the block of the 16 moments held by threads 0..active-1 (active <=
+// kThreads), through shared memory in a fixed order: value k of thread i at
+// scratch[k * kThreads + i]; thread (k, g) = (tid % 16, tid / 16) adds entries
+// g, g + 16, ...; thread k adds the 16 group sums. The record goes to dst.
+__device__ __forceinline__ void em_block_moments(const df (&v)[kEmNV], int active, df* scratch, df* dst) {
+  static_assert(kEmNV == 16 && kThreads % 16 == 0, "16 moments");
+  const int tid = threadIdx.x;
+  df* part = scratch + kEmNV * kThreads;
+  if (tid < active)
+#pragma unroll
+    for (int k = 0; k < kEmNV; ++k) scratch[k * kThreads + tid] = v[k];
+  __syncthreads();
+  {
+    const int k = tid % kEmNV, g = tid / kEmNV;
+    df s = df_make(0.f);
+    for (int i = g; i < active; i += kThreads / kEmNV) df_add(s, scratch[k * kThreads + i]);
+    part[k * (kThreads / kEmNV) + g] = s;
+  }
+  __syncthreads();
+  if (tid < kEmNV) {
+    df s = part[tid * (kThreads / kEmNV)];
+#pragma unroll
+    for (int g = 1; g < kThreads / kEmNV; ++g) df_add(s, part[tid * (kThreads / kEmNV) + g]);
+    __stcg(reinterpret_cast<float2*>(dst + tid), make_float2(s.hi, s.lo));
+  }
+  __syncthreads();
+}
 
 // Centres and cross-covariance from the 16 EM-ICP moments (centred frame):
 // Xc = sum u / L, Yc = sum lambda y / L, S = sum u y^T - L Xc Yc^T
