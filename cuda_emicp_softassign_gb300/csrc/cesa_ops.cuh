@@ -144,9 +144,25 @@ __device__ __forceinline__ void em_block_moments(const df (&v)[kEmNV], int activ
   __syncthreads();
 }
 
+__device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df precision
+  df r = df_make(0.f);
+  df_add_prod(r, a.hi, b);
+  r.lo = __fmaf_rn(a.lo, b, r.lo);
+  return r;
+}
+__device__ __forceinline__ df dsub(df a, const df& b) {
+  df_add(a, df{-b.hi, -b.lo});
+  return a;
+}
+
 // Centres and cross-covariance from the 16 EM-ICP moments (centred frame):
-// Xc = sum u / L, Yc = sum lambda y / L, S = sum u y^T - L Xc Yc^T
-// (S is translation invariant).
+// Xc = sum u / L, Yc = sum lambda y / L and
+//   S = sum u y^T - Xc (sum lambda y)^T - (sum u) Yc^T + L Xc Yc^T,
+// the expansion of sum (u - lambda Xc)(y - Yc)^T (src/emicp.cu's centring of
+// X' and Y before the product), every product in df. With the FP32-rounded
+// centres the first-order rounding terms cancel and L dXc dYc^T remains, so a
+// cloud that sits off the origin (raw moments thousands of times S) keeps S
+// to FP32 precision; S = sum u y^T - L Xc Yc^T with rounded Xc would not.
 __device__ __forceinline__ void em_moments_to_S(const df* tot, float Xc[3], float Yc[3], float S[9]) {
   const float L = df_val(tot[0]);
   for (int i = 0; i < 3; ++i) {
@@ -156,7 +172,9 @@ __device__ __forceinline__ void em_moments_to_S(const df* tot, float Xc[3], floa
   for (int j = 0; j < 3; ++j)
     for (int i = 0; i < 3; ++i) {
       df a = tot[7 + i + 3 * j];
-      df_add_prod(a, -L * Xc[i], Yc[j]);
+      df_add(a, dmul(tot[4 + j], -Xc[i]));
+      df_add(a, dmul(tot[1 + i], -Yc[j]));
+      df_add(a, dmul(dmul(tot[0], Xc[i]), Yc[j]));
       S[i + 3 * j] = df_val(a);
     }
 }
@@ -244,17 +262,6 @@ struct FinalFin {
 };
 
 // df helpers for the moment assembly
-__device__ __forceinline__ df dmul(df a, float b) {  // (a.hi + a.lo) * b, ~df precision
-  df r = df_make(0.f);
-  df_add_prod(r, a.hi, b);
-  r.lo = __fmaf_rn(a.lo, b, r.lo);
-  return r;
-}
-__device__ __forceinline__ df dsub(df a, const df& b) {
-  df_add(a, df{-b.hi, -b.lo});
-  return a;
-}
-
 // Softassign S and centres from the 32 moments, one value per thread
 // (tid 0..8: S_ij, tid 9..11: centres). oX, oY: centring offsets; yh: mean(Y').
 //   Yc = (B2 + oY B1)/A1, alpha = Yhat + oY, beta = alpha - Yc,

@@ -26,7 +26,8 @@ def _pose(seed, deg=5.0):
     return W.random_rotation(rng, deg), rng.uniform(-0.02, 0.02, 3)
 
 
-@pytest.mark.parametrize("n,m", [(1007, 1007), (300, 200), (129, 777)])
+# 64 x 80000: a block's share of the rows exceeds one pass of 256 threads
+@pytest.mark.parametrize("n,m", [(1007, 1007), (300, 200), (129, 777), (64, 80000)])
 @pytest.mark.parametrize("sigma_p2", [1e-2, 1e-3, 1e-4, 1.06e-5])
 def test_estep_rows_and_moments(cesa, oracle, torch_cuda, n, m, sigma_p2):
     from cuda_emicp_softassign_gb300 import workloads as W
@@ -88,7 +89,7 @@ def test_reference_golden_cases(cesa):
 
 
 @pytest.mark.parametrize("n,m", [(1, 1), (2, 3), (15, 16), (16, 17), (33, 127), (128, 128), (129, 1),
-                                 (513, 200), (1000, 2049)])
+                                 (513, 200), (1000, 2049), (64, 80000)])
 def test_ragged_sizes_match_oracle(cesa, oracle, n, m):
     from cuda_emicp_softassign_gb300 import workloads as W
     X, Y, _, _ = W.uniform_pair(n=n, m=m, seed=3 * n + m, max_deg=10.0, t_range=0.03)
