@@ -154,24 +154,26 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// Monotonic-counter barrier across all blocks of a cooperative launch.
-// `epoch` counts the barriers this block has passed (kept by the caller).
-// Thread 0 arrives with a release add and polls with acquire loads; the
-// __syncthreads on either side extend the ordering to the whole block.
-// Returns false when the wait exceeded timeout_ns or another block recorded an
-// error while this one waited; the caller must then leave the kernel.
-__device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nblocks,
-                                          uint64_t timeout_ns, int where) {
+// Monotonic-counter barrier over `nblocks` blocks of a cooperative launch that
+// share the counter `bar` (every block of the grid, or a fixed group of them).
+// `epoch` counts the barriers this block has passed on that counter (kept by
+// the caller). Thread 0 arrives with a release add and polls with acquire
+// loads; the __syncthreads on either side extend the ordering to the whole
+// block. Returns false when the wait exceeded timeout_ns or another block
+// recorded an error while this one waited; the caller must then leave the
+// kernel, or skip its work while still meeting its cluster barriers.
+__device__ __forceinline__ bool counter_sync(unsigned* bar, Ctl* ctl, unsigned& epoch, unsigned nblocks,
+                                             uint64_t timeout_ns, int where) {
   __shared__ int s_ok;
   __syncthreads();
   epoch += 1;
   if (threadIdx.x == 0) {
     const unsigned target = epoch * nblocks;
-    red_release_add(&ctl->bar, 1u);
+    red_release_add(bar, 1u);
     int ok = 1;
     uint64_t t0 = 0;
     unsigned spins = 0;
-    while ((int)(ld_acquire(&ctl->bar) - target) < 0) {
+    while ((int)(ld_acquire(bar) - target) < 0) {
       if ((++spins & 31u) == 0) {
         if (ld_status(ctl) != kStatusOk) {
           ok = 0;
@@ -191,6 +193,12 @@ __device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nb
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// The barrier across all blocks of the launch.
+__device__ __forceinline__ bool grid_sync(Ctl* ctl, unsigned& epoch, unsigned nblocks,
+                                          uint64_t timeout_ns, int where) {
+  return counter_sync(&ctl->bar, ctl, epoch, nblocks, timeout_ns, where);
 }
 
 // ---------------------------------------------------------------- clusters

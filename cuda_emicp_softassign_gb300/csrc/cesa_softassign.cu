@@ -75,6 +75,9 @@ struct SoftArgs {
 // Sums of the S slice partials of points i0 and i1 (i1 only when has1), the
 // deferred completion: each point's partials are added in slice order, and a
 // batch's loads for both points (8 each) are in flight before the first add.
+// A last partial batch is padded with zeros (the partials are sums of
+// positive terms, so adding +0 leaves each sum bitwise unchanged): S = 7 at
+// 20,000 points is one batch of 14 loads, not 7 round trips.
 __device__ __forceinline__ void slice_sum2(const float* part, int S, int ld, int i0, int i1, bool has1, float& s0,
                                            float& s1) {
   s0 = 0.f;
@@ -91,11 +94,16 @@ __device__ __forceinline__ void slice_sum2(const float* part, int S, int ld, int
 #pragma unroll
     for (int j = 0; j < 8; ++j) s1 += v1[j];
   }
-  for (; k < S; ++k) {
-    const float a = __ldcg(part + (size_t)k * ld + i0);
-    const float b = has1 ? __ldcg(part + (size_t)k * ld + i1) : 0.f;
-    s0 += a;
-    s1 += b;
+  if (k < S) {
+    float v0[8], v1[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v0[j] = k + j < S ? __ldcg(part + (size_t)(k + j) * ld + i0) : 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v1[j] = has1 && k + j < S ? __ldcg(part + (size_t)(k + j) * ld + i1) : 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s0 += v0[j];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s1 += v1[j];
   }
 }
 

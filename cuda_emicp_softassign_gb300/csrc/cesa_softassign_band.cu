@@ -16,9 +16,10 @@
 //    band's rows (rs, a, s) itself. A row pass therefore ends at a cluster
 //    barrier, not at a grid barrier.
 //  - Column pass: each CTA sums K a over the band's rows for its tile's
-//    columns and stores the partial; after the grid barrier, every CTA holding
-//    tile j adds the nb band partials of its columns (in band order) and
-//    completes the pass (cs, b, u) itself.
+//    columns and stores the partial; after a barrier over the nb CTAs holding
+//    tile j (a counter per tile, not the grid), each of them adds the nb band
+//    partials of its columns (in band order) and completes the pass (cs, b, u)
+//    itself.
 //  - Final row sweep: w, mu and Vhat over the tile, added across the cluster;
 //    the band's rows are finalised by the cluster's CTAs in 64 / CS row
 //    shares and the tiles' columns in shares c = band (mod nb); their 28 row
@@ -26,16 +27,17 @@
 //    record per band.
 //    One grid barrier, then every CTA reduces the nb records and solves the
 //    pose.
-// Per pose update: I1 + 1 grid barriers and I1 + 2 cluster barriers, against
-// 2 I1 + 1 grid barriers in the matrix-free kernel. Row-side state (a, s) is
+// Per pose update: I1 tile-group barriers, 1 grid barrier and I1 + 2 cluster
+// barriers, against 2 I1 + 1 grid barriers in the matrix-free kernel. Row-side state (a, s) is
 // held, identical, by every CTA of a band and column-side state (b, u) by
 // every CTA of a tile column, so no pass writes a scaling vector to global
 // memory. Results agree with the matrix-free kernel to FP32 rounding (other
 // summation orders), not bitwise.
 //
 // Cluster barriers have no time limit: every CTA runs the same sequence of
-// them whatever happens. A grid barrier that gives up (time limit, or a status
-// already set by another CTA) only turns off the rest of this CTA's work.
+// them whatever happens. A grid or tile-group barrier that gives up (time
+// limit, or a status already set by another CTA) only turns off the rest of
+// this CTA's work.
 #include <mutex>
 
 #include "cesa_kernels.h"
@@ -62,6 +64,7 @@ struct BandArgs {
   float* w_out;
   float* pc;           // column-pass partials [2][nb][Mp] (by pass parity)
   df* mom;             // [2][nb][32] moment records per band
+  unsigned* gbar;      // [CS][32]: barrier counter of each column tile's nb CTAs (one 128-byte line each)
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -342,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
   float2 qx[kRowPairs][3];  // the band's rows, owned by the lanes in row sweeps
   own_pairs(sm.xr, qx);
 
-  unsigned epoch = 0, cpass = 0;
+  unsigned epoch = 0, gepoch = 0, cpass = 0;
   int xpar = 0, step = 0;
   bool ok = true;
   float T = A.T0;
@@ -423,7 +426,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_band_kernel(const Band
         if (tid < Wt) __stcg(A.pc + (size_t)(cpass & 1u) * pc_stride + (size_t)band * A.Mp + c0 + tid, tot[0]);
         ++cpass;
         tl.mark(4);
-        if (ok) ok = grid_sync(A.ctl, epoch, gridDim.x, A.timeout_ns, 72);
+        // the completion of tile `rank`'s columns reads only the partials of
+        // the nb CTAs of that tile: a barrier over that group, not the grid
+        if (ok) ok = counter_sync(A.gbar + (size_t)rank * 32, A.ctl, gepoch, (unsigned)A.nb, A.timeout_ns, 72);
         tl.mark(5);
       }
       // final row sweep: completes the last column pass, accumulates w, mu, Vhat
@@ -621,6 +626,7 @@ struct BandCarved {
   float4* cols;
   float* pc;
   df* mom;
+  unsigned* gbar;
   int Mp;
 };
 
@@ -639,6 +645,7 @@ BandCarved carve_band(void* base, const BandPlan& P, int N, int M, size_t* total
   w.cols = static_cast<float4*>(take(sizeof(float4) * (size_t)M));
   w.pc = static_cast<float*>(take(sizeof(float) * 2 * (size_t)P.nb * w.Mp));
   w.mom = static_cast<df*>(take(sizeof(df) * 2 * (size_t)P.nb * 32));
+  w.gbar = static_cast<unsigned*>(take(sizeof(unsigned) * 32 * (size_t)P.CS));
   if (total) *total = off;
   return w;
 }
@@ -675,6 +682,7 @@ int enqueue_softassign_band(const SoftassignLaunch& L, void* ws, size_t ws_bytes
   if (total > ws_bytes) return (int)cudaErrorInvalidValue;
   if (grid_used) *grid_used = P.grid;
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.gbar, 0, sizeof(unsigned) * 32 * (size_t)P.CS, st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
@@ -710,6 +718,7 @@ int enqueue_softassign_band(const SoftassignLaunch& L, void* ws, size_t ws_bytes
   A.w_out = L.w_out;
   A.pc = w.pc;
   A.mom = w.mom;
+  A.gbar = w.gbar;
   A.ctl = w.ctl;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;
