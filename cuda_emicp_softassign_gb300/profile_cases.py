@@ -52,7 +52,8 @@ def c2_timeline():
     _, _, tl, rep = C.softassign(X, Y, param=p, timeline=256 * 800)
     rows = C.timeline_table(tl, rep.grid_blocks)
     names = {1: "start", 2: "final: last column pass completed", 3: "row pass completed (cluster)",
-             4: "column sweep + partial store (final: record store)", 5: "grid barrier", 6: "moment records reduced",
+             4: "column sweep + partial store (final: record store)",
+             5: "barrier (column tile's CTAs; the grid before the pose)", 6: "moment records reduced",
              7: "Horn solve", 8: "cluster barrier (final sweep included after 2)", 10: "moments: cluster barrier",
              11: "final rows finalised", 12: "moments summed", 13: "S formed",
              14: "column pass completed (band partials)", 15: "row sweep + warp reduction"}
@@ -64,6 +65,27 @@ def c2_timeline():
     for i in range(1, len(segs[0])):
         d = np.mean([s[i, 1] - s[i - 1, 1] for s in segs])
         print("  %2d  %-42s %6.0f ns" % (i, names.get(int(segs[0][i, 0]), "next update"), d))
+
+
+def c2_horn():
+    """The pose solve over a whole config-2 registration (banded form): how
+    many updates the certified inverse iteration takes (the trace's gap is -1
+    there) and the solve's duration per update from the timeline."""
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c2_softassign_2000", seed=0)
+    p = C.Params.default(sinkhorn_form=C.SINKHORN_BANDED)
+    _, _, tr, _ = C.softassign(X, Y, param=p, trace=True)
+    fast = tr[:, 30] == -1
+    print("pose updates %d, certified inverse iteration %d, Jacobi fallback at updates %s"
+          % (len(fast), int(fast.sum()), np.where(~fast)[0].tolist()))
+    _, _, tl, rep = C.softassign(X, Y, param=p, timeline=256 * 12000)
+    b0 = C.timeline_table(tl, rep.grid_blocks)
+    b0 = b0[b0[:, 0] == 0][:, 1:]
+    i13 = np.where(b0[:-1, 0] == 13)[0]
+    d = b0[i13 + 1, 1] - b0[i13, 1]
+    print("solve (S formed -> pose), ns over %d updates: mean %.0f, median %.0f, p90 %.0f, max %.0f"
+          % (len(d), d.mean(), np.median(d), np.percentile(d, 90), d.max()))
 
 
 def c5_update():
@@ -159,7 +181,7 @@ def icp_grid_20000():
     _icp(2)  # CESA_ICP_SEARCH_GRID
 
 
-CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c5_update, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c2_horn, c5_update, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
                                   icp_grid_20000)}
 
 if __name__ == "__main__":
