@@ -588,10 +588,16 @@ __device__ __noinline__ void horn_update(const BPair& P, const float S[9], const
 }
 
 __device__ __noinline__ void em_finalize(const BPair& P, const Ph& ph, df* s_red, df* s_tot) {
+  __shared__ float s_emS[15];
   reduce_block_partials<kEmNV>(P.rec, P.g0.nblk, s_red, s_tot);
+  em_moments_to_S_block(s_tot, s_emS);
   if (threadIdx.x == 0) {
     float Xc[3], Yc[3], S[9];
-    em_moments_to_S(s_tot, Xc, Yc, S);
+    for (int k = 0; k < 9; ++k) S[k] = s_emS[k];
+    for (int k = 0; k < 3; ++k) {
+      Xc[k] = s_emS[9 + k];
+      Yc[k] = s_emS[12 + k];
+    }
     horn_update(P, S, Xc, Yc, ph.step, ph.step + 1 == P.nsteps);
     __stcg(P.state + 12, __ldcg(P.state + 12) * P.sigma_factor);  // FP32, src/emicp.cu:668
   }

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   __shared__ df s_red[kThreads];
   __shared__ OwnCache oc_rows;
   __shared__ df s_tot[kEmNV];
+  __shared__ float s_emS[15];  // S, Xc, Yc of the step
   __shared__ float s_hdr[12];
 
   const int tid = threadIdx.x;
@@ -174,9 +175,14 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     // ---- grid-wide moments -> pose (every block computes the same pose)
     reduce_block_partials<kEmNV>(rb, (int)G, s_red, s_tot);
     tl.mark(6);
+    em_moments_to_S_block(s_tot, s_emS);
     if (tid == 0) {
       float Xc[3], Yc[3], S[9];
-      em_moments_to_S(s_tot, Xc, Yc, S);
+      for (int k = 0; k < 9; ++k) S[k] = s_emS[k];
+      for (int k = 0; k < 3; ++k) {
+        Xc[k] = s_emS[9 + k];
+        Yc[k] = s_emS[12 + k];
+      }
       float q[4], gap = 0.f, lmax = 0.f, Rn[9], tn[3];
       // the pose: certified inverse iteration (Jacobi fallback); the same with
       // and without a tape, so that both forwards agree bitwise

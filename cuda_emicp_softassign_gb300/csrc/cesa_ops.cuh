@@ -163,6 +163,15 @@ __device__ __forceinline__ df dsub(df a, const df& b) {
 // centres the first-order rounding terms cancel and L dXc dYc^T remains, so a
 // cloud that sits off the origin (raw moments thousands of times S) keeps S
 // to FP32 precision; S = sum u y^T - L Xc Yc^T with rounded Xc would not.
+__device__ __forceinline__ float em_S_entry(const df* tot, int i, int j, float xi, float yj) {
+  df a = tot[7 + i + 3 * j];
+  df_add(a, dmul(tot[4 + j], -xi));
+  df_add(a, dmul(tot[1 + i], -yj));
+  df_add(a, dmul(dmul(tot[0], xi), yj));
+  return df_val(a);
+}
+
+// One thread forms everything (the adjoint's recomputation of a step).
 __device__ __forceinline__ void em_moments_to_S(const df* tot, float Xc[3], float Yc[3], float S[9]) {
   const float L = df_val(tot[0]);
   for (int i = 0; i < 3; ++i) {
@@ -170,13 +179,25 @@ __device__ __forceinline__ void em_moments_to_S(const df* tot, float Xc[3], floa
     Yc[i] = df_val(tot[4 + i]) / L;
   }
   for (int j = 0; j < 3; ++j)
-    for (int i = 0; i < 3; ++i) {
-      df a = tot[7 + i + 3 * j];
-      df_add(a, dmul(tot[4 + j], -Xc[i]));
-      df_add(a, dmul(tot[1 + i], -Yc[j]));
-      df_add(a, dmul(dmul(tot[0], Xc[i]), Yc[j]));
-      S[i + 3 * j] = df_val(a);
+    for (int i = 0; i < 3; ++i) S[i + 3 * j] = em_S_entry(tot, i, j, Xc[i], Yc[j]);
+}
+
+// Block-wide (every thread calls it), bitwise the same values: thread i + 3 j
+// (< 9) forms S_ij, threads 9..14 the centres, into out[0..8] = S,
+// out[9..11] = Xc, out[12..14] = Yc (shared). The nine df chains then run side
+// by side instead of one after another in one thread. Synchronises the block.
+__device__ __forceinline__ void em_moments_to_S_block(const df* tot, float* out) {
+  const int t = threadIdx.x;
+  if (t < 15) {
+    const float L = df_val(tot[0]);
+    if (t < 9) {
+      const int i = t % 3, j = t / 3;
+      out[t] = em_S_entry(tot, i, j, df_val(tot[1 + i]) / L, df_val(tot[4 + j]) / L);
+    } else {
+      out[t] = df_val(tot[t - 8]) / L;  // t = 9..11: tot[1..3] (Xc); 12..14: tot[4..6] (Yc)
     }
+  }
+  __syncthreads();
 }
 
 // ------------------------------------------------------------------ Softassign
