@@ -67,6 +67,28 @@ def c2_timeline():
         print("  %2d  %-42s %6.0f ns" % (i, names.get(int(segs[0][i, 0]), "next update"), d))
 
 
+def c1_timeline():
+    """Phases of a config-1 EM-ICP sigma step (block 0, mean over the steps)."""
+    import cuda_emicp_softassign_gb300 as C
+    from cuda_emicp_softassign_gb300 import workloads as W
+    _, X, Y, _, _ = W.make("c1_emicp_1007", seed=0)
+    C.emicp(X, Y)
+    _, _, tl, rep = C.emicp(X, Y, timeline=304 * 4000)
+    rows = C.timeline_table(tl, rep.grid_blocks)
+    names = {1: "start", 2: "a unit's first chunk landed", 3: "unit swept", 4: "unit's row partials stored",
+             5: "grid barrier after the sweep", 8: "rows completed, block moments, grid barrier",
+             6: "moment records reduced", 7: "S (nine threads) + pose solve"}
+    b0 = rows[rows[:, 0] == 0][:, 1:]
+    starts = np.where(b0[:, 0] == 1)[0]
+    segs = [b0[a:b + 1] for a, b in zip(starts[1:-1], starts[2:])]
+    segs = [sg for sg in segs if len(sg) == len(segs[0])]
+    print("grid %d, sigma step (block 0, mean of %d): %.0f ns"
+          % (rep.grid_blocks, len(segs), np.mean([sg[-1, 1] - sg[0, 1] for sg in segs])))
+    for i in range(1, len(segs[0])):
+        d = np.mean([sg[i, 1] - sg[i - 1, 1] for sg in segs])
+        print("  %2d  %-46s %6.0f ns" % (i, names.get(int(segs[0][i, 0]), "next step"), d))
+
+
 def c2_horn():
     """The pose solve over a whole config-2 registration (banded form): how
     many updates the certified inverse iteration takes (the trace's gap is -1
@@ -181,7 +203,7 @@ def icp_grid_20000():
     _icp(2)  # CESA_ICP_SEARCH_GRID
 
 
-CASES = {f.__name__: f for f in (c2_one, c2_one_mf, c2_timeline, c2_horn, c5_update, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
+CASES = {f.__name__: f for f in (c1_timeline, c2_one, c2_one_mf, c2_timeline, c2_horn, c5_update, c3_short, batch_mid, mat_8000, adj_20000, sa_adj_20000, icp_20000,
                                   icp_grid_20000)}
 
 if __name__ == "__main__":
