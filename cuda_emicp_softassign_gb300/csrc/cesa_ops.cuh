@@ -128,6 +128,17 @@ __device__ __forceinline__ void em_block_moments(const df (&v)[kEmNV], int activ
 #pragma unroll
     for (int k = 0; k < kEmNV; ++k) scratch[k * kThreads + tid] = v[k];
   __syncthreads();
+  if (active <= kThreads / kEmNV) {
+    // one entry per group: thread k adds the active threads' values in order,
+    // bitwise what the two-level sum gives (its other terms are zeros)
+    if (tid < kEmNV) {
+      df s = df_make(0.f);
+      for (int i = 0; i < active; ++i) df_add(s, scratch[tid * kThreads + i]);
+      __stcg(reinterpret_cast<float2*>(dst + tid), make_float2(s.hi, s.lo));
+    }
+    __syncthreads();
+    return;
+  }
   {
     const int k = tid % kEmNV, g = tid / kEmNV;
     df s = df_make(0.f);

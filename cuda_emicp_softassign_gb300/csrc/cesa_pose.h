@@ -355,11 +355,15 @@ CESA_HD void shifted4(const T (&N)[4][4], T sigma, T c, const T (&v)[4], T (&A)[
 // solve.
 template <typename T>
 CESA_HD bool horn_top_inverse(const T (&N)[4][4], const T (&q0)[4], T (&q)[4], T* lmax) {
-  T scale = T(0);
+  // max |N_ij| as a tree (the same value as a running maximum, fewer dependent steps)
+  T mx[16];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int k = 0; k < 16; ++k) mx[k] = t_abs(N[k / 4][k % 4]);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) scale = t_abs(N[i][j]) > scale ? t_abs(N[i][j]) : scale;
+  for (int w = 8; w >= 1; w /= 2)
+#pragma unroll
+    for (int k = 0; k < w; ++k) mx[k] = mx[k + w] > mx[k] ? mx[k + w] : mx[k];
+  const T scale = mx[0];
   if (!(scale > T(1e-30)) || !t_finite(scale)) return false;
   T v[4], x[4], Nv[4], A[4][4], L[4][4], rd[4];
 #pragma unroll
