@@ -3,7 +3,7 @@
 //
 // Some callers must not call cudaMalloc. A plugin inside a host application may
 // own no device heap. A pre-sized real-time pipeline may forbid allocation after
-// start-up. Code between cudaStreamBeginCapture/EndCapture must not allocate.
+// start-up.
 // cesa_emicp_device() takes its workspace from a cudaMalloc'd cache. This entry
 // point runs the same fused EM-ICP kernels on a fixed scratch array instead: a
 // file-scope __device__ array of kNoAllocScratchBytes that every GPU which loads

@@ -183,9 +183,8 @@ int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* report)
 /*
  * EM-ICP with no device allocation. No counterpart in the reference: this is
  * for callers that cannot call cudaMalloc, such as a plugin inside a host
- * application that owns no device heap, a real-time pipeline that forbids
- * allocation after start-up, or code recorded between cudaStreamBeginCapture
- * and cudaStreamEndCapture. It computes the same result as
+ * application that owns no device heap, or a real-time pipeline that forbids
+ * allocation after start-up. It computes the same result as
  * cesa_emicp_device (same arguments and conventions), but its scratch is a
  * fixed 16 MiB device array inside libcesa.so, held on every GPU that loads
  * the library until the process exits. That is enough for about N = M =

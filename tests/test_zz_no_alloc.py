@@ -1,10 +1,11 @@
 """The no-allocation EM-ICP entry point (cesa_emicp_device_noalloc).
 
 It serves callers that cannot call cudaMalloc, such as a plugin without a
-device heap of its own or code inside stream capture. Its scratch is a fixed
-16 MiB array inside libcesa.so. This file is collected last, so that a run
-stopping at the first failure has already run every other test. It also
-passes on its own in a fresh process.
+device heap of its own or a real-time pipeline that forbids allocation
+after start-up. Its scratch is a fixed 16 MiB array inside libcesa.so.
+This file is collected last, so that a run stopping at the first failure
+has already run every other test. It also passes on its own in a fresh
+process.
 """
 import numpy as np
 import pytest
