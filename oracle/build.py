@@ -74,7 +74,9 @@ def build_reference(force=False):
         return REF_SO
     tramp_o = os.path.join(REF_DIR, "blas_trampoline.o")
     _run(["gcc", "-O2", "-fPIC", "-c", ours[1], "-o", tramp_o])
-    inc = ["-I", os.path.join(HERE, "stubs"), "-I", os.path.join(REPO, "include"), "-I", src]
+    # The reference tree comes before ours, so ref_entry.cpp sees the reference's own
+    # 3dregistration.h (which declares emicp_cpu); ours supplies cesa_pcl_compat.h.
+    inc = ["-I", os.path.join(HERE, "stubs"), "-I", src, "-I", os.path.join(REPO, "include")]
     _run(["g++", "-O3", "-fPIC", "-shared", "-fopenmp", "-DNOVIEWER", "-w"] + inc +
          [needed[0], needed[1], needed[2], ours[0], tramp_o, "-o", REF_SO,
           blas, "-Wl,-rpath," + os.path.dirname(blas)])
