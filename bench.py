@@ -46,7 +46,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2_softassign_2000")
@@ -161,6 +161,14 @@ class ClockSampler:
                  "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # nvidia-smi takes a moment to start: wait (at most 5 s) for its first row, so that the
+        # samples cover the timed region that follows rather than only its end.
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
@@ -247,7 +255,7 @@ def run_reference(args, rank, world):
         return
     if args.workload == BATCH_WORKLOAD:
         pairs = batch_workload(args.seed)
-        per_step = max(2.0, args.cpu_sample_s / max(1, args.steps + args.warmup))
+        per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
         vals = []
         for i in range(args.warmup + args.steps):
             v, desc, thr = batch_cpu_baseline(pairs, per_step)
@@ -265,7 +273,7 @@ def run_reference(args, rank, world):
         return
     kind, X, Y = workload(args.workload, args.seed)
     p = RefDefaults()
-    per_step = max(2.0, args.cpu_sample_s / max(1, args.steps + args.warmup))
+    per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
     vals = []
     for i in range(args.warmup + args.steps):
         v, desc, thr = cpu_baseline(kind, X, Y, p, per_step)
