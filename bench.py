@@ -2,31 +2,47 @@
 """Benchmark of the soft-correspondence registration path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2_softassign_2000|c1_emicp_1007|c3_emicp_40097|c5_softassign_20000|icp_40097|
-                                c4_batch_256]
+                    [--workload c3_emicp_40097|c1_emicp_1007|c2_softassign_2000|c5_softassign_20000|
+                                icp_40097|c4_batch_256]
 
 One step is one complete registration (the whole annealing schedule) of the
-workload's seeded synthetic pair. The default workload is config 2: Softassign
-with N ~ M ~ 2000 and JMAX=100, I0=5, I1=3, i.e. 500 pose updates.
+workload's seeded synthetic pair. The default workload is config 3: EM-ICP
+with N = M = 40,097 (two ~70% views of a union of 3 ellipsoids, 5% uniform
+outliers, rotation up to 20 degrees), the default schedule of 66 sigma steps.
+Its points are the ones stored with the FP64 oracle's result in
+tests/golden/c3_emicp_40097.npz, so the line can state the result's error
+against that oracle ("accuracy").
 
 ours:      `value` times the device-pointer C ABI entry point (inputs already
            in HBM) with CUDA events on the launching stream. L2 is flushed
            (256 MiB write) between steps, outside the timed events. `e2e`
            times the host-pointer entry point (pinned host SoA in, R,t out,
            copies included) by wall clock.
-reference: times the reference algorithm on the host cores (the oracle's FP32
-           port of the path, all threads) on a bounded sample of the same
-           workload, scaled to registrations/s.
+reference: times the reference's CPU implementation on the host cores: its own
+           emicp_cpu() (src/emicp_cpu.cpp, compiled unmodified into
+           oracle/_ref by oracle/build.py) for EM-ICP workloads, else the
+           oracle's FP32 port of the reference algorithm (the reference has
+           no CPU Softassign or exact ICP). Each step is a bounded sample of
+           one registration: a whole number of sigma steps or pose updates of
+           the full-size pair; `ms_per_step` is the time of that sample and
+           `value` scales it to registrations/s.
 
 c4_batch_256: one step is one batched launch (cesa_register_batch_device) of
 the 256 pairs of config 4; value counts every pair as one registration. The
 line also reports the same pairs registered one pair per launch.
+
+Profiling cases: --size, --sigma-inf, --jmax, --i0 and --pairs run a smaller
+case of a workload (same generator), and --no-cpu-baseline / --no-adjoint
+skip the legs that are not being profiled. --timeline prints the in-kernel
+phase timeline of one registration (EM-ICP or the banded Softassign form)
+instead of a bench line.
 
 Multi-GPU: one process per GPU (torchrun), independent replicas of the same
 workload; value = registrations done by all ranks / max rank time.
 Rank 0 prints one JSON line.
 """
 import argparse
+import copy
 import ctypes
 import json
 import os
@@ -41,6 +57,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 L2_FLUSH_BYTES = 256 << 20
+GOLDEN = os.path.join(HERE, "tests", "golden")
+DEFAULT_WORKLOAD = "c3_emicp_40097"
+BATCH_WORKLOAD = "c4_batch_256"
+ROT_BOUND_DEG = 1e-3
+T_BOUND_REL = 1e-5
 
 
 def parse_args():
@@ -49,18 +70,27 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2_softassign_2000")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0,
                     help="target seconds of CPU work for the CPU-baseline sample")
     ap.add_argument("--sinkhorn-form", default="auto", choices=["auto", "matrix_free", "materialised", "banded"],
                     help="Softassign Sinkhorn form (auto: the library's recorded choice for the size, "
-                         "matrix-free when none)")
+                         "else its default by size)")
     ap.add_argument("--tune", action="store_true",
                     help="run the Sinkhorn autotuner for the workload's size before timing (records the "
                          "choice that auto then uses, and reports both forms' times)")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the forward + backward timing reported under 'adjoint'")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--size", type=int, default=None,
+                    help="points per cloud (the workload's generator at a smaller size; profiling)")
+    ap.add_argument("--sigma-inf", type=float, default=None, help="EM-ICP schedule end (profiling)")
+    ap.add_argument("--jmax", type=int, default=None, help="Softassign JMAX (profiling)")
+    ap.add_argument("--i0", type=int, default=None, help="Softassign I0 (profiling)")
+    ap.add_argument("--pairs", type=int, default=256, help="pairs of the batch workload (profiling)")
+    ap.add_argument("--timeline", action="store_true",
+                    help="print the in-kernel phase timeline of one registration instead of a bench line")
     return ap.parse_args()
 
 
@@ -71,32 +101,68 @@ def dist_env():
     return rank, world, local
 
 
-def workload(name, seed):
-    from cuda_emicp_softassign_gb300 import workloads as W
-    kind, X, Y, Rt, tt = W.make(name, seed=seed)
-    return kind, X, Y
-
-
+# ------------------------------------------------------------------ workload
 class RefDefaults:
-    """The reference CLI defaults (src/main.cpp:280-315), without loading libcesa."""
-    JMAX, I0, I1, alpha, T_0, TFACTOR = 100, 5, 3, 3.0, 100.0, 0.95
+    """The reference CLI defaults (src/main.cpp:280-315), as FP32 values,
+    without loading libcesa."""
+    JMAX, I0, I1 = 100, 5, 3
+    alpha = float(np.float32(3.0))
+    T_0 = float(np.float32(100.0))
+    TFACTOR = float(np.float32(0.95))
     moutlier = float(np.float32(np.exp(np.float32(-1.0)) / np.sqrt(np.float32(100.0))))
-    sigma_p2, sigma_inf, sigma_factor, d_02 = 0.01, 1e-5, 0.9, 0.01
+    sigma_p2 = float(np.float32(0.01))
+    sigma_inf = float(np.float32(1e-5))
+    sigma_factor = float(np.float32(0.9))
+    d_02 = float(np.float32(0.01))
     maxIteration = 30
+
+
+def schedule(args):
+    """The workload's parameters: the reference defaults with the profiling
+    overrides applied (identical in both arms)."""
+    p = RefDefaults()
+    if args.sigma_inf is not None:
+        p.sigma_inf = float(np.float32(args.sigma_inf))
+    if args.jmax is not None:
+        p.JMAX = args.jmax
+    if args.i0 is not None:
+        p.I0 = args.i0
+    return p
+
+
+def cesa_params(cesa, p, form="auto"):
+    return cesa.Params.default(JMAX=p.JMAX, I0=p.I0, I1=p.I1, sigma_inf=p.sigma_inf, sinkhorn_form=FORMS[form])
 
 
 FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2, "banded": 3}
 FORM_NAMES = {1: "matrix_free", 2: "materialised", 3: "banded"}
 
 
-def params_for(cesa, kind, form="auto"):
-    return cesa.Params.default(sinkhorn_form=FORMS[form])
+def fixture_for(args, p):
+    """The committed FP64-oracle fixture whose inputs and schedule are this
+    run's, or None."""
+    if args.size is not None or args.seed != 0:
+        return None
+    d = RefDefaults()
+    if args.workload == "c3_emicp_40097" and p.sigma_inf == d.sigma_inf:
+        path = os.path.join(GOLDEN, "c3_emicp_40097.npz")
+    elif args.workload == "c5_softassign_20000" and p.JMAX == 2 and p.I0 == d.I0:
+        path = os.path.join(GOLDEN, "c5_softassign_20000_jmax2.npz")
+    else:
+        return None
+    return path if os.path.exists(path) else None
 
 
-def materialised_bytes(N, M, p):
-    """HBM bytes of one registration in the materialised form: per pose update
-    4 B per element written (K) and 4 B read by each of the 2*I1 later passes."""
-    return 4.0 * (1 + 2 * p.I1) * float(N) * float(M) * p.JMAX * p.I0
+def load_workload(args, p):
+    """(kind, X, Y, fixture) for the run: the fixture's stored points where
+    one matches the run, else the seeded generator."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    kind, X, Y, _, _ = W.make(args.workload, seed=args.seed, n=args.size)
+    fx = fixture_for(args, p)
+    if fx is not None:
+        g = np.load(fx)
+        X, Y = g["X"], g["Y"]
+    return kind, X, Y, fx
 
 
 def pose_updates(kind, p):
@@ -104,11 +170,16 @@ def pose_updates(kind, p):
         return p.JMAX * p.I0
     if kind == "icp":
         return p.maxIteration
-    n, s = 0, np.float32(p.sigma_p2)
+    return len(sigma_sequence(p))
+
+
+def sigma_sequence(p):
+    """sigma_p2 of every EM-ICP step (the reference's FP32 loop, src/emicp.cu:443,668)."""
+    out, s = [], np.float32(p.sigma_p2)
     while s > np.float32(p.sigma_inf):
-        n += 1
+        out.append(float(s))
         s = np.float32(s * np.float32(p.sigma_factor))
-    return n
+    return out
 
 
 def algorithmic_work(kind, N, M, p):
@@ -126,10 +197,16 @@ def algorithmic_work(kind, N, M, p):
     e = float(N) * float(M)
     if kind == "emicp":
         return 12.0 * e * n, e * n, e * n
-    if kind == "icp":  # 3 FADD, FMUL + 2 FFMA per element; the compare-select runs on the ALU pipe
+    if kind == "icp":
         return 6.0 * e * n, 0.0, e * n
     sweeps = 2 * p.I1
     return e * n * (8.0 * sweeps + 12.0), e * n * (sweeps + 1), e * n * (sweeps + 1)
+
+
+def materialised_bytes(N, M, p):
+    """HBM bytes of one registration in the materialised form: per pose update
+    4 B per element written (K) and 4 B read by each of the 2*I1 later passes."""
+    return 4.0 * (1 + 2 * p.I1) * float(N) * float(M) * p.JMAX * p.I0
 
 
 def kernels_per_registration(kind, form=None):
@@ -140,6 +217,23 @@ def kernels_per_registration(kind, form=None):
     return 4
 
 
+def config_of(args, kind, X, Y, p, fixture):
+    c = {"workload": args.workload, "algorithm": kind, "N": int(len(X)), "M": int(len(Y)),
+         "pose_updates_per_registration": pose_updates(kind, p), "seed": args.seed,
+         "inputs": ("points stored in %s (the seeded generator's output)" % os.path.relpath(fixture, HERE)
+                    if fixture else "seeded generator, cuda_emicp_softassign_gb300/workloads.py"),
+         "l2": "flushed between steps (256 MiB write), outside the timed region",
+         "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+    if kind == "softassign":
+        c.update(JMAX=p.JMAX, I0=p.I0, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR)
+    elif kind == "icp":
+        c.update(maxIteration=p.maxIteration)
+    else:
+        c.update(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_inf, sigma_factor=p.sigma_factor, d_02=p.d_02)
+    return c
+
+
+# ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -201,109 +295,141 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(kind, X, Y, p, target_s, threads=None):
-    """Times the oracle's FP32 port of the reference algorithm on the host on a
-    bounded sample; returns (registrations/s, description, threads)."""
+# ------------------------------------------------------------------ CPU arm
+def sigma_inf_after(p, k):
+    """sigma_inf that makes the reference's loop run exactly its first k steps."""
+    return sigma_sequence(p)[k - 1] * float(np.float32(p.sigma_factor)) if k > 0 else p.sigma_p2
+
+
+def cpu_sample(kind, X, Y, p, target_s, threads=None):
+    """One bounded sample of a registration on the host cores.
+
+    EM-ICP: the reference's own emicp_cpu() where oracle/_ref built it (else
+    the oracle's FP32 port), over the first k sigma steps of the schedule, k
+    sized to about target_s. Softassign / ICP: the oracle's FP32 port over
+    the first k pose updates (the reference has no CPU Softassign and its
+    ICP needs FLANN). Returns dict(seconds, fraction, kind, impl, threads),
+    fraction = the share of one registration the sample covers."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
     O.set_threads(threads)
     n_full = pose_updates(kind, p)
-    # calibrate with one pose update, then size the sample to ~target_s
     if kind == "emicp":
-        s1 = np.float32(p.sigma_p2) * np.float32(p.sigma_factor)
-        t0 = time.perf_counter()
-        O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=float(s1), sigma_factor=p.sigma_factor,
-                d_02=p.d_02, precision="f32", trace=False)
-        one = time.perf_counter() - t0
-        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
-        sig = np.float32(p.sigma_p2)
-        for _ in range(k):
-            sig = np.float32(sig * np.float32(p.sigma_factor))
-        t0 = time.perf_counter()
-        O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=float(sig), sigma_factor=p.sigma_factor,
-                d_02=p.d_02, precision="f32", trace=False)
-        dt = time.perf_counter() - t0
+        use_ref = O.ref() is not None
+        impl = ("the reference's own emicp_cpu() (src/emicp_cpu.cpp, FP32 + OpenBLAS, OpenMP), compiled "
+                "unmodified by oracle/build.py" if use_ref else "the oracle's FP32 port of emicp_cpu() (OpenMP)")
+
+        def run(k):
+            si = sigma_inf_after(p, k)
+            if use_ref:
+                O.ref_emicp_cpu(X, Y, sigma_p2=p.sigma_p2, sigma_inf=si, sigma_factor=p.sigma_factor, d_02=p.d_02)
+            else:
+                O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=si, sigma_factor=p.sigma_factor, d_02=p.d_02,
+                        precision="f32", trace=False)
+        unit, kind_out = "sigma steps", ("reference" if use_ref else "port")
     elif kind == "icp":
-        t0 = time.perf_counter()
-        O.icp(X, Y, maxIteration=1, precision="f32", trace=False)
-        one = time.perf_counter() - t0
-        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
-        t0 = time.perf_counter()
-        O.icp(X, Y, maxIteration=k, precision="f32", trace=False)
-        dt = time.perf_counter() - t0
+        impl = "the oracle's FP32 port of icp() with an exhaustive search (the reference's FLANN is absent)"
+
+        def run(k):
+            O.icp(X, Y, maxIteration=k, precision="f32", trace=False)
+        unit, kind_out = "iterations", "port"
+    else:
+        impl = "the oracle's FP32 port of softassign() (OpenMP; the reference has no CPU Softassign)"
+
+        def run(k):
+            O.softassign(X, Y, JMAX=1, I0=k, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
+                         moutlier=p.moutlier, precision="f32", trace=False)
+        unit, kind_out = "pose updates", "port"
+    t0 = time.perf_counter()
+    run(1)
+    one = time.perf_counter() - t0
+    k = int(max(1, min(n_full, round(target_s / max(one, 1e-6)))))
+    if k == 1:
+        dt = one
     else:
         t0 = time.perf_counter()
-        O.softassign(X, Y, JMAX=1, I0=1, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
-                     moutlier=p.moutlier, precision="f32", trace=False)
-        one = time.perf_counter() - t0
-        k = int(max(1, min(n_full, target_s / max(one, 1e-6))))
-        t0 = time.perf_counter()
-        O.softassign(X, Y, JMAX=1, I0=k, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
-                     moutlier=p.moutlier, precision="f32", trace=False)
+        run(k)
         dt = time.perf_counter() - t0
-    per_update = dt / k
-    regs_per_s = 1.0 / (per_update * n_full)
-    desc = ("first %d of %d pose updates of one registration (FP32 port of the reference algorithm, "
-            "OpenMP), scaled to a full registration" % (k, n_full))
-    if kind == "icp":
-        desc += "; ICP's port searches exhaustively (the reference's FLANN kd-tree is not available)"
-    return regs_per_s, desc, threads
+    return {"seconds": dt, "fraction": k / n_full, "kind": kind_out, "threads": threads,
+            "sample": "first %d of the %d %s of one registration of the full-size pair: %s; scaled to a "
+                      "registration by the share of the schedule it covers" % (k, n_full, unit, impl)}
+
+
+def cpu_baseline(kind, X, Y, p, target_s):
+    s = cpu_sample(kind, X, Y, p, target_s)
+    return {"value": s["fraction"] / s["seconds"], "unit": "registrations/s", "cores": s["threads"],
+            "kind": s["kind"], "sample": s["sample"]}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     if args.workload == BATCH_WORKLOAD:
-        pairs = batch_workload(args.seed)
-        per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
-        vals = []
-        for i in range(args.warmup + args.steps):
-            v, desc, thr = batch_cpu_baseline(pairs, per_step)
-            if i >= args.warmup:
-                vals.append(v)
-        value = float(np.mean(vals))
-        line = {"impl": "reference", "metric": "registrations/s", "value": value, "unit": "registrations/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(pairs) / value,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": batch_config(args, pairs),
-                "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": thr, "kind": "port",
-                                 "sample": desc},
-                "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
-    kind, X, Y = workload(args.workload, args.seed)
-    p = RefDefaults()
+        return run_reference_batch(args, world)
+    p = schedule(args)
+    kind, X, Y, fx = load_workload(args, p)
     per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
-    vals = []
+    secs, fracs = [], []
+    t_all = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        v, desc, thr = cpu_baseline(kind, X, Y, p, per_step)
+        s = cpu_sample(kind, X, Y, p, per_step)
         if i >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+            secs.append(s["seconds"])
+            fracs.append(s["fraction"])
+    value = float(np.sum(fracs) / np.sum(secs))
     line = {"impl": "reference", "metric": "registrations/s", "value": value, "unit": "registrations/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * float(np.mean(secs)),
+            "registrations_per_step": float(np.mean(fracs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config_of(args, kind, X, Y, p),
-            "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": thr, "kind": "port",
-                             "sample": desc},
-            "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic", "config": config_of(args, kind, X, Y, p, fx),
+            "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": s["threads"], "kind": s["kind"],
+                             "sample": s["sample"]},
+            "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_all,
+            "note": "each step is the sample named in cpu_baseline.sample (ms_per_step is its duration); value = "
+                    "registrations covered by the timed samples / their total time"}
     print(json.dumps(line), flush=True)
 
 
-def config_of(args, kind, X, Y, p):
-    c = {"workload": args.workload, "algorithm": kind, "N": int(len(X)), "M": int(len(Y)),
-         "pose_updates_per_registration": pose_updates(kind, p), "seed": args.seed,
-         "l2": "flushed between steps (256 MiB write), outside the timed events",
-         "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
-    if kind == "softassign":
-        c.update(JMAX=p.JMAX, I0=p.I0, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR)
-    elif kind == "icp":
-        c.update(maxIteration=p.maxIteration, search="exhaustive nearest neighbour")
+# ------------------------------------------------------------------ accuracy
+def accuracy(kind, X, Y, p, R, t, fixture):
+    """Error of a registration against the FP64 oracle on the same inputs:
+    the committed fixture where one matches, else the oracle run here when it
+    is cheap (at most 2e10 affinity evaluations), else None."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    src = None
+    if fixture:
+        g = np.load(fixture)
+        Ro, to = g["R"], g["t"]
+        gap = float(g["trace"][-1, 30])
+        src = "FP64 oracle (oracle/cesa_oracle.c), stored in %s" % os.path.relpath(fixture, HERE)
     else:
-        c.update(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_inf, sigma_factor=p.sigma_factor, d_02=p.d_02)
-    return c
+        _, _, elems = algorithmic_work(kind, len(X), len(Y), p)
+        if elems > 2e10:
+            return {"vs": None, "note": "the FP64 oracle is not run at this size here (%.2g affinity evaluations); "
+                                        "the tests compare a cut schedule with a stored oracle result" % elems}
+        from oracle import oracle as O
+        O.set_threads(os.cpu_count() or 1)
+        if kind == "emicp":
+            Ro, to, tr = O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=p.sigma_inf, sigma_factor=p.sigma_factor,
+                                 d_02=p.d_02)
+        elif kind == "softassign":
+            Ro, to, tr = O.softassign(X, Y, JMAX=p.JMAX, I0=p.I0, I1=p.I1, alpha=p.alpha, T_0=p.T_0,
+                                      TFACTOR=p.TFACTOR, moutlier=p.moutlier)
+        else:
+            Ro, to, tr, _ = O.icp(X, Y, maxIteration=p.maxIteration)
+        gap = float(tr[-1, 30]) if len(tr) else None
+        src = "FP64 oracle (oracle/cesa_oracle.c), run here on the same inputs"
+    extent = float(np.ptp(np.asarray(X, np.float64), 0).max())
+    e_r = W.rotation_error_deg(np.asarray(R, np.float64).reshape(3, 3), Ro)
+    e_t = float(np.abs(np.asarray(t, np.float64) - to).max() / extent)
+    return {"vs": src, "rot_err_deg": e_r, "t_err_over_extent": e_t, "bound_rot_deg": ROT_BOUND_DEG,
+            "bound_t_over_extent": T_BOUND_REL, "within_bound": bool(e_r <= ROT_BOUND_DEG and e_t <= T_BOUND_REL),
+            "horn_eigen_gap_final": gap}
 
 
+# ------------------------------------------------------------------ helpers
 def load_peaks():
     from cuda_emicp_softassign_gb300 import build
     L = ctypes.CDLL(build.PEAKS_LIB)
@@ -330,9 +456,22 @@ def whole_job_rate(steps, world, seconds):
     return steps * world / seconds
 
 
-BATCH_WORKLOAD = "c4_batch_256"
+def stored_traffic(roofline, key):
+    """dram bytes per launch of the workload's kernel from a stored ncu capture
+    (profiles/ncu_traffic.json, summarised in profiles/*.md). ncu cannot run
+    inside the bench, so this figure is copied from that capture, not
+    measured in this run; the line says so."""
+    path = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return
+    entry = json.load(open(path)).get(key)
+    if entry:
+        roofline["traffic"] = entry["bytes_per_launch"]
+        roofline["traffic_source"] = ("copied from a stored ncu capture (profiles/ncu_traffic.json, %s), "
+                                      "not measured in this run" % entry.get("profile", "profiles/"))
 
 
+# ------------------------------------------------------------------ batch
 def batch_workload(seed, count=256):
     """Config 4: 256 pairs, N and M log-uniform in [500, 20000], config-1
     generator per pair; even pairs EM-ICP (default parameters), odd pairs
@@ -340,11 +479,23 @@ def batch_workload(seed, count=256):
     import cuda_emicp_softassign_gb300 as cesa
     from cuda_emicp_softassign_gb300 import workloads as W
     out = []
-    for kind, X, Y, _, _ in W.batch_pairs(count=count, seed=seed):
+    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=seed)[:count]:
         if kind == "emicp":
             out.append((cesa.ALGO_EMICP, X, Y, cesa.Params.default()))
         else:
             out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa.Params.default(JMAX=60)))
+    return out
+
+
+def batch_pairs_cpu(seed, count=256):
+    """The config-4 pairs without loading libcesa: (algorithm, X, Y, params)."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    out = []
+    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=seed)[:count]:
+        p = RefDefaults()
+        if kind != "emicp":
+            p.JMAX = 60
+        out.append((0 if kind == "emicp" else 1, X, Y, p))
     return out
 
 
@@ -366,31 +517,35 @@ def batch_config(args, pairs):
             "softassign_pairs": sum(1 for a, _, _, _ in pairs if a == 1),
             "N_range": [int(min(n)), int(max(n))], "M_range": [int(min(m)), int(max(m))],
             "softassign_JMAX": 60, "seed": args.seed,
-            "l2": "flushed between steps (256 MiB write), outside the timed events",
+            "l2": "flushed between steps (256 MiB write), outside the timed region",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
-def batch_cpu_baseline(pairs, target_s):
-    """FP32 port of the reference algorithm on the host: time per affinity
-    element measured on the first pose updates of a few pairs of the batch,
-    scaled to the batch's total elements. Returns (registrations/s, desc, threads)."""
+def batch_cpu_sample(pairs, target_s):
+    """One bounded CPU sample of the batch: the first pose updates of the
+    first pairs (EM-ICP through the reference's own emicp_cpu() where built,
+    Softassign through the FP32 port), timed per affinity element and scaled
+    to the batch's total elements. Returns (registrations/s, seconds, desc,
+    kind, threads)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     O.set_threads(threads)
+    use_ref = O.ref() is not None
     _, _, total = batch_work(pairs)
-    spent = 0.0
-    elems = 0.0
+    spent = elems = 0.0
     used = 0
-    for algo, X, Y, p in pairs[:8]:
+    for algo, X, Y, p in pairs:
         if spent > target_s:
             break
         t0 = time.perf_counter()
         if algo == 0:
-            O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=p.sigma_p2 * 0.5, sigma_factor=p.sigma_factor,
-                    d_02=p.d_02, precision="f32", trace=False)
-            n = pose_updates("emicp", type("P", (), dict(sigma_p2=p.sigma_p2, sigma_inf=p.sigma_p2 * 0.5,
-                                                          sigma_factor=p.sigma_factor))())
-            elems += float(len(X)) * len(Y) * n
+            si = sigma_inf_after(p, 6)
+            if use_ref:
+                O.ref_emicp_cpu(X, Y, sigma_p2=p.sigma_p2, sigma_inf=si, sigma_factor=p.sigma_factor, d_02=p.d_02)
+            else:
+                O.emicp(X, Y, sigma_p2=p.sigma_p2, sigma_inf=si, sigma_factor=p.sigma_factor, d_02=p.d_02,
+                        precision="f32", trace=False)
+            elems += float(len(X)) * len(Y) * 6
         else:
             O.softassign(X, Y, JMAX=1, I0=1, I1=p.I1, alpha=p.alpha, T_0=p.T_0, TFACTOR=p.TFACTOR,
                          moutlier=p.moutlier, precision="f32", trace=False)
@@ -399,9 +554,30 @@ def batch_cpu_baseline(pairs, target_s):
         used += 1
     per_elem = spent / elems
     regs = len(pairs) / (per_elem * total)
-    desc = ("first pose updates of %d of the %d pairs (FP32 port of the reference algorithm, OpenMP): "
-            "%.3g s per affinity element, scaled to the batch's %.3g elements" % (used, len(pairs), per_elem, total))
-    return regs, desc, threads
+    desc = ("first pose updates of %d of the %d pairs (EM-ICP: %s; Softassign: the FP32 port): %.3g s per affinity "
+            "element, scaled to the batch's %.3g elements"
+            % (used, len(pairs), "the reference's own emicp_cpu()" if use_ref else "the FP32 port", per_elem, total))
+    return regs, spent, desc, ("reference+port" if use_ref else "port"), threads
+
+
+def run_reference_batch(args, world):
+    pairs = batch_pairs_cpu(args.seed, args.pairs)
+    per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
+    secs, regs = [], []
+    for i in range(args.warmup + args.steps):
+        v, dt, desc, kind, thr = batch_cpu_sample(pairs, per_step)
+        if i >= args.warmup:
+            secs.append(dt)
+            regs.append(v * dt)
+    value = float(np.sum(regs) / np.sum(secs))
+    line = {"impl": "reference", "metric": "registrations/s", "value": value, "unit": "registrations/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(secs)),
+            "registrations_per_step": float(np.mean(regs)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": batch_config(args, pairs),
+            "cpu_baseline": {"value": value, "unit": "registrations/s", "cores": thr, "kind": kind, "sample": desc},
+            "e2e": {"value": value, "unit": "registrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args, rank, world, local):
@@ -412,7 +588,7 @@ def run_batch(args, rank, world, local):
     import cuda_emicp_softassign_gb300 as cesa
 
     torch.cuda.set_device(local)
-    pairs = batch_workload(args.seed)
+    pairs = batch_workload(args.seed, args.pairs)
     dev = []
     pose0 = torch.tensor(np.r_[np.eye(3).reshape(-1), np.zeros(3)], dtype=torch.float32, device="cuda")
     for algo, X, Y, p in pairs:
@@ -456,8 +632,10 @@ def run_batch(args, rank, world, local):
     assert cesa.stream_status(stream) == 0 and int(status.item()) == 0
     total_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
 
-    # the same pairs, one pair per launch (single-pair device entry points)
+    # the same pairs, one pair per launch (single-pair device entry points); per pair the time of
+    # its own launch sequence, so that the sum of the pairs' latency floors is known too
     single_ms = 0.0
+    per_pair_ms = []
     for algo, dX, dY, dRt, p in dev:
         dRt.copy_(pose0)
         flush.zero_()
@@ -467,7 +645,8 @@ def run_batch(args, rank, world, local):
                                                                       stream=stream)
         e1.record(stream)
         e1.synchronize()
-        single_ms += e0.elapsed_time(e1)
+        per_pair_ms.append(e0.elapsed_time(e1))
+        single_ms += per_pair_ms[-1]
 
     # end to end through the host-pointer batch entry point
     e2e_steps = max(1, min(args.steps, 3))
@@ -497,7 +676,16 @@ def run_batch(args, rank, world, local):
                 "ex2_achieved_tops": ex2_ops / mean_s / 1e12,
                 "ex2_peak_tops": ex2_peak / 1e12 if ex2_peak else None,
                 "ops_per_batch": fp32_ops}
-    cpu_v, cpu_desc, cpu_thr = batch_cpu_baseline(pairs, args.cpu_sample_s)
+    # Lower bound of the batch's time: the work at the measured FP32 peak, and no pair can finish
+    # faster than its own latency floor (its single-pair launch, which already runs at or near the
+    # peak for large pairs). The batch cannot beat max(total work / peak, longest single pair).
+    work_s = fp32_ops / fp32_peak if fp32_peak else None
+    longest = max(per_pair_ms) * 1e-3
+    bound_s = max(work_s or 0.0, longest)
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt, desc, kind, thr = batch_cpu_sample(pairs, args.cpu_sample_s)
+        cpu = {"value": v, "unit": "registrations/s", "cores": thr, "kind": kind, "sample": desc}
     h2d = sum((len(X) + len(Y)) * 3 * 4 + 48 for _, X, Y, _ in pairs)
     line = {"metric": "registrations/s", "value": value, "unit": "registrations/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -507,9 +695,13 @@ def run_batch(args, rank, world, local):
             "gelem_per_s": elems * args.steps * world / (total_ms * 1e-3) / 1e9,
             "one_pair_per_launch": {"value": world * npairs / (single_ms * 1e-3), "unit": "registrations/s",
                                     "ms": single_ms, "batched_speedup": single_ms / (total_ms / args.steps)},
+            "batch_time_bound": {"ms": bound_s * 1e3, "work_at_fp32_peak_ms": work_s * 1e3 if work_s else None,
+                                 "longest_single_pair_ms": longest * 1e3,
+                                 "max_speedup_vs_one_pair_per_launch": single_ms * 1e-3 / bound_s,
+                                 "note": "the batch cannot finish before its FP32 work at the measured peak, "
+                                         "nor before its longest pair alone"},
             "roofline": roofline,
-            "cpu_baseline": {"value": cpu_v, "unit": "registrations/s", "cores": cpu_thr, "kind": "port",
-                             "sample": cpu_desc},
+            "cpu_baseline": cpu,
             "e2e": {"value": world * npairs / e2e_s, "unit": "registrations/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 48 * npairs},
             "clocks": clocks,
@@ -518,6 +710,7 @@ def run_batch(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ adjoint
 def measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0, reps=3):
     """Forward + adjoint (cesa_<kind>_forward_device then
     cesa_<kind>_backward_device for the loss |R - I|^2 + |t|^2), CUDA events.
@@ -525,7 +718,6 @@ def measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0, reps=3):
     reps) and (taped forward + backward) / plain forward. Softassign's taped
     forward runs the matrix-free kernel, so its plain forward is timed in that
     form too."""
-    import copy
     import torch
     L = cesa.lib()
     tape_bytes = getattr(L, "cesa_%s_tape_bytes" % kind)
@@ -567,21 +759,68 @@ def measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0, reps=3):
                 min(best[2], e4.elapsed_time(e5))]
     note = ("taped forward records pose, moments, Horn eigenbasis and per-row C, lambda, u per step; "
             "the backward recomputes the affinities (no N x M storage)") if kind == "emicp" else \
-        ("taped forward (matrix-free) records the input pose and slack s, u of every pose update; the backward "
-         "recomputes each update's Sinkhorn scalings and affinities (no N x M storage)")
+        ("taped forward (matrix-free) records every Sinkhorn pass's scalings and sums; the backward recomputes "
+         "the affinities in each K product (no N x M storage)")
     return {"fwd_ms": best[0], "fwd_taped_ms": best[1], "bwd_ms": best[2],
             "fwd_plus_bwd_over_fwd": (best[1] + best[2]) / best[0], "tape_bytes": int(nbytes),
             "loss": "|R - I|_F^2 + |t|^2 of the registered pose", "note": note}
 
 
+# ------------------------------------------------------------------ timeline
+TL_NAMES = {
+    "emicp": {1: "start", 2: "a unit's first chunk landed", 3: "unit swept", 4: "unit's row partials stored",
+              5: "grid barrier after the sweep", 8: "rows completed, block moments, grid barrier",
+              6: "moment records reduced", 7: "S (nine threads) + pose solve"},
+    "softassign": {1: "start", 2: "final: last column pass completed", 3: "row pass completed (cluster)",
+                   4: "column sweep + partial store (final: record store)",
+                   5: "barrier (column tile's CTAs; the grid before the pose)", 6: "moment records reduced",
+                   7: "Horn solve", 8: "cluster barrier (final sweep included after 2)",
+                   10: "moments: cluster barrier", 11: "final rows finalised", 12: "moments summed",
+                   13: "S formed", 14: "column pass completed (band partials)", 15: "row sweep + warp reduction"},
+}
+
+
+def run_timeline(args):
+    """Mean duration of each phase of a pose update in block 0 of the
+    persistent grid (the library's %globaltimer timeline, cesa_report), and
+    for Softassign how many updates the certified pose solve took."""
+    import cuda_emicp_softassign_gb300 as cesa
+    p = schedule(args)
+    kind, X, Y, _ = load_workload(args, p)
+    form = "banded" if (kind == "softassign" and args.sinkhorn_form == "auto") else args.sinkhorn_form
+    q = cesa_params(cesa, p, form)
+    fn = cesa.emicp if kind == "emicp" else cesa.softassign
+    _, _, tr, _ = fn(X, Y, param=q, trace=True)
+    cap = 320 * 40 * max(1, pose_updates(kind, p))  # blocks x entries per update x updates
+    _, _, tl, rep = fn(X, Y, param=q, timeline=cap)
+    rows = cesa.timeline_table(tl, rep.grid_blocks)
+    b0 = rows[rows[:, 0] == 0][:, 1:]
+    starts = np.where(b0[:, 0] == 1)[0]
+    segs = [b0[a:b + 1] for a, b in zip(starts[1:-1], starts[2:])]
+    segs = [sg for sg in segs if len(sg) == len(segs[0])]
+    names = TL_NAMES["emicp" if kind == "emicp" else "softassign"]
+    out = {"workload": args.workload, "N": len(X), "M": len(Y), "grid_blocks": rep.grid_blocks,
+           "sinkhorn_form": FORM_NAMES.get(rep.sinkhorn_form) if kind == "softassign" else None,
+           "updates_in_mean": len(segs),
+           "ns_per_update": float(np.mean([sg[-1, 1] - sg[0, 1] for sg in segs])), "phases": []}
+    for i in range(1, len(segs[0])):
+        out["phases"].append((names.get(int(segs[0][i, 0]), "next update"),
+                              float(np.mean([sg[i, 1] - sg[i - 1, 1] for sg in segs]))))
+    if len(tr):
+        out["certified_pose_solves"] = int((tr[:, 30] == -1).sum())
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ ours
 def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
     import cuda_emicp_softassign_gb300 as cesa
 
     torch.cuda.set_device(local)
-    kind, X, Y = workload(args.workload, args.seed)
-    p = params_for(cesa, kind, args.sinkhorn_form)
+    sp = schedule(args)
+    kind, X, Y, fx = load_workload(args, sp)
+    p = cesa_params(cesa, sp, args.sinkhorn_form)
     N, M = len(X), len(Y)
     tuned = None
     if kind == "softassign" and args.tune:
@@ -598,13 +837,10 @@ def run_ours(args, rank, world, local):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def one_step():
-        dRt.copy_(pose0)
-        dev_call(dX, dY, dRt, param=p, d_status=status, stream=stream)
-
     for _ in range(args.warmup):
         flush.zero_()
-        one_step()
+        dRt.copy_(pose0)
+        dev_call(dX, dY, dRt, param=p, d_status=status, stream=stream)
     torch.cuda.synchronize()
     assert cesa.stream_status(stream) == 0
     if world > 1:
@@ -664,7 +900,7 @@ def run_ours(args, rank, world, local):
 
     regs = args.steps * world
     value = whole_job_rate(args.steps, world, total_ms * 1e-3)
-    fp32_ops, ex2_ops, elems = algorithmic_work(kind, N, M, p)
+    fp32_ops, ex2_ops, elems = algorithmic_work(kind, N, M, sp)
     mean_s = total_ms * 1e-3 / args.steps
     fp32_peak, ex2_peak = load_peaks()
     achieved = fp32_ops / mean_s / 1e12
@@ -682,7 +918,6 @@ def run_ours(args, rank, world, local):
     form_used = None
     if kind == "softassign":
         # the form the library resolved for this request (AUTO: tuned or by size), as it reports it
-        import copy
         q = copy.copy(p)
         q.JMAX = 1
         rep = cesa.softassign(X, Y, param=q, trace=True)[3]
@@ -692,54 +927,48 @@ def run_ours(args, rank, world, local):
                              "keeps the tile in shared memory for the other 2*I1 sweeps, so it executes "
                              "fewer operations than this per-sweep count: per element and pose update 1 ex2 "
                              "and %d FP32 ops (the first row sweep 8, each later Sinkhorn sweep 1, the final "
-                             "sweep 5)" % (8 + (2 * p.I1 - 1) + 5))
+                             "sweep 5)" % (8 + (2 * sp.I1 - 1) + 5))
         roofline["kernel"] = "softassign_band_kernel"
-        roofline["executed_fp32_ops_per_registration"] = float(N) * float(M) * pose_updates(kind, p) * (
-            8 + (2 * p.I1 - 1) + 5)
+        roofline["executed_fp32_ops_per_registration"] = float(N) * float(M) * pose_updates(kind, sp) * (
+            8 + (2 * sp.I1 - 1) + 5)
     if form_used == "materialised":
         hbm_peak = None
         try:
             hbm_peak = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))["hbm_gbs"]
         except (OSError, KeyError, ValueError):
             pass
-        gbs = materialised_bytes(N, M, p) / mean_s / 1e9
+        gbs = materialised_bytes(N, M, sp) / mean_s / 1e9
         roofline = {"bound": "hbm", "kernel": "softassign_mat_kernel", "achieved": gbs,
                     "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak if hbm_peak else None,
                     "traffic": None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
-                    "bytes_per_registration": materialised_bytes(N, M, p),
+                    "bytes_per_registration": materialised_bytes(N, M, sp),
                     "note": "achieved = algorithmic HBM bytes (4 B per element written once and read by "
                             "each of the 2*I1 later passes, per pose update) / event time"}
-    traffic_file = os.path.join(HERE, "profiles", "ncu_traffic.json")
-    if os.path.exists(traffic_file):
-        key = args.workload + (":" + form_used if form_used in ("materialised", "banded") else "")
-        entry = json.load(open(traffic_file)).get(key)
-        if entry:
-            roofline["traffic"] = entry["bytes_per_launch"]
-            roofline["traffic_source"] = "ncu dram bytes per launch, profiles/ncu_traffic.json"
-    cpu_v, cpu_desc, cpu_thr = cpu_baseline(kind, X, Y, p, args.cpu_sample_s)
+    if args.size is None and args.sigma_inf is None and args.jmax is None and args.i0 is None:
+        stored_traffic(roofline, args.workload + (":" + form_used if form_used in ("materialised", "banded") else ""))
+    cpu = None if args.no_cpu_baseline else cpu_baseline(kind, X, Y, sp, args.cpu_sample_s)
+    acc = accuracy(kind, X, Y, sp, R_dev[:9], R_dev[9:12], fx)
     h2d = (N + M) * 3 * 4 + 12 * 4
     line = {"metric": "registrations/s", "value": value, "unit": "registrations/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator of the workload; see cuda_emicp_softassign_gb300/workloads.py)",
-            "config": config_of(args, kind, X, Y, p),
+            "config": config_of(args, kind, X, Y, sp, fx),
+            "accuracy": acc,
             "gelem_per_s": elems * regs / (total_ms * 1e-3) / 1e9,
             "roofline": roofline,
-            "cpu_baseline": {"value": cpu_v, "unit": "registrations/s", "cores": cpu_thr, "kind": "port",
-                             "sample": cpu_desc},
+            "cpu_baseline": cpu,
             "e2e": {"value": whole_job_rate(args.steps, world, e2e_s), "unit": "registrations/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * 4},
             "clocks": clocks,
             "gpu_launches": kernels_per_registration(kind, form_used) * args.steps,
             "wall_s_timed_region": t_wall}
     if kind == "softassign":
-        line["config"]["sinkhorn_form"] = form_used
-        line["config"]["sinkhorn_tuner"] = tuned
+        line["sinkhorn"] = {"form": form_used, "requested": args.sinkhorn_form, "tuner": tuned}
     if kind == "icp":
         # value is the default search (a uniform grid from 4096 target points on), whose work depends
         # on the data; the FP32 roofline is that of the exhaustive search, timed here on the same pair
-        import copy
         pe = copy.copy(p)
         pe.icp_search = cesa.ICP_SEARCH_EXHAUSTIVE
         exh = []
@@ -778,6 +1007,8 @@ def run_ours(args, rank, world, local):
 def main():
     args = parse_args()
     rank, world, local = dist_env()
+    if args.timeline:
+        return run_timeline(args)
     if world > 1:
         import torch
         import torch.distributed as dist

@@ -80,7 +80,31 @@ std::mutex g_mu;
 std::map<std::pair<int, cudaStream_t>, StreamCtx> g_ctx;
 std::map<int, cudaStream_t> g_own_stream;
 
-StreamCtx& ctx_for(int dev, cudaStream_t st) { return g_ctx[std::make_pair(dev, st)]; }
+// Streams whose last call was cesa_emicp_device_noalloc, with the control
+// block of its fixed scratch. A fixed table, so that recording a no-allocation
+// call allocates nothing, not even host memory; when it is full the oldest
+// record is replaced. Guarded by g_mu.
+struct NoallocRec {
+  int dev = -1;
+  cudaStream_t st = nullptr;
+  void* ctl = nullptr;
+};
+constexpr int kNoallocRecs = 64;
+NoallocRec g_noalloc_rec[kNoallocRecs];
+int g_noalloc_next = 0;
+
+NoallocRec* noalloc_rec(int dev, cudaStream_t st) {
+  for (auto& r : g_noalloc_rec)
+    if (r.ctl && r.dev == dev && r.st == st) return &r;
+  return nullptr;
+}
+
+// The context of a call that enqueues work on (dev, st): from here on the
+// stream's status is that of this call's workspace.
+StreamCtx& ctx_for(int dev, cudaStream_t st) {
+  if (NoallocRec* r = noalloc_rec(dev, st)) *r = NoallocRec{};
+  return g_ctx[std::make_pair(dev, st)];
+}
 
 int map_cuda(cudaError_t e) {
   if (e == cudaSuccess) return CESA_OK;
@@ -90,6 +114,10 @@ int map_cuda(cudaError_t e) {
   return CESA_ERR_CUDA;
 }
 
+}  // namespace
+
+// Argument checks and schedule length shared by the entry points of this
+// file and cesa_noalloc.cu (declared in cesa_kernels.h).
 uint64_t timeout_ns_of(const cesa_params* p) {
   const int ms = (p && p->timeout_ms > 0) ? p->timeout_ms : 10000;
   return (uint64_t)ms * 1000000ull;
@@ -122,6 +150,8 @@ int check_emicp_params(const cesa_params* p) {
   if (p->sigma_p2 > p->sigma_inf && !(p->sigma_factor < 1.f)) return CESA_ERR_INVALID_ARGUMENT;
   return CESA_OK;
 }
+
+namespace {
 
 int check_sa_params(const cesa_params* p) {
   if (!p) return CESA_ERR_INVALID_ARGUMENT;
@@ -406,6 +436,20 @@ uint64_t batch_timeout_ns(const cesa_pair* pairs, int npairs) {
 }
 
 }  // namespace
+
+std::mutex& api_mutex() { return g_mu; }
+
+void note_noalloc_call(int dev, cudaStream_t st, void* scratch) {
+  NoallocRec* r = noalloc_rec(dev, st);
+  if (!r) {
+    r = &g_noalloc_rec[g_noalloc_next];
+    g_noalloc_next = (g_noalloc_next + 1) % kNoallocRecs;
+  }
+  r->dev = dev;
+  r->st = st;
+  r->ctl = scratch;
+}
+
 }  // namespace cesa
 
 using namespace cesa;
@@ -1053,10 +1097,16 @@ int cesa_stream_status(cesa_stream_t stream) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
   std::lock_guard<std::mutex> lock(g_mu);
-  auto it = g_ctx.find(std::make_pair(dev, (cudaStream_t)stream));
-  if (it == g_ctx.end() || !it->second.ws.p) return CESA_ERR_INVALID_ARGUMENT;
+  void* ctl = nullptr;
+  if (NoallocRec* r = noalloc_rec(dev, (cudaStream_t)stream)) {
+    ctl = r->ctl;
+  } else {
+    auto it = g_ctx.find(std::make_pair(dev, (cudaStream_t)stream));
+    if (it != g_ctx.end()) ctl = it->second.ws.p;
+  }
+  if (!ctl) return CESA_ERR_INVALID_ARGUMENT;
   int status = 0, steps = 0;
-  const int e = read_ws_status(it->second.ws.p, (cudaStream_t)stream, &status, &steps);
+  const int e = read_ws_status(ctl, (cudaStream_t)stream, &status, &steps);
   if (e) return map_cuda((cudaError_t)e);
   return status;
 }

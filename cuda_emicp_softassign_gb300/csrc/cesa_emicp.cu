@@ -20,6 +20,8 @@
 // Coordinates are centred on the device (FP32 offsets oX, oY) before the
 // loop. EM-ICP's S is translation invariant, so only Xc, Yc and t are shifted
 // back; the pose enters and leaves in the caller's frame.
+#include <atomic>
+
 #include "cesa_kernels.h"
 #include "cesa_ops.cuh"
 #include "cesa_pose.h"
@@ -387,11 +389,15 @@ int read_ws_status(void* ws, cudaStream_t st, int* status, int* steps, int* tl_w
 
 // Smem opt-in and occupancy for a persistent kernel: blocks per SM x SMs.
 int persistent_grid_limit(int device, const void* kernel, size_t smem) {
-  static int cached_dev = -1;
-  static int sms = 0;
-  if (cached_dev != device) {
+  // SM count per device, filled on first use; each entry is written once with
+  // its device's own value, so concurrent callers on other devices cannot mix
+  // them up.
+  static std::atomic<int> sms_of[64];
+  int sms = 0;
+  if (device >= 0 && device < 64) sms = sms_of[device].load(std::memory_order_relaxed);
+  if (sms <= 0) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cached_dev = device;
+    if (device >= 0 && device < 64 && sms > 0) sms_of[device].store(sms, std::memory_order_relaxed);
   }
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 0;

@@ -4,7 +4,25 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
+struct cesa_params;
+
 namespace cesa {
+
+// Argument checks of the C ABI (cesa_api.cu), shared by every entry point:
+// CESA_OK or CESA_ERR_INVALID_ARGUMENT.
+int check_points(const float* X, int N, const float* Y, int M);
+int check_emicp_params(const cesa_params* p);
+// Sigma steps of the EM-ICP schedule (stepped in FP32), or -1 if it never ends.
+long emicp_steps(float sigma_p2, float sigma_inf, float sigma_factor);
+// Limit of the device-side waits in ns (p->timeout_ms, 0 selects 10 s).
+uint64_t timeout_ns_of(const cesa_params* p);
+// The lock every entry point holds while it plans and enqueues.
+std::mutex& api_mutex();
+// Records that the last call on (dev, st) ran on the no-allocation scratch,
+// whose control block cesa_stream_status then reads. Call with api_mutex held.
+void note_noalloc_call(int dev, cudaStream_t st, void* scratch);
 
 struct SweepGeomH {
   int n_own, n_stream, nblk, slices, slice_len, units;

@@ -1,7 +1,9 @@
-// C++ drop-in layer: emicp(), softassign(), icp(), findRTfromS() and cloud2data()
-// with the reference's signatures (src/3dregistration.h:82-116), implemented
+// C++ drop-in layer: emicp(), softassign(), emicp_cpu(), icp(), findRTfromS(),
+// printRT() and cloud2data() with the reference's signatures
+// (src/3dregistration.h:82-116), implemented
 // over the C ABI of libcesa.so. Compile this file into the program (as the
 // reference README asks for emicp.cu / softassign.cu) and link -lcesa.
+#include <atomic>
 #include <cstdio>
 #include <vector>
 
@@ -62,6 +64,17 @@ void emicp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
   run("emicp", cesa_emicp, cloud_target, cloud_source, h_R, h_t, param);
 }
 
+void emicp_cpu(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
+               const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float* h_R, float* h_t,
+               const registrationParameters& param) {
+  // There is no CPU registration path in this library (a CPU fallback would
+  // hide a missing GPU); the reference CLI's -emicpcpu flag is handled alike.
+  static std::atomic<bool> noted{false};
+  if (!noted.exchange(true))
+    std::fprintf(stderr, "emicp_cpu: runs the GPU EM-ICP (this library has no CPU registration path)\n");
+  run("emicp_cpu", cesa_emicp, cloud_target, cloud_source, h_R, h_t, param);
+}
+
 void icp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
          const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float* h_R, float* h_t,
          const registrationParameters& param) {
@@ -79,6 +92,12 @@ void findRTfromS(const float* h_Xc, const float* h_Yc, const float* h_S, float* 
   // src/findRTfromS.cpp:110)
   thread_local float q_pre[4] = {1.f, 0.f, 0.f, 0.f};
   cesa_find_rt_from_s(h_Xc, h_Yc, h_S, h_R, h_t, q_pre);
+}
+
+void printRT(const float* R, const float* t) {
+  std::printf("R\n");
+  for (int i = 0; i < 3; ++i) std::printf("%f %f %f \n", R[3 * i], R[3 * i + 1], R[3 * i + 2]);
+  std::printf("t\n%f %f %f \n", t[0], t[1], t[2]);
 }
 
 void cloud2data(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud, float** X, int& Xsize) {

@@ -1,9 +1,10 @@
 /*
  * Drop-in replacement for the reference's public header
  * (src/3dregistration.h): the same registrationParameters fields, in the same
- * order, and the same entry points emicp(), softassign(), icp(), findRTfromS() and
- * cloud2data(). Their implementation (registration.cpp in the package's csrc/
- * directory) runs the GB300 kernels of libcesa.so through the C ABI in cesa.h.
+ * order, and the same entry points emicp(), softassign(), emicp_cpu(), icp(),
+ * findRTfromS(), printRT() and cloud2data(). Their implementation
+ * (registration.cpp in the package's csrc/ directory) runs the GB300 kernels
+ * of libcesa.so through the C ABI in cesa.h.
  *
  * With a real PCL installation this header includes PCL, like the reference.
  * Without one (or with CESA_NO_PCL defined) it uses the minimal PointXYZ /
@@ -78,11 +79,24 @@ void emicp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
            const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float *h_R, float *h_t,
            const registrationParameters &param);
 
+/* The reference's CPU EM-ICP (src/emicp_cpu.cpp:186-547, declared at
+ * src/3dregistration.h:91-95). This library has no CPU registration path: the
+ * call runs the GPU EM-ICP of emicp() with the same parameters, and says so
+ * once on stderr. Its result is emicp()'s. */
+void emicp_cpu(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
+               const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float *h_R, float *h_t,
+               const registrationParameters &param);
+
 void icp(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_target,
          const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud_source, float *h_R, float *h_t,
          const registrationParameters &param);
 
 void findRTfromS(const float *h_Xc, const float *h_Yc, const float *h_S, float *h_R, float *h_t);
+
+/* Prints R (three rows) and t on stdout in the reference CLI's layout
+ * (src/main.cpp:184-195, declared at src/3dregistration.h:111): a line "R",
+ * three lines of three "%f " entries, a line "t", one line of three. */
+void printRT(const float *R, const float *t);
 
 void cloud2data(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud, float **X, int &Xsize);
 void cloud2data(const pcl::PointCloud<pcl::PointXYZ>::Ptr cloud, boost::shared_array<float> &X,

@@ -185,22 +185,28 @@ int cesa_register_batch(const cesa_pair* pairs, int npairs, cesa_report* report)
  * for callers that cannot call cudaMalloc, such as a plugin inside a host
  * application that owns no device heap, or a real-time pipeline that forbids
  * allocation after start-up. It computes the same result as
- * cesa_emicp_device (same arguments and conventions), but its scratch is a
- * fixed 16 MiB device array inside libcesa.so, held on every GPU that loads
- * the library until the process exits. That is enough for about N = M =
- * 100,000 points. Larger problems return CESA_ERR_NOALLOC_LIMIT, and nothing
- * is enqueued. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * Every call on a device shares the one array: calls that overlap on the GPU
- * (different streams, or a second call enqueued before the first has
- * finished on another stream) race and corrupt each other's results.
- * Serialise them on one stream or synchronise between them. No cudaMalloc,
- * cudaFree or allocating library routine is called.
+ * cesa_emicp_device, bit for bit (same arguments and conventions), but its
+ * scratch is a fixed 16 MiB device array inside libcesa.so, held on every GPU
+ * that loads the library until the process exits. N = M = 100,000 points fit
+ * on a GB300 (the workspace grows with N + M and with the SM count). Larger
+ * problems return CESA_ERR_NOALLOC_LIMIT, and nothing is enqueued. The
+ * device-side status goes to *d_status when it is non-NULL; either way
+ * cesa_stream_status(stream) reports it, read from the fixed scratch, until
+ * another call is enqueued on that stream. The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture. Every call on a device shares the one
+ * array, which keeps the last call's contents (each call clears what must
+ * start at zero): calls that overlap on the GPU (different streams, or a
+ * second call enqueued before the first has finished on another stream) race
+ * and corrupt each other's results. Serialise them on one stream or
+ * synchronise between them. No cudaMalloc, cudaFree or allocating library
+ * routine is called.
  */
 int cesa_emicp_device_noalloc(const float* dX, int N, const float* dY, int M, float* dRt,
                               const cesa_params* p, int* d_status, cesa_stream_t stream);
 
-/* Status of the last registration enqueued on `stream` (synchronises it). */
+/* Status of the last registration enqueued on `stream` (synchronises it);
+ * CESA_ERR_INVALID_ARGUMENT when nothing has been enqueued on it. */
 int cesa_stream_status(cesa_stream_t stream);
 
 /*

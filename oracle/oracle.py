@@ -22,6 +22,7 @@ T_XC, T_YC, T_S, T_R, T_T, T_GAP, T_LMAX = slice(3, 6), slice(6, 9), slice(9, 18
 
 _lib = None
 _ref = None
+_ref_gpu = None
 
 _f = ctypes.c_float
 _i = ctypes.c_int
@@ -81,6 +82,27 @@ def ref():
         _ref.ref_find_rt_from_s.restype = None
         _ref.ref_find_rt_from_s.argtypes = [_p] * 5
     return _ref
+
+
+def ref_gpu():
+    """The reference's own GPU code (softassign(), emicp()) run on the host
+    (oracle/emu), or None where it cannot be built."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        so = None
+        try:
+            so = _build.build_reference_gpu()
+        except Exception:  # noqa: BLE001 -- optional
+            so = None
+        if so is None or not os.path.exists(so):
+            return None
+        os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+        _ref_gpu = ctypes.CDLL(so)
+        _ref_gpu.ref_softassign.restype = _i
+        _ref_gpu.ref_softassign.argtypes = [_p, _i, _p, _i, _p, _p, _i, _i, _i, _f, _f, _f, _f, _p, _i, _i]
+        _ref_gpu.ref_emicp_gpu.restype = _i
+        _ref_gpu.ref_emicp_gpu.argtypes = [_p, _i, _p, _i, _p, _p, _f, _f, _f, _f, _p, _i, _i]
+    return _ref_gpu
 
 
 def set_threads(n):
@@ -235,3 +257,54 @@ def ref_find_rt_from_s(Xc, Yc, S):
     t = np.zeros(3, np.float32)
     L.ref_find_rt_from_s(_ptr(Xc), _ptr(Yc), _ptr(S), _ptr(R), _ptr(t))
     return R.reshape(3, 3).astype(np.float64), t.astype(np.float64)
+
+
+def ref_softassign(X, Y, R0=None, t0=None, JMAX=100, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR=0.95,
+                   moutlier=None):
+    """The reference's own softassign() (src/softassign.cu:256-886; its CUDA
+    kernels and cuBLAS calls run on the host by oracle/emu). Returns (R, t,
+    trace) with the reference's own per-update record (Xc, Yc, S, R, t, as
+    passed to and returned by its findRTfromS), or None where unavailable."""
+    L = ref_gpu()
+    if L is None:
+        return None
+    if moutlier is None:
+        moutlier = float(np.float32(1.0 / np.sqrt(np.float32(T_0)) * np.exp(np.float32(-1.0))))
+    Xs, Ys = soa(X), soa(Y)
+    R = np.ascontiguousarray(np.eye(3) if R0 is None else R0, dtype=np.float32).reshape(-1).copy()
+    t = np.ascontiguousarray(np.zeros(3) if t0 is None else t0, dtype=np.float32).reshape(-1).copy()
+    cap = max(JMAX * I0, 1)
+    tr = np.zeros((cap, TRACE_STRIDE))
+    n = L.ref_softassign(_ptr(Xs), len(X), _ptr(Ys), len(Y), _ptr(R), _ptr(t), JMAX, I0, I1, alpha, T_0, TFACTOR,
+                         moutlier, _ptr(tr), cap, 1)
+    # the record's schedule field: T of each update (T_0 * TFACTOR^j in FP32, src/softassign.cu:820)
+    T = np.float32(T_0)
+    for j in range(JMAX):
+        for i in range(I0):
+            if j * I0 + i < cap:
+                tr[j * I0 + i, 1] = float(T)
+        T = np.float32(T * np.float32(TFACTOR))
+    return R.reshape(3, 3).astype(np.float64), t.astype(np.float64), tr[: min(n, cap)]
+
+
+def ref_emicp_gpu(X, Y, R0=None, t0=None, sigma_p2=0.01, sigma_inf=1e-5, sigma_factor=0.9, d_02=0.01):
+    """The reference's own GPU emicp() (src/emicp.cu:247-716; its CUDA kernels
+    and cuBLAS calls run on the host by oracle/emu). Returns (R, t, trace)
+    with the reference's own per-step record, or None where unavailable."""
+    L = ref_gpu()
+    if L is None:
+        return None
+    Xs, Ys = soa(X), soa(Y)
+    R = np.ascontiguousarray(np.eye(3) if R0 is None else R0, dtype=np.float32).reshape(-1).copy()
+    t = np.ascontiguousarray(np.zeros(3) if t0 is None else t0, dtype=np.float32).reshape(-1).copy()
+    sig = []
+    s = np.float32(sigma_p2)
+    while s > np.float32(sigma_inf):
+        sig.append(float(s))
+        s = np.float32(s * np.float32(sigma_factor))
+    cap = max(len(sig), 1)
+    tr = np.zeros((cap, TRACE_STRIDE))
+    n = L.ref_emicp_gpu(_ptr(Xs), len(X), _ptr(Ys), len(Y), _ptr(R), _ptr(t), sigma_p2, sigma_inf, sigma_factor,
+                        d_02, _ptr(tr), cap, 1)
+    tr[: len(sig), 1] = sig
+    return R.reshape(3, 3).astype(np.float64), t.astype(np.float64), tr[: min(n, cap)]

@@ -1,6 +1,7 @@
 // A user program written against the reference API (src/3dregistration.h):
-// reads SoA clouds from argv files, runs emicp(), softassign() or icp() with the
-// reference defaults, prints R (row-major) and t.
+// reads SoA clouds from argv files, runs emicp(), emicp_cpu(), softassign() or
+// icp() with the reference defaults, prints R (row-major) and t. The mode
+// "printRT" runs emicp() and prints the pose with the API's printRT() instead.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -33,8 +34,15 @@ int main(int argc, char** argv) {
   if (argc > 4) param.JMAX = std::atoi(argv[4]);
   float h_R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, h_t[3] = {0, 0, 0};
   pcl::PointCloud<pcl::PointXYZ>::Ptr X = load(argv[2]), Y = load(argv[3]);
+  if (std::strcmp(argv[1], "printRT") == 0) {
+    emicp(X, Y, h_R, h_t, param);
+    printRT(h_R, h_t);
+    return 0;
+  }
   if (std::strcmp(argv[1], "emicp") == 0)
     emicp(X, Y, h_R, h_t, param);
+  else if (std::strcmp(argv[1], "emicp_cpu") == 0)
+    emicp_cpu(X, Y, h_R, h_t, param);
   else if (std::strcmp(argv[1], "icp") == 0)
     icp(X, Y, h_R, h_t, param);
   else

@@ -74,9 +74,10 @@ printf("pair_Rt %zu\n", offsetof(cesa_pair, Rt)); }
 def test_registration_parameters_layout_matches_reference():
     """include/3dregistration.h keeps the reference's registrationParameters
     field order and offsets (src/3dregistration.h:39-76)."""
-    ref_src = os.path.join(os.environ.get("CESA_REFERENCE_DIR", "/root/reference"), "src")
-    if not os.path.exists(os.path.join(ref_src, "3dregistration.h")):
-        pytest.skip("reference tree not available")
+    from oracle import build as ob
+    ref_src = ob.reference_sources()  # the reference tree, or the copies staged from it
+    if ref_src is None:
+        pytest.skip("reference sources not available")
     fields = ["JMAX", "I0", "I1", "alpha", "T_0", "TFACTOR", "moutlier", "sigma_p2", "sigma_inf",
               "sigma_factor", "d_02", "maxIteration", "noviewer", "nostop", "notimer", "argc", "argv",
               "viewer", "source_trans_color", "cloud_source", "cloud_source_trans", "cloud_target"]

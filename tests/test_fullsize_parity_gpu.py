@@ -1,0 +1,182 @@
+"""Parity at the benchmark configs' full sizes, against FP64-oracle results
+stored by tests/golden/make_fullsize_golden.py (the oracle restates
+src/emicp_cpu.cpp:303-528 and src/softassign.cu:486-822 in FP64).
+
+Tolerances (the benchmark spec's, stated per result):
+  * final R within 1e-3 degrees of the oracle's, t within 1e-5 x cloud extent;
+  * per EM-ICP step, the cross-covariance S (and sum lambda, Xc, Yc) of one
+    E-step taken from the oracle's own input pose within 1e-5 relative;
+  * per-row values (C_r, lambda_r, lambda_r X'_r) within max(1e-5, 2x the
+    worst error of the reference's FP32 arithmetic on the same rows);
+  * Softassign: the same final-pose bounds, for every Sinkhorn form.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err, rot_err_deg, soa_tensor
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    path = os.path.join(GOLD, name)
+    if not os.path.exists(path):
+        pytest.fail("fixture %s missing: run tests/golden/make_fullsize_golden.py" % name)
+    return np.load(path)
+
+
+def _extent(X):
+    return float(np.ptp(np.asarray(X, np.float64), 0).max())
+
+
+@pytest.fixture(scope="module")
+def c3():
+    return _load("c3_emicp_40097.npz")
+
+
+def test_c3_registration_matches_fp64_oracle(cesa, c3):
+    """Config 3 (N = M = 40,097, the default 66-step schedule): final pose and
+    the whole trajectory against the FP64 oracle."""
+    X, Y = c3["X"], c3["Y"]
+    R, t, tr, rep = cesa.emicp(X, Y, trace=True)
+    assert rep.steps == 66 and len(tr) == 66
+    ext = _extent(X)
+    e_r, e_t = rot_err_deg(R, c3["R"]), np.abs(t - c3["t"]).max() / ext
+    assert e_r < 1e-3 and e_t < 1e-5, (e_r, e_t)
+    tro = c3["trace"]
+    for k in range(66):
+        assert rot_err_deg(tr[k, 18:27].reshape(3, 3), tro[k, 18:27].reshape(3, 3)) < 1e-3, k
+        assert np.abs(tr[k, 27:30] - tro[k, 27:30]).max() < 1e-5 * ext, k
+
+
+def test_c3_every_step_moments_from_the_oracle_pose(cesa, torch_cuda, c3):
+    """Each of the 66 E-steps, taken from the oracle's input pose of that step
+    at its sigma: sum lambda, Xc, Yc and S within 1e-5 of the oracle's."""
+    torch = torch_cuda
+    X, Y = c3["X"], c3["Y"]
+    dX, dY = soa_tensor(torch, X), soa_tensor(torch, Y)
+    tro = c3["trace"]
+    d_02 = float(c3["params"][3])
+    ext = _extent(X)
+    worst = 0.0
+    for k in range(len(tro)):
+        R = np.eye(3) if k == 0 else tro[k - 1, 18:27].reshape(3, 3)
+        t = np.zeros(3) if k == 0 else tro[k - 1, 27:30]
+        mom = cesa.emicp_step(dX, dY, R, t, float(tro[k, 1]), d_02)
+        assert abs(mom[0] - tro[k, 2]) <= 1e-5 * tro[k, 2], k
+        assert np.abs(mom[1:4] - tro[k, 3:6]).max() < 1e-5 * ext, k
+        assert np.abs(mom[4:7] - tro[k, 6:9]).max() < 1e-5 * ext, k
+        e = rel_err(mom[7:16], tro[k, 9:18])
+        worst = max(worst, e)
+        assert e < 1e-5, (k, e)
+    print("config 3: worst per-step relative error of S %.2e" % worst)
+
+
+@pytest.mark.parametrize("step", [0, 40])
+def test_c3_row_values_at_full_size(cesa, oracle, torch_cuda, c3, step):
+    """Per-row C_r, lambda_r, lambda_r X'_r over all 40,097 rows at two sigma
+    steps (from the oracle's input pose), against the FP64 oracle run here."""
+    torch = torch_cuda
+    X, Y = c3["X"], c3["Y"]
+    tro = c3["trace"]
+    R = np.eye(3) if step == 0 else tro[step - 1, 18:27].reshape(3, 3)
+    t = np.zeros(3) if step == 0 else tro[step - 1, 27:30]
+    sig, d_02 = float(tro[step, 1]), float(c3["params"][3])
+    dX, dY = soa_tensor(torch, X), soa_tensor(torch, Y)
+    rows = torch.zeros(len(Y) * 5, dtype=torch.float32, device="cuda")
+    cesa.emicp_step(dX, dY, R, t, sig, d_02, row_out=rows)
+    torch.cuda.synchronize()
+    got = rows.cpu().numpy().reshape(len(Y), 5)
+    R32, t32 = R.astype(np.float32), t.astype(np.float32)
+    ref = oracle.emicp_step(X, Y, R32, t32, sig, d_02)
+    port = oracle.emicp_step(X, Y, R32, t32, sig, d_02, precision="f32")
+
+    def worst(a, b, floor):
+        return float((np.abs(a - b) / np.maximum(np.abs(b), floor)).max())
+
+    for col, key, floor in ((0, "C", 1e-30), (1, "lam", 1e-3)):
+        e_gpu, e_port = worst(got[:, col], ref[key], floor), worst(port[key], ref[key], floor)
+        assert e_gpu <= max(1e-5, 2.0 * e_port), (key, e_gpu, e_port)
+    e_gpu, e_port = rel_err(got[:, 2:5], ref["U"]), rel_err(port["U"], ref["U"])
+    assert e_gpu <= max(1e-5, 2.0 * e_port), ("U", e_gpu, e_port)
+
+
+def test_c3_reference_emicp_cpu_agrees_with_the_oracle(c3):
+    """Where the fixture holds the reference's own emicp_cpu() result on the
+    same pair (its FP32 + OpenBLAS arithmetic), it lands within the
+    tolerance of the FP64 oracle that pins the GPU result above."""
+    if "ref_R" not in c3.files:
+        pytest.skip("fixture made without the reference tree")
+    ext = _extent(c3["X"])
+    assert rot_err_deg(c3["ref_R"], c3["R"]) < 1e-3
+    assert np.abs(c3["ref_t"] - c3["t"]).max() < 1e-5 * ext
+
+
+FORMS = ("matrix_free", "materialised", "banded")
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_c5_truncated_schedule_matches_fp64_oracle(cesa, form):
+    """Config 5 (N = M = 20,000) with the schedule cut to JMAX = 2 (10 pose
+    updates): the final pose in every Sinkhorn form. The banded form does not
+    fit 20,000 columns (at most 2048) and runs the matrix-free form, which
+    the report states."""
+    g = _load("c5_softassign_20000_jmax2.npz")
+    X, Y = g["X"], g["Y"]
+    JMAX, I0, I1, alpha, T_0, TFACTOR = g["sched"]
+    code = {"matrix_free": cesa.SINKHORN_MATRIX_FREE, "materialised": cesa.SINKHORN_MATERIALISED,
+            "banded": cesa.SINKHORN_BANDED}[form]
+    p = cesa.Params.default(JMAX=int(JMAX), I0=int(I0), I1=int(I1), sinkhorn_form=code)
+    R, t, tr, rep = cesa.softassign(X, Y, param=p, trace=True)
+    assert rep.steps == 10
+    assert rep.sinkhorn_form == (cesa.SINKHORN_MATRIX_FREE if form == "banded" else code)
+    ext = _extent(X)
+    e_r, e_t = rot_err_deg(R, g["R"]), np.abs(t - g["t"]).max() / ext
+    e_port = rot_err_deg(g["port_R"], g["R"])
+    print("config 5 (JMAX = 2), %s: R %.2e deg, t %.2e x extent (reference FP32 arithmetic: %.2e deg)"
+          % (form, e_r, e_t, e_port))
+    assert e_r < 1e-3 and e_t < 1e-5, (e_r, e_t, e_port)
+    tro = g["trace"]
+    for k in range(10):
+        assert rot_err_deg(tr[k, 18:27].reshape(3, 3), tro[k, 18:27].reshape(3, 3)) < 1e-3, k
+
+
+def _pair_sha(X, Y):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(X, dtype=np.float32).tobytes())
+    h.update(np.ascontiguousarray(Y, dtype=np.float32).tobytes())
+    return h.hexdigest()
+
+
+def test_c4_emicp_pairs_match_fp64_oracle_batched_and_single(cesa):
+    """Config 4's own 128 EM-ICP pairs (N, M log-uniform in [500, 20000]),
+    registered in the batched launch of all 256 pairs and one pair per call:
+    each within 1e-3 degrees / 1e-5 x extent of the FP64 oracle."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    g = _load("c4_emicp_pairs.npz")
+    pairs = W.batch_pairs(count=256, seed=0)
+    args = []
+    for kind, X, Y, _, _ in pairs:
+        if kind == "emicp":
+            args.append((cesa.ALGO_EMICP, X, Y, cesa.Params.default()))
+        else:
+            args.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa.Params.default(JMAX=60)))
+    out = cesa.register_batch(args)
+    worst_b = worst_s = 0.0
+    for j, k in enumerate(g["index"]):
+        kind, X, Y, _, _ = pairs[k]
+        assert kind == "emicp"
+        assert _pair_sha(X, Y) == str(g["sha"][j]), "the generator no longer reproduces pair %d" % k
+        ext = _extent(X)
+        Rb, tb = out[k]
+        e_b = rot_err_deg(Rb, g["R"][j])
+        assert e_b < 1e-3 and np.abs(tb - g["t"][j]).max() < 1e-5 * ext, (k, e_b)
+        Rs, ts = cesa.emicp(X, Y)
+        e_s = rot_err_deg(Rs, g["R"][j])
+        assert e_s < 1e-3 and np.abs(ts - g["t"][j]).max() < 1e-5 * ext, (k, e_s)
+        worst_b, worst_s = max(worst_b, e_b), max(worst_s, e_s)
+    print("config 4 EM-ICP pairs: worst rotation error batched %.2e, single %.2e deg" % (worst_b, worst_s))
