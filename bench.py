@@ -89,6 +89,9 @@ def parse_args():
     ap.add_argument("--jmax", type=int, default=None, help="Softassign JMAX (profiling)")
     ap.add_argument("--i0", type=int, default=None, help="Softassign I0 (profiling)")
     ap.add_argument("--pairs", type=int, default=256, help="pairs of the batch workload (profiling)")
+    ap.add_argument("--iterations", type=int, default=None, help="ICP iterations (profiling)")
+    ap.add_argument("--icp-search", default="auto", choices=["auto", "exhaustive", "grid"],
+                    help="ICP nearest-neighbour search of the timed runs")
     ap.add_argument("--timeline", action="store_true",
                     help="print the in-kernel phase timeline of one registration instead of a bench line")
     return ap.parse_args()
@@ -127,11 +130,17 @@ def schedule(args):
         p.JMAX = args.jmax
     if args.i0 is not None:
         p.I0 = args.i0
+    if args.iterations is not None:
+        p.maxIteration = args.iterations
     return p
 
 
-def cesa_params(cesa, p, form="auto"):
-    return cesa.Params.default(JMAX=p.JMAX, I0=p.I0, I1=p.I1, sigma_inf=p.sigma_inf, sinkhorn_form=FORMS[form])
+def cesa_params(cesa, p, form="auto", icp_search="auto"):
+    return cesa.Params.default(JMAX=p.JMAX, I0=p.I0, I1=p.I1, sigma_inf=p.sigma_inf, maxIteration=p.maxIteration,
+                               sinkhorn_form=FORMS[form], icp_search=ICP_SEARCH[icp_search])
+
+
+ICP_SEARCH = {"auto": 0, "exhaustive": 1, "grid": 2}
 
 
 FORMS = {"auto": 0, "matrix_free": 1, "materialised": 2, "banded": 3}
@@ -144,6 +153,8 @@ def fixture_for(args, p):
     if args.size is not None or args.seed != 0:
         return None
     d = RefDefaults()
+    if p.maxIteration != d.maxIteration:
+        return None
     if args.workload == "c3_emicp_40097" and p.sigma_inf == d.sigma_inf:
         path = os.path.join(GOLDEN, "c3_emicp_40097.npz")
     elif args.workload == "c5_softassign_20000" and p.JMAX == 2 and p.I0 == d.I0:
@@ -472,30 +483,44 @@ def stored_traffic(roofline, key):
 
 
 # ------------------------------------------------------------------ batch
-def batch_workload(seed, count=256):
+def batch_schedules(args):
+    """(EM-ICP, Softassign) parameters of the batch's pairs: the defaults, and
+    JMAX = 60 for Softassign (config 4), with the profiling overrides."""
+    em, sa = RefDefaults(), RefDefaults()
+    sa.JMAX = 60
+    if args.sigma_inf is not None:
+        em.sigma_inf = float(np.float32(args.sigma_inf))
+    if args.jmax is not None:
+        sa.JMAX = args.jmax
+    if args.i0 is not None:
+        sa.I0 = args.i0
+    return em, sa
+
+
+def batch_workload(args):
     """Config 4: 256 pairs, N and M log-uniform in [500, 20000], config-1
     generator per pair; even pairs EM-ICP (default parameters), odd pairs
-    Softassign (config-2 parameters, JMAX = 60)."""
+    Softassign (config-2 parameters, JMAX = 60). --pairs keeps the first
+    pairs."""
     import cuda_emicp_softassign_gb300 as cesa
     from cuda_emicp_softassign_gb300 import workloads as W
+    em, sa = batch_schedules(args)
     out = []
-    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=seed)[:count]:
+    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=args.seed)[:args.pairs]:
         if kind == "emicp":
-            out.append((cesa.ALGO_EMICP, X, Y, cesa.Params.default()))
+            out.append((cesa.ALGO_EMICP, X, Y, cesa_params(cesa, em)))
         else:
-            out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa.Params.default(JMAX=60)))
+            out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa_params(cesa, sa)))
     return out
 
 
-def batch_pairs_cpu(seed, count=256):
+def batch_pairs_cpu(args):
     """The config-4 pairs without loading libcesa: (algorithm, X, Y, params)."""
     from cuda_emicp_softassign_gb300 import workloads as W
+    em, sa = batch_schedules(args)
     out = []
-    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=seed)[:count]:
-        p = RefDefaults()
-        if kind != "emicp":
-            p.JMAX = 60
-        out.append((0 if kind == "emicp" else 1, X, Y, p))
+    for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=args.seed)[:args.pairs]:
+        out.append((0, X, Y, em) if kind == "emicp" else (1, X, Y, sa))
     return out
 
 
@@ -512,11 +537,12 @@ def batch_work(pairs):
 def batch_config(args, pairs):
     n = [len(X) for _, X, _, _ in pairs]
     m = [len(Y) for _, _, Y, _ in pairs]
+    em, sa = batch_schedules(args)
     return {"workload": BATCH_WORKLOAD, "pairs": len(pairs),
             "emicp_pairs": sum(1 for a, _, _, _ in pairs if a == 0),
             "softassign_pairs": sum(1 for a, _, _, _ in pairs if a == 1),
             "N_range": [int(min(n)), int(max(n))], "M_range": [int(min(m)), int(max(m))],
-            "softassign_JMAX": 60, "seed": args.seed,
+            "emicp_sigma_inf": em.sigma_inf, "softassign_JMAX": sa.JMAX, "softassign_I0": sa.I0, "seed": args.seed,
             "l2": "flushed between steps (256 MiB write), outside the timed region",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
@@ -561,7 +587,7 @@ def batch_cpu_sample(pairs, target_s):
 
 
 def run_reference_batch(args, world):
-    pairs = batch_pairs_cpu(args.seed, args.pairs)
+    pairs = batch_pairs_cpu(args)
     per_step = max(0.5, args.cpu_sample_s / max(1, args.steps + args.warmup))
     secs, regs = [], []
     for i in range(args.warmup + args.steps):
@@ -588,7 +614,7 @@ def run_batch(args, rank, world, local):
     import cuda_emicp_softassign_gb300 as cesa
 
     torch.cuda.set_device(local)
-    pairs = batch_workload(args.seed, args.pairs)
+    pairs = batch_workload(args)
     dev = []
     pose0 = torch.tensor(np.r_[np.eye(3).reshape(-1), np.zeros(3)], dtype=torch.float32, device="cuda")
     for algo, X, Y, p in pairs:
@@ -820,7 +846,7 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     sp = schedule(args)
     kind, X, Y, fx = load_workload(args, sp)
-    p = cesa_params(cesa, sp, args.sinkhorn_form)
+    p = cesa_params(cesa, sp, args.sinkhorn_form, args.icp_search)
     N, M = len(X), len(Y)
     tuned = None
     if kind == "softassign" and args.tune:
@@ -989,7 +1015,8 @@ def run_ours(args, rank, world, local):
         roofline["note"] = ("achieved = 6 FP32-pipe ops per point pair (squared distance; the compare-select "
                             "of (distance, index) runs on the ALU pipe) x N x M x iterations / event time of "
                             "the exhaustive search on the same pair")
-        line["icp_search"] = {"value_search": "grid" if N >= 4096 else "exhaustive",
+        used = args.icp_search if args.icp_search != "auto" else ("grid" if N >= 4096 else "exhaustive")
+        line["icp_search"] = {"value_search": used,
                               "ms_per_step": total_ms / args.steps, "exhaustive_ms_per_step": exh_s * 1e3,
                               "note": "both searches are exact and return the same matches"}
     if not args.no_adjoint and kind != "icp":
