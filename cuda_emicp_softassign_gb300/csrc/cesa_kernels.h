@@ -210,6 +210,13 @@ int softassign_bwd_prepare(const SoftassignBackward& B, const SaUpdate* host_tab
                            cudaStream_t st);
 int softassign_bwd_update(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st);
 int softassign_bwd_finish(const SoftassignBackward& B, void* ws, size_t ws_bytes, cudaStream_t st);
+// The whole backward as one persistent cooperative launch (the updates in
+// reverse, the stages separated by grid barriers with a time limit); writes
+// dL/dX, dL/dY, dL/d(R0, t0) and the device status (d_status, nullable, and
+// the workspace's control block). cudaErrorCooperativeLaunchTooLarge when it
+// cannot be launched on this device.
+int softassign_bwd_persistent(const SoftassignBackward& B, const SaUpdate* host_tab, void* ws, size_t ws_bytes,
+                              cudaStream_t st, int* d_status, uint64_t timeout_ns);
 
 // ICP (exhaustive nearest neighbours): maxIteration iterations in one launch.
 struct IcpLaunch {

@@ -83,18 +83,18 @@ struct SweepIO {
   int S, len;
 };
 
-// Owned point of (thread, pair p, lane l): coalesced per (p, l).
-__device__ __forceinline__ int own_index(int p, int l) {
-  return blockIdx.x * kOwnBlk + (2 * p + l) * kSwT + (int)threadIdx.x;
+// Owned point of (thread, pair p, lane l) in owned block ob: coalesced per (p, l).
+__device__ __forceinline__ int own_index(int ob, int p, int l) {
+  return ob * kOwnBlk + (2 * p + l) * kSwT + (int)threadIdx.x;
 }
 
-__device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, float2 (&q)[2][3]) {
+__device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, int ob, float2 (&q)[2][3]) {
 #pragma unroll
   for (int p = 0; p < 2; ++p) {
     float v[2][3];
 #pragma unroll
     for (int l = 0; l < 2; ++l) {
-      const int i = own_index(p, l);
+      const int i = own_index(ob, p, l);
       float4 o = i < io.n_own ? io.own[i] : make_float4(0.f, 0.f, 0.f, 0.f);
       if (io.own_posed) o = posed(P, o);
       v[l][0] = -o.x;
@@ -116,24 +116,31 @@ __device__ __forceinline__ void kernel_consts(float T, float alpha, float& nk, f
   c0 = fmaf(alpha, kk, -0.5f * log2f(T));
 }
 
-// part[sl][m][i] = sum over slice sl of K(own_i, str_j) w_m[j], m < NW.
+// Rank-1 terms of dL/dK: own side alpha, streamed side beta.
+struct Terms {
+  const float* own[kMaxTerms];
+  const float* str[kMaxTerms];
+  int n;
+};
+
+// Shared memory of one sweep tile (the streamed points and their weights).
+struct SweepSmem {
+  float4 pt[kTile];
+  float w[kMaxTerms][kTile];
+};
+
+// One tile of a K product: part[sl][m][i] = sum over slice sl of
+// K(own_i, str_j) w_m[j], m < NW, for the owned block ob (kSwT threads).
 template <int NW>
-__global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, const float* w, int ldw,
-                                                    float* part) {
-  const float T = pose[kRecT], alpha = pose[kRecAlpha];
-  __shared__ float4 s_pt[kTile];
-  __shared__ float s_w[NW > 1 ? NW - 1 : 1][kTile];
-  float nk, c0;
-  kernel_consts(T, alpha, nk, c0);
-  const Pose12 P = load_pose(pose);
+__device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& P, float nk, float c0, const float* w,
+                                               int ldw, float* part, int ob, int sl, SweepSmem& sm) {
   float2 q[2][3];
-  load_owned(io, P, q);
+  load_owned(io, P, ob, q);
   float2 acc[2][NW];
 #pragma unroll
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int m = 0; m < NW; ++m) acc[p][m] = make_float2(0.f, 0.f);
-  const int sl = blockIdx.y;
   const int jb = sl * io.len, je = min(jb + io.len, io.n_str);
   for (int j0 = jb; j0 < je; j0 += kTile) {
     const int n = min(kTile, je - j0);
@@ -144,17 +151,17 @@ __global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pos
       if (io.str_posed) s = posed(P, s);
       s.w = w[j];
 #pragma unroll
-      for (int m = 1; m < NW; ++m) s_w[m - 1][threadIdx.x] = w[(size_t)m * ldw + j];
-      s_pt[threadIdx.x] = s;
+      for (int m = 1; m < NW; ++m) sm.w[m - 1][threadIdx.x] = w[(size_t)m * ldw + j];
+      sm.pt[threadIdx.x] = s;
     }
     __syncthreads();
 #pragma unroll 2
     for (int j = 0; j < n; ++j) {
-      const float4 s = s_pt[j];
+      const float4 s = sm.pt[j];
       float wm[NW];
       wm[0] = s.w;
 #pragma unroll
-      for (int m = 1; m < NW; ++m) wm[m] = s_w[m - 1][j];
+      for (int m = 1; m < NW; ++m) wm[m] = sm.w[m - 1][j];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q[p], s), dup2(nk), dup2(c0)));
@@ -167,37 +174,25 @@ __global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pos
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int l = 0; l < 2; ++l) {
-      const int i = own_index(p, l);
+      const int i = own_index(ob, p, l);
       if (i < io.n_own)
 #pragma unroll
         for (int m = 0; m < NW; ++m) part[((size_t)sl * NW + m) * io.n_own + i] = l ? acc[p][m].y : acc[p][m].x;
     }
 }
 
-// Rank-1 terms of dL/dK: own side alpha, streamed side beta.
-struct Terms {
-  const float* own[kMaxTerms];
-  const float* str[kMaxTerms];
-  int n;
-};
-
-// part[sl][d][i] = (2/T) sum over slice sl of G_ij (s_j - o_i)_d with
-// G_ij = K_ij sum_m own_m[i] str_m[j].
-__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
-  const float T = pose[kRecT], alpha = pose[kRecAlpha];
-  __shared__ float4 s_pt[kTile];
-  __shared__ float s_b[kMaxTerms][kTile];
-  float nk, c0;
-  kernel_consts(T, alpha, nk, c0);
-  const Pose12 P = load_pose(pose);
+// One tile of a gradient sweep: part[sl][d][i] = (2/T) sum over slice sl of
+// G_ij (s_j - o_i)_d with G_ij = K_ij sum_m own_m[i] str_m[j].
+__device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12& P, float nk, float c0, float T,
+                                                const Terms& tm, float* part, int ob, int sl, SweepSmem& sm) {
   float2 q[2][3];
-  load_owned(io, P, q);
+  load_owned(io, P, ob, q);
   float2 al[2][kMaxTerms];
 #pragma unroll
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int m = 0; m < kMaxTerms; ++m) {
-      const int i0 = own_index(p, 0), i1 = own_index(p, 1);
+      const int i0 = own_index(ob, p, 0), i1 = own_index(ob, p, 1);
       al[p][m] = make_float2(m < tm.n && i0 < io.n_own ? tm.own[m][i0] : 0.f,
                              m < tm.n && i1 < io.n_own ? tm.own[m][i1] : 0.f);
     }
@@ -206,7 +201,6 @@ __global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* po
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int d = 0; d < 3; ++d) g[p][d] = make_float2(0.f, 0.f);
-  const int sl = blockIdx.y;
   const int jb = sl * io.len, je = min(jb + io.len, io.n_str);
   for (int j0 = jb; j0 < je; j0 += kTile) {
     const int n = min(kTile, je - j0);
@@ -215,16 +209,16 @@ __global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* po
       const int j = j0 + threadIdx.x;
       float4 s = io.str[j];
       if (io.str_posed) s = posed(P, s);
-      s_pt[threadIdx.x] = s;
+      sm.pt[threadIdx.x] = s;
 #pragma unroll
-      for (int m = 0; m < kMaxTerms; ++m) s_b[m][threadIdx.x] = m < tm.n ? tm.str[m][j] : 0.f;
+      for (int m = 0; m < kMaxTerms; ++m) sm.w[m][threadIdx.x] = m < tm.n ? tm.str[m][j] : 0.f;
     }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
-      const float4 s = s_pt[j];
+      const float4 s = sm.pt[j];
       float b[kMaxTerms];
 #pragma unroll
-      for (int m = 0; m < kMaxTerms; ++m) b[m] = s_b[m][j];
+      for (int m = 0; m < kMaxTerms; ++m) b[m] = sm.w[m][j];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const float2 dx = __fadd2_rn(dup2(s.x), q[p][0]);
@@ -249,11 +243,29 @@ __global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* po
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int l = 0; l < 2; ++l) {
-      const int i = own_index(p, l);
+      const int i = own_index(ob, p, l);
       if (i < io.n_own)
 #pragma unroll
         for (int d = 0; d < 3; ++d) part[((size_t)sl * 3 + d) * io.n_own + i] = sc * (l ? g[p][d].y : g[p][d].x);
     }
+}
+
+// The per-update launches' sweeps: one tile per block (x: owned block, y: slice).
+template <int NW>
+__global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, const float* w, int ldw,
+                                                    float* part) {
+  __shared__ SweepSmem sm;
+  float nk, c0;
+  kernel_consts(pose[kRecT], pose[kRecAlpha], nk, c0);
+  sweep_sum_tile<NW>(io, load_pose(pose), nk, c0, w, ldw, part, blockIdx.x, blockIdx.y, sm);
+}
+
+__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
+  __shared__ SweepSmem sm;
+  const float T = pose[kRecT];
+  float nk, c0;
+  kernel_consts(T, pose[kRecAlpha], nk, c0);
+  sweep_grad_tile(io, load_pose(pose), nk, c0, T, tm, part, blockIdx.x, blockIdx.y, sm);
 }
 
 // out[m][i] (+)= sum over slices of part[sl][m][i], in slice order.
@@ -332,14 +344,17 @@ __global__ void k_fill(float* p, int n, float v) {
 
 // h_j = b_j (cs_j y_j - Yc) = b_j (cs_j y'_j - Yd + (cs_j - 1) oY), [3][M]
 // (b = b^{I1}, cs = cs^{I1-1}, Yd = Yc - oY).
-__global__ void k_h(Vecs A) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= A.M) return;
+__device__ __forceinline__ void h_col(const Vecs& A, int j) {
   const float b = b_at(A, A.I1, j), cs = cs_at(A, A.I1 - 1, j);
   const float4 y = A.Y[j];
   const float yv[3] = {y.x, y.y, y.z};
   for (int d = 0; d < 3; ++d)
     A.h[(size_t)d * A.M + j] = b * (fmaf(cs, yv[d], -A.rec[23 + d]) + (cs - 1.f) * A.hdr->oY[d]);
+}
+
+__global__ void k_h(Vecs A) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < A.M) h_col(A, j);
 }
 
 // p_i = w_i x_i - Xc = w_i x'_i - Xc' + (w_i - 1) oX, and V_i from the final sweep's sums.
@@ -355,12 +370,12 @@ __device__ __forceinline__ void pv_of(const Vecs& A, int i, float& w, float p[3]
   }
 }
 
-// Horn adjoint (one thread): dL/d(R, t) of the output pose in the caller's
-// frame, where (R, t) = (R(q), Xc - R Yc) -> dL/dS, dL/dXc, dL/dYc.
-__global__ void k_horn_adjoint(Vecs A) {
+// Horn adjoint: dL/d(R, t) of the output pose in the caller's frame (g_pose),
+// where (R, t) = (R(q), Xc - R Yc) -> dL/dS, dL/dXc, dL/dYc into scal.
+__device__ __forceinline__ void horn_adjoint_into(const Vecs& A, const float* g_pose, double* scal) {
   float gRo[9], gto[3], S[9], Xc[3], Yc[3], q[4], V[4][4], gS[9], gXc[3], gYc[3];
-  for (int k = 0; k < 9; ++k) gRo[k] = A.g_pose[k];
-  for (int k = 0; k < 3; ++k) gto[k] = A.g_pose[9 + k];
+  for (int k = 0; k < 9; ++k) gRo[k] = g_pose[k];
+  for (int k = 0; k < 3; ++k) gto[k] = g_pose[9 + k];
   for (int k = 0; k < 9; ++k) S[k] = A.rec[26 + k];
   for (int k = 0; k < 3; ++k) {
     Xc[k] = A.rec[14 + k];
@@ -370,38 +385,43 @@ __global__ void k_horn_adjoint(Vecs A) {
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) V[i][j] = A.rec[39 + 4 * i + j];
   horn_pose_adjoint<float>(S, Xc, Yc, q, V, gRo, gto, gS, gXc, gYc);
-  for (int k = 0; k < 9; ++k) A.scal[kSgS + k] = gS[k];
+  for (int k = 0; k < 9; ++k) scal[kSgS + k] = gS[k];
   for (int k = 0; k < 3; ++k) {
-    A.scal[kSgXc + k] = gXc[k];
-    A.scal[kSgYc + k] = gYc[k];
+    scal[kSgXc + k] = gXc[k];
+    scal[kSgYc + k] = gYc[k];
   }
 }
 
-// One block, per row: g(p_i) = a_i gS V_i, g(V_i) = a_i gS^T p_i, dL/da_i from
-// S (S[p + 3 q] = sum a p_p V_q); dL/dXc -= sum g(p).
+__global__ void k_horn_adjoint(Vecs A) { horn_adjoint_into(A, A.g_pose, A.scal); }
+
+// Row i of S's adjoint: g(p_i) = a_i gS V_i, g(V_i) = a_i gS^T p_i, dL/da_i
+// from S (S[p + 3 q] = sum a p_p V_q); adds a_i g(p_i) to v (for dL/dXc).
+__device__ __forceinline__ void back_S_row(const Vecs& A, const float (&gS)[9], int i, df (&v)[3]) {
+  const float* aF = a_of(A, A.I1);
+  float w, p[3], Vi[3];
+  pv_of(A, i, w, p, Vi);
+  float ga = 0.f;
+  for (int pp = 0; pp < 3; ++pp) {
+    float gp = 0.f, gv = 0.f;
+    for (int qq = 0; qq < 3; ++qq) {
+      gp = fmaf(gS[pp + 3 * qq], Vi[qq], gp);
+      gv = fmaf(gS[qq + 3 * pp], p[qq], gv);
+    }
+    ga = fmaf(gp, p[pp], ga);
+    A.gp[(size_t)pp * A.N + i] = aF[i] * gp;
+    A.gV[(size_t)pp * A.N + i] = aF[i] * gv;
+    df_add(v[pp], aF[i] * gp);
+  }
+  A.ga[i] = ga;
+}
+
+// One block: the rows of S's adjoint; dL/dXc -= sum g(p).
 __global__ void __launch_bounds__(kOneBlock) k_back_S(Vecs A) {
   __shared__ df red[3 * (kOneBlock / 32)];
-  const float* aF = a_of(A, A.I1);
   float gS[9];
   for (int k = 0; k < 9; ++k) gS[k] = (float)A.scal[kSgS + k];
   df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
-  for (int i = threadIdx.x; i < A.N; i += blockDim.x) {
-    float w, p[3], Vi[3];
-    pv_of(A, i, w, p, Vi);
-    float ga = 0.f;
-    for (int pp = 0; pp < 3; ++pp) {
-      float gp = 0.f, gv = 0.f;
-      for (int qq = 0; qq < 3; ++qq) {
-        gp = fmaf(gS[pp + 3 * qq], Vi[qq], gp);
-        gv = fmaf(gS[qq + 3 * pp], p[qq], gv);
-      }
-      ga = fmaf(gp, p[pp], ga);
-      A.gp[(size_t)pp * A.N + i] = aF[i] * gp;
-      A.gV[(size_t)pp * A.N + i] = aF[i] * gv;
-      df_add(v[pp], aF[i] * gp);
-    }
-    A.ga[i] = ga;
-  }
+  for (int i = threadIdx.x; i < A.N; i += blockDim.x) back_S_row(A, gS, i, v);
   block_reduce_df<3>(v, red);
   if (threadIdx.x == 0)
     for (int k = 0; k < 3; ++k) A.scal[kSgXc + k] -= df_dbl(v[k]);
@@ -409,9 +429,7 @@ __global__ void __launch_bounds__(kOneBlock) k_back_S(Vecs A) {
 
 // Per row: the part of dL/dw known before dL/dsumM, gw = x . (g(p) + gXc/sumM);
 // direct dL/dx += w (g(p) + gXc/sumM); the weights of the K^T sweep.
-__global__ void k_back_w(Vecs A) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= A.N) return;
+__device__ __forceinline__ void back_w_row(const Vecs& A, const double* scal, int i) {
   const float a = a_of(A, A.I1)[i];
   const float w = a * A.fin[i];
   const float inv = (float)(1.0 / sumM_of(A));
@@ -419,7 +437,7 @@ __global__ void k_back_w(Vecs A) {
   const float xv[3] = {x.x, x.y, x.z};
   float gw = 0.f;
   for (int d = 0; d < 3; ++d) {
-    const float g = fmaf((float)A.scal[kSgXc + d], inv, A.gp[(size_t)d * A.N + i]);
+    const float g = fmaf((float)scal[kSgXc + d], inv, A.gp[(size_t)d * A.N + i]);
     gw = fmaf(xv[d] + A.hdr->oX[d], g, gw);
     A.gX[(size_t)d * A.N + i] += w * g;
     A.wt4[(size_t)d * A.N + i] = A.gV[(size_t)d * A.N + i];
@@ -428,42 +446,50 @@ __global__ void k_back_w(Vecs A) {
   A.wt4[3 * (size_t)A.N + i] = a * gw;
 }
 
-// One block after the K^T sweep: dL/dYc -= sum_j b_j g(h_j);
-// dL/dsumM = -(gXc . Xc + gYc . Yc) / sumM.
+__global__ void k_back_w(Vecs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.N) back_w_row(A, A.scal, i);
+}
+
+// Column j's share of dL/dYc: v += b_j g(h_j).
+__device__ __forceinline__ void back_Yc_col(const Vecs& A, int j, df (&v)[3]) {
+  const float b = b_at(A, A.I1, j);
+  for (int d = 0; d < 3; ++d) df_add_prod(v[d], b, A.gh[(size_t)d * A.M + j]);
+}
+
+// dL/dYc -= the columns' sum; dL/dsumM = -(gXc . Xc + gYc . Yc) / sumM.
+__device__ __forceinline__ void finish_Yc(const Vecs& A, const df (&v)[3], double* scal) {
+  double g = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    scal[kSgYc + d] -= df_dbl(v[d]);
+    g -= scal[kSgXc + d] * (double)A.rec[14 + d] + scal[kSgYc + d] * (double)A.rec[17 + d];
+  }
+  scal[kSgsum] = g / sumM_of(A);
+}
+
+// One block after the K^T sweep: dL/dYc and dL/dsumM.
 __global__ void __launch_bounds__(kOneBlock) k_back_Yc(Vecs A) {
   __shared__ df red[3 * (kOneBlock / 32)];
   df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
-  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
-    const float b = b_at(A, A.I1, j);
-    for (int d = 0; d < 3; ++d) df_add_prod(v[d], b, A.gh[(size_t)d * A.M + j]);
-  }
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x) back_Yc_col(A, j, v);
   block_reduce_df<3>(v, red);
-  if (threadIdx.x == 0) {
-    double g = 0.0;
-    for (int d = 0; d < 3; ++d) {
-      A.scal[kSgYc + d] -= df_dbl(v[d]);
-      g -= A.scal[kSgXc + d] * (double)A.rec[14 + d] + A.scal[kSgYc + d] * (double)A.rec[17 + d];
-    }
-    A.scal[kSgsum] = g / sumM_of(A);
-  }
+  if (threadIdx.x == 0) finish_Yc(A, v, A.scal);
 }
 
 // Rows (i < N): g(rho) = a (gw + gsum); dL/da^{I1} += (gw + gsum) rho.
-// Columns (j = i - N < M), final stage: dL/db^{I1} = (cs y - Yc) . g(h) + K^T g(rho),
-// where K^T g(rho) = K^T (a gw) + gsum c^{I1-1}; dL/dcs^{I1-1} = y . (b g(h) + gYc / sumM);
+__device__ __forceinline__ void back_final_row(const Vecs& A, const double* scal, int i) {
+  const float gsum = (float)scal[kSgsum];
+  const float a = a_of(A, A.I1)[i];
+  const float gw = A.gw[i] + gsum;
+  A.grho[i] = a * gw;
+  A.ga[i] = fmaf(gw, A.fin[i], A.ga[i]);
+}
+
+// Columns, final stage: dL/db^{I1} = (cs y - Yc) . g(h) + K^T g(rho), where
+// K^T g(rho) = K^T (a gw) + gsum c^{I1-1}; dL/dcs^{I1-1} = y . (b g(h) + gYc / sumM);
 // direct dL/dy += cs (b g(h) + gYc / sumM).
-__global__ void k_back_final(Vecs A) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const float gsum = (float)A.scal[kSgsum];
-  if (i < A.N) {
-    const float a = a_of(A, A.I1)[i];
-    const float gw = A.gw[i] + gsum;
-    A.grho[i] = a * gw;
-    A.ga[i] = fmaf(gw, A.fin[i], A.ga[i]);
-    return;
-  }
-  const int j = i - A.N;
-  if (j >= A.M) return;
+__device__ __forceinline__ void back_final_col(const Vecs& A, const double* scal, int j) {
+  const float gsum = (float)scal[kSgsum];
   const int k = A.I1 - 1;
   const float b = b_at(A, A.I1, j), cs = cs_at(A, k, j), c = c_at(A, k, j);
   const float inv = (float)(1.0 / sumM_of(A));
@@ -472,13 +498,23 @@ __global__ void k_back_final(Vecs A) {
   float gb = fmaf(gsum, c, A.gh[3 * (size_t)A.M + j]), gcs = 0.f;
   for (int d = 0; d < 3; ++d) {
     const float ghd = A.gh[(size_t)d * A.M + j];
-    const float gy = fmaf(b, ghd, (float)A.scal[kSgYc + d] * inv);
+    const float gy = fmaf(b, ghd, (float)scal[kSgYc + d] * inv);
     gb = fmaf(fmaf(cs, yv[d], -A.rec[23 + d]) + (cs - 1.f) * A.hdr->oY[d], ghd, gb);
     gcs = fmaf(yv[d] + A.hdr->oY[d], gy, gcs);
     A.gY[(size_t)d * A.M + j] += cs * gy;
   }
   A.gb[j] = gb;
   A.gcs[j] = gcs;
+}
+
+__global__ void k_back_final(Vecs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.N) {
+    back_final_row(A, A.scal, i);
+    return;
+  }
+  const int j = i - A.N;
+  if (j < A.M) back_final_col(A, A.scal, j);
 }
 
 // Slice partials of a K or K^T product: the sum over slices, in order.
@@ -493,9 +529,7 @@ __device__ __forceinline__ float slices_sum(const float* part, int S, int n, int
 // g(c^k) = dL/dcs^k b^k. d(b/cs)/dcs = -b^{k+1}/cs: the new scalings are used
 // instead of b^k/cs^2, whose square overflows FP32 at low temperature
 // (K ~ e^(alpha/T)).
-__global__ void k_back_colpass(Vecs A, int k, const float* part, int S) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= A.M) return;
+__device__ __forceinline__ void back_colpass(const Vecs& A, int k, const float* part, int S, int j) {
   const float bk = b_at(A, k, j), cs = cs_at(A, k, j), c = c_at(A, k, j);
   const float b1 = b_at(A, k + 1, j), u1 = u_at(A, k + 1, j);
   float gb1 = A.gb[j];
@@ -508,11 +542,27 @@ __global__ void k_back_colpass(Vecs A, int k, const float* part, int S) {
   A.gcs[j] = 0.f;
 }
 
+// The same with the K^T g(r^{k+1}) sum already formed (0 for the last pass).
+__device__ __forceinline__ void back_colpass_sum(const Vecs& A, int k, float pending, int j) {
+  const float bk = b_at(A, k, j), cs = cs_at(A, k, j), c = c_at(A, k, j);
+  const float b1 = b_at(A, k + 1, j), u1 = u_at(A, k + 1, j);
+  const float gb1 = A.gb[j] + pending;
+  const float gu1 = A.gu[j];
+  const float gcs = A.gcs[j] - fmaf(gb1, b1, gu1 * u1) / cs;
+  A.gc[(size_t)k * A.M + j] = gcs * bk;
+  A.gb[j] = fmaf(gcs, c, gb1 / cs);
+  A.gu[j] = gu1 / cs + gcs;
+  A.gcs[j] = 0.f;
+}
+
+__global__ void k_back_colpass(Vecs A, int k, const float* part, int S) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < A.M) back_colpass(A, k, part, S, j);
+}
+
 // Row pass k backward: from dL/da^{k+1} (+ the pending K g(c^k) slice partials)
 // and dL/ds^{k+1}: dL/da^k, dL/ds^k and g(r^k) = dL/drs^k a^k.
-__global__ void k_back_rowpass(Vecs A, int k, const float* part, int S) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= A.N) return;
+__device__ __forceinline__ void back_rowpass(const Vecs& A, int k, const float* part, int S, int i) {
   const float ak = a_at(A, k, i), rs = rs_at(A, k, i), r = r_at(A, k, i);
   const float a1 = a_at(A, k + 1, i), s1 = s_at(A, k + 1, i);
   const float ga1 = A.ga[i] + slices_sum(part, S, A.N, i);
@@ -523,6 +573,45 @@ __global__ void k_back_rowpass(Vecs A, int k, const float* part, int S) {
   A.gs[i] = gs1 / rs + grs;
 }
 
+// The same with the K g(c^k) sum already formed.
+__device__ __forceinline__ void back_rowpass_sum(const Vecs& A, int k, float pending, int i) {
+  const float ak = a_at(A, k, i), rs = rs_at(A, k, i), r = r_at(A, k, i);
+  const float a1 = a_at(A, k + 1, i), s1 = s_at(A, k + 1, i);
+  const float ga1 = A.ga[i] + pending;
+  const float gs1 = A.gs[i];
+  const float grs = -fmaf(ga1, a1, gs1 * s1) / rs;
+  A.gr[(size_t)k * A.N + i] = grs * ak;
+  A.ga[i] = fmaf(grs, r, ga1 / rs);
+  A.gs[i] = gs1 / rs + grs;
+}
+
+__global__ void k_back_rowpass(Vecs A, int k, const float* part, int S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.N) back_rowpass(A, k, part, S, i);
+}
+
+// Column j's share of the input pose's gradient (sum gz y^T, sum gz, caller
+// frame y = y' + oY through oY below), and dL/dy += R^T gz.
+__device__ __forceinline__ void pose_grad_col(const Vecs& A, const float (&R)[9], int j, df (&v)[12]) {
+  const float4 y = A.Y[j];
+  const float yv[3] = {y.x, y.y, y.z};
+  const float g[3] = {A.gZ[j], A.gZ[(size_t)A.M + j], A.gZ[2 * (size_t)A.M + j]};
+  for (int i = 0; i < 3; ++i) {
+    for (int jj = 0; jj < 3; ++jj) df_add_prod(v[3 * i + jj], g[i], yv[jj]);
+    df_add(v[9 + i], g[i]);
+  }
+  for (int jj = 0; jj < 3; ++jj) A.gY[(size_t)jj * A.M + j] += R[jj] * g[0] + R[3 + jj] * g[1] + R[6 + jj] * g[2];
+}
+
+// dL/d(R, t) of the input pose from the summed values.
+__device__ __forceinline__ void pose_grad_from(const Vecs& A, const df (&v)[12], float* g_pose) {
+  for (int i = 0; i < 3; ++i) {
+    const float gt = df_val(v[9 + i]);
+    g_pose[9 + i] = gt;
+    for (int j = 0; j < 3; ++j) g_pose[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
+  }
+}
+
 // One block: dL/dR = sum gz y^T, dL/dt = sum gz (caller frame, y = y' + oY);
 // per column dL/dy += R^T gz; writes dL/d(R, t) of the input pose.
 __global__ void __launch_bounds__(kOneBlock) k_pose_grad(Vecs A) {
@@ -531,24 +620,10 @@ __global__ void __launch_bounds__(kOneBlock) k_pose_grad(Vecs A) {
   for (int k = 0; k < 9; ++k) R[k] = A.rec[k];
   df v[12];
   for (int k = 0; k < 12; ++k) v[k] = df_make(0.f);
-  for (int j = threadIdx.x; j < A.M; j += blockDim.x) {
-    const float4 y = A.Y[j];
-    const float yv[3] = {y.x, y.y, y.z};
-    const float g[3] = {A.gZ[j], A.gZ[(size_t)A.M + j], A.gZ[2 * (size_t)A.M + j]};
-    for (int i = 0; i < 3; ++i) {
-      for (int jj = 0; jj < 3; ++jj) df_add_prod(v[3 * i + jj], g[i], yv[jj]);
-      df_add(v[9 + i], g[i]);
-    }
-    for (int jj = 0; jj < 3; ++jj)
-      A.gY[(size_t)jj * A.M + j] += R[jj] * g[0] + R[3 + jj] * g[1] + R[6 + jj] * g[2];
-  }
+  for (int j = threadIdx.x; j < A.M; j += blockDim.x) pose_grad_col(A, R, j, v);
   block_reduce_df<12>(v, red);
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 3; ++i) {
-      const float gt = df_val(v[9 + i]);
-      A.g_pose[9 + i] = gt;
-      for (int j = 0; j < 3; ++j) A.g_pose[3 * i + j] = fmaf(gt, A.hdr->oY[j], df_val(v[3 * i + j]));
-    }
+    pose_grad_from(A, v, A.g_pose);
     *A.cur -= 1;  // the next update back
   }
 }
@@ -571,6 +646,296 @@ __global__ void k_load_update(const SaUpdate* tab, const int* cur, float* rec, f
 // SoA outputs and the input pose's gradient out of the accumulators.
 __global__ void k_copy(float* dst, const float* src, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// ------------------------------------------------------------- persistent backward
+// Block partial records of the persistent backward: three rotating slots of
+// kBwdPartNV double-float values per block (at most kBwdMaxGrid blocks).
+constexpr int kBwdMaxGrid = 1200;
+constexpr int kBwdPartNV = 16;
+
+// The whole backward in one cooperative launch: the updates in reverse, each
+// one the stages of the launch sequence above separated by grid barriers
+// instead of launch boundaries (17 barriers per update at I1 = 3). Every block
+// runs Horn's adjoint and the fixed-order reductions of the block partials
+// itself, so the O(1) steps need no barrier of their own. Sweeps are split
+// into (owned block, slice) tiles dealt over the blocks; the slice partials
+// are summed, in slice order, by the per-point stage that consumes them.
+struct BwdArgs {
+  Vecs A;               // workspace vectors (tape slices set per update)
+  const SaUpdate* tab;  // [nsteps] the updates' tape slices and temperatures
+  long nsteps;
+  float alpha;
+  SweepIO rows, cols;   // rows: own X, stream Y (posed); cols: own Y (posed), stream X
+  float* part_r;        // slice partials of rows-owned sweeps
+  float* part_c;        // slice partials of columns-owned sweeps
+  df* bpart;            // [3][gridDim.x][kBwdPartNV]
+  Ctl* ctl;
+  float* g_in;          // [12] dL/d(R, t) of the initial pose (written at the end)
+  int* d_status;
+  uint64_t timeout_ns;
+};
+
+// Sum over slices of one element's partials (part[k * stride + i], k < S),
+// in slice order, with the loads issued 16 at a time ahead of the adds.
+__device__ __forceinline__ float slice_sum16(const float* part, int S, size_t stride, int i) {
+  float s = 0.f;
+  for (int k0 = 0; k0 < S; k0 += 16) {
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = k0 + k < S ? __ldcg(part + (size_t)(k0 + k) * stride + i) : 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += v[k];
+  }
+  return s;
+}
+
+// Sum over the blocks' records of NV values into tot, in every block, in a
+// fixed order: lane group g (NVP lanes, one per value) adds the records of
+// blocks g, g + G, ... in order, loads issued 8 at a time, then the G group
+// sums are added in order. kSwT threads.
+template <int NV>
+__device__ __forceinline__ void sum_block_records(const df* rec, int nblk, df* scratch, df* tot) {
+  constexpr int NVP = NV <= 4 ? 4 : 16;
+  constexpr int G = kSwT / NVP;
+  const int v = threadIdx.x % NVP, grp = threadIdx.x / NVP;
+  df a = df_make(0.f);
+  if (v < NV) {
+    int b = grp;
+    for (; b + 7 * G < nblk; b += 8 * G) {
+      float2 x[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        x[k] = __ldcg(reinterpret_cast<const float2*>(rec + (size_t)(b + k * G) * kBwdPartNV + v));
+#pragma unroll
+      for (int k = 0; k < 8; ++k) df_add(a, df{x[k].x, x[k].y});
+    }
+    for (; b < nblk; b += G) {
+      const float2 x = __ldcg(reinterpret_cast<const float2*>(rec + (size_t)b * kBwdPartNV + v));
+      df_add(a, df{x.x, x.y});
+    }
+  }
+  scratch[grp * NVP + v] = a;
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    df t = scratch[threadIdx.x];
+    for (int g = 1; g < G; ++g) df_add(t, scratch[g * NVP + threadIdx.x]);
+    tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// This block's record of NV values (summed over its threads) into slot rec.
+template <int NV>
+__device__ __forceinline__ void store_block_record(df (&v)[NV], df* red, df* rec) {
+  block_reduce_df<NV>(v, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      __stcg(reinterpret_cast<float2*>(rec + (size_t)blockIdx.x * kBwdPartNV + k), make_float2(v[k].hi, v[k].lo));
+}
+
+#ifndef CESA_BWD_MIN_BLOCKS
+#define CESA_BWD_MIN_BLOCKS 3  // blocks per SM the register budget is set for
+#endif
+__global__ void __launch_bounds__(kSwT, CESA_BWD_MIN_BLOCKS) softassign_bwd_kernel(const BwdArgs B) {
+  __shared__ SweepSmem sm;
+  __shared__ double s_scal[kScalN];
+  __shared__ float s_gpose[12];
+  __shared__ df s_red[12 * (kSwT / 32)];
+  __shared__ df s_scr[kSwT];
+  __shared__ df s_tot[kBwdPartNV];
+  const int tid = threadIdx.x, nblk = gridDim.x;
+  const int gtid = blockIdx.x * kSwT + tid, gstride = nblk * kSwT;
+  const int N = B.A.N, M = B.A.M, I1 = B.A.I1;
+  const SweepIO& io_r = B.rows;
+  const SweepIO& io_c = B.cols;
+  const int nob_r = (N + kOwnBlk - 1) / kOwnBlk, nob_c = (M + kOwnBlk - 1) / kOwnBlk;
+  const int units_r = nob_r * io_r.S, units_c = nob_c * io_c.S;
+  unsigned epoch = 0;
+  bool ok = true;
+  int slot = 0;
+  auto next_slot = [&]() {
+    df* r = B.bpart + (size_t)slot * nblk * kBwdPartNV;
+    slot = slot == 2 ? 0 : slot + 1;
+    return r;
+  };
+  auto sync = [&](int where) {
+    if (ok) ok = grid_sync(B.ctl, epoch, nblk, B.timeout_ns, where);
+    return ok;
+  };
+  if (tid < 12) s_gpose[tid] = B.A.g_pose[tid];
+  __syncthreads();
+
+  for (long n = B.nsteps - 1; n >= 0 && ok; --n) {
+    const SaUpdate U = B.tab[n];
+    Vecs A = B.A;
+    A.rec = U.rec;
+    A.s0 = U.s0;
+    A.u0 = U.u0;
+    A.rows = U.rows;
+    A.cols = U.cols;
+    A.fin = U.fin;
+    const float T = U.T;
+    float nk, c0;
+    kernel_consts(T, B.alpha, nk, c0);
+    const Pose12 P = load_pose(U.rec);
+    // ---- Horn's adjoint (every block), then S's adjoint per row and h per column
+    if (tid == 0) horn_adjoint_into(A, s_gpose, s_scal);
+    __syncthreads();
+    {
+      float gS[9];
+      for (int k = 0; k < 9; ++k) gS[k] = (float)s_scal[kSgS + k];
+      df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
+      for (int i = gtid; i < N; i += gstride) back_S_row(A, gS, i, v);
+      for (int j = gtid; j < M; j += gstride) h_col(A, j);
+      store_block_record<3>(v, s_red, next_slot());
+    }
+    if (!sync(80)) break;
+    // ---- dL/dXc, then the rows' dL/dw and the K^T sweep's weights
+    {
+      const df* rec = B.bpart + (size_t)((slot + 2) % 3) * nblk * kBwdPartNV;
+      sum_block_records<3>(rec, nblk, s_scr, s_tot);
+      if (tid == 0)
+        for (int k = 0; k < 3; ++k) s_scal[kSgXc + k] -= df_dbl(s_tot[k]);
+      __syncthreads();
+      for (int i = gtid; i < N; i += gstride) back_w_row(A, s_scal, i);
+    }
+    if (!sync(81)) break;
+    // ---- gh = K^T wt4 (columns own, rows stream), slice partials
+    for (int u = blockIdx.x; u < units_c; u += nblk)
+      sweep_sum_tile<4>(io_c, P, nk, c0, A.wt4, N, B.part_c, u % nob_c, u / nob_c, sm);
+    if (!sync(82)) break;
+    // ---- gh summed per (column, weight); the columns' share of dL/dYc
+    {
+      df v[3] = {df_make(0.f), df_make(0.f), df_make(0.f)};
+      for (int it = gtid; it < 4 * M; it += gstride) {
+        const int m = it / M, j = it - m * M;
+        const float g = slice_sum16(B.part_c + (size_t)m * M, io_c.S, (size_t)4 * M, j);
+        A.gh[(size_t)m * M + j] = g;
+        if (m < 3) df_add_prod(v[m], b_at(A, I1, j), g);
+      }
+      store_block_record<3>(v, s_red, next_slot());
+    }
+    if (!sync(83)) break;
+    // ---- dL/dYc, dL/dsumM; the final stage per row and column, fused with the
+    //      backward of the last column pass (column-local)
+    {
+      const df* rec = B.bpart + (size_t)((slot + 2) % 3) * nblk * kBwdPartNV;
+      sum_block_records<3>(rec, nblk, s_scr, s_tot);
+      if (tid == 0) {
+        df v[3] = {s_tot[0], s_tot[1], s_tot[2]};
+        finish_Yc(A, v, s_scal);
+      }
+      __syncthreads();
+      for (int i = gtid; i < N; i += gstride) back_final_row(A, s_scal, i);
+      for (int j = gtid; j < M; j += gstride) {
+        back_final_col(A, s_scal, j);
+        back_colpass_sum(A, I1 - 1, 0.f, j);
+      }
+    }
+    if (!sync(84)) break;
+    // ---- the row and column passes in reverse
+    for (int k = I1 - 1; k >= 0; --k) {
+      // dL/da^{k+1} += K g(c^k): rows own, columns stream
+      for (int u = blockIdx.x; u < units_r; u += nblk)
+        sweep_sum_tile<1>(io_r, P, nk, c0, A.gc + (size_t)k * M, M, B.part_r, u % nob_r, u / nob_r, sm);
+      if (!sync(85)) break;
+      for (int i = gtid; i < N; i += gstride) back_rowpass_sum(A, k, slice_sum16(B.part_r, io_r.S, N, i), i);
+      if (!sync(86)) break;
+      if (k == 0) break;
+      // dL/db^k += K^T g(r^k), then the column pass k - 1 (b^0 = 1 is a constant)
+      for (int u = blockIdx.x; u < units_c; u += nblk)
+        sweep_sum_tile<1>(io_c, P, nk, c0, A.gr + (size_t)k * N, N, B.part_c, u % nob_c, u / nob_c, sm);
+      if (!sync(87)) break;
+      for (int j = gtid; j < M; j += gstride) back_colpass_sum(A, k - 1, slice_sum16(B.part_c, io_c.S, M, j), j);
+      if (!sync(88)) break;
+    }
+    if (!ok) break;
+    // ---- the gradient sweeps: dL/dx (rows own) and dL/dz (columns own), in
+    //      chunks of kMaxTerms rank-1 terms of dL/dK
+    const int nterms = 4 + 2 * I1;
+    for (int t0 = 0; t0 < nterms && ok; t0 += kMaxTerms) {
+      Terms tr{}, tc{};
+      tr.n = tc.n = min(kMaxTerms, nterms - t0);
+      for (int m = 0; m < tr.n; ++m) {
+        const int t = t0 + m;
+        const float *ta, *tb;
+        if (t < 3) {
+          ta = A.gV + (size_t)t * N;
+          tb = A.h + (size_t)t * M;
+        } else if (t == 3) {
+          ta = A.grho;
+          tb = A.cols + (size_t)(I1 - 1) * 4 * M;  // b^{I1}
+        } else if (t < 4 + I1) {
+          const int k = t - 4;
+          ta = A.rows + (size_t)k * 4 * N;  // a^{k+1}
+          tb = A.gc + (size_t)k * M;
+        } else {
+          const int k = t - 4 - I1;
+          ta = A.gr + (size_t)k * N;
+          tb = k == 0 ? A.ones : A.cols + (size_t)(k - 1) * 4 * M;  // b^k
+        }
+        tr.own[m] = ta;
+        tr.str[m] = tb;
+        tc.own[m] = tb;
+        tc.str[m] = ta;
+      }
+      for (int u = blockIdx.x; u < units_r + units_c; u += nblk) {
+        if (u < units_r)
+          sweep_grad_tile(io_r, P, nk, c0, T, tr, B.part_r, u % nob_r, u / nob_r, sm);
+        else
+          sweep_grad_tile(io_c, P, nk, c0, T, tc, B.part_c, (u - units_r) % nob_c, (u - units_r) / nob_c, sm);
+      }
+      if (!sync(89)) break;
+      const bool last = t0 + kMaxTerms >= nterms;
+      float R[9];
+      for (int k = 0; k < 9; ++k) R[k] = U.rec[k];
+      df v[12];
+      for (int k = 0; k < 12; ++k) v[k] = df_make(0.f);
+      for (int it = gtid; it < 3 * N; it += gstride) {
+        const int d = it / N, i = it - d * N;
+        A.gX[(size_t)d * N + i] += slice_sum16(B.part_r + (size_t)d * N, io_r.S, (size_t)3 * N, i);
+      }
+      for (int it = gtid; it < 3 * M; it += gstride) {
+        const int d = it / M, j = it - d * M;
+        float g = slice_sum16(B.part_c + (size_t)d * M, io_c.S, (size_t)3 * M, j);
+        if (t0 > 0) g += A.gZ[(size_t)d * M + j];
+        A.gZ[(size_t)d * M + j] = g;
+        if (last) {  // this component's share of sum gz y^T and sum gz
+          const float4 y = A.Y[j];
+          df_add_prod(v[3 * d], g, y.x);
+          df_add_prod(v[3 * d + 1], g, y.y);
+          df_add_prod(v[3 * d + 2], g, y.z);
+          df_add(v[9 + d], g);
+        }
+      }
+      if (last) store_block_record<12>(v, s_red, next_slot());
+      if (!sync(90)) break;
+      if (last) {
+        // dL/dy += R^T gz (all three components of gz are in place now)
+        for (int j = gtid; j < M; j += gstride) {
+          const float g[3] = {A.gZ[j], A.gZ[(size_t)M + j], A.gZ[2 * (size_t)M + j]};
+          for (int jj = 0; jj < 3; ++jj) A.gY[(size_t)jj * M + j] += R[jj] * g[0] + R[3 + jj] * g[1] + R[6 + jj] * g[2];
+        }
+        // dL/d(R, t) of this update's input pose = the output pose of the update before
+        const df* rec = B.bpart + (size_t)((slot + 2) % 3) * nblk * kBwdPartNV;
+        sum_block_records<12>(rec, nblk, s_scr, s_tot);
+        if (tid == 0) {
+          df t[12];
+          for (int k = 0; k < 12; ++k) t[k] = s_tot[k];
+          pose_grad_from(A, t, s_gpose);
+        }
+        __syncthreads();
+      }
+    }
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    const int st = ld_status(B.ctl);
+    if (st == kStatusOk)
+      for (int k = 0; k < 12; ++k) B.g_in[k] = s_gpose[k];
+    if (B.d_status) *B.d_status = st;
+  }
 }
 
 // ------------------------------------------------------------------ host side
@@ -617,7 +982,10 @@ Plan make_plan(int N, int M) {
 
 struct Layout {
   Vecs V;
-  float* part;
+  Ctl* ctl;      // status and grid-barrier counter of the persistent backward
+  float* part;   // slice partials (rows-owned sweeps in the persistent backward)
+  float* part2;  // slice partials of the columns-owned sweeps (persistent backward)
+  df* bpart;     // [3][kBwdMaxGrid][kBwdPartNV]
   float *rec, *s0, *u0, *rows, *cols, *fin;  // the current update's tape slices (copies)
   float4 *X, *Y;                             // the packed clouds (copies)
   CenterHdr* hdr;
@@ -632,6 +1000,7 @@ Layout carve(void* base, int N, int M, int I1, long nsteps, const Plan& P) {
   A.N = N;
   A.M = M;
   A.I1 = I1;
+  L.ctl = c.take<Ctl>(1);  // first: read_ws_status reads the status here
   A.cur = c.take<int>(1);
   A.g_pose = c.take<float>(16);
   A.gs = c.take<float>(N);
@@ -670,6 +1039,8 @@ Layout carve(void* base, int N, int M, int I1, long nsteps, const Plan& P) {
   A.fin = L.fin;
   const size_t pr = (size_t)P.rows.S * 4 * N, pc = (size_t)P.cols.S * 4 * M;
   L.part = c.take<float>(std::max(pr, pc));
+  L.part2 = c.take<float>(std::max(pr, pc));
+  L.bpart = c.take<df>((size_t)3 * kBwdMaxGrid * kBwdPartNV);
   // last, so that every other offset is the same whatever the schedule's length
   L.tab = c.take<SaUpdate>((size_t)(nsteps > 0 ? nsteps : 1));
   L.total = c.off;
@@ -837,6 +1208,76 @@ int softassign_bwd_finish(const SoftassignBackward& B, void* ws, size_t ws_bytes
   k_copy<<<std::min(blocks(3 * M), 1024), kGlue, 0, st>>>(B.gY, c.A.gY, 3 * M);
   k_copy<<<1, 32, 0, st>>>(B.g_in, c.A.g_pose, 12);
   return (int)cudaGetLastError();
+}
+
+namespace {
+// Slices of a sweep in the persistent backward: enough tiles to about fill the
+// grid, slices of at least 64 streamed points, and no more slices than the
+// workspace's partial buffers hold (the launch sequence's plan, S_cap).
+void plan_persistent(SweepIO& io, int grid, int S_cap) {
+  const int nb = (io.n_own + kOwnBlk - 1) / kOwnBlk;
+  int S = std::max(1, grid / nb);
+  S = std::min(S, std::max(1, (io.n_str + 63) / 64));
+  S = std::min(S, std::max(1, S_cap));
+  io.len = (io.n_str + S - 1) / S;
+  io.S = (io.n_str + io.len - 1) / io.len;
+}
+}  // namespace
+
+int softassign_bwd_persistent(const SoftassignBackward& B, const SaUpdate* host_tab, void* ws, size_t ws_bytes,
+                              cudaStream_t st, int* d_status, uint64_t timeout_ns) {
+  Ctx c;
+  int r = make_ctx(B, ws, ws_bytes, c);
+  if (r) return r;
+  int device = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, softassign_bwd_kernel, kSwT, 0);
+  if (e != cudaSuccess) return (int)e;
+  if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
+  // Blocks: one per SM at least, more (up to the resident limit) while there
+  // are 32 points of X and Y per block. Every block reduces all blocks'
+  // records three times per update, so small problems run on fewer blocks.
+  const int N = B.N, M = B.M;
+  const int want = std::max(sms, (int)(((long)N + M) / 32));
+  const int grid = std::min(std::min(per_sm * sms, kBwdMaxGrid), want);
+  const Layout& L = c.L;
+  e = cudaMemsetAsync(L.ctl, 0, sizeof(Ctl), st);
+  if (e == cudaSuccess && B.nsteps > 0)
+    e = cudaMemcpyAsync(L.tab, host_tab, sizeof(SaUpdate) * (size_t)B.nsteps, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(L.X, B.X, sizeof(float4) * (size_t)N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(L.Y, B.Y, sizeof(float4) * (size_t)M, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(L.hdr, B.hdr, sizeof(CenterHdr), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.A.g_pose, B.g_out, sizeof(float) * 12, cudaMemcpyDeviceToDevice, st);
+  // the output slack of the last update does not feed the loss; dL/dX, dL/dY accumulate in the outputs
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gs, 0, sizeof(float) * N, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.A.gu, 0, sizeof(float) * M, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.gX, 0, sizeof(float) * 3 * (size_t)N, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.gY, 0, sizeof(float) * 3 * (size_t)M, st);
+  if (e != cudaSuccess) return (int)e;
+  k_fill<<<std::min(blocks(M), 1024), kGlue, 0, st>>>(c.A.ones, M, 1.f);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  BwdArgs a{};
+  a.A = c.A;
+  a.A.gX = B.gX;
+  a.A.gY = B.gY;
+  a.tab = L.tab;
+  a.nsteps = B.nsteps;
+  a.alpha = B.alpha;
+  a.rows = c.P.rows;
+  a.cols = c.P.cols;
+  plan_persistent(a.rows, grid, c.P.rows.S);
+  plan_persistent(a.cols, grid, c.P.cols.S);
+  a.part_r = L.part;
+  a.part_c = L.part2;
+  a.bpart = L.bpart;
+  a.ctl = L.ctl;
+  a.g_in = B.g_in;
+  a.d_status = d_status;
+  a.timeout_ns = timeout_ns;
+  void* args[] = {(void*)&a};
+  return (int)cudaLaunchCooperativeKernel((const void*)softassign_bwd_kernel, dim3(grid), dim3(kSwT), args, 0, st);
 }
 
 }  // namespace cesa

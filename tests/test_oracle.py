@@ -244,3 +244,16 @@ def test_oracle_softassign_live_against_reference_gpu_code(oracle):
         sch = dict(base, T_0=T0)
         Rr, tr_, trr = oracle.ref_softassign(X, Y, **sch)
         _check_softassign_against_reference(oracle, X, Y, sch, Rr, trr, (n, m, T0))
+
+
+def test_c3_reference_emicp_cpu_agrees_with_the_fp64_oracle_at_full_size():
+    """Config 3 at full size (N = M = 40,097, 66 steps): the reference's own
+    emicp_cpu() result stored in the fixture lands within 1e-4 degrees /
+    1e-6 x extent of the FP64 oracle's stored result on the same pair, which
+    the GPU tests compare the fused kernel with."""
+    g = np.load(os.path.join(GOLD, "c3_emicp_40097.npz"))
+    if "ref_R" not in g.files:
+        pytest.skip("fixture made without the reference tree")
+    ext = float(np.ptp(g["X"].astype(np.float64), 0).max())
+    assert rot_err_deg(g["ref_R"], g["R"]) < 1e-4
+    assert np.abs(g["ref_t"] - g["t"]).max() < 1e-6 * ext
