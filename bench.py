@@ -157,6 +157,8 @@ def fixture_for(args, p):
         return None
     if args.workload == "c3_emicp_40097" and p.sigma_inf == d.sigma_inf:
         path = os.path.join(GOLDEN, "c3_emicp_40097.npz")
+    elif args.workload == "c2_softassign_2000" and (p.JMAX, p.I0) == (d.JMAX, d.I0):
+        path = os.path.join(GOLDEN, "c2_softassign_2000.npz")
     elif args.workload == "c5_softassign_20000" and p.JMAX == 2 and p.I0 == d.I0:
         path = os.path.join(GOLDEN, "c5_softassign_20000_jmax2.npz")
     else:

@@ -1,6 +1,6 @@
 """Generates the full-size parity fixtures of the benchmark configs.
 
-    python tests/golden/make_fullsize_golden.py [c3] [c5] [c4] [--no-reference]
+    python tests/golden/make_fullsize_golden.py [c3] [c5] [c4] [c2] [--no-reference]
 
 Each fixture holds the FP64 oracle's result (oracle/cesa_oracle.c, a line-cited
 restatement of src/emicp_cpu.cpp:303-528 and src/softassign.cu:486-822) on the
@@ -14,6 +14,9 @@ GPU tests and bench.py compare against exactly the points the oracle saw:
   pair (6.4 GB for its dense A matrix; about 10 minutes on 8 cores).
 * c5_softassign_20000_jmax2.npz -- config 5 (N = M = 20,000) with the schedule
   cut to JMAX = 2 (10 pose updates, I0 = 5, I1 = 3): per-update trace and pose.
+* c2_softassign_2000.npz -- config 2 (N = M = 2000), the whole default
+  500-update schedule: per-update trace and pose (the trajectory the device
+  pose solver is checked along).
 * c4_emicp_pairs.npz -- the 128 EM-ICP pairs of config 4 (256 pairs, N and M
   log-uniform in [500, 20000]; the even indices of workloads.batch_pairs(256,
   seed 0)). These store no points: each pair's SHA-256 over its float32 X and Y
@@ -73,6 +76,15 @@ def make_c5():
                                        dtype=np.float64), sha=np.array(pair_sha(X, Y)))
 
 
+def make_c2():
+    _, X, Y, Rt, tt = W.make("c2_softassign_2000", seed=0)
+    t0 = time.time()
+    R, t, tr = O.softassign(X, Y)
+    print("c2 oracle f64: %d updates, %.0f s" % (len(tr), time.time() - t0), flush=True)
+    np.savez_compressed(os.path.join(HERE, "c2_softassign_2000.npz"), X=X, Y=Y, R=R, t=t, trace=tr,
+                        sha=np.array(pair_sha(X, Y)))
+
+
 def make_c4():
     idx, sha, N, M, Rs, ts, Rps = [], [], [], [], [], [], []
     t0 = time.time()
@@ -94,7 +106,7 @@ def make_c4():
 
 
 def main():
-    which = [a for a in sys.argv[1:] if not a.startswith("--")] or ["c3", "c5", "c4"]
+    which = [a for a in sys.argv[1:] if not a.startswith("--")] or ["c3", "c5", "c4", "c2"]
     O.set_threads(os.cpu_count() or 1)
     if "c3" in which:
         make_c3(with_reference="--no-reference" not in sys.argv)
@@ -102,6 +114,8 @@ def main():
         make_c5()
     if "c4" in which:
         make_c4()
+    if "c2" in which:
+        make_c2()
 
 
 if __name__ == "__main__":

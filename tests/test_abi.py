@@ -309,3 +309,33 @@ def test_device_pose_solver_random_cold(pose_harness, oracle):
         Ro, _, info = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), S)
         if info["gap"] > 1e-6:
             assert rot_err_deg(_quat_R(q), Ro) < 1e-7
+
+
+def test_device_pose_solvers_along_config_trajectories(pose_harness, oracle):
+    """Both FP32 pose solves of the kernels -- the warm-started Jacobi (taped
+    and matrix-free kernels) and the certified inverse iteration with its
+    Jacobi fallback (EM-ICP, banded Softassign, ICP) -- along the S sequences
+    of whole registrations: config 3's 66 EM-ICP steps and config 2's 500
+    Softassign updates, from the FP64 oracle's stored traces. Against the
+    FP64 solve of each S: within 1e-4 degrees per step wherever Horn's
+    relative eigen-gap exceeds 1e-3 (every step of both sequences here), and
+    the gap itself within 1e-4."""
+    for name in ("c3_emicp_40097.npz", "c2_softassign_2000.npz"):
+        g = np.load(os.path.join(GOLD, name))
+        S32 = np.ascontiguousarray(g["trace"][:, 9:18].astype(np.float32))
+        K = len(S32)
+        qj = np.zeros((K, 4), np.float32)
+        gap = np.zeros(K, np.float32)
+        pose_harness.pose_sequence_f32(S32.ctypes.data_as(ctypes.c_void_p), K, qj.ctypes.data_as(ctypes.c_void_p),
+                                       gap.ctypes.data_as(ctypes.c_void_p))
+        qf, _, _ = _fast_sequence(pose_harness, S32)
+        worst_j = worst_f = 0.0
+        for k in range(K):
+            Ro, _, info = oracle.find_rt_from_s(np.zeros(3), np.zeros(3), S32[k].astype(np.float64))
+            assert info["gap"] > 1e-3, (name, k, info["gap"])
+            e_j = rot_err_deg(_quat_R(qj[k].astype(np.float64)), Ro)
+            e_f = rot_err_deg(_quat_R(qf[k].astype(np.float64)), Ro)
+            assert e_j < 1e-4 and e_f < 1e-4, (name, k, e_j, e_f, info["gap"])
+            assert abs(gap[k] - info["gap"]) < 1e-4 * max(1.0, info["gap"]), (name, k)
+            worst_j, worst_f = max(worst_j, e_j), max(worst_f, e_f)
+        print("%s: %d solves, worst %.2e deg (Jacobi), %.2e deg (certified)" % (name, K, worst_j, worst_f))
