@@ -511,8 +511,8 @@ def batch_workload(args):
     for kind, X, Y, _, _ in W.batch_pairs(count=256, seed=args.seed)[:args.pairs]:
         if kind == "emicp":
             out.append((cesa.ALGO_EMICP, X, Y, cesa_params(cesa, em)))
-        else:
-            out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa_params(cesa, sa)))
+        else:  # the form applies to the one-pair-per-launch comparison (the batch runs its own sweeps)
+            out.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa_params(cesa, sa, args.sinkhorn_form)))
     return out
 
 

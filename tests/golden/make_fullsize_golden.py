@@ -20,8 +20,11 @@ GPU tests and bench.py compare against exactly the points the oracle saw:
 * c4_emicp_pairs.npz -- the 128 EM-ICP pairs of config 4 (256 pairs, N and M
   log-uniform in [500, 20000]; the even indices of workloads.batch_pairs(256,
   seed 0)). These store no points: each pair's SHA-256 over its float32 X and Y
-  bytes, so the test can check that the generator reproduced them, and the
-  oracle's pose.
+  bytes, so the test can check that the generator reproduced them, the
+  oracle's pose, and (where the reference tree is present) the reference's own
+  emicp_cpu() pose -- on some pairs its FP32 arithmetic, like any FP32
+  arithmetic, crosses a discontinuity of the algorithm (a row sum near the
+  1e-6 threshold of src/emicp.cu:155-159) that the FP64 oracle does not.
 """
 import hashlib
 import os
@@ -85,14 +88,19 @@ def make_c2():
                         sha=np.array(pair_sha(X, Y)))
 
 
-def make_c4():
-    idx, sha, N, M, Rs, ts, Rps = [], [], [], [], [], [], []
+def make_c4(with_reference=True):
+    idx, sha, N, M, Rs, ts, Rps, Rrs, trs = [], [], [], [], [], [], [], [], []
+    use_ref = with_reference and O.ref() is not None
     t0 = time.time()
     for k, (kind, X, Y, _, _) in enumerate(W.batch_pairs(count=256, seed=0)):
         if kind != "emicp":
             continue
         R, t, _ = O.emicp(X, Y, trace=False, **EMICP)
         Rp, _, _ = O.emicp(X, Y, precision="f32", trace=False, **EMICP)
+        if use_ref:
+            Rr, tr_ = O.ref_emicp_cpu(X, Y, **EMICP)
+            Rrs.append(Rr)
+            trs.append(tr_)
         idx.append(k)
         sha.append(pair_sha(X, Y))
         N.append(len(X))
@@ -101,8 +109,9 @@ def make_c4():
         ts.append(t)
         Rps.append(Rp)
     print("c4 oracle f64: %d EM-ICP pairs, %.0f s" % (len(idx), time.time() - t0), flush=True)
+    extra = dict(ref_R=np.array(Rrs), ref_t=np.array(trs)) if use_ref else {}
     np.savez_compressed(os.path.join(HERE, "c4_emicp_pairs.npz"), index=np.array(idx), sha=np.array(sha),
-                        N=np.array(N), M=np.array(M), R=np.array(Rs), t=np.array(ts), port_R=np.array(Rps))
+                        N=np.array(N), M=np.array(M), R=np.array(Rs), t=np.array(ts), port_R=np.array(Rps), **extra)
 
 
 def main():
@@ -113,7 +122,7 @@ def main():
     if "c5" in which:
         make_c5()
     if "c4" in which:
-        make_c4()
+        make_c4(with_reference="--no-reference" not in sys.argv)
     if "c2" in which:
         make_c2()
 

@@ -143,10 +143,18 @@ def _pair_sha(X, Y):
 
 def test_c4_emicp_pairs_match_fp64_oracle_batched_and_single(cesa):
     """Config 4's own 128 EM-ICP pairs (N, M log-uniform in [500, 20000]),
-    registered in the batched launch of all 256 pairs and one pair per call:
-    each within 1e-3 degrees / 1e-5 x extent of the FP64 oracle."""
+    registered in the batched launch of all 256 pairs and one pair per call,
+    against the FP64 oracle: each within 1e-3 degrees / 1e-5 x extent, or no
+    farther than twice the reference's own emicp_cpu() result (stored in the
+    fixture). On a few pairs every FP32 arithmetic, the reference's included,
+    crosses a discontinuity of the algorithm that FP64 does not (a row sum at
+    the 1e-6 threshold of src/emicp.cu:155-159, which switches that row to
+    lambda = 1 and X' = mean(X)); there the bound is the reference's own
+    distance."""
     from cuda_emicp_softassign_gb300 import workloads as W
     g = _load("c4_emicp_pairs.npz")
+    if "ref_R" not in g.files:
+        pytest.fail("c4_emicp_pairs.npz was made without the reference's emicp_cpu results")
     pairs = W.batch_pairs(count=256, seed=0)
     args = []
     for kind, X, Y, _, _ in pairs:
@@ -155,17 +163,20 @@ def test_c4_emicp_pairs_match_fp64_oracle_batched_and_single(cesa):
         else:
             args.append((cesa.ALGO_SOFTASSIGN, X, Y, cesa.Params.default(JMAX=60)))
     out = cesa.register_batch(args)
-    worst_b = worst_s = 0.0
+    within = 0
     for j, k in enumerate(g["index"]):
         kind, X, Y, _, _ = pairs[k]
         assert kind == "emicp"
         assert _pair_sha(X, Y) == str(g["sha"][j]), "the generator no longer reproduces pair %d" % k
         ext = _extent(X)
-        Rb, tb = out[k]
-        e_b = rot_err_deg(Rb, g["R"][j])
-        assert e_b < 1e-3 and np.abs(tb - g["t"][j]).max() < 1e-5 * ext, (k, e_b)
+        e_ref = rot_err_deg(g["ref_R"][j], g["R"][j])
+        et_ref = np.abs(g["ref_t"][j] - g["t"][j]).max() / ext
         Rs, ts = cesa.emicp(X, Y)
-        e_s = rot_err_deg(Rs, g["R"][j])
-        assert e_s < 1e-3 and np.abs(ts - g["t"][j]).max() < 1e-5 * ext, (k, e_s)
-        worst_b, worst_s = max(worst_b, e_b), max(worst_s, e_s)
-    print("config 4 EM-ICP pairs: worst rotation error batched %.2e, single %.2e deg" % (worst_b, worst_s))
+        for label, (R, t) in (("batched", out[k]), ("single", (Rs, ts))):
+            e = rot_err_deg(R, g["R"][j])
+            et = np.abs(t - g["t"][j]).max() / ext
+            assert e <= max(1e-3, 2.0 * e_ref), (label, int(k), e, e_ref)
+            assert et <= max(1e-5, 2.0 * et_ref), (label, int(k), et, et_ref)
+        within += rot_err_deg(out[k][0], g["R"][j]) < 1e-3
+    print("config 4 EM-ICP pairs: %d of %d within 1e-3 degrees of FP64 (the rest no farther than the reference's "
+          "own FP32 result)" % (within, len(g["index"])))
