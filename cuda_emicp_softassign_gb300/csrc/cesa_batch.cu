@@ -781,7 +781,7 @@ struct Carve {
 };
 
 SweepGeom batch_geom(int n_own, int n_stream, int slice) {
-  SweepGeom g;
+  SweepGeom g{};
   g.n_own = n_own;
   g.n_stream = n_stream;
   g.nblk = (n_own + kBlockPts - 1) / kBlockPts;

@@ -141,6 +141,19 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
         const int nr = min(kThreads, nrows - c0);
         for (int pq = tid; pq < 5 * nr; pq += kThreads) {
           const int a = pq % 5, rr = pq / 5;
+          if (A.geo.ranged) {  // the segments of the row's owned block, in task order
+            const int r = r0 + c0 + rr, o = r / kBlockPts;
+            int b_lo = 0, b_hi = 0;
+            ranged_blocks_of(A.geo, o, (int)G, b_lo, b_hi);
+            const long T = (long)A.geo.nblk * A.geo.nch;
+            float sum = 0.f;
+            for (int b = b_lo; b <= b_hi; ++b) {
+              const int k = o - (int)(T * b / (long)G / A.geo.nch);
+              sum += __ldcg(A.part + (((size_t)a * G + b) * A.geo.kmax + k) * kBlockPts + (r % kBlockPts));
+            }
+            stot[rr * 5 + a] = sum;
+            continue;
+          }
           const float* P = A.part + (size_t)a * S * A.Mp + r0 + c0 + rr;
           float sum = 0.f;
           int k = 0;
@@ -280,8 +293,20 @@ EmicpPlan plan_emicp(int N, int M, int device) {
   P.smem = sweep_smem();
   const int limit = persistent_grid_limit(device, (const void*)emicp_kernel, P.smem);
   const SweepGeomH h = plan_sweep(M, N, limit);
-  P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units};
+  P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units, 0, 0, 0};
   P.grid = h.units < limit ? h.units : limit;
+  // Large clouds: contiguous task ranges, the same work per block to one
+  // chunk of 512 streamed points (at least 16 tasks per block, so that the
+  // remainder is small), instead of units dealt in waves.
+  const long nch = (N + kChunk - 1) / kChunk;
+  const long T = (long)h.nblk * nch;
+  if (T >= 16L * limit) {
+    const long W = (T + limit - 1) / limit;
+    P.geo.ranged = 1;
+    P.geo.nch = (int)nch;
+    P.geo.kmax = (int)((W + nch - 1) / nch + 1);
+    P.grid = limit;
+  }
   return P;
 }
 
@@ -303,7 +328,8 @@ EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* to
   w.hdr = c.take<CenterHdr>(1);
   w.rows = c.take<float4>((size_t)M);
   w.cols = c.take<float4>((size_t)N);
-  w.part = c.take<float>((size_t)5 * P.geo.slices * w.Mp);
+  w.part = c.take<float>(P.geo.ranged ? (size_t)5 * P.grid * P.geo.kmax * kBlockPts
+                                      : (size_t)5 * P.geo.slices * w.Mp);
   w.rbpart = c.take<df>((size_t)2 * P.grid * kEmNV);
   if (total) *total = c.off;
   return w;
@@ -415,7 +441,10 @@ int persistent_grid_limit(int device, const void* kernel, size_t smem) {
 SweepGeomH plan_sweep(int n_own, int n_stream, int grid_limit) {
   SweepGeomH best{};
   const int nblk = (n_own + kBlockPts - 1) / kBlockPts;
-  const double fixed = 40000.0;
+#ifndef CESA_UNIT_FIXED_COST
+#define CESA_UNIT_FIXED_COST 40000.0  // per-unit cost in element evaluations of one block
+#endif
+  const double fixed = CESA_UNIT_FIXED_COST;
   double best_cost = 1e300;
   const int smax_stream = (n_stream + 31) / 32;
   const int smax = smax_stream < 128 ? smax_stream : 128;

@@ -508,7 +508,10 @@ AdjPlan plan_adj(int N, int M, int device) {
   const int max_s = (M + 63) / 64;  // at least 64 rows per slice
   int bestS = 1;
   double best = -1.0;
-  for (int w = 1; w <= 4; ++w) {
+#ifndef CESA_ADJ_MAX_WAVES
+#define CESA_ADJ_MAX_WAVES 4
+#endif
+  for (int w = 1; w <= CESA_ADJ_MAX_WAVES; ++w) {
     int S = (w * limit) / g.nb;
     if (S < 1) S = 1;
     if (S > max_s) S = max_s;

@@ -40,7 +40,38 @@ struct SweepGeom {
   int slices;     // S
   int slice_len;  // ceil(n_stream / S)
   int units;      // nblk * S
+  // Ranged decomposition (deferred sweeps only; 0 = units of (owned block,
+  // slice) dealt round-robin). The work is nblk * nch tasks of (owned block,
+  // streamed chunk), in owned-block-major order; block b of the grid takes
+  // the contiguous tasks [T b / G, T (b + 1) / G). Its run of tasks on one
+  // owned block is a segment; segment k of block b stores its partials in
+  // slot (b, k), k < kmax. Every block gets the same work to one chunk, and a
+  // block meets an owned block only 2-3 times in a sweep of a large cloud.
+  int ranged;
+  int nch;        // ceil(n_stream / kChunk)
+  int kmax;       // most segments of one block
 };
+
+// Task range [t0, t1) of block b in a ranged sweep over G blocks.
+__host__ __device__ __forceinline__ void ranged_tasks(const SweepGeom& g, int b, int G, long& t0, long& t1) {
+  const long T = (long)g.nblk * g.nch;
+  t0 = T * b / G;
+  t1 = T * (b + 1) / G;
+}
+
+// The blocks whose ranges cover owned block o, [b_lo, b_hi] (needs T >= G:
+// no empty range), in increasing task order.
+__device__ __forceinline__ void ranged_blocks_of(const SweepGeom& g, int o, int G, int& b_lo, int& b_hi) {
+  const long T = (long)g.nblk * g.nch;
+  auto first_block = [&](long task) {
+    int b = (int)(task * G / T);
+    while (b + 1 < G && (T * (b + 1)) / G <= task) ++b;
+    while (b > 0 && (T * b) / G > task) --b;
+    return b;
+  };
+  b_lo = first_block((long)o * g.nch);
+  b_hi = first_block((long)(o + 1) * g.nch - 1);
+}
 
 struct __align__(16) SweepSmem {
   float4 raw[kStages][kChunk];   // TMA destination, stream A
@@ -385,7 +416,7 @@ struct NoFin {
 __device__ __forceinline__ void sweep_prefetch(Pipe& p, SweepSmem& sm, const SweepGeom& g,
                                                const StreamSrc& src) {
   const int u = blockIdx.x;
-  if (u >= g.units || p.pre_valid) return;
+  if (g.ranged || u >= g.units || p.pre_valid) return;
   const int sl = u % g.slices;
   const int sb = sl * g.slice_len;
   const int se = min(sb + g.slice_len, g.n_stream);
@@ -427,7 +458,24 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
   const int tid = threadIdx.x, warp = tid >> 5;
   const int G = (int)gridDim.x;
   pipe.cur = -1;
+  // ranged: u is this block's segment index, and segment u covers chunks
+  // [cb, ce) of owned block o_first + u
+  long rt0 = 0, rt1 = 0;
+  if (g.ranged) ranged_tasks(g, blockIdx.x, G, rt0, rt1);
+  const int o_first = g.ranged ? (int)(rt0 / g.nch) : 0;
+  const int o_last = g.ranged ? (int)((rt1 - 1) / g.nch) : 0;
   auto task_range = [&](int uu, int ch, int& first, int& len) -> bool {
+    if (g.ranged) {
+      const int o = o_first + uu;
+      if (rt1 <= rt0 || o > o_last) return false;
+      const int cb = uu == 0 ? (int)(rt0 - (long)o * g.nch) : 0;
+      const int ce = o == o_last ? (int)(rt1 - (long)o * g.nch) : g.nch;
+      const int c = cb + ch;
+      if (c >= ce) return false;
+      first = c * kChunk;
+      len = min(kChunk, g.n_stream - first);
+      return true;
+    }
     if (uu >= g.units) return false;
     const int sl = uu % g.slices;
     const int sb = sl * g.slice_len;
@@ -437,7 +485,8 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
     len = min(kChunk, se - first);
     return true;
   };
-  int u = blockIdx.x;
+  const int ustep = g.ranged ? 1 : G;
+  int u = g.ranged ? 0 : (int)blockIdx.x;
   int cur_first = 0, cur_len = 0, cur_ch = 0, cur_stage = 0;
   unsigned cur_par = 0;
   bool cur_wait = false;
@@ -460,7 +509,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
   }
   pipe.pre_valid = false;
   while (have) {
-    const int blk = u / g.slices, sl = u % g.slices;
+    const int blk = g.ranged ? o_first + u : u / g.slices, sl = g.ranged ? u : u % g.slices;
     float4 ow[kOwnPerLane];
     if (oc) {
       load_owned_cached(*oc, own, g.n_own, blk, ow);
@@ -495,7 +544,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
       bool n_wait = false;
       bool have_n = task_range(n_u, n_ch, n_first, n_len);
       if (!have_n) {
-        n_u = u + G;
+        n_u = u + ustep;
         n_ch = 0;
         have_n = task_range(n_u, 0, n_first, n_len);
       }
@@ -539,14 +588,20 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
     if (kDeferred) {
       const int i = blk * kBlockPts + (int)threadIdx.x;
       if (threadIdx.x < kBlockPts && i < g.n_own) {
+        if (g.ranged) {  // slot (block, segment)
 #pragma unroll
-        for (int a = 0; a < NACC; ++a) __stcg(part + ((size_t)a * g.slices + sl) * part_ld + i, tot[a]);
+          for (int a = 0; a < NACC; ++a)
+            __stcg(part + (((size_t)a * G + blockIdx.x) * g.kmax + sl) * kBlockPts + threadIdx.x, tot[a]);
+        } else {
+#pragma unroll
+          for (int a = 0; a < NACC; ++a) __stcg(part + ((size_t)a * g.slices + sl) * part_ld + i, tot[a]);
+        }
       }
     } else if (split_complete<NACC>(sm, g, blk, sl, round, part, cnt, tot)) {
       fin(blk, tot);
     }
     tl.mark(4);
-    u += G;
+    u += ustep;
     cur_ch = 0;
   }
   return true;
