@@ -38,7 +38,8 @@ struct EmicpArgs {
   int nsteps;
   const CenterHdr* hdr;
   float* dRt;           // PoseIO in/out, caller frame
-  float* part;          // row partials [5][S][Mp] (accumulator, column slice, row)
+  float* part;          // row partials [5][S][Mp] (accumulator, column slice, row); ranged: [5][nblk][kmax][128]
+  float4* xs;           // ranged sweeps: X' scaled for the step, [2][N] by step parity
   int Mp;
   df* rbpart;           // [2][grid][kEmNV] moments per block (step parity)
   Ctl* ctl;
@@ -59,6 +60,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   __shared__ float s_pose[12];
   __shared__ df s_red[kThreads];
   __shared__ OwnCache oc_rows;
+  __shared__ RangedShare rs_rows;  // this block's share of a ranged sweep
   __shared__ df s_tot[kEmNV];
   __shared__ float s_emS[15];  // S, Xc, Yc of the step
   __shared__ float s_hdr[12];
@@ -81,6 +83,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     for (int k = 0; k < 9; ++k) s_pose[k] = R[k];
     for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
     oc_rows.blk = -1;
+    rs_rows = ranged_share(A.geo, blockIdx.x, (int)gridDim.x);
   }
   __syncthreads();
 
@@ -96,9 +99,26 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   const StreamSrc src{A.cols, nullptr, true};
   float s2 = A.sigma0;
   Timeline tl{A.tl, A.tl_cap, 0};
+  // Ranged sweeps stream X' scaled by sc = sqrt(log2(e) / (2 s2)) (and scale the
+  // owned rows alike), so that an element needs no scale of its own. Each step's
+  // copy is written by all blocks during the previous step's row completion.
+  auto scale_x = [&](float4* dst, float sc) {
+    for (int i = (int)blockIdx.x * kThreads + tid; i < A.N; i += (int)G * kThreads) {
+      const float4 x = ld_cg(A.cols + i);
+      __stcg(dst + i, make_float4(x.x * sc, x.y * sc, x.z * sc, 0.f));
+    }
+  };
+  bool started = true;  // false: the barrier after the first scaled copy gave up
+  if (A.geo.ranged && A.nsteps > 0) {
+    scale_x(A.xs, sqrtf(kLog2e / (2.f * s2)));
+    started = grid_sync(A.ctl, epoch, G, A.timeout_ns, 22);
+  }
 
-  for (int step = 0; step < A.nsteps; ++step) {
+  for (int step = 0; step < A.nsteps && started; ++step) {
     tl.mark(1);
+    // the scaled X' was written by other blocks' ordinary stores, ahead of a
+    // grid barrier; the bulk copies that stream it read through the async proxy
+    if (A.geo.ranged && tid == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
     const float outlier = expf(-A.d_02 / s2);  // src/emicp.cu:489
     float R[9], tc[3];
 #pragma unroll
@@ -109,13 +129,30 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
 
     // e = exp(-d2 / (2 s2)) = 2^(nk d2). Every unit stores its rows' partial
     // sums over its column slice (deferred: no completion counter).
-    const EmicpElem elem{-kLog2e / (2.f * s2)};
-    if (!sweep_units<5, EmicpElem, NoPrep, NoFin, true>(sm, pipe, A.geo, src, A.rows, true, R, tc, 0u, A.part,
-                                                         nullptr, elem, NoPrep{}, NoFin{}, A.ctl, A.timeout_ns, 10,
-                                                         tl, A.Mp, &oc_rows))
-      break;
+    const float sc = sqrtf(kLog2e / (2.f * s2));
+    if (A.geo.ranged) {
+      float Rs[9], tcs[3];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Rs[k] = R[k] * sc;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) tcs[k] = tc[k] * sc;
+      const StreamSrc xsrc{A.xs + (size_t)(step & 1) * A.N, nullptr, false};
+      if (!sweep_units<5, EmicpElemScaled, NoPrep, NoFin, true, 1>(sm, pipe, A.geo, xsrc, A.rows, true, Rs, tcs, 0u,
+                                                                A.part, nullptr, EmicpElemScaled{}, NoPrep{}, NoFin{},
+                                                                A.ctl, A.timeout_ns, 10, tl, A.Mp, &oc_rows, &rs_rows))
+        break;
+    } else {
+      const EmicpElem elem{-kLog2e / (2.f * s2)};
+      if (!sweep_units<5, EmicpElem, NoPrep, NoFin, true, 0>(sm, pipe, A.geo, src, A.rows, true, R, tc, 0u, A.part,
+                                                           nullptr, elem, NoPrep{}, NoFin{}, A.ctl, A.timeout_ns, 10,
+                                                           tl, A.Mp, &oc_rows))
+        break;
+    }
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
     tl.mark(5);
+    // the next step's scaled X' (its buffer was last read by the previous step's sweep)
+    if (A.geo.ranged && step + 1 < A.nsteps)
+      scale_x(A.xs + (size_t)((step + 1) & 1) * A.N, sqrtf(kLog2e / (2.f * (s2 * A.sigma_factor))));
 
     // ---- rows completed, each block a contiguous share of them; its 16
     // moments are one record. Thread t first sums the slice partials of
@@ -124,6 +161,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     df* rb = A.rbpart + (size_t)(step & 1) * G * kEmNV;
     {
       const int S = A.geo.slices;
+      const float inv_sc = 1.f / sc;
       const int rpc = (A.M + (int)G - 1) / (int)G;
       const int r0 = (int)blockIdx.x * rpc;
       const int nrows = max(0, min(rpc, A.M - r0));
@@ -141,17 +179,18 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
         const int nr = min(kThreads, nrows - c0);
         for (int pq = tid; pq < 5 * nr; pq += kThreads) {
           const int a = pq % 5, rr = pq / 5;
-          if (A.geo.ranged) {  // the segments of the row's owned block, in task order
-            const int r = r0 + c0 + rr, o = r / kBlockPts;
-            int b_lo = 0, b_hi = 0;
-            ranged_blocks_of(A.geo, o, (int)G, b_lo, b_hi);
-            const long T = (long)A.geo.nblk * A.geo.nch;
+          if (A.geo.ranged) {  // the kmax slots of the row's owned block, in task order
+            const int kmax = A.geo.kmax;
+            const float* P = A.part + (size_t)a * A.geo.nblk * kmax * kBlockPts + ranged_slot0(r0 + c0 + rr, kmax);
             float sum = 0.f;
-            for (int b = b_lo; b <= b_hi; ++b) {
-              const int k = o - (int)(T * b / (long)G / A.geo.nch);
-              sum += __ldcg(A.part + (((size_t)a * G + b) * A.geo.kmax + k) * kBlockPts + (r % kBlockPts));
+            for (int j = 0; j < kmax; j += 4) {  // 4 loads in flight, then added in slot order
+              float w[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) w[q] = j + q < kmax ? __ldcg(P + (size_t)(j + q) * kBlockPts) : 0.f;
+#pragma unroll
+              for (int q = 0; q < 4; ++q) sum += w[q];
             }
-            stot[rr * 5 + a] = sum;
+            stot[rr * 5 + a] = a >= 2 ? sum * inv_sc : sum;  // the scaled coordinates' sums
             continue;
           }
           const float* P = A.part + (size_t)a * S * A.Mp + r0 + c0 + rr;
@@ -296,15 +335,9 @@ EmicpPlan plan_emicp(int N, int M, int device) {
   P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units, 0, 0, 0};
   P.grid = h.units < limit ? h.units : limit;
   // Large clouds: contiguous task ranges, the same work per block to one
-  // chunk of 512 streamed points (at least 16 tasks per block, so that the
-  // remainder is small), instead of units dealt in waves.
-  const long nch = (N + kChunk - 1) / kChunk;
-  const long T = (long)h.nblk * nch;
-  if (T >= 16L * limit) {
-    const long W = (T + limit - 1) / limit;
-    P.geo.ranged = 1;
-    P.geo.nch = (int)nch;
-    P.geo.kmax = (int)((W + nch - 1) / nch + 1);
+  // chunk of 512 streamed points, instead of units dealt in waves.
+  if (ranged_pays(h.nblk, N, limit)) {
+    make_ranged(P.geo, limit);
     P.grid = limit;
   }
   return P;
@@ -315,6 +348,7 @@ struct EmicpCarved {
   CenterHdr* hdr;
   float4* rows;
   float4* cols;
+  float4* xs;
   float* part;
   df* rbpart;
   int Mp;
@@ -328,7 +362,8 @@ EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* to
   w.hdr = c.take<CenterHdr>(1);
   w.rows = c.take<float4>((size_t)M);
   w.cols = c.take<float4>((size_t)N);
-  w.part = c.take<float>(P.geo.ranged ? (size_t)5 * P.grid * P.geo.kmax * kBlockPts
+  w.xs = c.take<float4>(P.geo.ranged ? (size_t)2 * N : 0);
+  w.part = c.take<float>(P.geo.ranged ? (size_t)5 * P.geo.nblk * P.geo.kmax * kBlockPts
                                       : (size_t)5 * P.geo.slices * w.Mp);
   w.rbpart = c.take<df>((size_t)2 * P.grid * kEmNV);
   if (total) *total = c.off;
@@ -360,8 +395,11 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   EmicpCarved w = carve_emicp(ws, P, L.N, L.M, &total);
   if (total > ws_bytes) return (int)cudaErrorInvalidValue;
   if (grid_used) *grid_used = P.grid;
-  // the control block starts at zero every launch
+  // the control block starts at zero every launch, and so do the ranged
+  // partial slots (those no block writes must read as zero)
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
+  if (e == cudaSuccess && P.geo.ranged)
+    e = cudaMemsetAsync(w.part, 0, sizeof(float) * 5 * (size_t)P.geo.nblk * P.geo.kmax * kBlockPts, st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
@@ -384,6 +422,7 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.hdr = w.hdr;
   A.dRt = L.dRt;
   A.part = w.part;
+  A.xs = w.xs;
   A.Mp = w.Mp;
   A.rbpart = w.rbpart;
   A.ctl = w.ctl;

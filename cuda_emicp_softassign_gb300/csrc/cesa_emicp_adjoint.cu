@@ -151,24 +151,29 @@ struct AdjSmem {
   unsigned flag;
 };
 
-// The record of one streamed row (one thread per row): -z, -gA/s2, -gB/s2,
-// -2gC/s2 and gB, interleaved with the other row of its pair.
+// The record of one streamed row (one thread per row), in coordinates scaled
+// by sc = sqrt(log2(e) / (2 s2)), so that e = 2^-|x' - z'|^2 needs no scale
+// per element: -z', -gA/s2, -gB/(s2 sc), -2gC/s2 and gB sc, interleaved with
+// the other row of its pair. (-gB/s2 multiplies the unscaled x = x'/sc; gB sc
+// and the scaled differences make the sweep's dL/dx and dL/dz sc times the
+// true ones, which the unit divides out once.)
 __device__ __forceinline__ void build_row_record(AdjSmem& sm, int i, bool valid, float4 y, const float (&rt)[5],
-                                                 const float* R, const float* t, const float* coef, float inv_s2) {
+                                                 const float* R, const float* t, const float* coef, float inv_s2,
+                                                 float sc, float inv_sc) {
   float v[11];
   if (valid) {
     const RowCoef c = row_coef(y, true, rt, R, t, coef);
-    v[0] = -c.z[0];
-    v[1] = -c.z[1];
-    v[2] = -c.z[2];
+    v[0] = -c.z[0] * sc;
+    v[1] = -c.z[1] * sc;
+    v[2] = -c.z[2] * sc;
     v[3] = -c.gA * inv_s2;
-    v[4] = -c.gB[0] * inv_s2;
-    v[5] = -c.gB[1] * inv_s2;
-    v[6] = -c.gB[2] * inv_s2;
+    v[4] = -c.gB[0] * inv_s2 * inv_sc;
+    v[5] = -c.gB[1] * inv_s2 * inv_sc;
+    v[6] = -c.gB[2] * inv_s2 * inv_sc;
     v[7] = -c.gC2 * inv_s2;
-    v[8] = c.gB[0];
-    v[9] = c.gB[1];
-    v[10] = c.gB[2];
+    v[8] = c.gB[0] * sc;
+    v[9] = c.gB[1] * sc;
+    v[10] = c.gB[2] * sc;
   } else {  // far away, no coefficients: every term it feeds is 0
     v[0] = v[1] = v[2] = kFar;
 #pragma unroll
@@ -220,8 +225,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
     const float* t = s_pose + 9;
     const float* coef = s_coef;
     const float s2 = s_pose[12];
-    const float nk = -kLog2e / (2.f * s2), inv_s2 = 1.f / s2;
-    const float2 nk2 = dup2(nk);
+    const float inv_s2 = 1.f / s2;
+    const float sc = sqrtf(kLog2e / (2.f * s2)), inv_sc = 1.f / sc;  // coordinate scale
     const float* rtape = A.row_tape + (size_t)k * A.M * 5;
     df* recs = A.rec + (size_t)par * g.S * 16;
     float4* px = A.part_x + (size_t)par * g.S * A.N;
@@ -235,9 +240,9 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
       for (int j = 0; j < kAdjCols; ++j) {
         const int c = cb * kAdjColBlk + j * kThreads + tid;
         const float4 x = c < A.N ? ld_cg(A.cols + c) : make_float4(kFar, kFar, kFar, 0.f);
-        xd[j][0] = dup2(x.x);
-        xd[j][1] = dup2(x.y);
-        xd[j][2] = dup2(x.z);
+        xd[j][0] = dup2(x.x * sc);
+        xd[j][1] = dup2(x.y * sc);
+        xd[j][2] = dup2(x.z * sc);
 #pragma unroll
         for (int a = 0; a < 3; ++a) gx[j][a] = make_float2(0.f, 0.f);
       }
@@ -249,9 +254,14 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
 #pragma unroll
         for (int q = 0; q < 5; ++q) rtn[q] = __ldcg(rtape + (size_t)(rb + tid) * 5 + q);
       }
+      // Two barriers per chunk: the record build of chunk n + 1 touches only
+      // rec, which every warp has finished reading at the barrier after the
+      // sweep of chunk n, and the sweep of chunk n + 1 (which writes wsum)
+      // starts only after the barrier that follows that build, by which time
+      // every thread has consumed wsum of chunk n.
+      __syncthreads();  // the previous unit's shared-memory use is over
       for (int r0 = rb; r0 < re; r0 += kAdjRows) {
-        __syncthreads();  // the previous chunk's records and sums are consumed
-        build_row_record(sm, tid, r0 + tid < re, yn, rtn, R, t, coef, inv_s2);
+        build_row_record(sm, tid, r0 + tid < re, yn, rtn, R, t, coef, inv_s2, sc, inv_sc);
         __syncthreads();
         // the next chunk's row, in flight during this chunk's sweep
         const int rn = r0 + kAdjRows + tid;
@@ -281,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
               float2 d2 = __fmul2_rn(dx, dx);
               d2 = __ffma2_rn(dy, dy, d2);
               d2 = __ffma2_rn(dz, dz, d2);
-              const float2 e = ex2_pair(__fmul2_rn(d2, nk2));
+              const float2 e = ex2_neg_pair(d2);
               float2 nge = __ffma2_rn(ngB0, xd[j][0], ngA);
               nge = __ffma2_rn(ngB1, xd[j][1], nge);
               nge = __ffma2_rn(ngB2, xd[j][2], nge);
@@ -333,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
             float v = sm.wsum[a][0][tid];
 #pragma unroll
             for (int w = 1; w < kWarps; ++w) v += sm.wsum[a][w][tid];
-            gz[a] = -v;
+            gz[a] = -v * inv_sc;
           }
           __stcg(A.part_z + (size_t)cb * A.M + r0 + tid, make_float4(gz[0], gz[1], gz[2], 0.f));
         }
@@ -344,7 +354,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
         const int c = cb * kAdjColBlk + j * kThreads + tid;
         if (c < A.N)
           __stcg(px + (size_t)sl * A.N + c,
-                 make_float4(gx[j][0].x + gx[j][0].y, gx[j][1].x + gx[j][1].y, gx[j][2].x + gx[j][2].y, 0.f));
+                 make_float4((gx[j][0].x + gx[j][0].y) * inv_sc, (gx[j][1].x + gx[j][1].y) * inv_sc,
+                             (gx[j][2].x + gx[j][2].y) * inv_sc, 0.f));
       }
       // split completion of the row slice: the last of its nb units
       __threadfence();

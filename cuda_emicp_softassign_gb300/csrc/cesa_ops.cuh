@@ -25,6 +25,10 @@ __device__ __forceinline__ float2 dist2_pair(const float2 (&q)[3], float4 s) {
 
 __device__ __forceinline__ float2 ex2_pair(float2 t) { return make_float2(ex2_approx(t.x), ex2_approx(t.y)); }
 
+// 2^-t of a packed pair (the negation is the exponential's operand, not a
+// separate instruction).
+__device__ __forceinline__ float2 ex2_neg_pair(float2 t) { return make_float2(ex2_approx(-t.x), ex2_approx(-t.y)); }
+
 // ------------------------------------------------------------------ EM-ICP
 constexpr int kEmNV = 16;  // moments: sum lambda, sum u (3), sum lambda y (3), sum u y^T (9)
 
@@ -34,6 +38,20 @@ struct EmicpElem {
   float nk;  // -log2(e) / (2 sigma_p2)
   __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 x, float4) const {
     const float2 e = ex2_pair(__fmul2_rn(dist2_pair(q, x), dup2(nk)));
+    acc[0] = __ffma2_rn(e, e, acc[0]);
+    acc[1] = __fadd2_rn(acc[1], e);
+    acc[2] = __ffma2_rn(e, dup2(x.x), acc[2]);
+    acc[3] = __ffma2_rn(e, dup2(x.y), acc[3]);
+    acc[4] = __ffma2_rn(e, dup2(x.z), acc[4]);
+  }
+};
+
+// The same with both clouds scaled by sc = sqrt(log2(e) / (2 sigma_p2)) (the
+// streamed X' and the owned R y + t): e = 2^-|x' - z'|^2, one packed multiply
+// fewer per pair; the e x sums come out sc times too large.
+struct EmicpElemScaled {
+  __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 x, float4) const {
+    const float2 e = ex2_neg_pair(dist2_pair(q, x));
     acc[0] = __ffma2_rn(e, e, acc[0]);
     acc[1] = __fadd2_rn(acc[1], e);
     acc[2] = __ffma2_rn(e, dup2(x.x), acc[2]);
@@ -223,11 +241,34 @@ struct SinkElem {
   }
 };
 
+// The same with both clouds scaled by sc = sqrt(log2(e) / T) and 2^c0 folded
+// into the streamed weight (w = 2^c0 b): K / 2^c0 = 2^-|x' - y'|^2, one packed
+// op fewer per pair.
+struct SinkElemScaled {
+  __device__ __forceinline__ void operator()(float2 (&acc)[1], const float2 (&q)[3], float4 s, float4) const {
+    const float2 e = ex2_neg_pair(dist2_pair(q, s));
+    acc[0] = __ffma2_rn(e, dup2(s.w), acc[0]);
+  }
+};
+
 // Final row sweep element: w += K b, mu += K delta, Vhat += K g (y' - Yhat).
 struct FinalElem {
   float nk, c0;
   __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 s, float4 h) const {
     const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q, s), dup2(nk), dup2(c0)));
+    acc[0] = __ffma2_rn(e, dup2(s.w), acc[0]);
+    acc[1] = __ffma2_rn(e, dup2(h.w), acc[1]);
+    acc[2] = __ffma2_rn(e, dup2(h.x), acc[2]);
+    acc[3] = __ffma2_rn(e, dup2(h.y), acc[3]);
+    acc[4] = __ffma2_rn(e, dup2(h.z), acc[4]);
+  }
+};
+
+// The final sweep element on scaled clouds, with 2^c0 folded into the four
+// streamed weights (b, delta, g (y' - Yhat)), as in SinkElemScaled.
+struct FinalElemScaled {
+  __device__ __forceinline__ void operator()(float2 (&acc)[5], const float2 (&q)[3], float4 s, float4 h) const {
+    const float2 e = ex2_neg_pair(dist2_pair(q, s));
     acc[0] = __ffma2_rn(e, dup2(s.w), acc[0]);
     acc[1] = __ffma2_rn(e, dup2(h.w), acc[1]);
     acc[2] = __ffma2_rn(e, dup2(h.x), acc[2]);

@@ -17,10 +17,14 @@
 // sums. The next pass completes it while preparing the points it streams
 // (deferred completion: no completion counters or serial finalize on the
 // critical path). A designated unit per point stores the new scaling and slack
-// in ping-pong buffers. Each sweep element costs 3 FADD + FMUL + 2 FFMA
-// (direct-difference d^2), 1 FFMA (exponent), 1 MUFU ex2 and 1 FFMA (weighted
-// sum): 8 FP32 ops + 1 MUFU op. Per pose update there are 2*I1 + 1 sweeps and
-// 2*I1 + 1 grid barriers.
+// in ping-pong buffers. The sweeps see both clouds scaled by
+// sqrt(log2(e) / T), with the factor 2^c0 of K folded into the streamed
+// weights, so a Sinkhorn element costs 3 FADD + FMUL + 2 FFMA (direct-
+// difference d'^2), 1 MUFU ex2 (of -d'^2) and 1 FFMA (weighted sum): 7 FP32 ops
+// + 1 MUFU op. Per pose update there are 2*I1 + 1 sweeps and 2*I1 + 1 grid
+// barriers. Large clouds take the ranged decomposition in the Sinkhorn
+// passes, and their prepare steps are double-buffered (one block barrier per
+// chunk).
 //
 // The reference's S is not translation invariant, because X is weighted and
 // only then centred. Coordinates are shifted by exact offsets (see
@@ -48,15 +52,16 @@ struct SoftArgs {
   float* w_out;        // optional [N]
   int N, M, Np, Mp;
   SweepGeom gr, gc;    // row sweeps (own X, stream Y) / column sweeps (own Y, stream X)
+  SweepGeom gf;        // the final row sweep (never ranged: it completes through counters)
   int JMAX, I0, I1;
   float alpha, T0, TFACTOR;
   const CenterHdr* hdr;
   float* dRt;
-  float* pr;           // row-pass partials [S_r][Np]
-  float* pc;           // column-pass partials [S_c][Mp]
-  float* part_f;       // final-sweep split partials [units_r][5][128]
+  float* pr;           // row-pass partials [S_r][Np]; ranged: [nblk_r][kmax_r][128]
+  float* pc;           // column-pass partials [S_c][Mp]; ranged: [nblk_c][kmax_c][128]
+  float* part_f;       // final-sweep split partials [units_f][5][128]
   unsigned* cnt_f;     // [nblk_r]
-  df* mom;             // [2][nblk_r + S_c][32] moment records: row blocks, then column slices
+  df* mom;             // [2][nblk_r + S_f][32] moment records: row blocks, then column slices
   Ctl* ctl;
   double* trace;
   int trace_cap;
@@ -72,14 +77,30 @@ struct SoftArgs {
   float* tape_fin;     // optional [nsteps][5][N]
 };
 
-// Sums of the S slice partials of points i0 and i1 (i1 only when has1), the
-// deferred completion: each point's partials are added in slice order, and a
+// Where the partials of one streamed point lie in a deferred sweep's partial
+// array: S values ld apart, from index at(i). Slices: [S][ld], point i at i.
+// Ranged: [nblk][kmax][kBlockPts], point i's kmax slots from ranged_slot0.
+struct PartView {
+  const float* p;
+  int S, ld, kr;  // kr: kmax of a ranged layout, 0 for slices
+  __device__ __forceinline__ int at(int i) const { return kr ? ranged_slot0(i, kr) : i; }
+};
+
+__device__ __forceinline__ PartView part_view(const float* p, const SweepGeom& g, int ld) {
+  return g.ranged ? PartView{p, g.kmax, kBlockPts, g.kmax} : PartView{p, g.slices, ld, 0};
+}
+
+// Sums of the partials of points i0 and i1 (i1 only when has1), the deferred
+// completion: each point's partials are added in slice (or slot) order, and a
 // batch's loads for both points (8 each) are in flight before the first add.
 // A last partial batch is padded with zeros (the partials are sums of
 // positive terms, so adding +0 leaves each sum bitwise unchanged): S = 7 at
 // 20,000 points is one batch of 14 loads, not 7 round trips.
-__device__ __forceinline__ void slice_sum2(const float* part, int S, int ld, int i0, int i1, bool has1, float& s0,
-                                           float& s1) {
+__device__ __forceinline__ void slice_sum2(const PartView& pv, int i0, int i1, bool has1, float& s0, float& s1) {
+  const float* part = pv.p;
+  const int S = pv.S, ld = pv.ld;
+  i0 = pv.at(i0);
+  i1 = has1 ? pv.at(i1) : i0;
   s0 = 0.f;
   s1 = 0.f;
   int k = 0;
@@ -117,8 +138,7 @@ static_assert(kChunk == 2 * kThreads, "two streamed points per thread in a prep 
 //   cs = b_old * (column sum of K a) + u_old,  b_new = b_old / cs,  u_new = u_old / cs.
 // The unit designated for c (block index 0 of its sweep) stores the results.
 struct ColDone {
-  const float* pc;
-  int S, ld;
+  PartView pc;
   const float* b_old;  // nullptr: b_old = 1 (first pass of an inner iteration)
   const float* u_old;
   float* b_new;
@@ -147,7 +167,7 @@ struct ColDone {
   __device__ __forceinline__ void pair(int c0, int c1, bool has1, bool store, float& bn0, float& csv0, float& bn1,
                                        float& csv1) const {
     float sum0, sum1;
-    slice_sum2(pc, S, ld, c0, c1, has1, sum0, sum1);
+    slice_sum2(pc, c0, c1, has1, sum0, sum1);
     const float bo0 = b_old ? __ldcg(b_old + c0) : 1.f;
     const float uo0 = __ldcg(u_old + c0);
     const float bo1 = has1 ? (b_old ? __ldcg(b_old + c1) : 1.f) : 1.f;
@@ -157,30 +177,41 @@ struct ColDone {
   }
 };
 
+// The Sinkhorn passes' prepare steps write chunks alternately into prep and
+// prep2 (double-buffered; the sweep loop places the one barrier per chunk).
+__device__ __forceinline__ float4* prep_buffer(SweepSmem& sm, int& par) {
+  float4* b = par ? sm.prep2 : sm.prep;
+  par ^= 1;
+  return b;
+}
+
 // Streamed Y columns for Sinkhorn row sweeps: (R y' + t', b_c). b_c := 1 in
 // the first pass of an inner iteration, else the completed previous column pass.
 struct RowPrep {
-  float R[9], tc[3];
+  static constexpr bool kDoubleBuffered = true;
+  float R[9], tc[3];  // the pose times sc (scaled clouds)
+  float wsc;          // 2^c0, folded into the weight
   bool fresh;
   ColDone cd;
+  mutable int par = 0;
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
+    float4* buf = prep_buffer(sm, par);
     const int c0 = threadIdx.x, c1 = threadIdx.x + kThreads;
     if (c0 < len) {
       const bool h1 = c1 < len;
       float w0 = 1.f, w1 = 1.f, cs0, cs1;
       if (!fresh) cd.pair(first + c0, first + c1, h1, blk == 0, w0, cs0, w1, cs1);
-      put(sm, stage, c0, w0);
-      if (h1) put(sm, stage, c1, w1);
+      put(sm, buf, stage, c0, w0);
+      if (h1) put(sm, buf, stage, c1, w1);
     }
-    __syncthreads();
-    return PrepOut{sm.prep, sm.raw2[stage]};
+    return PrepOut{buf, sm.raw2[stage]};
   }
-  __device__ __forceinline__ void put(SweepSmem& sm, int stage, int c, float w) const {
+  __device__ __forceinline__ void put(SweepSmem& sm, float4* buf, int stage, int c, float w) const {
     const float4 y = sm.raw[stage][c];
-    sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
+    buf[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
                              R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w);
+                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], w * wsc);
   }
   __device__ __forceinline__ void unit_end(int, int) const {}
 };
@@ -189,8 +220,8 @@ struct RowPrep {
 // previous row pass (normalizeMbySinkhorn_row + Saxpy, src/softassign.cu:538-561):
 //   rs = a_old * (row sum of K b) + s_old,  a_new = a_old / rs,  s_new = s_old / rs.
 struct ColPrep {
-  const float* pr;
-  int S, ld;
+  static constexpr bool kDoubleBuffered = true;
+  PartView pr;
   const float* a_old;  // nullptr: a_old = 1
   const float* s_old;
   float* a_new;
@@ -198,26 +229,28 @@ struct ColPrep {
   float* rs_out;
   float* tape = nullptr;  // optional [4][N]: a_new, s_new, rs, row sum
   int N = 0;
+  float sc = 1.f, wsc = 1.f;  // coordinate scale, 2^c0 folded into the weight
+  mutable int par = 0;
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int first, int len,
                                                 int blk) const {
+    float4* buf = prep_buffer(sm, par);
     const int c0 = threadIdx.x, c1 = threadIdx.x + kThreads;
     if (c0 < len) {
       const bool h1 = c1 < len;
       const int r0 = first + c0, r1 = first + c1;
       float sum0, sum1;
-      slice_sum2(pr, S, ld, r0, r1, h1, sum0, sum1);
+      slice_sum2(pr, r0, r1, h1, sum0, sum1);
       const float ao0 = a_old ? __ldcg(a_old + r0) : 1.f;
       const float so0 = __ldcg(s_old + r0);
       const float ao1 = h1 ? (a_old ? __ldcg(a_old + r1) : 1.f) : 1.f;
       const float so1 = h1 ? __ldcg(s_old + r1) : 1.f;
-      row_done(sm, stage, c0, r0, sum0, ao0, so0, blk);
-      if (h1) row_done(sm, stage, c1, r1, sum1, ao1, so1, blk);
+      row_done(sm, buf, stage, c0, r0, sum0, ao0, so0, blk);
+      if (h1) row_done(sm, buf, stage, c1, r1, sum1, ao1, so1, blk);
     }
-    __syncthreads();
-    return PrepOut{sm.prep, sm.raw2[stage]};
+    return PrepOut{buf, sm.raw2[stage]};
   }
-  __device__ __forceinline__ void row_done(SweepSmem& sm, int stage, int c, int r, float sum, float ao, float so,
-                                           int blk) const {
+  __device__ __forceinline__ void row_done(SweepSmem& sm, float4* buf, int stage, int c, int r, float sum, float ao,
+                                           float so, int blk) const {
     const float4 x = sm.raw[stage][c];
     const float rsv = fmaf(ao, sum, so);
     const float an = ao / rsv;
@@ -233,7 +266,7 @@ struct ColPrep {
         __stcg(tape + 3 * (size_t)N + r, sum);
       }
     }
-    sm.prep[c] = make_float4(x.x, x.y, x.z, an);
+    buf[c] = make_float4(x.x * sc, x.y * sc, x.z * sc, an * wsc);
   }
   __device__ __forceinline__ void unit_end(int, int) const {}
 };
@@ -245,7 +278,8 @@ struct ColPrep {
 // accumulate the column moments sum cs and sum cs y' of their slice and store
 // them as one moment record per slice.
 struct FinalPrep {
-  float R[9], tc[3], yh[3];
+  float R[9], tc[3], yh[3];  // R, tc: the pose times sc (scaled clouds)
+  float wsc;                 // 2^c0, folded into the four weights
   ColDone cd;
   df* colacc;   // shared [kThreads][4], per-thread running sums
   df* red;      // shared scratch (kThreads dfs)
@@ -266,11 +300,11 @@ struct FinalPrep {
   }
   __device__ __forceinline__ void put(SweepSmem& sm, int stage, int c, float bn, float csv, int blk) const {
     const float4 y = sm.raw[stage][c];
-    const float g = bn * csv;
+    const float g = bn * csv * wsc;
     sm.prep[c] = make_float4(R[0] * y.x + R[1] * y.y + R[2] * y.z + tc[0],
                              R[3] * y.x + R[4] * y.y + R[5] * y.z + tc[1],
-                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn);
-    sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]), bn * (csv - 1.f));
+                             R[6] * y.x + R[7] * y.y + R[8] * y.z + tc[2], bn * wsc);
+    sm.prep2[c] = make_float4(g * (y.x - yh[0]), g * (y.y - yh[1]), g * (y.z - yh[2]), bn * (csv - 1.f) * wsc);
     if (blk == 0) {
       df* a = colacc + threadIdx.x * 4;
       df_add(a[0], csv);
@@ -309,6 +343,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   __shared__ df s_colacc[kThreads * 4];
   __shared__ df s_tmp4[4];
   __shared__ OwnCache oc_rows, oc_cols;
+  __shared__ RangedShare rs_rows, rs_cols;  // this block's shares of the ranged Sinkhorn passes
   __shared__ float s_hdr[12];
   __shared__ SaPoseScratch ps;
 
@@ -335,6 +370,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
     horn.reset();
     oc_rows.blk = -1;
     oc_cols.blk = -1;
+    rs_rows = ranged_share(A.gr, blockIdx.x, (int)gridDim.x);
+    rs_cols = ranged_share(A.gc, blockIdx.x, (int)gridDim.x);
   }
   for (int k = tid; k < kThreads * 4; k += kThreads) s_colacc[k] = df_make(0.f);
   __syncthreads();
@@ -352,17 +389,21 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
   const int Np = A.Np, Mp = A.Mp;
 
   for (int Titer = 0; Titer < A.JMAX && ok; ++Titer) {
-    // K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
+    // K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2) = 2^c0 2^-|x' - y'|^2
+    // for clouds scaled by sc = sqrt(-nk): the sweeps see the scaled clouds,
+    // and 2^c0 is folded into the streamed weights (a_r, b_c and the final
+    // sweep's four), so that an element costs 7 FP32 ops and one ex2.
     const float kk = kLog2e / T;
-    const float nk = -kk;
     const float c0 = fmaf(A.alpha, kk, -0.5f * log2f(T));
+    const float sc = sqrtf(kk), wsc = exp2f(c0);
+    const float Rdg[9] = {sc, 0.f, 0.f, 0.f, sc, 0.f, 0.f, 0.f, sc}, z3[3] = {0.f, 0.f, 0.f};  // owned X rows
     for (int iter0 = 0; iter0 < A.I0 && ok; ++iter0, ++step) {
       tl.mark(1);
-      float R[9], tc[3];
+      float R[9], tc[3];  // the pose, times sc
 #pragma unroll
-      for (int k = 0; k < 9; ++k) R[k] = s_pose[k];
+      for (int k = 0; k < 9; ++k) R[k] = s_pose[k] * sc;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k];
+      for (int k = 0; k < 3; ++k) tc[k] = s_pose[9 + k] * sc;
       if (kTape) {
         // the update's inputs for the adjoint: s and u are the current ping-pong
         // buffers, which are next overwritten two grid barriers from here
@@ -374,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
           A.tape_u[(size_t)step * A.M + i] = __ldcg(A.ubuf + (size_t)up * Mp + i);
       }
       __syncthreads();
-      const SinkElem se{nk, c0};
+      const SinkElemScaled se{};
       float* trow = kTape ? A.tape_rows + (size_t)step * A.I1 * 4 * A.N : nullptr;
       float* tcol = kTape ? A.tape_cols + (size_t)step * A.I1 * 4 * A.M : nullptr;
       for (int k = 0; k < A.I1 && ok; ++k) {
@@ -384,10 +425,9 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
         for (int q = 0; q < 9; ++q) rp.R[q] = R[q];
 #pragma unroll
         for (int q = 0; q < 3; ++q) rp.tc[q] = tc[q];
+        rp.wsc = wsc;
         rp.fresh = (k == 0);
-        rp.cd = ColDone{A.pc,
-                        A.gc.slices,
-                        Mp,
+        rp.cd = ColDone{part_view(A.pc, A.gc, Mp),
                         k >= 2 ? A.bbuf + (size_t)((k - 1) & 1) * Mp : nullptr,
                         A.ubuf + (size_t)up * Mp,
                         A.bbuf + (size_t)(k & 1) * Mp,
@@ -395,18 +435,20 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.cs};
         rp.cd.tape = (tcol && k >= 1) ? tcol + (size_t)(k - 1) * 4 * A.M : nullptr;  // column pass k-1
         rp.cd.M = A.M;
-        ok = sweep_units<1, SinkElem, RowPrep, NoFin, true>(sm, pipe, A.gr, src_cols, A.rows, false, R,
-                                                            tc, 0u, A.pr, nullptr, se, rp, NoFin{},
-                                                            A.ctl, A.timeout_ns, 30, tl, Np, &oc_rows);
+        ok = A.gr.ranged
+                 ? sweep_units<1, SinkElemScaled, RowPrep, NoFin, true, 1>(sm, pipe, A.gr, src_cols, A.rows, true, Rdg, z3,
+                                                                     0u, A.pr, nullptr, se, rp, NoFin{}, A.ctl,
+                                                                     A.timeout_ns, 30, tl, Np, &oc_rows, &rs_rows)
+                 : sweep_units<1, SinkElemScaled, RowPrep, NoFin, true, 0>(sm, pipe, A.gr, src_cols, A.rows, true, Rdg, z3,
+                                                                     0u, A.pr, nullptr, se, rp, NoFin{}, A.ctl,
+                                                                     A.timeout_ns, 30, tl, Np, &oc_rows);
         if (ok) sweep_prefetch(pipe, sm, A.gc, src_rows);
         ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 32);
         tl.mark(5);
         if (!ok) break;
         if (k >= 1) up ^= 1;  // the row pass completed column pass k-1
         // column pass k: own Y columns, stream X rows weighted by a^(k+1)
-        ColPrep cp{A.pr,
-                   A.gr.slices,
-                   Np,
+        ColPrep cp{part_view(A.pr, A.gr, Np),
                    k >= 1 ? A.abuf + (size_t)(k & 1) * Np : nullptr,
                    A.sbuf + (size_t)sp * Np,
                    A.abuf + (size_t)((k + 1) & 1) * Np,
@@ -414,10 +456,16 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                    A.rs};
         cp.tape = trow ? trow + (size_t)k * 4 * A.N : nullptr;  // row pass k
         cp.N = A.N;
-        ok = sweep_units<1, SinkElem, ColPrep, NoFin, true>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
-                                                           0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
-                                                           A.timeout_ns, 40, tl, Mp, &oc_cols);
-        if (ok) sweep_prefetch(pipe, sm, A.gr, src_cols);  // the next row pass or the final sweep
+        cp.sc = sc;
+        cp.wsc = wsc;
+        ok = A.gc.ranged
+                 ? sweep_units<1, SinkElemScaled, ColPrep, NoFin, true, 1>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
+                                                                     0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
+                                                                     A.timeout_ns, 40, tl, Mp, &oc_cols, &rs_cols)
+                 : sweep_units<1, SinkElemScaled, ColPrep, NoFin, true, 0>(sm, pipe, A.gc, src_rows, A.cols, true, R, tc,
+                                                                     0u, A.pc, nullptr, se, cp, NoFin{}, A.ctl,
+                                                                     A.timeout_ns, 40, tl, Mp, &oc_cols);
+        if (ok) sweep_prefetch(pipe, sm, k + 1 < A.I1 ? A.gr : A.gf, src_cols);  // the next row pass or the final sweep
         ok = ok && grid_sync(A.ctl, epoch, G, A.timeout_ns, 42);
         tl.mark(5);
         sp ^= 1;
@@ -426,6 +474,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       // final row sweep: completes the last column pass, accumulates w, mu, Vhat
       {
         FinalPrep fp;
+        fp.wsc = wsc;
 #pragma unroll
         for (int q = 0; q < 9; ++q) fp.R[q] = R[q];
 #pragma unroll
@@ -434,9 +483,7 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
           fp.yh[q] = s_hdr[6 + q];
         }
         const int kl = A.I1 - 1;
-        fp.cd = ColDone{A.pc,
-                        A.gc.slices,
-                        Mp,
+        fp.cd = ColDone{part_view(A.pc, A.gc, Mp),
                         kl >= 1 ? A.bbuf + (size_t)(kl & 1) * Mp : nullptr,
                         A.ubuf + (size_t)up * Mp,
                         A.bbuf + (size_t)(A.I1 & 1) * Mp,
@@ -444,12 +491,12 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                         A.cs};
         fp.cd.tape = tcol ? tcol + (size_t)kl * 4 * A.M : nullptr;  // the last column pass
         fp.cd.M = A.M;
-        df* mom = A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32;
+        df* mom = A.mom + (size_t)(step & 1) * (A.gf.nblk + A.gf.slices) * 32;
         fp.colacc = s_colacc;
         fp.red = s_red;
         fp.tmp = s_tmp4;
-        fp.colrec = mom + (size_t)A.gr.nblk * 32;
-        const FinalElem fe{nk, c0};
+        fp.colrec = mom + (size_t)A.gf.nblk * 32;
+        const FinalElemScaled fe{};
         // owned_block_sum<32> scratch (32 * (128 + 8) dfs) spans prep, prep2 and red
         static_assert(offsetof(SweepSmem, full) - offsetof(SweepSmem, prep) >= 32 * (kBlockPts + 8) * sizeof(df),
                       "moment scratch does not fit");
@@ -457,7 +504,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
                     reinterpret_cast<df*>(sm.prep), mom};
         ff.tape_fin = kTape ? A.tape_fin + (size_t)step * 5 * A.N : nullptr;
         const StreamSrc src_final{A.cols, nullptr, false};
-        ok = sweep_units<5>(sm, pipe, A.gr, src_final, A.rows, false, R, tc, round_f++, A.part_f,
+        ok = sweep_units<5, FinalElemScaled, FinalPrep, FinalFin, false, 0>(sm, pipe, A.gf, src_final, A.rows, true, Rdg, z3,
+                                                                            round_f++, A.part_f,
                             A.cnt_f, fe, fp, ff, A.ctl, A.timeout_ns, 50, tl, 0, &oc_rows);
         if (!ok) break;
         up ^= 1;
@@ -466,8 +514,8 @@ __global__ void __launch_bounds__(kThreads, 2) softassign_kernel(const SoftArgs 
       ok = grid_sync(A.ctl, epoch, G, A.timeout_ns, 52);
       tl.mark(5);
       if (!ok) break;
-      reduce_block_partials<32>(A.mom + (size_t)(step & 1) * (A.gr.nblk + A.gr.slices) * 32,
-                                A.gr.nblk + A.gr.slices, s_red, s_tot);
+      reduce_block_partials<32>(A.mom + (size_t)(step & 1) * (A.gf.nblk + A.gf.slices) * 32,
+                                A.gf.nblk + A.gf.slices, s_red, s_tot);
       tl.mark(6);
       float* tape_rec = kTape ? A.tape_pose + (size_t)step * kSaTape : nullptr;
       double* trace_rec = (A.trace && step < A.trace_cap) ? A.trace + (size_t)step * 32 : nullptr;
@@ -512,7 +560,7 @@ struct Carve {
 
 struct SaPlan {
   int grid;
-  SweepGeom gr, gc;
+  SweepGeom gr, gc, gf;
   size_t smem;
 };
 
@@ -525,10 +573,17 @@ SaPlan plan_sa(int N, int M, int device) {
   const int limit = lim0 < lim1 ? lim0 : lim1;
   const SweepGeomH r = plan_sweep(N, M, limit);
   const SweepGeomH c = plan_sweep(M, N, limit);
-  P.gr = SweepGeom{r.n_own, r.n_stream, r.nblk, r.slices, r.slice_len, r.units};
-  P.gc = SweepGeom{c.n_own, c.n_stream, c.nblk, c.slices, c.slice_len, c.units};
+  P.gr = SweepGeom{r.n_own, r.n_stream, r.nblk, r.slices, r.slice_len, r.units, 0, 0, 0};
+  P.gc = SweepGeom{c.n_own, c.n_stream, c.nblk, c.slices, c.slice_len, c.units, 0, 0, 0};
+  P.gf = P.gr;
   const int mu = r.units > c.units ? r.units : c.units;
   P.grid = mu < limit ? mu : limit;
+  // Large clouds: the Sinkhorn passes take contiguous task ranges (the same
+  // work per block to one chunk) instead of units dealt in waves.
+  const bool rr = ranged_pays(r.nblk, M, limit), rc = ranged_pays(c.nblk, N, limit);
+  if (rr || rc) P.grid = limit;
+  if (rr) make_ranged(P.gr, P.grid);
+  if (rc) make_ranged(P.gc, P.grid);
   return P;
 }
 
@@ -546,13 +601,18 @@ struct SaCarved {
   int Np, Mp;
 };
 
+// Floats of one Sinkhorn pass's partial array (see PartView).
+size_t pass_part_floats(const SweepGeom& g, int ld) {
+  return g.ranged ? (size_t)g.nblk * g.kmax * kBlockPts : (size_t)g.slices * ld;
+}
+
 SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
   Carve c(base);
   SaCarved w;
   w.Np = (N + 3) & ~3;
   w.Mp = (M + 3) & ~3;
   w.ctl = c.take<Ctl>(1);
-  w.cnt_f = c.take<unsigned>((size_t)P.gr.nblk);
+  w.cnt_f = c.take<unsigned>((size_t)P.gf.nblk);
   w.hdr = c.take<CenterHdr>(1);
   w.rows = c.take<float4>((size_t)N);
   w.cols = c.take<float4>((size_t)M);
@@ -562,10 +622,10 @@ SaCarved carve_sa(void* base, const SaPlan& P, int N, int M, size_t* total) {
   w.ubuf = c.take<float>((size_t)2 * w.Mp);
   w.rs = c.take<float>((size_t)w.Np);
   w.cs = c.take<float>((size_t)w.Mp);
-  w.pr = c.take<float>((size_t)P.gr.slices * w.Np);
-  w.pc = c.take<float>((size_t)P.gc.slices * w.Mp);
-  w.part_f = c.take<float>((size_t)P.gr.units * 5 * kBlockPts);
-  w.mom = c.take<df>((size_t)2 * (P.gr.nblk + P.gr.slices) * 32);
+  w.pr = c.take<float>(pass_part_floats(P.gr, w.Np));
+  w.pc = c.take<float>(pass_part_floats(P.gc, w.Mp));
+  w.part_f = c.take<float>((size_t)P.gf.units * 5 * kBlockPts);
+  w.mom = c.take<df>((size_t)2 * (P.gf.nblk + P.gf.slices) * 32);
   if (total) *total = c.off;
   return w;
 }
@@ -601,7 +661,10 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   if (total > ws_bytes) return (int)cudaErrorInvalidValue;
   if (grid_used) *grid_used = P.grid;
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt_f, 0, sizeof(unsigned) * (size_t)P.gr.nblk, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.cnt_f, 0, sizeof(unsigned) * (size_t)P.gf.nblk, st);
+  // ranged partial slots that no block writes must read as zero
+  if (e == cudaSuccess && P.gr.ranged) e = cudaMemsetAsync(w.pr, 0, sizeof(float) * pass_part_floats(P.gr, w.Np), st);
+  if (e == cudaSuccess && P.gc.ranged) e = cudaMemsetAsync(w.pc, 0, sizeof(float) * pass_part_floats(P.gc, w.Mp), st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
@@ -635,6 +698,7 @@ int enqueue_softassign(const SoftassignLaunch& L, void* ws, size_t ws_bytes, cud
   A.Mp = w.Mp;
   A.gr = P.gr;
   A.gc = P.gc;
+  A.gf = P.gf;
   A.JMAX = L.JMAX;
   A.I0 = L.I0;
   A.I1 = L.I1;

@@ -20,6 +20,8 @@
 // Units are assigned round-robin to the blocks of the persistent grid. The
 // host picks S so that the unit count is close to a multiple of the grid size.
 #pragma once
+#include <type_traits>
+
 #include "cesa_common.cuh"
 
 namespace cesa {
@@ -43,13 +45,17 @@ struct SweepGeom {
   // Ranged decomposition (deferred sweeps only; 0 = units of (owned block,
   // slice) dealt round-robin). The work is nblk * nch tasks of (owned block,
   // streamed chunk), in owned-block-major order; block b of the grid takes
-  // the contiguous tasks [T b / G, T (b + 1) / G). Its run of tasks on one
-  // owned block is a segment; segment k of block b stores its partials in
-  // slot (b, k), k < kmax. Every block gets the same work to one chunk, and a
-  // block meets an owned block only 2-3 times in a sweep of a large cloud.
+  // the contiguous tasks [T b / G, T (b + 1) / G). Every block gets the same
+  // work to one chunk, and a block meets an owned block only 2-3 times in a
+  // sweep of a large cloud. Owned block o is covered by the consecutive grid
+  // blocks b_lo(o) .. b_hi(o); the partials of the j-th of them are stored in
+  // slot (o, j), j < kmax. Slots that no block writes (j > b_hi - b_lo) hold
+  // zeros, set once per launch, so a consumer sums all kmax slots of a point
+  // in slot order (the grid blocks' task order) with no division: adding +0
+  // leaves a sum that starts at +0 bitwise unchanged.
   int ranged;
   int nch;        // ceil(n_stream / kChunk)
-  int kmax;       // most segments of one block
+  int kmax;       // most grid blocks covering one owned block
 };
 
 // Task range [t0, t1) of block b in a ranged sweep over G blocks.
@@ -59,18 +65,60 @@ __host__ __device__ __forceinline__ void ranged_tasks(const SweepGeom& g, int b,
   t1 = T * (b + 1) / G;
 }
 
-// The blocks whose ranges cover owned block o, [b_lo, b_hi] (needs T >= G:
-// no empty range), in increasing task order.
-__device__ __forceinline__ void ranged_blocks_of(const SweepGeom& g, int o, int G, int& b_lo, int& b_hi) {
+// The grid block whose task range holds `task`: the largest b with
+// floor(T b / G) <= task, i.e. floor(((task + 1) G - 1) / T).
+__host__ __device__ __forceinline__ int ranged_block_of(const SweepGeom& g, long task, int G) {
   const long T = (long)g.nblk * g.nch;
-  auto first_block = [&](long task) {
-    int b = (int)(task * G / T);
-    while (b + 1 < G && (T * (b + 1)) / G <= task) ++b;
-    while (b > 0 && (T * b) / G > task) --b;
-    return b;
-  };
-  b_lo = first_block((long)o * g.nch);
-  b_hi = first_block((long)(o + 1) * g.nch - 1);
+  return (int)(((task + 1) * (long)G - 1) / T);
+}
+
+// One grid block's share of a ranged sweep: owned blocks [o_first, o_last]
+// (o_last = -1: none), chunks [c_first, nch) of the first and [0, c_end) of the
+// last, and j_first, its index among the blocks covering o_first (it is the
+// first to cover every later owned block of its range). Computed once per
+// launch (the 64-bit divisions stay out of the sweeps).
+struct RangedShare {
+  int o_first, o_last, c_first, c_end, j_first;
+};
+
+__device__ __forceinline__ RangedShare ranged_share(const SweepGeom& g, int b, int G) {
+  RangedShare r{0, -1, 0, 0, 0};
+  if (!g.ranged) return r;
+  long t0 = 0, t1 = 0;
+  ranged_tasks(g, b, G, t0, t1);
+  if (t1 <= t0) return r;
+  r.o_first = (int)(t0 / g.nch);
+  r.o_last = (int)((t1 - 1) / g.nch);
+  r.c_first = (int)(t0 - (long)r.o_first * g.nch);
+  r.c_end = (int)(t1 - (long)r.o_last * g.nch);
+  r.j_first = b - ranged_block_of(g, (long)r.o_first * g.nch, G);
+  return r;
+}
+
+// Large sweeps take the ranged decomposition: at least 16 tasks per block, so
+// that the one-chunk remainder is small.
+__host__ __forceinline__ bool ranged_pays(int nblk, int n_stream, int G) {
+  const long nch = (n_stream + kChunk - 1) / kChunk;
+  return (long)nblk * nch >= 16L * G;
+}
+
+// Turns g into a ranged sweep over G blocks (host; requires ranged_pays).
+__host__ __forceinline__ void make_ranged(SweepGeom& g, int G) {
+  g.ranged = 1;
+  g.nch = (g.n_stream + kChunk - 1) / kChunk;
+  int kmax = 1;
+  for (int o = 0; o < g.nblk; ++o) {
+    const int lo = ranged_block_of(g, (long)o * g.nch, G);
+    const int hi = ranged_block_of(g, (long)(o + 1) * g.nch - 1, G);
+    kmax = hi - lo + 1 > kmax ? hi - lo + 1 : kmax;
+  }
+  g.kmax = kmax;
+}
+
+// Index of point i's first slot in a ranged partial array of one accumulator,
+// [nblk][kmax][kBlockPts]; its slots follow kBlockPts apart.
+__device__ __forceinline__ int ranged_slot0(int i, int kmax) {
+  return ((i / kBlockPts) * kmax) * kBlockPts + (i % kBlockPts);
 }
 
 struct __align__(16) SweepSmem {
@@ -393,6 +441,16 @@ struct PrepOut {
   const float4* b;
 };
 
+// A prepare step that copies each chunk into its own double buffer (and does
+// not read the stream stage after it returns, nor end with a barrier) sets
+// kDoubleBuffered: its sweep then needs one block barrier per chunk, after
+// the prepare step, and warps run one chunk apart (a warp may prepare chunk
+// n + 1 while others still sweep chunk n from the other buffer).
+template <class P, class = void>
+struct prep_double_buffered : std::false_type {};
+template <class P>
+struct prep_double_buffered<P, std::void_t<decltype(P::kDoubleBuffered)>> : std::bool_constant<P::kDoubleBuffered> {};
+
 // Prepare step that uses the streams as loaded.
 struct NoPrep {
   __device__ __forceinline__ PrepOut operator()(SweepSmem& sm, int stage, int, int, int) const {
@@ -416,11 +474,22 @@ struct NoFin {
 __device__ __forceinline__ void sweep_prefetch(Pipe& p, SweepSmem& sm, const SweepGeom& g,
                                                const StreamSrc& src) {
   const int u = blockIdx.x;
-  if (g.ranged || u >= g.units || p.pre_valid) return;
-  const int sl = u % g.slices;
-  const int sb = sl * g.slice_len;
-  const int se = min(sb + g.slice_len, g.n_stream);
-  const int first = sb, len = min(kChunk, se - sb);
+  if (p.pre_valid) return;
+  int first = 0, len = 0;
+  if (g.ranged) {  // the first task of this block's range
+    long t0 = 0, t1 = 0;
+    ranged_tasks(g, u, (int)gridDim.x, t0, t1);
+    if (t1 <= t0) return;
+    first = (int)(t0 % g.nch) * kChunk;
+    len = min(kChunk, g.n_stream - first);
+  } else {
+    if (u >= g.units) return;
+    const int sl = u % g.slices;
+    const int sb = sl * g.slice_len;
+    const int se = min(sb + g.slice_len, g.n_stream);
+    first = sb;
+    len = min(kChunk, se - sb);
+  }
   p.cur = -1;
   bool w = false;
   const int st = pipe_issue(p, sm, src, first, first, len, w);
@@ -447,29 +516,34 @@ __device__ __forceinline__ void sweep_prefetch(Pipe& p, SweepSmem& sm, const Swe
 // kDeferred: the owned totals of slice sl are stored at part[sl * part_ld + point]
 // and nothing is finalized here (no completion counter, no Fin); the sweep
 // that streams these points next sums the S slices itself.
-template <int NACC, class Elem, class Prep, class Fin, bool kDeferred = false>
+// kLayout: 1 for a ranged geometry (rs: this block's share of it, from
+// ranged_share), 0 for units of (owned block, slice), -1 to read g.ranged at
+// run time (a fixed layout keeps only its own bookkeeping live in registers).
+template <int NACC, class Elem, class Prep, class Fin, bool kDeferred = false, int kLayout = -1>
 __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const SweepGeom& g,
                                             const StreamSrc& src, const float4* own, bool xform_own,
                                             const float (&R)[9], const float (&tc)[3], unsigned round,
                                             float* part, unsigned* cnt, const Elem& elem,
                                             const Prep& prep, const Fin& fin, Ctl* ctl,
                                             uint64_t timeout_ns, int where, Timeline& tl,
-                                            int part_ld = 0, OwnCache* oc = nullptr) {
+                                            int part_ld = 0, OwnCache* oc = nullptr,
+                                            const RangedShare* rs = nullptr) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int G = (int)gridDim.x;
+  const bool ranged = kLayout < 0 ? g.ranged != 0 : kLayout == 1;
+  constexpr bool kDB = prep_double_buffered<Prep>::value;
   pipe.cur = -1;
   // ranged: u is this block's segment index, and segment u covers chunks
-  // [cb, ce) of owned block o_first + u
-  long rt0 = 0, rt1 = 0;
-  if (g.ranged) ranged_tasks(g, blockIdx.x, G, rt0, rt1);
-  const int o_first = g.ranged ? (int)(rt0 / g.nch) : 0;
-  const int o_last = g.ranged ? (int)((rt1 - 1) / g.nch) : 0;
+  // [cb, ce) of owned block o_first + u: chunks [c_first, nch) of the first,
+  // [0, c_end) of the last (o_last = -1 for an empty range). The share is read
+  // from shared memory where it is used, not held in registers.
   auto task_range = [&](int uu, int ch, int& first, int& len) -> bool {
-    if (g.ranged) {
-      const int o = o_first + uu;
-      if (rt1 <= rt0 || o > o_last) return false;
-      const int cb = uu == 0 ? (int)(rt0 - (long)o * g.nch) : 0;
-      const int ce = o == o_last ? (int)(rt1 - (long)o * g.nch) : g.nch;
+    if (ranged) {
+      const int o = rs->o_first + uu;
+      const int o_last = rs->o_last;
+      if (o > o_last) return false;
+      const int cb = uu == 0 ? rs->c_first : 0;
+      const int ce = o == o_last ? rs->c_end : g.nch;
       const int c = cb + ch;
       if (c >= ce) return false;
       first = c * kChunk;
@@ -485,8 +559,8 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
     len = min(kChunk, se - first);
     return true;
   };
-  const int ustep = g.ranged ? 1 : G;
-  int u = g.ranged ? 0 : (int)blockIdx.x;
+  const int ustep = ranged ? 1 : G;
+  int u = ranged ? 0 : (int)blockIdx.x;
   int cur_first = 0, cur_len = 0, cur_ch = 0, cur_stage = 0;
   unsigned cur_par = 0;
   bool cur_wait = false;
@@ -509,7 +583,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
   }
   pipe.pre_valid = false;
   while (have) {
-    const int blk = g.ranged ? o_first + u : u / g.slices, sl = g.ranged ? u : u % g.slices;
+    const int blk = ranged ? rs->o_first + u : u / g.slices, sl = ranged ? u : u % g.slices;
     float4 ow[kOwnPerLane];
     if (oc) {
       load_owned_cached(*oc, own, g.n_own, blk, ow);
@@ -554,13 +628,19 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
         n_par = (pipe.uses[n_stage] - 1u) & 1u;
       }
       const bool bad = cur_wait && !mbar_wait(&sm.full[cur_stage], cur_par, ctl, timeout_ns, where);
-      if (__syncthreads_or(bad)) {  // block-uniform decision
+      if (!kDB && __syncthreads_or(bad)) {  // block-uniform decision
         // leave only after the prefetched copy (if any) has landed
         if (have_n && n_wait) mbar_wait(&sm.full[n_stage], n_par, ctl, timeout_ns, where + 1);
         return false;
       }
       if (cur_ch == 0 && u == (int)blockIdx.x) tl.mark(2);
+      // (double-buffered: a stage that timed out is read as it is; the
+      // decision to leave is taken at the barrier after the prepare step)
       const PrepOut pb = prep(sm, cur_stage, cur_first, cur_len, blk);
+      if (kDB && __syncthreads_or(bad)) {
+        if (have_n && n_wait) mbar_wait(&sm.full[n_stage], n_par, ctl, timeout_ns, where + 1);
+        return false;
+      }
       const float4* __restrict__ bufA = pb.a;
       const float4* __restrict__ bufB = pb.b;
 #pragma unroll 2
@@ -570,7 +650,7 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
 #pragma unroll
         for (int k = 0; k < kPairs; ++k) elem(acc[k], q[k], a, b);
       }
-      __syncthreads();
+      if (!kDB) __syncthreads();  // the stage and the prepared chunk are consumed
       const bool unit_done = !(have_n && n_u == u);
       cur_first = n_first;
       cur_len = n_len;
@@ -588,10 +668,11 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
     if (kDeferred) {
       const int i = blk * kBlockPts + (int)threadIdx.x;
       if (threadIdx.x < kBlockPts && i < g.n_own) {
-        if (g.ranged) {  // slot (block, segment)
+        if (ranged) {  // slot (owned block, j): this block is the j-th to cover it
+          const int j = sl == 0 ? rs->j_first : 0;
 #pragma unroll
           for (int a = 0; a < NACC; ++a)
-            __stcg(part + (((size_t)a * G + blockIdx.x) * g.kmax + sl) * kBlockPts + threadIdx.x, tot[a]);
+            __stcg(part + (((size_t)a * g.nblk + blk) * g.kmax + j) * kBlockPts + threadIdx.x, tot[a]);
         } else {
 #pragma unroll
           for (int a = 0; a < NACC; ++a) __stcg(part + ((size_t)a * g.slices + sl) * part_ld + i, tot[a]);
