@@ -25,7 +25,11 @@ CESA_ERR_NO_DEVICE = 4
 CESA_ERR_OUT_OF_MEMORY = 5
 CESA_ERR_UNSUPPORTED = 6
 CESA_ERR_NOALLOC_LIMIT = 7
+CESA_ERR_INTERNAL = 8
 
+LAYOUT_AUTO = 0
+LAYOUT_SLICES = 1
+LAYOUT_RANGED = 2
 SINKHORN_AUTO = 0
 SINKHORN_MATRIX_FREE = 1
 SINKHORN_MATERIALISED = 2
@@ -61,7 +65,7 @@ class Params(ctypes.Structure):
         ("sigma_factor", ctypes.c_float), ("d_02", ctypes.c_float),
         ("maxIteration", ctypes.c_int),
         ("sinkhorn_form", ctypes.c_int), ("timeout_ms", ctypes.c_int), ("device", ctypes.c_int),
-        ("icp_search", ctypes.c_int), ("reserved", ctypes.c_int * 4),
+        ("icp_search", ctypes.c_int), ("emicp_backward_layout", ctypes.c_int), ("reserved", ctypes.c_int * 3),
     ]
 
     @classmethod

@@ -799,6 +799,8 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
   if (N < 1 || M < 1 || !tape || !d_gRt || !d_gX || !d_gY || !d_gRt0) return CESA_ERR_INVALID_ARGUMENT;
   int rc = check_emicp_params(p);
   if (rc) return rc;
+  if (p->emicp_backward_layout < CESA_LAYOUT_AUTO || p->emicp_backward_layout > CESA_LAYOUT_RANGED)
+    return CESA_ERR_INVALID_ARGUMENT;
   const long nsteps = emicp_steps(p->sigma_p2, p->sigma_inf, p->sigma_factor);
   if (nsteps < 0) return CESA_ERR_INVALID_ARGUMENT;
   int dev = 0;
@@ -806,7 +808,7 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lock(g_mu);
   StreamCtx& C = ctx_for(dev, st);
-  cudaError_t e = C.ws.ensure(emicp_adjoint_ws_need(N, M, dev));
+  cudaError_t e = C.ws.ensure(emicp_adjoint_ws_need(N, M, dev, p->emicp_backward_layout));
   if (e != cudaSuccess) return map_cuda(e);
   const TapeLayout T = tape_layout(N, M, nsteps);
   const char* tb = static_cast<const char*>(tape);
@@ -825,6 +827,7 @@ int cesa_emicp_backward_device(int N, int M, const cesa_params* p, const void* t
   L.g_in = d_gRt0;
   L.d_status = d_status;
   L.timeout_ns = timeout_ns_of(p);
+  L.layout = p->emicp_backward_layout;
   C.last_kind = 1;
   C.last_trace_steps = 0;
   return map_cuda((cudaError_t)enqueue_emicp_adjoint(L, C.ws.p, C.ws.bytes, st));
@@ -1304,6 +1307,7 @@ const char* cesa_status_string(int status) {
     case CESA_ERR_OUT_OF_MEMORY: return "out of memory";
     case CESA_ERR_UNSUPPORTED: return "unsupported request";
     case CESA_ERR_NOALLOC_LIMIT: return "problem exceeds the 16 MiB fixed scratch of cesa_emicp_device_noalloc";
+    case CESA_ERR_INTERNAL: return "internal consistency check failed in a kernel (the access was skipped)";
     default: return "unknown status";
   }
 }

@@ -20,6 +20,7 @@ namespace cesa {
 constexpr int kStatusOk = 0;
 constexpr int kStatusTimeout = 3;      // == CESA_ERR_TIMEOUT
 constexpr int kStatusUnsupported = 6;  // == CESA_ERR_UNSUPPORTED (a launch shape the kernel cannot run)
+constexpr int kStatusInternal = 8;     // == CESA_ERR_INTERNAL (an index check failed; the access was skipped)
 
 constexpr float kLog2e = 1.4426950408889634f;
 

@@ -21,17 +21,19 @@
 //                                             transposed shared-memory sum, then
 //                                             over the warps; one partial per
 //                                             column block and row);
-//   3. the block that completes a row slice (split completion over the column
-//      blocks) sums the row partials in column-block order, adds
-//      dL/dy_r = R^T dL/dz_r + lambda_r gP + gQ^T u_r and writes the slice's
-//      record of sum dL/dz_r y_r^T (row-major, as R), sum dL/dz_r and, for rows
-//      on the C_r <= 1e-6 branch (lambda = 1, u = mean X), sum gu_r;
-//   4. after the grid barrier every block reduces the records (the upstream
-//      gradient of the previous step's pose) and adds, for its share of the
-//      columns, the row-slice partials of dL/dx_c in a fixed order.
+//   3. after a grid barrier every block completes a contiguous share of the
+//      rows (all blocks at once, no serial tail): it sums the row partials in
+//      column-block order, adds dL/dy_r = R^T dL/dz_r + lambda_r gP + gQ^T u_r
+//      and writes its record of sum dL/dz_r y_r^T (row-major, as R),
+//      sum dL/dz_r and, for rows on the C_r <= 1e-6 branch (lambda = 1,
+//      u = mean X), sum gu_r;
+//   4. after a second grid barrier every block reduces the records (the
+//      upstream gradient of the previous step's pose) and adds, for its share
+//      of the columns, the row-slice partials of dL/dx_c in a fixed order.
 // Per element: 6 (distance) + 1 (exponent) + 4 (ge) + 1 (w, with 1/s2 folded
 // into the row coefficients) + 3 (dz) + 6 (dx) FP32 ops + 1 MUFU, against
 // 12 + 1 in the forward, on packed pairs of rows (FFMA2/FADD2/FMUL2).
+#include "cesa.h"
 #include "cesa_kernels.h"
 #include "cesa_ops.cuh"
 #include "cesa_pose.h"
@@ -50,9 +52,24 @@ constexpr int kScrStride = 36;                    // floats per transpose row (3
 constexpr float kFar = 1e15f;                     // padding coordinate: its affinities are exactly 0
 
 // Units: nb column blocks x S row slices of len rows (even), slice-major.
+// Ranged (large clouds): tasks of (column block, chunk of kAdjRows rows) in
+// column-block-major order, block b taking the contiguous tasks
+// [T b / G, T (b + 1) / G), as in the forward's ranged sweeps; the dL/dx
+// partials of the j-th grid block covering column block cb go to slot
+// (cb, j), j < kmax (slots no block writes stay zero from the launch).
 struct AdjGeom {
   int nb, S, len, units;
+  int ranged, nch, kmax;
 };
+
+// The adjoint's ranged tasks in the sweep geometry that ranged_share reads.
+__host__ __device__ inline SweepGeom adj_tasks(const AdjGeom& g) {
+  SweepGeom t{};
+  t.nblk = g.nb;
+  t.nch = g.nch;
+  t.ranged = g.ranged;
+  return t;
+}
 
 struct EmAdjArgs {
   const float4* rows;  // Y' centred (M)
@@ -68,9 +85,8 @@ struct EmAdjArgs {
   float4* gY;             // [M]
   float* g_in;            // [12] dL/d(R, t) of the initial pose, caller frame
   float4* part_z;         // [nb][M]: dL/dz per column block
-  unsigned* cnt;          // [S] slice completion counters (monotonic)
-  df* rec;                // [2][S][16]
-  float4* part_x;         // [2][S][N]: dL/dx per row slice
+  df* rec;                // [2][grid][16]: per-block records of the row completion
+  float4* part_x;         // [2][S][N]: dL/dx per row slice; ranged: [2][nb][kmax][kAdjColBlk]
   Ctl* ctl;
   int* d_status;
   uint64_t timeout_ns;
@@ -148,7 +164,6 @@ struct AdjSmem {
   float scr[kWarps][kAdjVals][kScrStride];    // per-warp transpose of the row partials
   float wsum[3][kWarps][kAdjRows];            // per-warp row totals of a chunk
   df red[16 * kWarps];
-  unsigned flag;
 };
 
 // The record of one streamed row (one thread per row), in coordinates scaled
@@ -192,11 +207,13 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
   __shared__ float s_pose[13];  // the step's input pose and sigma_p2
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[16];
+  __shared__ RangedShare rsh;  // this block's share of the ranged tasks
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned G = gridDim.x;
   const AdjGeom& g = A.geo;
   if (tid == 0) {
+    rsh = ranged_share(adj_tasks(g), blockIdx.x, (int)G);
     // caller frame -> centred frame: t = t' + oX - R oY, so dL/dt' = dL/dt and
     // dL/dR' = dL/dR - dL/dt oY^T
     for (int i = 0; i < 3; ++i) {
@@ -209,7 +226,6 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
   bool ok = true;
   for (int k = A.nsteps - 1; k >= 0 && ok; --k) {
     const int par = k & 1;
-    const unsigned round = (unsigned)(A.nsteps - 1 - k);
     const float* rec = A.tape + (size_t)k * kEmTape;
     if (tid == 0) {
       float gRo[9], gto[3], coef[16];
@@ -228,12 +244,33 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
     const float inv_s2 = 1.f / s2;
     const float sc = sqrtf(kLog2e / (2.f * s2)), inv_sc = 1.f / sc;  // coordinate scale
     const float* rtape = A.row_tape + (size_t)k * A.M * 5;
-    df* recs = A.rec + (size_t)par * g.S * 16;
-    float4* px = A.part_x + (size_t)par * g.S * A.N;
+    df* recs = A.rec + (size_t)par * G * 16;
+    const size_t px_len = g.ranged ? (size_t)g.nb * g.kmax * kAdjColBlk : (size_t)g.S * A.N;
+    float4* px = A.part_x + (size_t)par * px_len;
 
-    for (int u = blockIdx.x; u < g.units; u += G) {
-      const int sl = u / g.nb, cb = u - sl * g.nb;
-      const int rb = sl * g.len, re = min(rb + g.len, A.M);
+    const int u_end = g.ranged ? rsh.o_last - rsh.o_first + 1 : g.units;
+    for (int u = g.ranged ? 0 : (int)blockIdx.x; u < u_end; u += g.ranged ? 1 : (int)G) {
+      // unit: column block cb, rows [rb, re); its dL/dx partials go to px_dst
+      int cb, rb, re;
+      float4* px_dst;
+      if (g.ranged) {  // segment u of this block's task run
+        cb = rsh.o_first + u;
+        const int c0 = u == 0 ? rsh.c_first : 0;
+        const int c1 = cb == rsh.o_last ? rsh.c_end : g.nch;
+        rb = c0 * kAdjRows;
+        re = min(c1 * kAdjRows, A.M);
+        const int j = u == 0 ? rsh.j_first : 0;
+        // the slot must exist: an inconsistent plan records an error and
+        // stores nothing (px_dst = nullptr) rather than writing past the array
+        px_dst = j < g.kmax && cb < g.nb ? px + ((size_t)cb * g.kmax + j) * kAdjColBlk : nullptr;
+        if (!px_dst && tid == 0) set_status(A.ctl, kStatusInternal, 104);
+      } else {
+        const int sl = u / g.nb;
+        cb = u - sl * g.nb;
+        rb = sl * g.len;
+        re = min(rb + g.len, A.M);
+        px_dst = px + (size_t)sl * A.N + (size_t)cb * kAdjColBlk;
+      }
       // owned columns, duplicated into both halves of a packed pair
       float2 xd[kAdjCols][3], gx[kAdjCols][3];
 #pragma unroll
@@ -316,18 +353,21 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
             col[5 * kScrStride] = gz2.y;
           }
           __syncwarp();
-          // lane v < kAdjVals: the sum over the 32 lanes of value v, in lane order
+          // lane v < kAdjVals: the sum over the 32 lanes of value v, a fixed
+          // pairwise tree on packed pairs (15 FADD2 + 1 FADD)
           if (lane < kAdjVals) {
             const float4* src = reinterpret_cast<const float4*>(&sm.scr[warp][lane][0]);
-            float sum = 0.f;
+            float2 t2[8];
 #pragma unroll
             for (int qq = 0; qq < 8; ++qq) {
               const float4 v4 = src[qq];
-              sum += v4.x;
-              sum += v4.y;
-              sum += v4.z;
-              sum += v4.w;
+              t2[qq] = __fadd2_rn(make_float2(v4.x, v4.y), make_float2(v4.z, v4.w));
             }
+#pragma unroll
+            for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+              for (int qq = 0; qq < w; ++qq) t2[qq] = __fadd2_rn(t2[qq], t2[qq + w]);
+            const float sum = t2[0].x + t2[0].y;
             const int q = lane / 6, comp = lane - 6 * q;
             const int row = 2 * (pb + q) + (comp >= 3 ? 1 : 0);
             sm.wsum[comp % 3][warp][row] = sum;
@@ -348,96 +388,103 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
           __stcg(A.part_z + (size_t)cb * A.M + r0 + tid, make_float4(gz[0], gz[1], gz[2], 0.f));
         }
       }
-      // this row slice's dL/dx of the owned columns
+      // this unit's dL/dx of the owned columns
 #pragma unroll
       for (int j = 0; j < kAdjCols; ++j) {
         const int c = cb * kAdjColBlk + j * kThreads + tid;
-        if (c < A.N)
-          __stcg(px + (size_t)sl * A.N + c,
+        if (c < A.N && px_dst)
+          __stcg(px_dst + j * kThreads + tid,
                  make_float4((gx[j][0].x + gx[j][0].y) * inv_sc, (gx[j][1].x + gx[j][1].y) * inv_sc,
                              (gx[j][2].x + gx[j][2].y) * inv_sc, 0.f));
-      }
-      // split completion of the row slice: the last of its nb units
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) {
-        const unsigned old = atom_acq_rel_add(A.cnt + sl, 1u);
-        sm.flag = (old == (round + 1u) * (unsigned)g.nb - 1u) ? 1u : 0u;
-      }
-      __syncthreads();
-      if (sm.flag) {
-        __threadfence();
-        df vv[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) vv[q] = df_make(0.f);
-        for (int r = rb + tid; r < re; r += kThreads) {
-          float totz[3] = {0.f, 0.f, 0.f};
-          int b = 0;
-          for (; b + 8 <= g.nb; b += 8) {  // 8 loads in flight, added in column-block order
-            float4 p[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) p[j] = __ldcg(A.part_z + (size_t)(b + j) * A.M + r);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              totz[0] += p[j].x;
-              totz[1] += p[j].y;
-              totz[2] += p[j].z;
-            }
-          }
-          for (; b < g.nb; ++b) {
-            const float4 p = __ldcg(A.part_z + (size_t)b * A.M + r);
-            totz[0] += p.x;
-            totz[1] += p.y;
-            totz[2] += p.z;
-          }
-          const float4 y = ld_cg(A.rows + r);
-          const float* rt = rtape + (size_t)r * 5;
-          const float C = rt[0], lam = rt[1];
-          const float uu[3] = {rt[2], rt[3], rt[4]};
-          const float yy[3] = {y.x, y.y, y.z};
-          // dL/dy = R^T dL/dz + lambda gP + gQ^T u
-          float gy[3];
-          for (int jj = 0; jj < 3; ++jj)
-            gy[jj] = R[jj] * totz[0] + R[3 + jj] * totz[1] + R[6 + jj] * totz[2] + lam * coef[4 + jj] +
-                     coef[7 + 3 * jj] * uu[0] + coef[8 + 3 * jj] * uu[1] + coef[9 + 3 * jj] * uu[2];
-          float4 o = A.gY[r];
-          o.x += gy[0];
-          o.y += gy[1];
-          o.z += gy[2];
-          A.gY[r] = o;
-          for (int i = 0; i < 3; ++i) {
-            for (int jj = 0; jj < 3; ++jj) df_add_prod(vv[3 * i + jj], totz[i], yy[jj]);  // dL/dR_ij, row-major
-            df_add(vv[9 + i], totz[i]);
-          }
-          if (!(C > 10e-7f)) {  // branch rows: u = mean X
-            for (int i = 0; i < 3; ++i)
-              df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
-          }
-        }
-        // the slice's 16 sums, through shared memory (scr and wsum are free here)
-        static_assert(sizeof(sm.scr) + sizeof(sm.wsum) >= sizeof(df) * 17 * kThreads, "moment scratch");
-        em_block_moments(vv, min(kThreads, re - rb), reinterpret_cast<df*>(&sm.scr[0][0][0]),
-                         recs + (size_t)sl * 16);
       }
     }
     if (!ok || !grid_sync(A.ctl, epoch, G, A.timeout_ns, 102)) {
       ok = false;
       break;
     }
+    // Rows completed, each block a contiguous share of them (all blocks in
+    // parallel, no serial tail): the column blocks' dL/dz partials summed in
+    // column-block order, dL/dy = R^T dL/dz + lambda_r gP + gQ^T u_r, and the
+    // block's record of sum dL/dz y^T (row-major, as R), sum dL/dz and, for
+    // rows on the C_r <= 1e-6 branch (lambda = 1, u = mean X), sum gu_r.
+    {
+      const int rpc = (A.M + (int)G - 1) / (int)G;
+      const int r0 = (int)blockIdx.x * rpc;
+      const int nrows = max(0, min(rpc, A.M - r0));
+      df vv[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) vv[q] = df_make(0.f);
+      for (int r = r0 + tid; r < r0 + nrows; r += kThreads) {
+        float totz[3] = {0.f, 0.f, 0.f};
+        int b = 0;
+        for (; b + 8 <= g.nb; b += 8) {  // 8 loads in flight, added in column-block order
+          float4 pz[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) pz[j] = __ldcg(A.part_z + (size_t)(b + j) * A.M + r);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            totz[0] += pz[j].x;
+            totz[1] += pz[j].y;
+            totz[2] += pz[j].z;
+          }
+        }
+        for (; b < g.nb; ++b) {
+          const float4 pz = __ldcg(A.part_z + (size_t)b * A.M + r);
+          totz[0] += pz.x;
+          totz[1] += pz.y;
+          totz[2] += pz.z;
+        }
+        const float4 y = ld_cg(A.rows + r);
+        const float* rt = rtape + (size_t)r * 5;
+        const float C = rt[0], lam = rt[1];
+        const float uu[3] = {rt[2], rt[3], rt[4]};
+        const float yy[3] = {y.x, y.y, y.z};
+        float gy[3];
+        for (int jj = 0; jj < 3; ++jj)
+          gy[jj] = R[jj] * totz[0] + R[3 + jj] * totz[1] + R[6 + jj] * totz[2] + lam * coef[4 + jj] +
+                   coef[7 + 3 * jj] * uu[0] + coef[8 + 3 * jj] * uu[1] + coef[9 + 3 * jj] * uu[2];
+        float4 o = A.gY[r];
+        o.x += gy[0];
+        o.y += gy[1];
+        o.z += gy[2];
+        A.gY[r] = o;
+        for (int i = 0; i < 3; ++i) {
+          for (int jj = 0; jj < 3; ++jj) df_add_prod(vv[3 * i + jj], totz[i], yy[jj]);  // dL/dR_ij, row-major
+          df_add(vv[9 + i], totz[i]);
+        }
+        if (!(C > 10e-7f)) {  // branch rows: u = mean X
+          for (int i = 0; i < 3; ++i)
+            df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
+        }
+      }
+      // the block's 16 sums, through shared memory (scr and wsum are free here)
+      static_assert(sizeof(sm.scr) + sizeof(sm.wsum) >= sizeof(df) * 17 * kThreads, "moment scratch");
+      em_block_moments(vv, min(kThreads, nrows), reinterpret_cast<df*>(&sm.scr[0][0][0]),
+                       recs + (size_t)blockIdx.x * 16);
+    }
+    if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 103)) {
+      ok = false;
+      break;
+    }
     // upstream gradient of the previous step's output pose, identical in every block
-    reduce_block_partials<16>(recs, g.S, s_red, s_tot);
+    reduce_block_partials<16>(recs, (int)G, s_red, s_tot);
     if (tid < 12) s_g[tid] = df_val(s_tot[tid]);
     __syncthreads();
     const float gxb[3] = {df_val(s_tot[12]) / (float)A.N, df_val(s_tot[13]) / (float)A.N,
                           df_val(s_tot[14]) / (float)A.N};
-    // dL/dx_c: this block's share of the columns, row-slice partials in order
+    // dL/dx_c: this block's share of the columns, the row-slice (ranged: the
+    // kmax slot) partials in order
     for (int c = blockIdx.x * kThreads + tid; c < A.N; c += G * kThreads) {
       float sx = gxb[0], sy = gxb[1], sz = gxb[2];
+      const int cbk = c / kAdjColBlk;
+      const float4* src = g.ranged ? px + (size_t)cbk * g.kmax * kAdjColBlk + (c - cbk * kAdjColBlk) : px + c;
+      const size_t stride = g.ranged ? (size_t)kAdjColBlk : (size_t)A.N;
+      const int np = g.ranged ? g.kmax : g.S;
       int b = 0;
-      for (; b + 16 <= g.S; b += 16) {  // 16 loads in flight, summed in order
+      for (; b + 16 <= np; b += 16) {  // 16 loads in flight, summed in order
         float4 p[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) p[j] = __ldcg(px + (size_t)(b + j) * A.N + c);
+        for (int j = 0; j < 16; ++j) p[j] = __ldcg(src + (size_t)(b + j) * stride);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           sx += p[j].x;
@@ -445,8 +492,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
           sz += p[j].z;
         }
       }
-      for (; b < g.S; ++b) {
-        const float4 p = __ldcg(px + (size_t)b * A.N + c);
+      for (; b < np; ++b) {
+        const float4 p = __ldcg(src + (size_t)b * stride);
         sx += p.x;
         sy += p.y;
         sz += p.z;
@@ -510,7 +557,7 @@ struct AdjPlan {
 // Column blocks of kAdjColBlk columns and row slices of an even number of rows,
 // as many slices as fill whole waves of the co-resident grid best (up to 4 waves;
 // at least 64 rows per slice).
-AdjPlan plan_adj(int N, int M, int device) {
+AdjPlan plan_adj(int N, int M, int device, int layout) {
   AdjPlan P;
   P.smem = sizeof(AdjSmem);
   const int limit = persistent_grid_limit(device, (const void*)emicp_adjoint_kernel, P.smem);
@@ -538,26 +585,45 @@ AdjPlan plan_adj(int N, int M, int device) {
   g.len += g.len & 1;
   g.S = (M + g.len - 1) / g.len;
   g.units = g.nb * g.S;
+  g.ranged = 0;
+  g.nch = (M + kAdjRows - 1) / kAdjRows;
+  g.kmax = 0;
   P.geo = g;
   P.grid = g.units < limit ? g.units : limit;
+  // AUTO: ranged tasks where their longest run (in 256-row chunks) is shorter
+  // than the slice plan's (its waves times the chunks of a slice).
+  const long T = (long)g.nb * g.nch;
+  const long per = (T + limit - 1) / limit;
+  const int waves = (g.units + limit - 1) / limit;
+  const bool ranged = layout == CESA_LAYOUT_RANGED ||
+                      (layout == CESA_LAYOUT_AUTO && T >= 8L * limit && (double)per < (double)waves * g.len / kAdjRows);
+  if (ranged) {
+    P.geo.ranged = 1;
+    P.geo.kmax = ranged_kmax(adj_tasks(P.geo), limit);  // tasks of kAdjRows rows: g.nch as set above
+    P.grid = limit;
+  }
   return P;
+}
+
+// float4s of the dL/dx partials, both step parities
+size_t part_x_len(const AdjGeom& g, int N) {
+  return g.ranged ? (size_t)2 * g.nb * g.kmax * kAdjColBlk : (size_t)2 * g.S * N;
 }
 
 }  // namespace
 
 // Workspace of the adjoint: control block and counters (cleared), gradient
 // accumulators gX, gY (cleared), split partials, records and column partials.
-size_t emicp_adjoint_ws_need(int N, int M, int device) {
-  const AdjPlan P = plan_adj(N, M, device);
+size_t emicp_adjoint_ws_need(int N, int M, int device, int layout) {
+  const AdjPlan P = plan_adj(N, M, device, layout);
   Carve c(nullptr);
   c.take<Ctl>(1);
-  c.take<unsigned>((size_t)P.geo.S);
   c.take<float4>((size_t)N);
   c.take<float4>((size_t)M);
   c.take<float>(12);
   c.take<float4>((size_t)P.geo.nb * M);
-  c.take<df>((size_t)2 * P.geo.S * 16);
-  c.take<float4>((size_t)2 * P.geo.S * N);
+  c.take<df>((size_t)2 * P.grid * 16);
+  c.take<float4>(part_x_len(P.geo, N));
   return c.off;
 }
 
@@ -565,19 +631,20 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return (int)e;
-  const AdjPlan P = plan_adj(L.N, L.M, device);
+  const AdjPlan P = plan_adj(L.N, L.M, device, L.layout);
   Carve c(ws);
   Ctl* ctl = c.take<Ctl>(1);
-  unsigned* cnt = c.take<unsigned>((size_t)P.geo.S);
   float4* gX = c.take<float4>((size_t)L.N);
   float4* gY = c.take<float4>((size_t)L.M);
   float* g_in = c.take<float>(12);
   const size_t zero_bytes = c.off;
   float4* part_z = c.take<float4>((size_t)P.geo.nb * L.M);
-  df* rec = c.take<df>((size_t)2 * P.geo.S * 16);
-  float4* part_x = c.take<float4>((size_t)2 * P.geo.S * L.N);
+  df* rec = c.take<df>((size_t)2 * P.grid * 16);
+  float4* part_x = c.take<float4>(part_x_len(P.geo, L.N));
   if (c.off > ws_bytes) return (int)cudaErrorInvalidValue;
   e = cudaMemsetAsync(ws, 0, zero_bytes, st);
+  // ranged dL/dx slots that no block writes must read as zero
+  if (e == cudaSuccess && P.geo.ranged) e = cudaMemsetAsync(part_x, 0, sizeof(float4) * part_x_len(P.geo, L.N), st);
   if (e != cudaSuccess) return (int)e;
   EmAdjArgs A;
   A.rows = L.rows;
@@ -594,7 +661,6 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   A.gY = gY;
   A.g_in = g_in;
   A.part_z = part_z;
-  A.cnt = cnt;
   A.rec = rec;
   A.part_x = part_x;
   A.ctl = ctl;

@@ -170,8 +170,9 @@ struct EmicpAdjointLaunch {
   float* g_in;            // device [12]: dL/dR0, dL/dt0 of the initial pose, caller frame
   int* d_status;
   uint64_t timeout_ns;
+  int layout;             // CESA_LAYOUT_*
 };
-size_t emicp_adjoint_ws_need(int N, int M, int device);
+size_t emicp_adjoint_ws_need(int N, int M, int device, int layout);
 int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes, cudaStream_t st);
 // The forward workspace's packed clouds and centring header (for the tape).
 void emicp_ws_views(void* ws, int N, int M, int device, CenterHdr** hdr, float4** rows, float4** cols);

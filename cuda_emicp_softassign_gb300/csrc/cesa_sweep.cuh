@@ -102,17 +102,24 @@ __host__ __forceinline__ bool ranged_pays(int nblk, int n_stream, int G) {
   return (long)nblk * nch >= 16L * G;
 }
 
-// Turns g into a ranged sweep over G blocks (host; requires ranged_pays).
-__host__ __forceinline__ void make_ranged(SweepGeom& g, int G) {
-  g.ranged = 1;
-  g.nch = (g.n_stream + kChunk - 1) / kChunk;
+// The most grid blocks covering one owned block of a ranged geometry with
+// g.nblk owned blocks of g.nch tasks each (host; g.nblk, g.nch >= 1).
+__host__ __forceinline__ int ranged_kmax(const SweepGeom& g, int G) {
   int kmax = 1;
   for (int o = 0; o < g.nblk; ++o) {
     const int lo = ranged_block_of(g, (long)o * g.nch, G);
     const int hi = ranged_block_of(g, (long)(o + 1) * g.nch - 1, G);
     kmax = hi - lo + 1 > kmax ? hi - lo + 1 : kmax;
   }
-  g.kmax = kmax;
+  return kmax;
+}
+
+// Turns g into a ranged sweep over G blocks, tasks of kChunk streamed points
+// (host; requires ranged_pays).
+__host__ __forceinline__ void make_ranged(SweepGeom& g, int G) {
+  g.ranged = 1;
+  g.nch = (g.n_stream + kChunk - 1) / kChunk;
+  g.kmax = ranged_kmax(g, G);
 }
 
 // Index of point i's first slot in a ranged partial array of one accumulator,
@@ -670,9 +677,13 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
       if (threadIdx.x < kBlockPts && i < g.n_own) {
         if (ranged) {  // slot (owned block, j): this block is the j-th to cover it
           const int j = sl == 0 ? rs->j_first : 0;
+          if (j < g.kmax) {
 #pragma unroll
-          for (int a = 0; a < NACC; ++a)
-            __stcg(part + (((size_t)a * g.nblk + blk) * g.kmax + j) * kBlockPts + threadIdx.x, tot[a]);
+            for (int a = 0; a < NACC; ++a)
+              __stcg(part + (((size_t)a * g.nblk + blk) * g.kmax + j) * kBlockPts + threadIdx.x, tot[a]);
+          } else {
+            set_status(ctl, kStatusInternal, where + 3);  // the plan's kmax is inconsistent
+          }
         } else {
 #pragma unroll
           for (int a = 0; a < NACC; ++a) __stcg(part + ((size_t)a * g.slices + sl) * part_ld + i, tot[a]);

@@ -32,6 +32,7 @@ extern "C" {
 #define CESA_ERR_OUT_OF_MEMORY 5    /* device or host allocation failed */
 #define CESA_ERR_UNSUPPORTED 6      /* the request is outside what this build supports */
 #define CESA_ERR_NOALLOC_LIMIT 7    /* too large for the fixed scratch of cesa_emicp_device_noalloc */
+#define CESA_ERR_INTERNAL 8         /* a kernel's own consistency check failed (a bug; the access was skipped) */
 
 /* cudaStream_t without including cuda_runtime.h (same underlying type). */
 typedef struct CUstream_st* cesa_stream_t;
@@ -42,6 +43,13 @@ typedef struct CUstream_st* cesa_stream_t;
 #define CESA_SINKHORN_MATERIALISED 2 /* affinity matrix stored once per inner iteration */
 #define CESA_SINKHORN_BANDED 3       /* matrix-free, one thread-block cluster per band of 64 rows
                                         (M <= 2048 and all bands resident; else the matrix-free form) */
+
+/* Work decomposition of the EM-ICP backward's sweep (cesa_params.emicp_backward_layout).
+   Every layout computes the same gradient; they differ in the summation order of
+   the partial sums (each deterministic) and in speed. */
+#define CESA_LAYOUT_AUTO 0    /* by size: ranged where its longest task run is the shorter */
+#define CESA_LAYOUT_SLICES 1  /* units of (1536 X columns, slice of Y rows) dealt round-robin */
+#define CESA_LAYOUT_RANGED 2  /* each block a contiguous run of (1536 columns, 256 rows) tasks */
 
 /*
  * Registration parameters. The first twelve fields mirror
@@ -71,7 +79,8 @@ typedef struct cesa_params {
   int timeout_ms;    /* limit of any device-side wait; 0 selects 10000 ms */
   int device;        /* CUDA device ordinal for the host-pointer entry points; -1 = current */
   int icp_search;    /* CESA_ICP_SEARCH_*: nearest-neighbour search of cesa_icp */
-  int reserved[4];
+  int emicp_backward_layout; /* CESA_LAYOUT_*: work decomposition of cesa_emicp_backward_device */
+  int reserved[3];
 } cesa_params;
 
 /* ICP nearest-neighbour search (cesa_params.icp_search). Both are exact and

@@ -8,7 +8,10 @@ Config 3's check runs on an N = M = 500 copy (surface views, 5% outliers,
 rotation up to 20 degrees). Loss = |R - R_true|_F^2 + |t - t_true|^2.
 Tolerance: each gradient block (dL/dX, dL/dY, dL/d se(3)) within 2e-3 of the
 reference relative to the block's largest entry; the forward pass runs in
-FP32 and the gradient accumulates 66 steps of FP32 round-off.
+FP32 and the gradient accumulates 66 steps of FP32 round-off. Every work
+decomposition of the backward (emicp_backward_layout: by size, units of
+slices, ranged task runs; at this size AUTO takes the slices, and the ranged
+layout leaves most blocks without a task) is checked.
 """
 import numpy as np
 import pytest
@@ -67,16 +70,19 @@ def test_reference_gradient_pinned(c3_small, reference, oracle):
         assert abs(fd - ad) <= 1e-5 * max(np.abs(gw).max(), np.abs(gv).max()), (k, fd, ad)
 
 
-def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, c3_small, reference):
+@pytest.mark.parametrize("layout", ["auto", "slices", "ranged"])
+def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, c3_small, reference, layout):
     from cuda_emicp_softassign_gb300.autograd import emicp_autograd, se3_gradient
     torch = torch_cuda
+    p = cesa.Params.default(emicp_backward_layout={"auto": cesa.LAYOUT_AUTO, "slices": cesa.LAYOUT_SLICES,
+                                                   "ranged": cesa.LAYOUT_RANGED}[layout])
     X, Y, Rt, tt = c3_small
     loss_ref, gX, gY, gw, gv, Rr, tr = reference
     Xd = torch.tensor(X, dtype=torch.float32, device="cuda", requires_grad=True)
     Yd = torch.tensor(Y, dtype=torch.float32, device="cuda", requires_grad=True)
     R0 = torch.eye(3, device="cuda", requires_grad=True)
     t0 = torch.zeros(3, device="cuda", requires_grad=True)
-    R, t = emicp_autograd(Xd, Yd, R0, t0)
+    R, t = emicp_autograd(Xd, Yd, R0, t0, p)
     # the forward equals the plain device entry point
     Rp, tp = cesa.emicp(X.astype(np.float32), Y.astype(np.float32))
     assert np.array_equal(R.detach().cpu().numpy().astype(np.float64), Rp)
