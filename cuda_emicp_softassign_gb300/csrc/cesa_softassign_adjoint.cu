@@ -88,7 +88,8 @@ __device__ __forceinline__ int own_index(int ob, int p, int l) {
   return ob * kOwnBlk + (2 * p + l) * kSwT + (int)threadIdx.x;
 }
 
-__device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, int ob, float2 (&q)[2][3]) {
+// The lane's owned points, posed if the side is, negated and scaled by sc.
+__device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, float sc, int ob, float2 (&q)[2][3]) {
 #pragma unroll
   for (int p = 0; p < 2; ++p) {
     float v[2][3];
@@ -97,9 +98,9 @@ __device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, i
       const int i = own_index(ob, p, l);
       float4 o = i < io.n_own ? io.own[i] : make_float4(0.f, 0.f, 0.f, 0.f);
       if (io.own_posed) o = posed(P, o);
-      v[l][0] = -o.x;
-      v[l][1] = -o.y;
-      v[l][2] = -o.z;
+      v[l][0] = -o.x * sc;
+      v[l][1] = -o.y * sc;
+      v[l][2] = -o.z * sc;
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) q[p][d] = make_float2(v[0][d], v[1][d]);
@@ -109,11 +110,14 @@ __device__ __forceinline__ void load_owned(const SweepIO& io, const Pose12& P, i
 // The per-update record copy carries T and alpha in otherwise unused slots.
 constexpr int kRecT = 60, kRecAlpha = 61;
 
-__device__ __forceinline__ void kernel_consts(float T, float alpha, float& nk, float& c0) {
-  // K = exp((alpha - d^2)/T)/sqrt(T) = 2^(c0 + nk d^2), as the forward kernels form it
+// K = exp((alpha - d^2)/T)/sqrt(T) = 2^(c0 + nk d^2) = wsc 2^-|sc x - sc y|^2
+// with sc = sqrt(-nk) and wsc = 2^c0, as the forward's matrix-free kernel forms
+// it: the sweeps see the clouds scaled by sc and fold wsc into one side's
+// weights, so an element needs no exponent op of its own.
+__device__ __forceinline__ void kernel_consts(float T, float alpha, float& sc, float& wsc) {
   const float kk = kLog2e / T;
-  nk = -kk;
-  c0 = fmaf(alpha, kk, -0.5f * log2f(T));
+  sc = sqrtf(kk);
+  wsc = exp2f(fmaf(alpha, kk, -0.5f * log2f(T)));
 }
 
 // Rank-1 terms of dL/dK: own side alpha, streamed side beta.
@@ -132,10 +136,10 @@ struct SweepSmem {
 // One tile of a K product: part[sl][m][i] = sum over slice sl of
 // K(own_i, str_j) w_m[j], m < NW, for the owned block ob (kSwT threads).
 template <int NW>
-__device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& P, float nk, float c0, const float* w,
+__device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& P, float sc, float wsc, const float* w,
                                                int ldw, float* part, int ob, int sl, SweepSmem& sm) {
   float2 q[2][3];
-  load_owned(io, P, ob, q);
+  load_owned(io, P, sc, ob, q);
   float2 acc[2][NW];
 #pragma unroll
   for (int p = 0; p < 2; ++p)
@@ -149,9 +153,9 @@ __device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& 
       const int j = j0 + threadIdx.x;
       float4 s = io.str[j];
       if (io.str_posed) s = posed(P, s);
-      s.w = w[j];
+      s = make_float4(s.x * sc, s.y * sc, s.z * sc, w[j] * wsc);
 #pragma unroll
-      for (int m = 1; m < NW; ++m) sm.w[m - 1][threadIdx.x] = w[(size_t)m * ldw + j];
+      for (int m = 1; m < NW; ++m) sm.w[m - 1][threadIdx.x] = w[(size_t)m * ldw + j] * wsc;
       sm.pt[threadIdx.x] = s;
     }
     __syncthreads();
@@ -164,7 +168,7 @@ __device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& 
       for (int m = 1; m < NW; ++m) wm[m] = sm.w[m - 1][j];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const float2 e = ex2_pair(__ffma2_rn(dist2_pair(q[p], s), dup2(nk), dup2(c0)));
+        const float2 e = ex2_neg_pair(dist2_pair(q[p], s));
 #pragma unroll
         for (int m = 0; m < NW; ++m) acc[p][m] = __ffma2_rn(e, dup2(wm[m]), acc[p][m]);
       }
@@ -183,10 +187,10 @@ __device__ __forceinline__ void sweep_sum_tile(const SweepIO& io, const Pose12& 
 
 // One tile of a gradient sweep: part[sl][d][i] = (2/T) sum over slice sl of
 // G_ij (s_j - o_i)_d with G_ij = K_ij sum_m own_m[i] str_m[j].
-__device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12& P, float nk, float c0, float T,
+__device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12& P, float sc, float wsc, float T,
                                                 const Terms& tm, float* part, int ob, int sl, SweepSmem& sm) {
   float2 q[2][3];
-  load_owned(io, P, ob, q);
+  load_owned(io, P, sc, ob, q);
   float2 al[2][kMaxTerms];
 #pragma unroll
   for (int p = 0; p < 2; ++p)
@@ -209,9 +213,9 @@ __device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12&
       const int j = j0 + threadIdx.x;
       float4 s = io.str[j];
       if (io.str_posed) s = posed(P, s);
-      sm.pt[threadIdx.x] = s;
+      sm.pt[threadIdx.x] = make_float4(s.x * sc, s.y * sc, s.z * sc, 0.f);
 #pragma unroll
-      for (int m = 0; m < kMaxTerms; ++m) sm.w[m][threadIdx.x] = m < tm.n ? tm.str[m][j] : 0.f;
+      for (int m = 0; m < kMaxTerms; ++m) sm.w[m][threadIdx.x] = m < tm.n ? tm.str[m][j] * wsc : 0.f;  // wsc folded in
     }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
@@ -227,7 +231,7 @@ __device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12&
         float2 d2 = __fmul2_rn(dx, dx);
         d2 = __ffma2_rn(dy, dy, d2);
         d2 = __ffma2_rn(dz, dz, d2);
-        const float2 e = ex2_pair(__ffma2_rn(d2, dup2(nk), dup2(c0)));
+        const float2 e = ex2_neg_pair(d2);
         float2 gs = __fmul2_rn(al[p][0], dup2(b[0]));
 #pragma unroll
         for (int m = 1; m < kMaxTerms; ++m) gs = __ffma2_rn(al[p][m], dup2(b[m]), gs);
@@ -238,7 +242,7 @@ __device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12&
       }
     }
   }
-  const float sc = 2.f / T;
+  const float f = 2.f / T / sc;  // the differences were sc times the true ones
 #pragma unroll
   for (int p = 0; p < 2; ++p)
 #pragma unroll
@@ -246,7 +250,7 @@ __device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12&
       const int i = own_index(ob, p, l);
       if (i < io.n_own)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) part[((size_t)sl * 3 + d) * io.n_own + i] = sc * (l ? g[p][d].y : g[p][d].x);
+        for (int d = 0; d < 3; ++d) part[((size_t)sl * 3 + d) * io.n_own + i] = f * (l ? g[p][d].y : g[p][d].x);
     }
 }
 
@@ -255,17 +259,17 @@ template <int NW>
 __global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, const float* w, int ldw,
                                                     float* part) {
   __shared__ SweepSmem sm;
-  float nk, c0;
-  kernel_consts(pose[kRecT], pose[kRecAlpha], nk, c0);
-  sweep_sum_tile<NW>(io, load_pose(pose), nk, c0, w, ldw, part, blockIdx.x, blockIdx.y, sm);
+  float sc, wsc;
+  kernel_consts(pose[kRecT], pose[kRecAlpha], sc, wsc);
+  sweep_sum_tile<NW>(io, load_pose(pose), sc, wsc, w, ldw, part, blockIdx.x, blockIdx.y, sm);
 }
 
-__global__ void __launch_bounds__(kSwT) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
+__global__ void __launch_bounds__(kSwT, 5) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
   __shared__ SweepSmem sm;
   const float T = pose[kRecT];
-  float nk, c0;
-  kernel_consts(T, pose[kRecAlpha], nk, c0);
-  sweep_grad_tile(io, load_pose(pose), nk, c0, T, tm, part, blockIdx.x, blockIdx.y, sm);
+  float sc, wsc;
+  kernel_consts(T, pose[kRecAlpha], sc, wsc);
+  sweep_grad_tile(io, load_pose(pose), sc, wsc, T, tm, part, blockIdx.x, blockIdx.y, sm);
 }
 
 // out[m][i] (+)= sum over slices of part[sl][m][i], in slice order.
@@ -777,8 +781,8 @@ __global__ void __launch_bounds__(kSwT, CESA_BWD_MIN_BLOCKS) softassign_bwd_kern
     A.cols = U.cols;
     A.fin = U.fin;
     const float T = U.T;
-    float nk, c0;
-    kernel_consts(T, B.alpha, nk, c0);
+    float sc, wsc;
+    kernel_consts(T, B.alpha, sc, wsc);
     const Pose12 P = load_pose(U.rec);
     // ---- Horn's adjoint (every block), then S's adjoint per row and h per column
     if (tid == 0) horn_adjoint_into(A, s_gpose, s_scal);
@@ -804,7 +808,7 @@ __global__ void __launch_bounds__(kSwT, CESA_BWD_MIN_BLOCKS) softassign_bwd_kern
     if (!sync(81)) break;
     // ---- gh = K^T wt4 (columns own, rows stream), slice partials
     for (int u = blockIdx.x; u < units_c; u += nblk)
-      sweep_sum_tile<4>(io_c, P, nk, c0, A.wt4, N, B.part_c, u % nob_c, u / nob_c, sm);
+      sweep_sum_tile<4>(io_c, P, sc, wsc, A.wt4, N, B.part_c, u % nob_c, u / nob_c, sm);
     if (!sync(82)) break;
     // ---- gh summed per (column, weight); the columns' share of dL/dYc
     {
@@ -839,14 +843,14 @@ __global__ void __launch_bounds__(kSwT, CESA_BWD_MIN_BLOCKS) softassign_bwd_kern
     for (int k = I1 - 1; k >= 0; --k) {
       // dL/da^{k+1} += K g(c^k): rows own, columns stream
       for (int u = blockIdx.x; u < units_r; u += nblk)
-        sweep_sum_tile<1>(io_r, P, nk, c0, A.gc + (size_t)k * M, M, B.part_r, u % nob_r, u / nob_r, sm);
+        sweep_sum_tile<1>(io_r, P, sc, wsc, A.gc + (size_t)k * M, M, B.part_r, u % nob_r, u / nob_r, sm);
       if (!sync(85)) break;
       for (int i = gtid; i < N; i += gstride) back_rowpass_sum(A, k, slice_sum16(B.part_r, io_r.S, N, i), i);
       if (!sync(86)) break;
       if (k == 0) break;
       // dL/db^k += K^T g(r^k), then the column pass k - 1 (b^0 = 1 is a constant)
       for (int u = blockIdx.x; u < units_c; u += nblk)
-        sweep_sum_tile<1>(io_c, P, nk, c0, A.gr + (size_t)k * N, N, B.part_c, u % nob_c, u / nob_c, sm);
+        sweep_sum_tile<1>(io_c, P, sc, wsc, A.gr + (size_t)k * N, N, B.part_c, u % nob_c, u / nob_c, sm);
       if (!sync(87)) break;
       for (int j = gtid; j < M; j += gstride) back_colpass_sum(A, k - 1, slice_sum16(B.part_c, io_c.S, M, j), j);
       if (!sync(88)) break;
@@ -883,9 +887,9 @@ __global__ void __launch_bounds__(kSwT, CESA_BWD_MIN_BLOCKS) softassign_bwd_kern
       }
       for (int u = blockIdx.x; u < units_r + units_c; u += nblk) {
         if (u < units_r)
-          sweep_grad_tile(io_r, P, nk, c0, T, tr, B.part_r, u % nob_r, u / nob_r, sm);
+          sweep_grad_tile(io_r, P, sc, wsc, T, tr, B.part_r, u % nob_r, u / nob_r, sm);
         else
-          sweep_grad_tile(io_c, P, nk, c0, T, tc, B.part_c, (u - units_r) % nob_c, (u - units_r) / nob_c, sm);
+          sweep_grad_tile(io_c, P, sc, wsc, T, tc, B.part_c, (u - units_r) % nob_c, (u - units_r) / nob_c, sm);
       }
       if (!sync(89)) break;
       const bool last = t0 + kMaxTerms >= nterms;
