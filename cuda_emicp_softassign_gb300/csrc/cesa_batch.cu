@@ -356,6 +356,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
       const float* m = reinterpret_cast<const float*>(&sm.raw2[cur.stage][kMetaSlot]);
       if (threadIdx.x < 32) meta[threadIdx.x] = m[threadIdx.x];
       elem = ops.elem(m);
+      const float sc = ops.scale(m);  // the phase's coordinate scale (both clouds)
       const float4* os = &sm.raw2[cur.stage][kOwnSlot];
       float p[kOwnPerLane][3];
 #pragma unroll
@@ -363,13 +364,13 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
         const int i = lane + 32 * j;
         const float4 o = (U.blk * kBlockPts + i < g.n_own) ? os[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         if (xform) {
-          p[j][0] = m[0] * o.x + m[1] * o.y + m[2] * o.z + m[9];
-          p[j][1] = m[3] * o.x + m[4] * o.y + m[5] * o.z + m[10];
-          p[j][2] = m[6] * o.x + m[7] * o.y + m[8] * o.z + m[11];
+          p[j][0] = (m[0] * o.x + m[1] * o.y + m[2] * o.z + m[9]) * sc;
+          p[j][1] = (m[3] * o.x + m[4] * o.y + m[5] * o.z + m[10]) * sc;
+          p[j][2] = (m[6] * o.x + m[7] * o.y + m[8] * o.z + m[11]) * sc;
         } else {
-          p[j][0] = o.x;
-          p[j][1] = o.y;
-          p[j][2] = o.z;
+          p[j][0] = o.x * sc;
+          p[j][1] = o.y * sc;
+          p[j][2] = o.z * sc;
         }
       }
       pack_owned(p, q);
@@ -393,44 +394,60 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
   return true;
 }
 
-// E-step: the streamed X' as loaded.
-__device__ __forceinline__ PrepOut prep_raw(SweepSmem& sm, int stage) { return PrepOut{sm.raw[stage], sm.raw[stage]}; }
+// Every phase sweeps both clouds scaled by its exponent's factor sc (owned
+// points when loaded, streamed ones in the prepare step), and the Softassign
+// phases fold 2^c0 (wsc) into the streamed weights, so that the elements are
+// EmicpElemScaled / SinkElemScaled / FinalElemScaled.
 
-// Streamed Y' posed by (R, t') = meta[0..11]: (R y' + t', w) with w from the
-// stage's weights, or 1.
-__device__ __forceinline__ PrepOut prep_posed(SweepSmem& sm, int stage, int len, const float* m, bool unit_weight) {
+// E-step: the streamed X' times sc.
+__device__ __forceinline__ PrepOut prep_scaled(SweepSmem& sm, int stage, int len, float sc) {
+  for (int c = threadIdx.x; c < len; c += kThreads) {
+    const float4 x = sm.raw[stage][c];
+    sm.prep[c] = make_float4(x.x * sc, x.y * sc, x.z * sc, 0.f);
+  }
+  __syncthreads();
+  return PrepOut{sm.prep, sm.prep};
+}
+
+// Streamed Y' posed by (R, t') = meta[0..11]: sc (R y' + t') and w wsc, with w
+// from the stage's weights, or 1.
+__device__ __forceinline__ PrepOut prep_posed(SweepSmem& sm, int stage, int len, const float* m, bool unit_weight,
+                                              float sc, float wsc) {
   const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
   for (int c = threadIdx.x; c < len; c += kThreads) {
     const float4 y = sm.raw[stage][c];
-    sm.prep[c] = make_float4(m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9], m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10],
-                             m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11], unit_weight ? 1.f : w[c]);
+    sm.prep[c] = make_float4((m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9]) * sc,
+                             (m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10]) * sc,
+                             (m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11]) * sc, (unit_weight ? 1.f : w[c]) * wsc);
   }
   __syncthreads();
   return PrepOut{sm.prep, sm.prep};
 }
 
-// Streamed X' for a column pass: (x', a_r) with a from the completed row pass.
-__device__ __forceinline__ PrepOut prep_weighted(SweepSmem& sm, int stage, int len) {
+// Streamed X' for a column pass: (sc x', a_r wsc) with a from the completed row pass.
+__device__ __forceinline__ PrepOut prep_weighted(SweepSmem& sm, int stage, int len, float sc, float wsc) {
   const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
   for (int c = threadIdx.x; c < len; c += kThreads) {
     const float4 x = sm.raw[stage][c];
-    sm.prep[c] = make_float4(x.x, x.y, x.z, w[c]);
+    sm.prep[c] = make_float4(x.x * sc, x.y * sc, x.z * sc, w[c] * wsc);
   }
   __syncthreads();
   return PrepOut{sm.prep, sm.prep};
 }
 
-// Streamed Y' for the final sweep: (R y' + t', b) and (g (y' - Yhat), b (cs - 1))
-// with g = b cs, from the completed last column pass; Yhat = meta[28..30].
-__device__ __forceinline__ PrepOut prep_final(SweepSmem& sm, int stage, int len, const float* m) {
+// Streamed Y' for the final sweep: (sc (R y' + t'), b wsc) and
+// (g (y' - Yhat), b (cs - 1) wsc) with g = b cs wsc, from the completed last
+// column pass; Yhat = meta[28..30].
+__device__ __forceinline__ PrepOut prep_final(SweepSmem& sm, int stage, int len, const float* m, float sc, float wsc) {
   const float* w = reinterpret_cast<const float*>(&sm.raw2[stage][0]);
   for (int c = threadIdx.x; c < len; c += kThreads) {
     const float4 y = sm.raw[stage][c];
     const float bn = w[c], csv = w[kChunk + c];
-    const float g = bn * csv;
-    sm.prep[c] = make_float4(m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9], m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10],
-                             m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11], bn);
-    sm.prep2[c] = make_float4(g * (y.x - m[28]), g * (y.y - m[29]), g * (y.z - m[30]), bn * (csv - 1.f));
+    const float g = bn * csv * wsc;
+    sm.prep[c] = make_float4((m[0] * y.x + m[1] * y.y + m[2] * y.z + m[9]) * sc,
+                             (m[3] * y.x + m[4] * y.y + m[5] * y.z + m[10]) * sc,
+                             (m[6] * y.x + m[7] * y.y + m[8] * y.z + m[11]) * sc, bn * wsc);
+    sm.prep2[c] = make_float4(g * (y.x - m[28]), g * (y.y - m[29]), g * (y.z - m[30]), bn * (csv - 1.f) * wsc);
   }
   __syncthreads();
   return PrepOut{sm.prep, sm.prep2};
@@ -497,34 +514,42 @@ struct BColFin {
 
 // Per-phase operations of a sweep unit. meta: state floats [0..15] (R, t',
 // sigma_p2 or T at [12]), centring header [16..31] (oX, oY, xmean, ymean).
+// e = exp(-d^2 / (2 sigma_p2)) = 2^-|sc x - sc z|^2, sc = sqrt(log2(e) / (2 sigma_p2))
+__device__ __forceinline__ float em_scale(float s2) { return sqrtf(kLog2e / (2.f * s2)); }
+
 struct EmOps {  // EM-ICP E-step
-  using Elem = EmicpElem;
+  using Elem = EmicpElemScaled;
   const BPair* P;
   df* scratch;
-  __device__ __forceinline__ Elem elem(const float* m) const { return EmicpElem{-kLog2e / (2.f * m[12])}; }
-  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int, const float*) const {
-    return prep_raw(sm, stage);
+  __device__ __forceinline__ Elem elem(const float*) const { return Elem{}; }
+  __device__ __forceinline__ float scale(const float* m) const { return em_scale(m[12]); }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
+    return prep_scaled(sm, stage, len, em_scale(m[12]));
   }
   __device__ __forceinline__ void fin(int blk, const float (&tot)[5], const float* m) const {
+    const float inv_sc = 1.f / em_scale(m[12]);  // the e x sums came out sc times too large
+    const float t5[5] = {tot[0], tot[1], tot[2] * inv_sc, tot[3] * inv_sc, tot[4] * inv_sc};
     const EmicpFin f{P->own0, P->M, expf(-P->d_02 / m[12]),  // src/emicp.cu:489
                      {m[24], m[25], m[26]}, nullptr, {m[16], m[17], m[18]}, scratch, P->rec};
-    f(blk, tot);
+    f(blk, t5);
   }
 };
 
-// K = exp((alpha - d^2)/T) / sqrt(T) = 2^(c0 + nk d^2)
-__device__ __forceinline__ SinkElem sink_elem(float alpha, float T) {
+// K = exp((alpha - d^2)/T) / sqrt(T) = 2^c0 2^-|sc x - sc y|^2, sc = sqrt(log2(e) / T)
+__device__ __forceinline__ float sa_scale(float T) { return sqrtf(kLog2e / T); }
+__device__ __forceinline__ float sa_wscale(float alpha, float T) {
   const float kk = kLog2e / T;
-  return SinkElem{-kk, fmaf(alpha, kk, -0.5f * log2f(T))};
+  return exp2f(fmaf(alpha, kk, -0.5f * log2f(T)));
 }
 
 struct RowOps {  // Sinkhorn row pass k
-  using Elem = SinkElem;
+  using Elem = SinkElemScaled;
   const BPair* P;
   bool first;
-  __device__ __forceinline__ Elem elem(const float* m) const { return sink_elem(P->alpha, m[12]); }
+  __device__ __forceinline__ Elem elem(const float*) const { return Elem{}; }
+  __device__ __forceinline__ float scale(const float* m) const { return sa_scale(m[12]); }
   __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
-    return prep_posed(sm, stage, len, m, first);
+    return prep_posed(sm, stage, len, m, first, sa_scale(m[12]), sa_wscale(P->alpha, m[12]));
   }
   __device__ __forceinline__ void fin(int blk, const float (&tot)[1], const float*) const {
     const BRowFin f{P->a, P->s, P->rs, P->N, first};
@@ -533,13 +558,14 @@ struct RowOps {  // Sinkhorn row pass k
 };
 
 struct ColOps {  // Sinkhorn column pass k
-  using Elem = SinkElem;
+  using Elem = SinkElemScaled;
   const BPair* P;
   bool first, last;
   df* scratch;
-  __device__ __forceinline__ Elem elem(const float* m) const { return sink_elem(P->alpha, m[12]); }
-  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float*) const {
-    return prep_weighted(sm, stage, len);
+  __device__ __forceinline__ Elem elem(const float*) const { return Elem{}; }
+  __device__ __forceinline__ float scale(const float* m) const { return sa_scale(m[12]); }
+  __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
+    return prep_weighted(sm, stage, len, sa_scale(m[12]), sa_wscale(P->alpha, m[12]));
   }
   __device__ __forceinline__ void fin(int blk, const float (&tot)[1], const float*) const {
     const BColFin f{P->b, P->u, P->cs, P->M, first, last, P->own1, scratch, P->rec + (size_t)P->g0.nblk * 32};
@@ -548,15 +574,13 @@ struct ColOps {  // Sinkhorn column pass k
 };
 
 struct FinOps {  // Softassign final sweep
-  using Elem = FinalElem;
+  using Elem = FinalElemScaled;
   const BPair* P;
   df* scratch;
-  __device__ __forceinline__ Elem elem(const float* m) const {
-    const SinkElem e = sink_elem(P->alpha, m[12]);
-    return FinalElem{e.nk, e.c0};
-  }
+  __device__ __forceinline__ Elem elem(const float*) const { return Elem{}; }
+  __device__ __forceinline__ float scale(const float* m) const { return sa_scale(m[12]); }
   __device__ __forceinline__ PrepOut prep(SweepSmem& sm, int stage, int len, const float* m) const {
-    return prep_final(sm, stage, len, m);
+    return prep_final(sm, stage, len, m, sa_scale(m[12]), sa_wscale(P->alpha, m[12]));
   }
   __device__ __forceinline__ void fin(int blk, const float (&tot)[5], const float*) const {
     const FinalFin f{P->own0, P->a, nullptr, P->N, scratch, P->rec};
