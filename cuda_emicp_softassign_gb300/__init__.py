@@ -30,6 +30,9 @@ CESA_ERR_INTERNAL = 8
 LAYOUT_AUTO = 0
 LAYOUT_SLICES = 1
 LAYOUT_RANGED = 2
+SA_BACKWARD_AUTO = 0
+SA_BACKWARD_PERSISTENT = 1
+SA_BACKWARD_LAUNCHES = 2
 SINKHORN_AUTO = 0
 SINKHORN_MATRIX_FREE = 1
 SINKHORN_MATERIALISED = 2
@@ -65,7 +68,8 @@ class Params(ctypes.Structure):
         ("sigma_factor", ctypes.c_float), ("d_02", ctypes.c_float),
         ("maxIteration", ctypes.c_int),
         ("sinkhorn_form", ctypes.c_int), ("timeout_ms", ctypes.c_int), ("device", ctypes.c_int),
-        ("icp_search", ctypes.c_int), ("emicp_backward_layout", ctypes.c_int), ("reserved", ctypes.c_int * 3),
+        ("icp_search", ctypes.c_int), ("emicp_backward_layout", ctypes.c_int),
+        ("softassign_backward_form", ctypes.c_int), ("reserved", ctypes.c_int * 2),
     ]
 
     @classmethod

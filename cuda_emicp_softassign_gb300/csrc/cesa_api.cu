@@ -895,6 +895,8 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
   if (N < 1 || M < 1 || !tape || !d_gRt || !d_gX || !d_gY || !d_gRt0) return CESA_ERR_INVALID_ARGUMENT;
   int rc = check_sa_params(p);
   if (rc) return rc;
+  if (p->softassign_backward_form < CESA_SA_BACKWARD_AUTO || p->softassign_backward_form > CESA_SA_BACKWARD_LAUNCHES)
+    return CESA_ERR_INVALID_ARGUMENT;
   const long nsteps = (long)p->JMAX * p->I0;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return CESA_ERR_NO_DEVICE;
@@ -950,8 +952,10 @@ int cesa_softassign_backward_device(int N, int M, const cesa_params* p, const vo
   // persistent kernel). The sequence also stands in where the persistent
   // kernel cannot launch.
   int r = (int)cudaErrorCooperativeLaunchTooLarge;
-  if ((double)N * (double)M <= kSaBwdPersistentMaxElems)
-    r = softassign_bwd_persistent(B, tab.data(), C.ws.p, C.ws.bytes, st, d_status, timeout_ns_of(p));
+  const int form = p->softassign_backward_form;
+  const bool persistent = form == CESA_SA_BACKWARD_PERSISTENT ||
+                          (form == CESA_SA_BACKWARD_AUTO && (double)N * (double)M <= kSaBwdPersistentMaxElems);
+  if (persistent) r = softassign_bwd_persistent(B, tab.data(), C.ws.p, C.ws.bytes, st, d_status, timeout_ns_of(p));
   if (r != (int)cudaErrorCooperativeLaunchTooLarge) return map_cuda((cudaError_t)r);
   cudaGetLastError();
   r = softassign_bwd_prepare(B, tab.data(), C.ws.p, C.ws.bytes, st);

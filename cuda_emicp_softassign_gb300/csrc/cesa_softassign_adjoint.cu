@@ -18,9 +18,13 @@
 // reverse. Each pass's adjoint is one K or K^T product (K recomputed, never
 // stored). dL/dK is a sum of 4 + 2 I1 rank-1 terms alpha_m beta_m^T:
 //   (g(V)_d, h_d) d = 0..2,  (g(rho), b^{I1}),  (a^{k+1}, g(c^k)),  (g(r^k), b^k)
-// so dL/dx and dL/dz come from two more recomputing sweeps (own rows, own
-// columns): dL/dx_i = (2/T) sum_j G_ij (z_j - x_i), G = K .* dL/dK, and
-// likewise for z. dL/dy = R^T dL/dz plus the direct terms of Yc and h;
+// so dL/dx and dL/dz come from recomputing G = K .* dL/dK once more:
+// dL/dx_i = (2/T) sum_j G_ij (z_j - x_i) and likewise for z. The per-update
+// launches do it in one sweep that owns the rows and also sums each streamed
+// column over its owned block (a transposed shared-memory sum); the
+// persistent backward runs two sweeps (own rows, own columns), which keep its
+// latency-bound small sizes free of the transposes. dL/dy = R^T dL/dz plus the
+// direct terms of Yc and h;
 // dL/dR, dL/dt of the input pose are sum dL/dz y^T and sum dL/dz.
 // V_i = sum_j K_ij h_j comes from the final sweep's sums rho = K b,
 // m = K (b (cs - 1)) and v = K (b cs (y' - Yhat)):
@@ -254,6 +258,138 @@ __device__ __forceinline__ void sweep_grad_tile(const SweepIO& io, const Pose12&
     }
 }
 
+// Shared memory of the combined gradient sweep's column sums.
+constexpr int kG2Batch = 8;  // streamed columns per warp transpose
+constexpr int kG2Stride = 36;
+struct __align__(16) Grad2Smem {
+  float scr[kSwT / 32][3 * kG2Batch][kG2Stride];  // per-warp transposes: (column, axis) x lane
+  float wsum[kSwT / 32][3][kTile];                // per-warp column sums of a tile
+};
+
+// One tile of the combined gradient sweep (owns rows, streams the posed
+// columns): the rows' partials exactly as sweep_grad_tile writes them, and
+// for every streamed column j the owned block's share of dL/dz_j,
+// (2/T) sum over its rows i of G_ij (x_i - z_j), into pcol[ob][d][j]. G is the
+// same product the columns-owned sweep forms (same terms, same order), so one
+// recomputation of K serves both sides. A column's per-lane sums (over the
+// lane's 4 rows) are summed over the 32 lanes by a per-warp transpose through
+// shared memory (a packed pairwise tree), then over the 4 warps in order.
+__device__ __forceinline__ void sweep_grad2_tile(const SweepIO& io, const Pose12& P, float sc, float wsc, float T,
+                                                 const Terms& tm, float* part, float* pcol, int ob, int sl,
+                                                 SweepSmem& sm, Grad2Smem& sg) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float2 q[2][3];
+  load_owned(io, P, sc, ob, q);
+  float2 al[2][kMaxTerms];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int m = 0; m < kMaxTerms; ++m) {
+      const int i0 = own_index(ob, p, 0), i1 = own_index(ob, p, 1);
+      al[p][m] = make_float2(m < tm.n && i0 < io.n_own ? tm.own[m][i0] : 0.f,
+                             m < tm.n && i1 < io.n_own ? tm.own[m][i1] : 0.f);
+    }
+  float2 g[2][3];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[p][d] = make_float2(0.f, 0.f);
+  const float fcol = -2.f / T / sc;  // the differences were sc (z_j - x_i)
+  const int jb = sl * io.len, je = min(jb + io.len, io.n_str);
+  for (int j0 = jb; j0 < je; j0 += kTile) {
+    const int n = min(kTile, je - j0);
+    __syncthreads();  // the previous tile's points, weights and column sums are consumed
+    if ((int)threadIdx.x < n) {
+      const int j = j0 + threadIdx.x;
+      float4 s = io.str[j];
+      if (io.str_posed) s = posed(P, s);
+      sm.pt[threadIdx.x] = make_float4(s.x * sc, s.y * sc, s.z * sc, 0.f);
+#pragma unroll
+      for (int m = 0; m < kMaxTerms; ++m) sm.w[m][threadIdx.x] = m < tm.n ? tm.str[m][j] * wsc : 0.f;  // wsc folded in
+    }
+    __syncthreads();
+    for (int jb8 = 0; jb8 < n; jb8 += kG2Batch) {
+#pragma unroll
+      for (int jj = 0; jj < kG2Batch; ++jj) {
+        const int j = jb8 + jj;
+        float cs0 = 0.f, cs1 = 0.f, cs2 = 0.f;
+        if (j < n) {  // uniform over the block
+          const float4 s = sm.pt[j];
+          float b[kMaxTerms];
+#pragma unroll
+          for (int m = 0; m < kMaxTerms; ++m) b[m] = sm.w[m][j];
+          float2 c0 = make_float2(0.f, 0.f), c1 = c0, c2 = c0;
+#pragma unroll
+          for (int p = 0; p < 2; ++p) {
+            const float2 dx = __fadd2_rn(dup2(s.x), q[p][0]);
+            const float2 dy = __fadd2_rn(dup2(s.y), q[p][1]);
+            const float2 dz = __fadd2_rn(dup2(s.z), q[p][2]);
+            float2 d2 = __fmul2_rn(dx, dx);
+            d2 = __ffma2_rn(dy, dy, d2);
+            d2 = __ffma2_rn(dz, dz, d2);
+            const float2 e = ex2_neg_pair(d2);
+            float2 gs = __fmul2_rn(al[p][0], dup2(b[0]));
+#pragma unroll
+            for (int m = 1; m < kMaxTerms; ++m) gs = __ffma2_rn(al[p][m], dup2(b[m]), gs);
+            const float2 G = __fmul2_rn(e, gs);
+            g[p][0] = __ffma2_rn(G, dx, g[p][0]);
+            g[p][1] = __ffma2_rn(G, dy, g[p][1]);
+            g[p][2] = __ffma2_rn(G, dz, g[p][2]);
+            c0 = __ffma2_rn(G, dx, c0);
+            c1 = __ffma2_rn(G, dy, c1);
+            c2 = __ffma2_rn(G, dz, c2);
+          }
+          cs0 = c0.x + c0.y;
+          cs1 = c1.x + c1.y;
+          cs2 = c2.x + c2.y;
+        }
+        float* col = &sg.scr[warp][3 * jj][lane];
+        col[0] = cs0;
+        col[kG2Stride] = cs1;
+        col[2 * kG2Stride] = cs2;
+      }
+      __syncwarp();
+      if (lane < 3 * kG2Batch) {  // value (column jj, axis d) summed over the 32 lanes
+        const float4* src = reinterpret_cast<const float4*>(&sg.scr[warp][lane][0]);
+        float2 t2[8];
+#pragma unroll
+        for (int qq = 0; qq < 8; ++qq) {
+          const float4 v4 = src[qq];
+          t2[qq] = __fadd2_rn(make_float2(v4.x, v4.y), make_float2(v4.z, v4.w));
+        }
+#pragma unroll
+        for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+          for (int qq = 0; qq < w; ++qq) t2[qq] = __fadd2_rn(t2[qq], t2[qq + w]);
+        const int jj = lane / 3, d = lane - 3 * jj;
+        sg.wsum[warp][d][jb8 + jj] = t2[0].x + t2[0].y;  // jb8 + jj < kTile
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < n) {  // the block's share of the tile's columns: the warps in order
+      const int j = j0 + threadIdx.x;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float v = sg.wsum[0][d][threadIdx.x];
+#pragma unroll
+        for (int w = 1; w < kSwT / 32; ++w) v += sg.wsum[w][d][threadIdx.x];
+        pcol[((size_t)ob * 3 + d) * io.n_str + j] = v * fcol;
+      }
+    }
+  }
+  const float f = 2.f / T / sc;  // the differences were sc times the true ones
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int i = own_index(ob, p, l);
+      if (i < io.n_own)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) part[((size_t)sl * 3 + d) * io.n_own + i] = f * (l ? g[p][d].y : g[p][d].x);
+    }
+}
+
 // The per-update launches' sweeps: one tile per block (x: owned block, y: slice).
 template <int NW>
 __global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pose, const float* w, int ldw,
@@ -264,13 +400,18 @@ __global__ void __launch_bounds__(kSwT) k_sweep_sum(SweepIO io, const float* pos
   sweep_sum_tile<NW>(io, load_pose(pose), sc, wsc, w, ldw, part, blockIdx.x, blockIdx.y, sm);
 }
 
-__global__ void __launch_bounds__(kSwT, 5) k_sweep_grad(SweepIO io, const float* pose, Terms tm, float* part) {
+// The combined gradient sweep (rows owned): row partials into part, the
+// owned blocks' column partials into pcol.
+__global__ void __launch_bounds__(kSwT, 4) k_sweep_grad2(SweepIO io, const float* pose, Terms tm, float* part,
+                                                          float* pcol) {
   __shared__ SweepSmem sm;
+  __shared__ Grad2Smem sg;
   const float T = pose[kRecT];
   float sc, wsc;
   kernel_consts(T, pose[kRecAlpha], sc, wsc);
-  sweep_grad_tile(io, load_pose(pose), sc, wsc, T, tm, part, blockIdx.x, blockIdx.y, sm);
+  sweep_grad2_tile(io, load_pose(pose), sc, wsc, T, tm, part, pcol, blockIdx.x, blockIdx.y, sm, sg);
 }
+
 
 // out[m][i] (+)= sum over slices of part[sl][m][i], in slice order.
 __global__ void k_reduce_slices(const float* __restrict__ part, int S, int NW, int n, float* out, int ldo, int acc) {
@@ -1042,8 +1183,9 @@ Layout carve(void* base, int N, int M, int I1, long nsteps, const Plan& P) {
   A.cols = L.cols;
   A.fin = L.fin;
   const size_t pr = (size_t)P.rows.S * 4 * N, pc = (size_t)P.cols.S * 4 * M;
+  const size_t pcol = (size_t)((N + kOwnBlk - 1) / kOwnBlk) * 3 * M;  // the combined gradient sweep's column partials
   L.part = c.take<float>(std::max(pr, pc));
-  L.part2 = c.take<float>(std::max(pr, pc));
+  L.part2 = c.take<float>(std::max(std::max(pr, pc), pcol));
   L.bpart = c.take<df>((size_t)3 * kBwdMaxGrid * kBwdPartNV);
   // last, so that every other offset is the same whatever the schedule's length
   L.tab = c.take<SaUpdate>((size_t)(nsteps > 0 ? nsteps : 1));
@@ -1069,10 +1211,14 @@ void sum_sweep(const SweepIO& io, const Layout& L, const float* w, int ldw, floa
   k_reduce_slices<<<dim3(blocks(io.n_own), NW), kGlue, 0, st>>>(L.part, io.S, NW, io.n_own, out, ldo, acc ? 1 : 0);
 }
 
-void grad_sweep(const SweepIO& io, const Layout& L, const Terms& tm, float* out, bool acc, cudaStream_t st) {
-  dim3 g((io.n_own + kOwnBlk - 1) / kOwnBlk, io.S);
-  k_sweep_grad<<<g, kSwT, 0, st>>>(io, L.rec, tm, L.part);
-  k_reduce_slices<<<dim3(blocks(io.n_own), 3), kGlue, 0, st>>>(L.part, io.S, 3, io.n_own, out, io.n_own, acc ? 1 : 0);
+// dL/dx (added to gx) and dL/dz (gz; added when acc) of a chunk of terms by
+// one rows-owned sweep: its slice partials, then the owned blocks' column
+// partials, each summed in order.
+void grad2_sweep(const SweepIO& io, const Layout& L, const Terms& tm, float* gx, float* gz, bool acc, cudaStream_t st) {
+  const int nob = (io.n_own + kOwnBlk - 1) / kOwnBlk;
+  k_sweep_grad2<<<dim3(nob, io.S), kSwT, 0, st>>>(io, L.rec, tm, L.part, L.part2);
+  k_reduce_slices<<<dim3(blocks(io.n_own), 3), kGlue, 0, st>>>(L.part, io.S, 3, io.n_own, gx, io.n_own, 1);
+  k_reduce_slices<<<dim3(blocks(io.n_str), 3), kGlue, 0, st>>>(L.part2, nob, 3, io.n_str, gz, io.n_str, acc ? 1 : 0);
 }
 
 struct Ctx {
@@ -1188,16 +1334,13 @@ int softassign_bwd_update(const SoftassignBackward& B, void* ws, size_t ws_bytes
     tb[4 + I1 + k] = k == 0 ? A.ones : L.cols + (size_t)(k - 1) * 4 * M;  // b^k
   }
   for (int t0 = 0; t0 < nterms; t0 += kMaxTerms) {
-    Terms tr{}, tcol{};
-    tr.n = tcol.n = std::min(kMaxTerms, nterms - t0);
+    Terms tr{};
+    tr.n = std::min(kMaxTerms, nterms - t0);
     for (int m = 0; m < tr.n; ++m) {
       tr.own[m] = ta[t0 + m];
       tr.str[m] = tb[t0 + m];
-      tcol.own[m] = tb[t0 + m];
-      tcol.str[m] = ta[t0 + m];
     }
-    grad_sweep(P.rows, L, tr, A.gX, true, st);
-    grad_sweep(P.cols, L, tcol, A.gZ, t0 > 0, st);
+    grad2_sweep(P.rows, L, tr, A.gX, A.gZ, t0 > 0, st);
   }
   k_pose_grad<<<1, ob, 0, st>>>(A);
   return (int)cudaGetLastError();

@@ -51,6 +51,12 @@ typedef struct CUstream_st* cesa_stream_t;
 #define CESA_LAYOUT_SLICES 1  /* units of (1536 X columns, slice of Y rows) dealt round-robin */
 #define CESA_LAYOUT_RANGED 2  /* each block a contiguous run of (1536 columns, 256 rows) tasks */
 
+/* Execution of the Softassign backward (cesa_params.softassign_backward_form).
+   Both compute the same gradient up to the summation order of partial sums. */
+#define CESA_SA_BACKWARD_AUTO 0       /* by size: persistent up to N x M = 16e6, else per-update launches */
+#define CESA_SA_BACKWARD_PERSISTENT 1 /* one cooperative launch over all updates (the launches where it cannot) */
+#define CESA_SA_BACKWARD_LAUNCHES 2   /* each update's launch sequence, replayed as a CUDA graph */
+
 /*
  * Registration parameters. The first twelve fields mirror
  * registrationParameters (src/3dregistration.h:39-57) in name, type, order and
@@ -79,8 +85,9 @@ typedef struct cesa_params {
   int timeout_ms;    /* limit of any device-side wait; 0 selects 10000 ms */
   int device;        /* CUDA device ordinal for the host-pointer entry points; -1 = current */
   int icp_search;    /* CESA_ICP_SEARCH_*: nearest-neighbour search of cesa_icp */
-  int emicp_backward_layout; /* CESA_LAYOUT_*: work decomposition of cesa_emicp_backward_device */
-  int reserved[3];
+  int emicp_backward_layout;   /* CESA_LAYOUT_*: work decomposition of cesa_emicp_backward_device */
+  int softassign_backward_form; /* CESA_SA_BACKWARD_*: execution of cesa_softassign_backward_device */
+  int reserved[2];
 } cesa_params;
 
 /* ICP nearest-neighbour search (cesa_params.icp_search). Both are exact and

@@ -53,7 +53,7 @@ def test_params_mirror_matches_c_layout(cesa):
 #define F(x) printf("%s %zu\n", #x, offsetof(cesa_params, x));
 int main(){ printf("size %zu\n", sizeof(cesa_params));
 F(JMAX)F(I0)F(I1)F(alpha)F(T_0)F(TFACTOR)F(moutlier)F(sigma_p2)F(sigma_inf)F(sigma_factor)F(d_02)
-F(maxIteration)F(sinkhorn_form)F(timeout_ms)F(device)F(icp_search)F(emicp_backward_layout)F(reserved)
+F(maxIteration)F(sinkhorn_form)F(timeout_ms)F(device)F(icp_search)F(emicp_backward_layout)F(softassign_backward_form)F(reserved)
 printf("report %zu\n", sizeof(cesa_report));
 printf("pair %zu\n", sizeof(cesa_pair));
 printf("pair_params %zu\n", offsetof(cesa_pair, params));

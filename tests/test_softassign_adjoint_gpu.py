@@ -12,7 +12,11 @@ shortened schedule (JMAX = 20, I0 = 5, I1 = 3, T from 100 down by 0.8 per
 step: 100 pose updates). Loss = |R - R_true|_F^2 + |t - t_true|^2.
 Tolerance: each gradient block (dL/dX, dL/dY, dL/d se(3)) within 5e-3 of the
 reference relative to the block's largest entry; the forward runs in FP32
-and the backward accumulates 100 updates of FP32 round-off.
+and the backward accumulates 100 updates of FP32 round-off. The backward's
+two executions (softassign_backward_form: one persistent launch, the default
+at these sizes, and each update's launch sequence, the default for large
+clouds, whose gradient sweep owns the rows and sums the columns by a
+transpose) are both checked.
 """
 import numpy as np
 import pytest
@@ -87,13 +91,17 @@ def test_reference_pinned(case, reference, oracle):
         assert abs(fd - ad) <= 1e-3 * max(np.abs(gw).max(), np.abs(gv).max(), 1e-12), (k, fd, ad)
 
 
-def _gpu_grads(cesa, torch, X, Y, R0, t0, Rt, tt, **sched):
+FORMS = ("persistent", "launches")
+
+
+def _gpu_grads(cesa, torch, X, Y, R0, t0, Rt, tt, form="persistent", **sched):
     from cuda_emicp_softassign_gb300.autograd import se3_gradient, softassign_autograd
     Xd = torch.tensor(X, dtype=torch.float32, device="cuda", requires_grad=True)
     Yd = torch.tensor(Y, dtype=torch.float32, device="cuda", requires_grad=True)
     R0d = torch.tensor(R0, dtype=torch.float32, device="cuda", requires_grad=True)
     t0d = torch.tensor(t0, dtype=torch.float32, device="cuda", requires_grad=True)
-    R, t = softassign_autograd(Xd, Yd, R0d, t0d, cesa.Params.default(**sched))
+    code = {"persistent": cesa.SA_BACKWARD_PERSISTENT, "launches": cesa.SA_BACKWARD_LAUNCHES}[form]
+    R, t = softassign_autograd(Xd, Yd, R0d, t0d, cesa.Params.default(softassign_backward_form=code, **sched))
     loss = ((R - torch.tensor(Rt, dtype=torch.float32, device="cuda")) ** 2).sum() + \
         ((t - torch.tensor(tt, dtype=torch.float32, device="cuda")) ** 2).sum()
     loss.backward()
@@ -110,17 +118,19 @@ def test_forward_equals_the_matrix_free_entry_point(cesa, torch_cuda, case):
     assert np.array_equal(R.astype(np.float64), Rp) and np.array_equal(t.astype(np.float64), tp)
 
 
-def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, case, reference):
+@pytest.mark.parametrize("form", FORMS)
+def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, case, reference, form):
     X, Y, Rt, tt = case
     _, gX, gY, gw, gv, _, _ = reference
-    _, _, gXd, gYd, g6 = _gpu_grads(cesa, torch_cuda, X, Y, np.eye(3), np.zeros(3), Rt, tt, **SCHED)
+    _, _, gXd, gYd, g6 = _gpu_grads(cesa, torch_cuda, X, Y, np.eye(3), np.zeros(3), Rt, tt, form=form, **SCHED)
     assert _rel(gXd, gX) < TOL, _rel(gXd, gX)
     assert _rel(gYd, gY) < TOL, _rel(gYd, gY)
     assert _rel(g6, np.r_[gw, gv]) < TOL, (g6, np.r_[gw, gv])
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("n,m,I1,seed", [(333, 157, 1, 2), (120, 517, 5, 3), (37, 1000, 3, 4)])
-def test_ragged_sizes_and_inner_counts(cesa, torch_cuda, n, m, I1, seed):
+def test_ragged_sizes_and_inner_counts(cesa, torch_cuda, n, m, I1, seed, form):
     """One annealing step of I0 = 2 updates from a perturbed pose: ragged tiles,
     I1 = 1 (one column pass) and I1 = 5 (14 rank-1 terms: two gradient groups)."""
     from oracle import torch_ref as T
@@ -128,7 +138,7 @@ def test_ragged_sizes_and_inner_counts(cesa, torch_cuda, n, m, I1, seed):
     sched = dict(JMAX=1, I0=2, I1=I1, T_0=0.05, TFACTOR=0.9)
     R0, t0 = _se3(np.array([0.05, -0.02, 0.03]), np.array([0.01, 0.0, -0.01]))
     _, gX, gY, gw, gv, _, _ = T.softassign_loss_grads(X, Y, R0, t0, Rt, tt, **sched)
-    _, _, gXd, gYd, g6 = _gpu_grads(cesa, torch_cuda, X, Y, R0, t0, Rt, tt, **sched)
+    _, _, gXd, gYd, g6 = _gpu_grads(cesa, torch_cuda, X, Y, R0, t0, Rt, tt, form=form, **sched)
     assert np.all(np.isfinite(gXd)) and np.all(np.isfinite(gYd)) and np.all(np.isfinite(g6))
     assert _rel(gXd, gX) < TOL, _rel(gXd, gX)
     assert _rel(gYd, gY) < TOL, _rel(gYd, gY)
