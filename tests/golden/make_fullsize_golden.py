@@ -21,10 +21,18 @@ GPU tests and bench.py compare against exactly the points the oracle saw:
   log-uniform in [500, 20000]; the even indices of workloads.batch_pairs(256,
   seed 0)). These store no points: each pair's SHA-256 over its float32 X and Y
   bytes, so the test can check that the generator reproduced them, the
-  oracle's pose, and (where the reference tree is present) the reference's own
-  emicp_cpu() pose -- on some pairs its FP32 arithmetic, like any FP32
-  arithmetic, crosses a discontinuity of the algorithm (a row sum near the
-  1e-6 threshold of src/emicp.cu:155-159) that the FP64 oracle does not.
+  oracle's pose, the oracle's FP32 port's pose and (where the reference tree
+  is present) the reference's own emicp_cpu() pose, and `spread`: the largest
+  rotation (degrees) and translation (x extent) deviation from the FP64 pose
+  over C4_ENSEMBLE runs of the FP32 port on X perturbed by one ulp per
+  coordinate (seeded; the FP64 pose itself moves by under 2e-6 degrees under
+  such perturbations, and the port lands where it does unperturbed: its
+  deviation is a bias of its evaluation order). On about 40% of these pairs
+  FP32 computations of the same algorithm land apart (up to 175 degrees). As sigma^2 shrinks towards 1e-5 the weight exp(-d^2 / sigma^2)
+  multiplies the FP32 rounding of d^2 (about 1e-7 on unit-cube coordinates) by
+  d^2 / sigma^2, 10^2 to 10^3, so each FP32 evaluation order drifts from the
+  FP64 trajectory its own way, step after step (pair 250: 1e-5 degrees after
+  the first step, 3e-4 at sigma^2 = 8e-4, 0.7 at the end).
 """
 import hashlib
 import os
@@ -40,6 +48,7 @@ from cuda_emicp_softassign_gb300 import workloads as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 EMICP = dict(sigma_p2=0.01, sigma_inf=1e-5, sigma_factor=0.9, d_02=0.01)
+C4_ENSEMBLE = 4  # perturbed FP32 runs per config-4 pair
 C5_SCHED = dict(JMAX=2, I0=5, I1=3, alpha=3.0, T_0=100.0, TFACTOR=0.95)
 
 
@@ -88,15 +97,30 @@ def make_c2():
                         sha=np.array(pair_sha(X, Y)))
 
 
+def fp32_spread(X, Y, R, t, seed):
+    """Largest deviation of FP32 port runs on one-ulp perturbations of X from
+    the FP64 pose (R, t): (degrees, x extent)."""
+    rng = np.random.default_rng(seed)
+    ext = float(np.ptp(np.asarray(X, np.float64), 0).max())
+    dr = dt = 0.0
+    for _ in range(C4_ENSEMBLE):
+        Xp = np.asarray(X, np.float32) * (1 + rng.choice([-1, 0, 1], size=X.shape).astype(np.float32)
+                                          * np.float32(6e-8))
+        Re, te, _ = O.emicp(Xp.astype(np.float64), Y, precision="f32", trace=False, **EMICP)
+        dr = max(dr, W.rotation_error_deg(Re, R))
+        dt = max(dt, float(np.abs(te - t).max()) / ext)
+    return dr, dt
+
+
 def make_c4(with_reference=True):
-    idx, sha, N, M, Rs, ts, Rps, Rrs, trs = [], [], [], [], [], [], [], [], []
+    idx, sha, N, M, Rs, ts, Rps, tps, Rrs, trs, spr = [], [], [], [], [], [], [], [], [], [], []
     use_ref = with_reference and O.ref() is not None
     t0 = time.time()
     for k, (kind, X, Y, _, _) in enumerate(W.batch_pairs(count=256, seed=0)):
         if kind != "emicp":
             continue
         R, t, _ = O.emicp(X, Y, trace=False, **EMICP)
-        Rp, _, _ = O.emicp(X, Y, precision="f32", trace=False, **EMICP)
+        Rp, tp, _ = O.emicp(X, Y, precision="f32", trace=False, **EMICP)
         if use_ref:
             Rr, tr_ = O.ref_emicp_cpu(X, Y, **EMICP)
             Rrs.append(Rr)
@@ -108,10 +132,13 @@ def make_c4(with_reference=True):
         Rs.append(R)
         ts.append(t)
         Rps.append(Rp)
+        tps.append(tp)
+        spr.append(fp32_spread(X, Y, R, t, seed=1000 + k))
     print("c4 oracle f64: %d EM-ICP pairs, %.0f s" % (len(idx), time.time() - t0), flush=True)
     extra = dict(ref_R=np.array(Rrs), ref_t=np.array(trs)) if use_ref else {}
     np.savez_compressed(os.path.join(HERE, "c4_emicp_pairs.npz"), index=np.array(idx), sha=np.array(sha),
-                        N=np.array(N), M=np.array(M), R=np.array(Rs), t=np.array(ts), port_R=np.array(Rps), **extra)
+                        N=np.array(N), M=np.array(M), R=np.array(Rs), t=np.array(ts), port_R=np.array(Rps),
+                        port_t=np.array(tps), spread=np.array(spr), **extra)
 
 
 def main():
