@@ -148,6 +148,15 @@ def test_invalid_arguments_are_rejected(cesa):
         cesa.CESA_ERR_INVALID_ARGUMENT
     assert L.cesa_emicp_backward_device(0, 5, ctypes.byref(p), None, None, None, None, None, None, None) == \
         cesa.CESA_ERR_INVALID_ARGUMENT
+    # out-of-range execution controls (the pointers are checked for NULL only, never read)
+    d = ptr(X)
+    bad = cesa.Params.default(emicp_backward_layout=cesa.LAYOUT_RANGED + 1)
+    assert L.cesa_emicp_backward_device(5, 5, ctypes.byref(bad), d, d, d, d, d, None, None) == \
+        cesa.CESA_ERR_INVALID_ARGUMENT
+    bad = cesa.Params.default(softassign_backward_form=-1)
+    assert L.cesa_softassign_backward_device(5, 5, ctypes.byref(bad), d, d, d, d, d, None, None) == \
+        cesa.CESA_ERR_INVALID_ARGUMENT
+    assert cesa.status_string(cesa.CESA_ERR_INTERNAL).startswith("internal consistency check failed")
 
 
 def test_tape_sizes_grow_with_the_schedule(cesa):
