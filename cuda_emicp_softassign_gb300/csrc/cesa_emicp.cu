@@ -15,7 +15,9 @@
 //   C_r = sum e^2 + outlier,  lambda_r = sum e / sqrt(C_r),  lambda_r X'_r = sum e x / sqrt(C_r).
 // Per element that is 3 FADD (direct differences), FMUL + 2 FFMA (d^2),
 // FMUL (scale), 1 MUFU ex2, and FFMA + FADD + 3 FFMA (accumulators): 12 FP32
-// pipe ops + 1 MUFU op.
+// pipe ops + 1 MUFU op. Large clouds take the ranged sweep on clouds scaled by
+// sqrt(log2(e) / (2 sigma_p2)) (a scaled copy of X' per step), which drops the
+// scale multiply: 11 FP32 ops.
 //
 // Coordinates are centred on the device (FP32 offsets oX, oY) before the
 // loop. EM-ICP's S is translation invariant, so only Xc, Yc and t are shifted

@@ -19,6 +19,11 @@
 //
 // Units are assigned round-robin to the blocks of the persistent grid. The
 // host picks S so that the unit count is close to a multiple of the grid size.
+// Large clouds take the ranged decomposition instead (SweepGeom::ranged): each
+// block a contiguous run of (owned block, chunk) tasks, the same work to one
+// chunk, its deferred partials in per-(owned block, covering block) slots.
+// A prepare step that copies its chunk into a buffer of its own can be
+// double-buffered (prep_double_buffered): one block barrier per chunk.
 #pragma once
 #include <type_traits>
 
