@@ -378,7 +378,7 @@ __device__ bool run_sweep_unit(SweepSmem& sm, Ring& rg, const UnitRef& U, bool x
     const PrepOut pb = ops.prep(sm, cur.stage, len, meta);
     const float4* __restrict__ bufA = pb.a;
     const float4* __restrict__ bufB = pb.b;
-#pragma unroll 2
+#pragma unroll 8  // independent element chains (as the single-pair sweeps)
     for (int c = warp; c < len; c += kWarps) {
       const float4 a = bufA[c];
       const float4 b = bufB[c];

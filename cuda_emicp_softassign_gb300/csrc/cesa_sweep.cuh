@@ -655,7 +655,9 @@ __device__ __forceinline__ bool sweep_units(SweepSmem& sm, Pipe& pipe, const Swe
       }
       const float4* __restrict__ bufA = pb.a;
       const float4* __restrict__ bufB = pb.b;
-#pragma unroll 2
+// 8 streamed points per iteration: independent element chains for the
+      // scheduler (measured: C3 +7%, C5 +7%, the batch +8% over 2; 16 adds nothing)
+#pragma unroll 8
       for (int c = warp; c < cur_len; c += kWarps) {
         const float4 a = bufA[c];
         const float4 b = bufB[c];
