@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 2) icp_kernel(const IcpArgs A) {
         __syncthreads();
         for (int k = tid; k < n; k += kThreads) s_x[k] = ld_cg(A.cols + j0 + k);
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 8  // independent element chains (exhaustive search 58.5% -> 63.0% of FP32 over 4)
         for (int j = 0; j < n; ++j) {
           const float4 s = s_x[j];
 #pragma unroll
