@@ -114,7 +114,7 @@ template <int NACC, bool kStore>
 __device__ __forceinline__ void band_row_sweep(float* K, const float2 (&q)[3], float nk, float cK, const float4* sw,
                                                const float4* h, int len, float2 (&acc)[NACC]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll 2
+#pragma unroll 8  // independent element chains (C2 76.1 -> 77.3 reg/s over 2)
   for (int c = warp; c < len; c += kWarps) {
     const float4 y = sw[c];
     float2 e;
@@ -141,7 +141,7 @@ __device__ __forceinline__ void band_row_sweep(float* K, const float2 (&q)[3], f
 __device__ __forceinline__ void band_col_sweep(const float* K, const float4* sx, int len,
                                                float2 (&acc)[kColPairs][1]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll 2
+#pragma unroll 8
   for (int r = warp; r < len; r += kWarps) {
     const float a = sx[r].w;
 #pragma unroll
