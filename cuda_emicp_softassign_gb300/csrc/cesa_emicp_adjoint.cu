@@ -18,9 +18,11 @@
 //        dL/dx_c += e gB_r - w (x_c - z_r)   (per column, in registers)
 //        dL/dz_r += w (x_c - z_r)            (per row: summed over the lane's
 //                                             columns, then over the lanes by a
-//                                             transposed shared-memory sum, then
-//                                             over the warps; one partial per
-//                                             column block and row);
+//                                             ring of shuffles (each lane adds
+//                                             its columns to the sum it receives
+//                                             and passes it on), then over the
+//                                             warps; one partial per column
+//                                             block and row);
 //   3. after a grid barrier every block completes a contiguous share of the
 //      rows (all blocks at once, no serial tail): it sums the row partials in
 //      column-block order, adds dL/dy_r = R^T dL/dz_r + lambda_r gP + gQ^T u_r
@@ -30,9 +32,12 @@
 //   4. after a second grid barrier every block reduces the records (the
 //      upstream gradient of the previous step's pose) and adds, for its share
 //      of the columns, the row-slice partials of dL/dx_c in a fixed order.
-// Per element: 6 (distance) + 1 (exponent) + 4 (ge) + 1 (w, with 1/s2 folded
-// into the row coefficients) + 3 (dz) + 6 (dx) FP32 ops + 1 MUFU, against
-// 12 + 1 in the forward, on packed pairs of rows (FFMA2/FADD2/FMUL2).
+// Per element: 6 (distance) + 4 (ge, with 1/s2 folded into the row
+// coefficients) + 3 (t = gB - ge (x - z) / s2) + 3 (dx += e t) + 3 (dz += e t)
+// FP32 ops + 1 MUFU, against 12 + 1 in the forward, on packed pairs of rows
+// (FFMA2/FADD2/FMUL2). The row sums carry e gB, which sums to gB A_r =
+// gu_r lambda_r (A_r = sum_c e, lambda_r = A_r C_r^-1/2 from the tape) and is
+// subtracted once per row at its completion.
 #include "cesa.h"
 #include "cesa_kernels.h"
 #include "cesa_ops.cuh"
@@ -46,10 +51,15 @@ constexpr int kAdjCols = 6;                       // owned X columns per lane
 constexpr int kAdjColBlk = kThreads * kAdjCols;   // owned columns per unit
 constexpr int kAdjRows = kThreads;                // streamed Y rows per chunk (one record per thread)
 constexpr int kAdjRP = kAdjRows / 2;              // row pairs per chunk
-constexpr int kAdjBatch = 4;                      // row pairs per warp transpose-sum
-constexpr int kAdjVals = kAdjBatch * 6;           // values per transpose-sum (2 rows x 3 axes per pair)
-constexpr int kScrStride = 36;                    // floats per transpose row (32 lanes + pad)
-constexpr float kFar = 1e15f;                     // padding coordinate: its affinities are exactly 0
+constexpr int kAdjGroups = kAdjRP / 32;           // groups of 32 row pairs (one per lane) per chunk
+constexpr int kAdjRecStride = 14;                 // float2 per row-pair record (11 used; 112 bytes, so
+                                                  // 8 lanes reading 8 consecutive records hit 32 banks)
+constexpr float kFar = 1e15f;                     // padding row coordinate: its affinities are exactly 0
+// Padding column coordinate, already scaled: its squared distance to any row
+// (|z'| far below 2^26) is above 2^50, so its affinity is exactly 0, and its
+// term ge (x - z) + gB stays finite (for row coefficients below 2^70), so that
+// e times it is 0 and not 0 * inf.
+constexpr float kPadScaled = 67108864.f;          // 2^26
 
 // Units: nb column blocks x S row slices of len rows (even), slice-major.
 // Ranged (large clouds): tasks of (column block, chunk of kAdjRows rows) in
@@ -160,9 +170,8 @@ __device__ __forceinline__ RowCoef row_coef(const float4 y, bool valid, const fl
 }
 
 struct AdjSmem {
-  float2 rec[kAdjRP][12];                     // row-pair records (11 float2 used)
-  float scr[kWarps][kAdjVals][kScrStride];    // per-warp transpose of the row partials
-  float wsum[3][kWarps][kAdjRows];            // per-warp row totals of a chunk
+  float2 rec[2][kAdjRP][kAdjRecStride];       // row-pair records, two chunks
+  float wsum[2][3][kWarps][kAdjRows];         // per-warp row totals, two chunks
   df red[16 * kWarps];
 };
 
@@ -172,7 +181,7 @@ struct AdjSmem {
 // the other row of its pair. (-gB/s2 multiplies the unscaled x = x'/sc; gB sc
 // and the scaled differences make the sweep's dL/dx and dL/dz sc times the
 // true ones, which the unit divides out once.)
-__device__ __forceinline__ void build_row_record(AdjSmem& sm, int i, bool valid, float4 y, const float (&rt)[5],
+__device__ __forceinline__ void build_row_record(AdjSmem& sm, int buf, int i, bool valid, float4 y, const float (&rt)[5],
                                                  const float* R, const float* t, const float* coef, float inv_s2,
                                                  float sc, float inv_sc) {
   float v[11];
@@ -194,9 +203,26 @@ __device__ __forceinline__ void build_row_record(AdjSmem& sm, int i, bool valid,
 #pragma unroll
     for (int k = 3; k < 11; ++k) v[k] = 0.f;
   }
-  float* dst = reinterpret_cast<float*>(&sm.rec[i >> 1][0]) + (i & 1);
+  float* dst = reinterpret_cast<float*>(&sm.rec[buf][i >> 1][0]) + (i & 1);
 #pragma unroll
   for (int k = 0; k < 11; ++k) dst[2 * k] = v[k];
+}
+
+// dL/dz of row r (of a chunk ending before row `end`) from one column block:
+// the warps' row totals in warp order, unscaled, stored to the block's slot
+__device__ __forceinline__ void complete_chunk_rows(const AdjSmem& sm, int buf, int r, int end, int cb, float inv_sc,
+                                                    const EmAdjArgs& A) {
+  if (r >= end) return;
+  const int i = threadIdx.x;
+  float gz[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float v = sm.wsum[buf][a][0][i];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) v += sm.wsum[buf][a][w][i];
+    gz[a] = -v * inv_sc;
+  }
+  __stcg(A.part_z + (size_t)cb * A.M + r, make_float4(gz[0], gz[1], gz[2], 0.f));
 }
 
 __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjArgs A) {
@@ -276,10 +302,10 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
 #pragma unroll
       for (int j = 0; j < kAdjCols; ++j) {
         const int c = cb * kAdjColBlk + j * kThreads + tid;
-        const float4 x = c < A.N ? ld_cg(A.cols + c) : make_float4(kFar, kFar, kFar, 0.f);
-        xd[j][0] = dup2(x.x * sc);
-        xd[j][1] = dup2(x.y * sc);
-        xd[j][2] = dup2(x.z * sc);
+        const float4 x = c < A.N ? ld_cg(A.cols + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+        xd[j][0] = dup2(c < A.N ? x.x * sc : kPadScaled);
+        xd[j][1] = dup2(c < A.N ? x.y * sc : kPadScaled);
+        xd[j][2] = dup2(c < A.N ? x.z * sc : kPadScaled);
 #pragma unroll
         for (int a = 0; a < 3; ++a) gx[j][a] = make_float2(0.f, 0.f);
       }
@@ -291,15 +317,19 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
 #pragma unroll
         for (int q = 0; q < 5; ++q) rtn[q] = __ldcg(rtape + (size_t)(rb + tid) * 5 + q);
       }
-      // Two barriers per chunk: the record build of chunk n + 1 touches only
-      // rec, which every warp has finished reading at the barrier after the
-      // sweep of chunk n, and the sweep of chunk n + 1 (which writes wsum)
-      // starts only after the barrier that follows that build, by which time
-      // every thread has consumed wsum of chunk n.
+      // One barrier per chunk, records and row totals double-buffered: the
+      // build of chunk n writes rec[n & 1], last read by the sweep of chunk
+      // n - 2, which every warp finished before the barrier of chunk n - 1;
+      // the sweep of chunk n writes wsum[n & 1], last read by the completion
+      // of chunk n - 2, which every thread did before that same barrier; the
+      // completion of chunk n - 1 reads wsum[(n - 1) & 1] after the barrier of
+      // chunk n, by which time every warp has finished that sweep.
       __syncthreads();  // the previous unit's shared-memory use is over
-      for (int r0 = rb; r0 < re; r0 += kAdjRows) {
-        build_row_record(sm, tid, r0 + tid < re, yn, rtn, R, t, coef, inv_s2, sc, inv_sc);
+      int buf = 0;
+      for (int r0 = rb; r0 < re; r0 += kAdjRows, buf ^= 1) {
+        build_row_record(sm, buf, tid, r0 + tid < re, yn, rtn, R, t, coef, inv_s2, sc, inv_sc);
         __syncthreads();
+        if (r0 > rb) complete_chunk_rows(sm, buf ^ 1, r0 - kAdjRows + tid, r0, cb, inv_sc, A);
         // the next chunk's row, in flight during this chunk's sweep
         const int rn = r0 + kAdjRows + tid;
         if (rn < re) {
@@ -307,11 +337,34 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
 #pragma unroll
           for (int q = 0; q < 5; ++q) rtn[q] = __ldcg(rtape + (size_t)rn * 5 + q);
         }
-        const int npairs = min(kAdjRP, (re - r0 + 1) >> 1);
-        for (int pb = 0; pb < npairs; pb += kAdjBatch) {
+        // The warp's 32 lanes pass each row pair's dL/dz sum round a ring: at
+        // step s lane l takes pair (l - s) mod 32 of every group of 32 pairs,
+        // adds its columns' terms to the sum it received from lane l - 1 and
+        // hands it on; after 32 steps lane l holds the warp's whole sum for
+        // pair (l + 1) mod 32 of each group (fixed order: lane p first).
+        const int ng = (min(kAdjRP, (re - r0 + 1) >> 1) + 31) >> 5;  // groups holding a valid pair
+        float2 gz[kAdjGroups][3];
 #pragma unroll
-          for (int q = 0; q < kAdjBatch; ++q) {
-            const float4* rp = reinterpret_cast<const float4*>(&sm.rec[pb + q][0]);
+        for (int g2 = 0; g2 < kAdjGroups; ++g2)
+#pragma unroll
+          for (int a = 0; a < 3; ++a) gz[g2][a] = make_float2(0.f, 0.f);
+        const int from = (lane + 31) & 31;
+#pragma unroll 1
+        for (int st = 0; st < 32; ++st) {
+          if (st > 0) {
+#pragma unroll
+            for (int g2 = 0; g2 < kAdjGroups; ++g2)
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                gz[g2][a].x = __shfl_sync(0xffffffffu, gz[g2][a].x, from);
+                gz[g2][a].y = __shfl_sync(0xffffffffu, gz[g2][a].y, from);
+              }
+          }
+          const int pl = (lane - st) & 31;
+#pragma unroll
+          for (int g2 = 0; g2 < kAdjGroups; ++g2) {
+            if (g2 >= ng) break;  // warp-uniform: a ragged chunk's empty groups
+            const float4* rp = reinterpret_cast<const float4*>(&sm.rec[buf][g2 * 32 + pl][0]);
             const float4 a0 = rp[0], a1 = rp[1], a2 = rp[2], a3 = rp[3], a4 = rp[4], a5 = rp[5];
             const float2 nz0 = make_float2(a0.x, a0.y), nz1 = make_float2(a0.z, a0.w);
             const float2 nz2 = make_float2(a1.x, a1.y), ngA = make_float2(a1.z, a1.w);
@@ -319,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
             const float2 ngB2 = make_float2(a3.x, a3.y), ngC = make_float2(a3.z, a3.w);
             const float2 gB0 = make_float2(a4.x, a4.y), gB1 = make_float2(a4.z, a4.w);
             const float2 gB2 = make_float2(a5.x, a5.y);
-            float2 gz0 = make_float2(0.f, 0.f), gz1 = gz0, gz2 = gz0;  // sum of -w (x - z)
+            float2 gz0 = gz[g2][0], gz1 = gz[g2][1], gz2 = gz[g2][2];  // sum of e gB - w (x - z)
 #pragma unroll
             for (int j = 0; j < kAdjCols; ++j) {
               const float2 dx = __fadd2_rn(xd[j][0], nz0);
@@ -333,60 +386,42 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
               nge = __ffma2_rn(ngB1, xd[j][1], nge);
               nge = __ffma2_rn(ngB2, xd[j][2], nge);
               nge = __ffma2_rn(ngC, e, nge);
-              const float2 nw = __fmul2_rn(e, nge);  // -w
-              gz0 = __ffma2_rn(nw, dx, gz0);
-              gz1 = __ffma2_rn(nw, dy, gz1);
-              gz2 = __ffma2_rn(nw, dz, gz2);
-              gx[j][0] = __ffma2_rn(e, gB0, gx[j][0]);
-              gx[j][1] = __ffma2_rn(e, gB1, gx[j][1]);
-              gx[j][2] = __ffma2_rn(e, gB2, gx[j][2]);
-              gx[j][0] = __ffma2_rn(nw, dx, gx[j][0]);
-              gx[j][1] = __ffma2_rn(nw, dy, gx[j][1]);
-              gx[j][2] = __ffma2_rn(nw, dz, gx[j][2]);
+              // e (gB - ge (x - z) / s2): the column's term, and the row's
+              // plus e gB (removed once per row at its completion)
+              const float2 t0 = __ffma2_rn(nge, dx, gB0);
+              const float2 t1 = __ffma2_rn(nge, dy, gB1);
+              const float2 t2 = __ffma2_rn(nge, dz, gB2);
+              gz0 = __ffma2_rn(e, t0, gz0);
+              gz1 = __ffma2_rn(e, t1, gz1);
+              gz2 = __ffma2_rn(e, t2, gz2);
+              gx[j][0] = __ffma2_rn(e, t0, gx[j][0]);
+              gx[j][1] = __ffma2_rn(e, t1, gx[j][1]);
+              gx[j][2] = __ffma2_rn(e, t2, gx[j][2]);
             }
-            float* col = &sm.scr[warp][6 * q][lane];
-            col[0 * kScrStride] = gz0.x;
-            col[1 * kScrStride] = gz1.x;
-            col[2 * kScrStride] = gz2.x;
-            col[3 * kScrStride] = gz0.y;
-            col[4 * kScrStride] = gz1.y;
-            col[5 * kScrStride] = gz2.y;
+            gz[g2][0] = gz0;
+            gz[g2][1] = gz1;
+            gz[g2][2] = gz2;
           }
-          __syncwarp();
-          // lane v < kAdjVals: the sum over the 32 lanes of value v, a fixed
-          // pairwise tree on packed pairs (15 FADD2 + 1 FADD)
-          if (lane < kAdjVals) {
-            const float4* src = reinterpret_cast<const float4*>(&sm.scr[warp][lane][0]);
-            float2 t2[8];
+        }
+        {
+          const int pw = (lane + 1) & 31;  // the pair whose sum this lane holds
 #pragma unroll
-            for (int qq = 0; qq < 8; ++qq) {
-              const float4 v4 = src[qq];
-              t2[qq] = __fadd2_rn(make_float2(v4.x, v4.y), make_float2(v4.z, v4.w));
+          for (int g2 = 0; g2 < kAdjGroups; ++g2) {
+            if (g2 >= ng) break;
+            const int row = 2 * (g2 * 32 + pw);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              sm.wsum[buf][a][warp][row] = gz[g2][a].x;
+              sm.wsum[buf][a][warp][row + 1] = gz[g2][a].y;
             }
-#pragma unroll
-            for (int w = 4; w >= 1; w >>= 1)
-#pragma unroll
-              for (int qq = 0; qq < w; ++qq) t2[qq] = __fadd2_rn(t2[qq], t2[qq + w]);
-            const float sum = t2[0].x + t2[0].y;
-            const int q = lane / 6, comp = lane - 6 * q;
-            const int row = 2 * (pb + q) + (comp >= 3 ? 1 : 0);
-            sm.wsum[comp % 3][warp][row] = sum;
           }
-          __syncwarp();
         }
-        __syncthreads();
-        // this column block's dL/dz of the chunk's rows: the warps in order
-        if (r0 + tid < re) {
-          float gz[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            float v = sm.wsum[a][0][tid];
-#pragma unroll
-            for (int w = 1; w < kWarps; ++w) v += sm.wsum[a][w][tid];
-            gz[a] = -v * inv_sc;
-          }
-          __stcg(A.part_z + (size_t)cb * A.M + r0 + tid, make_float4(gz[0], gz[1], gz[2], 0.f));
-        }
+      }
+      // the unit's last chunk: its row totals are complete after this barrier
+      __syncthreads();
+      {
+        const int rl = rb + ((re - rb - 1) / kAdjRows) * kAdjRows;  // the last chunk's first row
+        complete_chunk_rows(sm, buf ^ 1, rl + tid, re, cb, inv_sc, A);
       }
       // this unit's dL/dx of the owned columns
 #pragma unroll
@@ -439,6 +474,13 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
         const float C = rt[0], lam = rt[1];
         const float uu[3] = {rt[2], rt[3], rt[4]};
         const float yy[3] = {y.x, y.y, y.z};
+        float gu[3];
+        for (int i = 0; i < 3; ++i)
+          gu[i] = coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2];
+        // the sweep summed e (gB - w (x - z)) over the columns: its e gB part,
+        // gB sum_c e = gu C^-1/2 A = gu lambda, comes off here
+        if (C > 10e-7f)
+          for (int i = 0; i < 3; ++i) totz[i] = fmaf(lam, gu[i], totz[i]);
         float gy[3];
         for (int jj = 0; jj < 3; ++jj)
           gy[jj] = R[jj] * totz[0] + R[3 + jj] * totz[1] + R[6 + jj] * totz[2] + lam * coef[4 + jj] +
@@ -453,13 +495,12 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
           df_add(vv[9 + i], totz[i]);
         }
         if (!(C > 10e-7f)) {  // branch rows: u = mean X
-          for (int i = 0; i < 3; ++i)
-            df_add(vv[12 + i], coef[1 + i] + coef[7 + i] * yy[0] + coef[10 + i] * yy[1] + coef[13 + i] * yy[2]);
+          for (int i = 0; i < 3; ++i) df_add(vv[12 + i], gu[i]);
         }
       }
       // the block's 16 sums, through shared memory (scr and wsum are free here)
-      static_assert(sizeof(sm.scr) + sizeof(sm.wsum) >= sizeof(df) * 17 * kThreads, "moment scratch");
-      em_block_moments(vv, min(kThreads, nrows), reinterpret_cast<df*>(&sm.scr[0][0][0]),
+      static_assert(sizeof(sm.wsum) >= sizeof(df) * 17 * kThreads, "moment scratch");
+      em_block_moments(vv, min(kThreads, nrows), reinterpret_cast<df*>(&sm.wsum[0][0][0][0]),
                        recs + (size_t)blockIdx.x * 16);
     }
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 103)) {
