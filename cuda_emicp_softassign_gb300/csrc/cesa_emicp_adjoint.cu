@@ -38,6 +38,8 @@
 // (FFMA2/FADD2/FMUL2). The row sums carry e gB, which sums to gB A_r =
 // gu_r lambda_r (A_r = sum_c e, lambda_r = A_r C_r^-1/2 from the tape) and is
 // subtracted once per row at its completion.
+#include <cstdlib>
+
 #include "cesa.h"
 #include "cesa_kernels.h"
 #include "cesa_ops.cuh"
@@ -55,6 +57,9 @@ constexpr int kAdjGroups = kAdjRP / 32;           // groups of 32 row pairs (one
 constexpr int kAdjRecStride = 14;                 // float2 per row-pair record (11 used; 112 bytes, so
                                                   // 8 lanes reading 8 consecutive records hit 32 banks)
 constexpr float kFar = 1e15f;                     // padding row coordinate: its affinities are exactly 0
+constexpr int kPairCap = 1024;                    // SM ids the pairing table covers
+constexpr int kPairNum = 3;                       // parts of a pair's units: the first kPairNum / kPairDen
+constexpr int kPairDen = 4;                       // go to the block the SM favours
 // Padding column coordinate, already scaled: its squared distance to any row
 // (|z'| far below 2^26) is above 2^50, so its affinity is exactly 0, and its
 // term ge (x - z) + gB stays finite (for row coefficients below 2^70), so that
@@ -98,6 +103,9 @@ struct EmAdjArgs {
   df* rec;                // [2][grid][16]: per-block records of the row completion
   float4* part_x;         // [2][S][N]: dL/dx per row slice; ranged: [2][nb][kmax][kAdjColBlk]
   Ctl* ctl;
+  unsigned* pair_tab;  // [2 kPairCap + 1] (cleared): blocks seen per SM, pair index + 1 per SM, pairs so far
+  float* pair_t;       // [grid]: sweep time of each (pair, part), ns
+  int pairs;           // 1: units dealt to SM pairs (two blocks per SM, slice layout)
   int* d_status;
   uint64_t timeout_ns;
 };
@@ -208,6 +216,58 @@ __device__ __forceinline__ void build_row_record(AdjSmem& sm, int buf, int i, bo
   for (int k = 0; k < 11; ++k) dst[2 * k] = v[k];
 }
 
+// SM pairs. With two blocks on an SM the warp scheduler favours the block it
+// started first: the other mostly fills the first one's idle issue slots and
+// runs at full speed only once the first is done, so equal shares leave the
+// SM half-used for the last part of every sweep. In the slice layout, where
+// every unit owns its partial slots, the units of each SM's pair of blocks
+// (dense pair index d, in order of arrival) are split kPairNum : kPairDen -
+// kPairNum, the larger part to the favoured block: taken to be the one that
+// arrived first, and the parts swap after a step whose larger part took over
+// 1.5 times as long as the smaller. The split decides which block computes a
+// unit, never what the unit computes, so the results do not depend on it.
+struct PairUnits {
+  int lo, split, hi;  // part 0: [lo, split), part 1: [split, hi)
+};
+
+__host__ __device__ inline PairUnits pair_units(int units, int npairs, int d) {
+  PairUnits r;
+  r.lo = (int)((long long)units * d / npairs);
+  r.hi = (int)((long long)units * (d + 1) / npairs);
+  r.split = r.lo + (kPairNum * (r.hi - r.lo) + kPairDen / 2) / kPairDen;
+  return r;
+}
+
+// Thread 0 of a block: its pair index and role (0: first on its SM), or
+// {-1, -1} when the SM id is out of the table, a third block arrives on one
+// SM or the first one's index did not appear within timeout_ns.
+__device__ __noinline__ int2 join_pair(const EmAdjArgs& A) {
+  unsigned sm_id;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(sm_id));
+  if (sm_id >= (unsigned)kPairCap) return make_int2(-1, -1);
+  const unsigned r = atomicAdd(&A.pair_tab[sm_id], 1u);
+  if (r == 0u) {
+    const unsigned d = atomicAdd(&A.pair_tab[2 * kPairCap], 1u);
+    red_release_add(&A.pair_tab[kPairCap + sm_id], d + 1u);  // the slot was 0
+    return make_int2((int)d, 0);
+  }
+  if (r != 1u) return make_int2(-1, -1);
+  uint64_t t0 = 0;
+  unsigned spins = 0;
+  for (;;) {
+    const unsigned v = ld_acquire(&A.pair_tab[kPairCap + sm_id]);
+    if (v != 0u) return make_int2((int)v - 1, 1);
+    if ((++spins & 31u) == 0) {
+      const uint64_t now = global_ns();
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > A.timeout_ns) {
+        return make_int2(-1, -1);
+      }
+    }
+  }
+}
+
 // dL/dz of row r (of a chunk ending before row `end`) from one column block:
 // the warps' row totals in warp order, unscaled, stored to the block's slot
 __device__ __forceinline__ void complete_chunk_rows(const AdjSmem& sm, int buf, int r, int end, int cb, float inv_sc,
@@ -234,12 +294,21 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
   __shared__ df s_red[kThreads];
   __shared__ df s_tot[16];
   __shared__ RangedShare rsh;  // this block's share of the ranged tasks
+  __shared__ int s_pair[3];    // SM pairs: pair index, role, parts swapped
+  __shared__ uint64_t s_tsweep;  // SM pairs: start of this step's sweep
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned G = gridDim.x;
   const AdjGeom& g = A.geo;
   if (tid == 0) {
     rsh = ranged_share(adj_tasks(g), blockIdx.x, (int)G);
+    if (A.pairs) {
+      const int2 pr = join_pair(A);
+      if (pr.x < 0 || pr.x >= (int)G / 2) set_status(A.ctl, kStatusInternal, 105);
+      s_pair[0] = pr.x < (int)G / 2 ? pr.x : -1;
+      s_pair[1] = pr.y;
+      s_pair[2] = 0;
+    }
     // caller frame -> centred frame: t = t' + oX - R oY, so dL/dt' = dL/dt and
     // dL/dR' = dL/dR - dL/dt oY^T
     for (int i = 0; i < 3; ++i) {
@@ -274,8 +343,23 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
     const size_t px_len = g.ranged ? (size_t)g.nb * g.kmax * kAdjColBlk : (size_t)g.S * A.N;
     float4* px = A.part_x + (size_t)par * px_len;
 
-    const int u_end = g.ranged ? rsh.o_last - rsh.o_first + 1 : g.units;
-    for (int u = g.ranged ? 0 : (int)blockIdx.x; u < u_end; u += g.ranged ? 1 : (int)G) {
+    int u_begin = (int)blockIdx.x, u_end = g.units, u_step = (int)G;
+    if (g.ranged) {
+      u_begin = 0;
+      u_end = rsh.o_last - rsh.o_first + 1;
+      u_step = 1;
+    } else if (A.pairs) {  // this block's part of its pair's units (none after a failed join)
+      u_begin = u_end = 0;
+      u_step = 1;
+      if (s_pair[0] >= 0) {
+        const PairUnits pu = pair_units(g.units, (int)G / 2, s_pair[0]);
+        const bool first = (s_pair[1] ^ s_pair[2]) == 0;
+        u_begin = first ? pu.lo : pu.split;
+        u_end = first ? pu.split : pu.hi;
+      }
+    }
+    if (A.pairs && tid == 0) s_tsweep = global_ns();
+    for (int u = u_begin; u < u_end; u += u_step) {
       // unit: column block cb, rows [rb, re); its dL/dx partials go to px_dst
       int cb, rb, re;
       float4* px_dst;
@@ -433,9 +517,16 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
                              (gx[j][2].x + gx[j][2].y) * inv_sc, 0.f));
       }
     }
+    if (A.pairs && tid == 0 && s_pair[0] >= 0)
+      A.pair_t[2 * s_pair[0] + (s_pair[1] ^ s_pair[2])] = (float)(global_ns() - s_tsweep);
     if (!ok || !grid_sync(A.ctl, epoch, G, A.timeout_ns, 102)) {
       ok = false;
       break;
+    }
+    if (A.pairs && tid == 0 && s_pair[0] >= 0) {  // both blocks of the pair read the same two times
+      const PairUnits pu = pair_units(g.units, (int)G / 2, s_pair[0]);
+      const float t0 = __ldcg(A.pair_t + 2 * s_pair[0]), t1 = __ldcg(A.pair_t + 2 * s_pair[0] + 1);
+      if (pu.split > pu.lo && pu.hi > pu.split && t0 > 1.5f * t1) s_pair[2] ^= 1;
     }
     // Rows completed, each block a contiguous share of them (all blocks in
     // parallel, no serial tail): the column blocks' dL/dz partials summed in
@@ -593,6 +684,7 @@ struct AdjPlan {
   int grid;
   AdjGeom geo;
   size_t smem;
+  int pairs;  // slice units dealt to SM pairs
 };
 
 // Column blocks of kAdjColBlk columns and row slices of an even number of rows,
@@ -643,6 +735,12 @@ AdjPlan plan_adj(int N, int M, int device, int layout) {
     P.geo.kmax = ranged_kmax(adj_tasks(P.geo), limit);  // tasks of kAdjRows rows: g.nch as set above
     P.grid = limit;
   }
+  // SM pairs: two blocks on every SM and at least four units per pair
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  P.pairs = !P.geo.ranged && sms > 0 && limit == 2 * sms && P.grid == limit && P.geo.units >= 2 * P.grid;
+  const char* ev = getenv("CESA_SM_PAIRS");  // "0": deal the units evenly (for comparisons)
+  if (ev && ev[0] == '0') P.pairs = 0;
   return P;
 }
 
@@ -662,6 +760,8 @@ size_t emicp_adjoint_ws_need(int N, int M, int device, int layout) {
   c.take<float4>((size_t)N);
   c.take<float4>((size_t)M);
   c.take<float>(12);
+  c.take<unsigned>(2 * kPairCap + 1);
+  c.take<float>((size_t)P.grid);
   c.take<float4>((size_t)P.geo.nb * M);
   c.take<df>((size_t)2 * P.grid * 16);
   c.take<float4>(part_x_len(P.geo, N));
@@ -678,7 +778,9 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   float4* gX = c.take<float4>((size_t)L.N);
   float4* gY = c.take<float4>((size_t)L.M);
   float* g_in = c.take<float>(12);
+  unsigned* pair_tab = c.take<unsigned>(2 * kPairCap + 1);
   const size_t zero_bytes = c.off;
+  float* pair_t = c.take<float>((size_t)P.grid);
   float4* part_z = c.take<float4>((size_t)P.geo.nb * L.M);
   df* rec = c.take<df>((size_t)2 * P.grid * 16);
   float4* part_x = c.take<float4>(part_x_len(P.geo, L.N));
@@ -705,6 +807,9 @@ int enqueue_emicp_adjoint(const EmicpAdjointLaunch& L, void* ws, size_t ws_bytes
   A.rec = rec;
   A.part_x = part_x;
   A.ctl = ctl;
+  A.pair_tab = pair_tab;
+  A.pair_t = pair_t;
+  A.pairs = P.pairs;
   A.d_status = L.d_status;
   A.timeout_ns = L.timeout_ns;
   if (L.nsteps > 0) {

@@ -98,3 +98,32 @@ def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, c3_small, referenc
     assert rel(Yd.grad.cpu().numpy(), gY) < 2e-3
     g6 = np.r_[gw, gv]
     assert rel(np.r_[gw_d.cpu().numpy(), gv_d.cpu().numpy()], g6) < 2e-3
+
+
+def test_sm_pairs_leave_gradients_unchanged(cesa, torch_cuda, monkeypatch):
+    """At config 3's size the slice units are dealt unequally to the two
+    blocks of each SM (the larger part to the block the SM favours); that
+    decides only which block computes a unit, so the gradients are bitwise
+    those of the even deal (CESA_SM_PAIRS=0)."""
+    from cuda_emicp_softassign_gb300 import workloads as W
+    from cuda_emicp_softassign_gb300.autograd import emicp_autograd
+    torch = torch_cuda
+    _, X, Y, _, _ = W.make("c3_emicp_40097", seed=0)
+    p = cesa.Params.default(emicp_backward_layout=cesa.LAYOUT_SLICES)
+
+    def grads():
+        Xd = torch.tensor(X, dtype=torch.float32, device="cuda", requires_grad=True)
+        Yd = torch.tensor(Y, dtype=torch.float32, device="cuda", requires_grad=True)
+        R0 = torch.eye(3, device="cuda", requires_grad=True)
+        t0 = torch.zeros(3, device="cuda", requires_grad=True)
+        R, t = emicp_autograd(Xd, Yd, R0, t0, p)
+        ((R ** 2).sum() + (t ** 2).sum()).backward()
+        return [v.detach().cpu().numpy() for v in (Xd.grad, Yd.grad, R0.grad, t0.grad)]
+
+    paired = grads()
+    again = grads()
+    monkeypatch.setenv("CESA_SM_PAIRS", "0")
+    even = grads()
+    for a, b, c in zip(paired, again, even):
+        assert np.isfinite(a).all()
+        assert np.array_equal(a, b) and np.array_equal(a, c)
