@@ -23,6 +23,7 @@
 // loop. EM-ICP's S is translation invariant, so only Xc, Yc and t are shifted
 // back; the pose enters and leaves in the caller's frame.
 #include <atomic>
+#include <cstdlib>
 
 #include "cesa_kernels.h"
 #include "cesa_ops.cuh"
@@ -45,6 +46,8 @@ struct EmicpArgs {
   int Mp;
   df* rbpart;           // [2][grid][kEmNV] moments per block (step parity)
   Ctl* ctl;
+  unsigned* pair_tab;   // SM pairs (geo.pair_num): [2 kPairCap + 1], zero at launch
+  float* pair_t;        // SM pairs: [grid] sweep time of each virtual block, ns
   double* trace;
   int trace_cap;
   float* row_out;       // optional [M][5] (centred-frame u)
@@ -63,6 +66,8 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
   __shared__ df s_red[kThreads];
   __shared__ OwnCache oc_rows;
   __shared__ RangedShare rs_rows;  // this block's share of a ranged sweep
+  __shared__ int s_pair[3];        // SM pairs: pair index (-1: none), role, parts swapped
+  __shared__ uint64_t s_tsweep;    // SM pairs: start of the step's sweep
   __shared__ df s_tot[kEmNV];
   __shared__ float s_emS[15];  // S, Xc, Yc of the step
   __shared__ float s_hdr[12];
@@ -85,7 +90,20 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     for (int k = 0; k < 9; ++k) s_pose[k] = R[k];
     for (int k = 0; k < 3; ++k) s_pose[9 + k] = tc[k];
     oc_rows.blk = -1;
-    rs_rows = ranged_share(A.geo, blockIdx.x, (int)gridDim.x);
+    int vb = (int)blockIdx.x;  // the virtual block whose share this block sweeps
+    s_pair[0] = -1;
+    if (A.geo.pair_num) {
+      const int2 pr = join_sm_pair(A.pair_tab, A.timeout_ns);
+      if (pr.x >= 0 && pr.x < (int)G / 2) {
+        s_pair[0] = pr.x;
+        s_pair[1] = pr.y;
+        s_pair[2] = 0;
+        vb = 2 * pr.x + pr.y;
+      } else {
+        set_status(A.ctl, kStatusInternal, 23);  // the launch ends at its first grid barrier
+      }
+    }
+    rs_rows = A.geo.pair_num && s_pair[0] < 0 ? RangedShare{0, -1, 0, 0, 0} : ranged_share(A.geo, vb, (int)G);
   }
   __syncthreads();
 
@@ -139,10 +157,13 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) tcs[k] = tc[k] * sc;
       const StreamSrc xsrc{A.xs + (size_t)(step & 1) * A.N, nullptr, false};
+      if (tid == 0 && s_pair[0] >= 0) s_tsweep = global_ns();
       if (!sweep_units<5, EmicpElemScaled, NoPrep, NoFin, true, 1>(sm, pipe, A.geo, xsrc, A.rows, true, Rs, tcs, 0u,
                                                                 A.part, nullptr, EmicpElemScaled{}, NoPrep{}, NoFin{},
                                                                 A.ctl, A.timeout_ns, 10, tl, A.Mp, &oc_rows, &rs_rows))
         break;
+      if (tid == 0 && s_pair[0] >= 0)
+        A.pair_t[2 * s_pair[0] + (s_pair[1] ^ s_pair[2])] = (float)(global_ns() - s_tsweep);
     } else {
       const EmicpElem elem{-kLog2e / (2.f * s2)};
       if (!sweep_units<5, EmicpElem, NoPrep, NoFin, true, 0>(sm, pipe, A.geo, src, A.rows, true, R, tc, 0u, A.part,
@@ -152,6 +173,15 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_kernel(const EmicpArgs A) {
     }
     if (!grid_sync(A.ctl, epoch, G, A.timeout_ns, 20)) break;
     tl.mark(5);
+    if (tid == 0 && s_pair[0] >= 0) {  // SM pairs: the parts change blocks when the times show the other favoured
+      long lo = 0, sp = 0, hi = 0;
+      ranged_tasks(A.geo, 2 * s_pair[0], (int)G, lo, sp);
+      ranged_tasks(A.geo, 2 * s_pair[0] + 1, (int)G, sp, hi);
+      if (pair_swap(lo, sp, hi, A.pair_t, s_pair[0])) {
+        s_pair[2] ^= 1;
+        rs_rows = ranged_share(A.geo, 2 * s_pair[0] + (s_pair[1] ^ s_pair[2]), (int)G);
+      }
+    }
     // the next step's scaled X' (its buffer was last read by the previous step's sweep)
     if (A.geo.ranged && step + 1 < A.nsteps)
       scale_x(A.xs + (size_t)((step + 1) & 1) * A.N, sqrtf(kLog2e / (2.f * (s2 * A.sigma_factor))));
@@ -334,11 +364,17 @@ EmicpPlan plan_emicp(int N, int M, int device) {
   P.smem = sweep_smem();
   const int limit = persistent_grid_limit(device, (const void*)emicp_kernel, P.smem);
   const SweepGeomH h = plan_sweep(M, N, limit);
-  P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units, 0, 0, 0};
+  P.geo = SweepGeom{h.n_own, h.n_stream, h.nblk, h.slices, h.slice_len, h.units, 0, 0, 0, 0};
   P.grid = h.units < limit ? h.units : limit;
   // Large clouds: contiguous task ranges, the same work per block to one
-  // chunk of 512 streamed points, instead of units dealt in waves.
+  // chunk of 512 streamed points, instead of units dealt in waves; with two
+  // blocks on every SM, each SM's pair splits its range 13 : 3, the larger
+  // part to the block the SM favours.
   if (ranged_pays(h.nblk, N, limit)) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const char* ev = getenv("CESA_SM_PAIRS");  // "0": equal shares (for comparisons)
+    if (sms > 0 && limit == 2 * sms && !(ev && ev[0] == '0')) P.geo.pair_num = 13;
     make_ranged(P.geo, limit);
     P.grid = limit;
   }
@@ -353,6 +389,8 @@ struct EmicpCarved {
   float4* xs;
   float* part;
   df* rbpart;
+  unsigned* pair_tab;
+  float* pair_t;
   int Mp;
 };
 
@@ -368,6 +406,8 @@ EmicpCarved carve_emicp(void* base, const EmicpPlan& P, int N, int M, size_t* to
   w.part = c.take<float>(P.geo.ranged ? (size_t)5 * P.geo.nblk * P.geo.kmax * kBlockPts
                                       : (size_t)5 * P.geo.slices * w.Mp);
   w.rbpart = c.take<df>((size_t)2 * P.grid * kEmNV);
+  w.pair_tab = c.take<unsigned>(P.geo.pair_num ? 2 * kPairCap + 1 : 0);
+  w.pair_t = c.take<float>(P.geo.pair_num ? (size_t)P.grid : 0);
   if (total) *total = c.off;
   return w;
 }
@@ -402,6 +442,8 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   e = cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), st);
   if (e == cudaSuccess && P.geo.ranged)
     e = cudaMemsetAsync(w.part, 0, sizeof(float) * 5 * (size_t)P.geo.nblk * P.geo.kmax * kBlockPts, st);
+  if (e == cudaSuccess && P.geo.pair_num)
+    e = cudaMemsetAsync(w.pair_tab, 0, sizeof(unsigned) * (2 * kPairCap + 1), st);
   if (e != cudaSuccess) return (int)e;
   prep_center_kernel<<<1, 1024, 0, st>>>(L.dX, L.N, L.dY, L.M, w.hdr);
   const int pb = 256, pg_x = (L.N + pb - 1) / pb, pg_y = (L.M + pb - 1) / pb;
@@ -428,6 +470,8 @@ int enqueue_emicp(const EmicpLaunch& L, void* ws, size_t ws_bytes, cudaStream_t 
   A.Mp = w.Mp;
   A.rbpart = w.rbpart;
   A.ctl = w.ctl;
+  A.pair_tab = w.pair_tab;
+  A.pair_t = w.pair_t;
   A.trace = L.trace;
   A.trace_cap = L.trace_cap;
   A.row_out = L.row_out;

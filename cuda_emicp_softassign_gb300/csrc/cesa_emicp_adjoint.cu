@@ -57,9 +57,8 @@ constexpr int kAdjGroups = kAdjRP / 32;           // groups of 32 row pairs (one
 constexpr int kAdjRecStride = 14;                 // float2 per row-pair record (11 used; 112 bytes, so
                                                   // 8 lanes reading 8 consecutive records hit 32 banks)
 constexpr float kFar = 1e15f;                     // padding row coordinate: its affinities are exactly 0
-constexpr int kPairCap = 1024;                    // SM ids the pairing table covers
-constexpr int kPairNum = 3;                       // parts of a pair's units: the first kPairNum / kPairDen
-constexpr int kPairDen = 4;                       // go to the block the SM favours
+constexpr int kAdjPairNum = 12;                   // SM pairs: the first 12/16 of a pair's units go to the
+                                                  // block its SM favours
 // Padding column coordinate, already scaled: its squared distance to any row
 // (|z'| far below 2^26) is above 2^50, so its affinity is exactly 0, and its
 // term ge (x - z) + gB stays finite (for row coefficients below 2^70), so that
@@ -216,16 +215,11 @@ __device__ __forceinline__ void build_row_record(AdjSmem& sm, int buf, int i, bo
   for (int k = 0; k < 11; ++k) dst[2 * k] = v[k];
 }
 
-// SM pairs. With two blocks on an SM the warp scheduler favours the block it
-// started first: the other mostly fills the first one's idle issue slots and
-// runs at full speed only once the first is done, so equal shares leave the
-// SM half-used for the last part of every sweep. In the slice layout, where
-// every unit owns its partial slots, the units of each SM's pair of blocks
-// (dense pair index d, in order of arrival) are split kPairNum : kPairDen -
-// kPairNum, the larger part to the favoured block: taken to be the one that
-// arrived first, and the parts swap after a step whose larger part took over
-// 1.5 times as long as the smaller. The split decides which block computes a
-// unit, never what the unit computes, so the results do not depend on it.
+// SM pairs (join_sm_pair): in the slice layout, where every unit owns its
+// partial slots, the units of each SM's pair of blocks are split 12 : 4, the
+// larger part to the block the SM favours, so that both finish together. The
+// split decides which block computes a unit, never what the unit computes, so
+// the results do not depend on it.
 struct PairUnits {
   int lo, split, hi;  // part 0: [lo, split), part 1: [split, hi)
 };
@@ -234,38 +228,8 @@ __host__ __device__ inline PairUnits pair_units(int units, int npairs, int d) {
   PairUnits r;
   r.lo = (int)((long long)units * d / npairs);
   r.hi = (int)((long long)units * (d + 1) / npairs);
-  r.split = r.lo + (kPairNum * (r.hi - r.lo) + kPairDen / 2) / kPairDen;
+  r.split = (int)pair_split(r.lo, r.hi, kAdjPairNum);
   return r;
-}
-
-// Thread 0 of a block: its pair index and role (0: first on its SM), or
-// {-1, -1} when the SM id is out of the table, a third block arrives on one
-// SM or the first one's index did not appear within timeout_ns.
-__device__ __noinline__ int2 join_pair(const EmAdjArgs& A) {
-  unsigned sm_id;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(sm_id));
-  if (sm_id >= (unsigned)kPairCap) return make_int2(-1, -1);
-  const unsigned r = atomicAdd(&A.pair_tab[sm_id], 1u);
-  if (r == 0u) {
-    const unsigned d = atomicAdd(&A.pair_tab[2 * kPairCap], 1u);
-    red_release_add(&A.pair_tab[kPairCap + sm_id], d + 1u);  // the slot was 0
-    return make_int2((int)d, 0);
-  }
-  if (r != 1u) return make_int2(-1, -1);
-  uint64_t t0 = 0;
-  unsigned spins = 0;
-  for (;;) {
-    const unsigned v = ld_acquire(&A.pair_tab[kPairCap + sm_id]);
-    if (v != 0u) return make_int2((int)v - 1, 1);
-    if ((++spins & 31u) == 0) {
-      const uint64_t now = global_ns();
-      if (t0 == 0) {
-        t0 = now;
-      } else if (now - t0 > A.timeout_ns) {
-        return make_int2(-1, -1);
-      }
-    }
-  }
 }
 
 // dL/dz of row r (of a chunk ending before row `end`) from one column block:
@@ -303,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
   if (tid == 0) {
     rsh = ranged_share(adj_tasks(g), blockIdx.x, (int)G);
     if (A.pairs) {
-      const int2 pr = join_pair(A);
+      const int2 pr = join_sm_pair(A.pair_tab, A.timeout_ns);
       if (pr.x < 0 || pr.x >= (int)G / 2) set_status(A.ctl, kStatusInternal, 105);
       s_pair[0] = pr.x < (int)G / 2 ? pr.x : -1;
       s_pair[1] = pr.y;
@@ -525,8 +489,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
     }
     if (A.pairs && tid == 0 && s_pair[0] >= 0) {  // both blocks of the pair read the same two times
       const PairUnits pu = pair_units(g.units, (int)G / 2, s_pair[0]);
-      const float t0 = __ldcg(A.pair_t + 2 * s_pair[0]), t1 = __ldcg(A.pair_t + 2 * s_pair[0] + 1);
-      if (pu.split > pu.lo && pu.hi > pu.split && t0 > 1.5f * t1) s_pair[2] ^= 1;
+      if (pair_swap(pu.lo, pu.split, pu.hi, A.pair_t, s_pair[0])) s_pair[2] ^= 1;
     }
     // Rows completed, each block a contiguous share of them (all blocks in
     // parallel, no serial tail): the column blocks' dL/dz partials summed in

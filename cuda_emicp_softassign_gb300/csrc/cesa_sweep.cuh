@@ -61,11 +61,34 @@ struct SweepGeom {
   int ranged;
   int nch;        // ceil(n_stream / kChunk)
   int kmax;       // most grid blocks covering one owned block
+  // SM pairs (ranged only; 0 = off). The G blocks are P = G / 2 pairs, two on
+  // each SM, and pair d takes the tasks [T d / P, T (d + 1) / P), split at
+  // pair_num / kPairDen of their count: virtual block 2 d the first part,
+  // 2 d + 1 the rest. The partition, and so every slot's contents, is fixed;
+  // which block of the pair computes which part is chosen at run time (the
+  // block its SM favours takes the larger part: join_sm_pair, pair_swap).
+  // Where a "block" b indexes tasks and slots below, it is the virtual index.
+  int pair_num;
 };
+
+constexpr int kPairDen = 16;
+constexpr int kPairCap = 1024;  // SM ids a pairing table covers
+
+// The split point of a pair's tasks [lo, hi).
+__host__ __device__ __forceinline__ long pair_split(long lo, long hi, int pair_num) {
+  return lo + ((hi - lo) * pair_num + kPairDen / 2) / kPairDen;
+}
 
 // Task range [t0, t1) of block b in a ranged sweep over G blocks.
 __host__ __device__ __forceinline__ void ranged_tasks(const SweepGeom& g, int b, int G, long& t0, long& t1) {
   const long T = (long)g.nblk * g.nch;
+  if (g.pair_num) {
+    const int P = G / 2, d = b >> 1;
+    const long lo = T * d / P, hi = T * (d + 1) / P, sp = pair_split(lo, hi, g.pair_num);
+    t0 = (b & 1) ? sp : lo;
+    t1 = (b & 1) ? hi : sp;
+    return;
+  }
   t0 = T * b / G;
   t1 = T * (b + 1) / G;
 }
@@ -74,6 +97,12 @@ __host__ __device__ __forceinline__ void ranged_tasks(const SweepGeom& g, int b,
 // floor(T b / G) <= task, i.e. floor(((task + 1) G - 1) / T).
 __host__ __device__ __forceinline__ int ranged_block_of(const SweepGeom& g, long task, int G) {
   const long T = (long)g.nblk * g.nch;
+  if (g.pair_num) {  // the pair, then the part
+    const int P = G / 2;
+    const int d = (int)(((task + 1) * (long)P - 1) / T);
+    const long lo = T * d / P, hi = T * (d + 1) / P;
+    return 2 * d + (task >= pair_split(lo, hi, g.pair_num) ? 1 : 0);
+  }
   return (int)(((task + 1) * (long)G - 1) / T);
 }
 
@@ -98,6 +127,52 @@ __device__ __forceinline__ RangedShare ranged_share(const SweepGeom& g, int b, i
   r.c_end = (int)(t1 - (long)r.o_last * g.nch);
   r.j_first = b - ranged_block_of(g, (long)r.o_first * g.nch, G);
   return r;
+}
+
+// SM pairs. With two blocks on an SM the warp scheduler favours the block it
+// started first: the other mostly fills the first one's idle issue slots, and
+// runs at full speed only once the first is done, so equal shares leave the SM
+// half-used for the last part of every sweep. Thread 0 of each block joins its
+// SM's pair: table [2 kPairCap + 1] (zero at launch) counts the blocks seen
+// per SM id, holds each SM's dense pair index + 1 and, last, the pairs so far.
+// Returns (pair index, role: 0 for the first block on its SM), or (-1, -1)
+// when the SM id is out of the table, a third block arrives on one SM or the
+// first one's index did not appear within timeout_ns. The first arrival is
+// taken to be the favoured block; pair_swap corrects that from the times.
+static __device__ __noinline__ int2 join_sm_pair(unsigned* tab, uint64_t timeout_ns) {
+  unsigned sm_id;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(sm_id));
+  if (sm_id >= (unsigned)kPairCap) return make_int2(-1, -1);
+  const unsigned r = atomicAdd(&tab[sm_id], 1u);
+  if (r == 0u) {
+    const unsigned d = atomicAdd(&tab[2 * kPairCap], 1u);
+    red_release_add(&tab[kPairCap + sm_id], d + 1u);  // the slot was 0
+    return make_int2((int)d, 0);
+  }
+  if (r != 1u) return make_int2(-1, -1);
+  uint64_t t0 = 0;
+  unsigned spins = 0;
+  for (;;) {
+    const unsigned v = ld_acquire(&tab[kPairCap + sm_id]);
+    if (v != 0u) return make_int2((int)v - 1, 1);
+    if ((++spins & 31u) == 0) {
+      const uint64_t now = global_ns();
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > timeout_ns) {
+        return make_int2(-1, -1);
+      }
+    }
+  }
+}
+
+// Whether pair d's parts should change blocks: both parts hold work and the
+// first part's sweep (time t[2 d], ns) took over 1.5 times the second's
+// (t[2 d + 1]). Both blocks of the pair read the same two times after a grid
+// barrier, so they agree.
+__device__ __forceinline__ bool pair_swap(long lo, long split, long hi, const float* t, int d) {
+  const float t0 = __ldcg(t + 2 * d), t1 = __ldcg(t + 2 * d + 1);
+  return split > lo && hi > split && t0 > 1.5f * t1;
 }
 
 // Large sweeps take the ranged decomposition: at least 16 tasks per block, so

@@ -101,29 +101,34 @@ def test_gpu_adjoint_matches_fp64_reference(cesa, torch_cuda, c3_small, referenc
 
 
 def test_sm_pairs_leave_gradients_unchanged(cesa, torch_cuda, monkeypatch):
-    """At config 3's size the slice units are dealt unequally to the two
-    blocks of each SM (the larger part to the block the SM favours); that
-    decides only which block computes a unit, so the gradients are bitwise
-    those of the even deal (CESA_SM_PAIRS=0)."""
+    """At config 3's size the backward's slice units are dealt unequally to
+    the two blocks of each SM (the larger part to the block the SM favours);
+    that decides only which block computes a unit, so the gradients are
+    bitwise those of the even deal (CESA_SM_PAIRS=0 set between the forward
+    and the backward, so that both backwards differentiate the same taped
+    forward)."""
     from cuda_emicp_softassign_gb300 import workloads as W
     from cuda_emicp_softassign_gb300.autograd import emicp_autograd
     torch = torch_cuda
     _, X, Y, _, _ = W.make("c3_emicp_40097", seed=0)
     p = cesa.Params.default(emicp_backward_layout=cesa.LAYOUT_SLICES)
 
-    def grads():
+    def grads(even_backward):
         Xd = torch.tensor(X, dtype=torch.float32, device="cuda", requires_grad=True)
         Yd = torch.tensor(Y, dtype=torch.float32, device="cuda", requires_grad=True)
         R0 = torch.eye(3, device="cuda", requires_grad=True)
         t0 = torch.zeros(3, device="cuda", requires_grad=True)
         R, t = emicp_autograd(Xd, Yd, R0, t0, p)
-        ((R ** 2).sum() + (t ** 2).sum()).backward()
+        loss = (R ** 2).sum() + (t ** 2).sum()
+        if even_backward:
+            monkeypatch.setenv("CESA_SM_PAIRS", "0")
+        loss.backward()
+        monkeypatch.delenv("CESA_SM_PAIRS", raising=False)
         return [v.detach().cpu().numpy() for v in (Xd.grad, Yd.grad, R0.grad, t0.grad)]
 
-    paired = grads()
-    again = grads()
-    monkeypatch.setenv("CESA_SM_PAIRS", "0")
-    even = grads()
+    paired = grads(False)
+    again = grads(False)
+    even = grads(True)
     for a, b, c in zip(paired, again, even):
         assert np.isfinite(a).all()
         assert np.array_equal(a, b) and np.array_equal(a, c)
