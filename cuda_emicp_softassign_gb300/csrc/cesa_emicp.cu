@@ -374,7 +374,7 @@ EmicpPlan plan_emicp(int N, int M, int device) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const char* ev = getenv("CESA_SM_PAIRS");  // "0": equal shares (for comparisons)
-    if (sms > 0 && limit == 2 * sms && !(ev && ev[0] == '0')) P.geo.pair_num = 13;
+    if (sms > 0 && limit == 2 * sms && !(ev && ev[0] == '0')) P.geo.pair_num = 208;  // 13 / 16
     make_ranged(P.geo, limit);
     P.grid = limit;
   }

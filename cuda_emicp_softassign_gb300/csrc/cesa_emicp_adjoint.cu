@@ -57,8 +57,12 @@ constexpr int kAdjGroups = kAdjRP / 32;           // groups of 32 row pairs (one
 constexpr int kAdjRecStride = 14;                 // float2 per row-pair record (11 used; 112 bytes, so
                                                   // 8 lanes reading 8 consecutive records hit 32 banks)
 constexpr float kFar = 1e15f;                     // padding row coordinate: its affinities are exactly 0
-constexpr int kAdjPairNum = 12;                   // SM pairs: the first 12/16 of a pair's units go to the
-                                                  // block its SM favours
+constexpr int kAdjPairNum = 192;                  // SM pairs, slices: the first 192/256 of a pair's units go
+                                                  // to the block its SM favours
+#ifndef CESA_ADJ_RANGED_PAIR
+#define CESA_ADJ_RANGED_PAIR 193
+#endif
+constexpr int kAdjRangedPairNum = CESA_ADJ_RANGED_PAIR;  // SM pairs, ranged: the favoured block's share of tasks, /256
 // Padding column coordinate, already scaled: its squared distance to any row
 // (|z'| far below 2^26) is above 2^50, so its affinity is exactly 0, and its
 // term ge (x - z) + gB stays finite (for row coefficients below 2^70), so that
@@ -74,6 +78,7 @@ constexpr float kPadScaled = 67108864.f;          // 2^26
 struct AdjGeom {
   int nb, S, len, units;
   int ranged, nch, kmax;
+  int pair_num;  // ranged: SM pairs (SweepGeom::pair_num), 0 = off
 };
 
 // The adjoint's ranged tasks in the sweep geometry that ranged_share reads.
@@ -82,6 +87,7 @@ __host__ __device__ inline SweepGeom adj_tasks(const AdjGeom& g) {
   t.nblk = g.nb;
   t.nch = g.nch;
   t.ranged = g.ranged;
+  t.pair_num = g.pair_num;
   return t;
 }
 
@@ -265,14 +271,17 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
   const unsigned G = gridDim.x;
   const AdjGeom& g = A.geo;
   if (tid == 0) {
-    rsh = ranged_share(adj_tasks(g), blockIdx.x, (int)G);
-    if (A.pairs) {
+    s_pair[0] = -1;
+    int vb = (int)blockIdx.x;  // ranged: the virtual block whose share this block sweeps
+    if (A.pairs || g.pair_num) {
       const int2 pr = join_sm_pair(A.pair_tab, A.timeout_ns);
       if (pr.x < 0 || pr.x >= (int)G / 2) set_status(A.ctl, kStatusInternal, 105);
-      s_pair[0] = pr.x < (int)G / 2 ? pr.x : -1;
+      s_pair[0] = pr.x >= 0 && pr.x < (int)G / 2 ? pr.x : -1;
       s_pair[1] = pr.y;
       s_pair[2] = 0;
+      vb = 2 * pr.x + pr.y;
     }
+    rsh = g.pair_num && s_pair[0] < 0 ? RangedShare{0, -1, 0, 0, 0} : ranged_share(adj_tasks(g), vb, (int)G);
     // caller frame -> centred frame: t = t' + oX - R oY, so dL/dt' = dL/dt and
     // dL/dR' = dL/dR - dL/dt oY^T
     for (int i = 0; i < 3; ++i) {
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
         u_end = first ? pu.split : pu.hi;
       }
     }
-    if (A.pairs && tid == 0) s_tsweep = global_ns();
+    if (tid == 0 && s_pair[0] >= 0) s_tsweep = global_ns();
     for (int u = u_begin; u < u_end; u += u_step) {
       // unit: column block cb, rows [rb, re); its dL/dx partials go to px_dst
       int cb, rb, re;
@@ -481,15 +490,27 @@ __global__ void __launch_bounds__(kThreads, 2) emicp_adjoint_kernel(const EmAdjA
                              (gx[j][2].x + gx[j][2].y) * inv_sc, 0.f));
       }
     }
-    if (A.pairs && tid == 0 && s_pair[0] >= 0)
+    if (tid == 0 && s_pair[0] >= 0)
       A.pair_t[2 * s_pair[0] + (s_pair[1] ^ s_pair[2])] = (float)(global_ns() - s_tsweep);
     if (!ok || !grid_sync(A.ctl, epoch, G, A.timeout_ns, 102)) {
       ok = false;
       break;
     }
-    if (A.pairs && tid == 0 && s_pair[0] >= 0) {  // both blocks of the pair read the same two times
-      const PairUnits pu = pair_units(g.units, (int)G / 2, s_pair[0]);
-      if (pair_swap(pu.lo, pu.split, pu.hi, A.pair_t, s_pair[0])) s_pair[2] ^= 1;
+    if (tid == 0 && s_pair[0] >= 0) {  // both blocks of the pair read the same two times
+      long lo = 0, sp = 0, hi = 0;
+      if (g.pair_num) {
+        ranged_tasks(adj_tasks(g), 2 * s_pair[0], (int)G, lo, sp);
+        ranged_tasks(adj_tasks(g), 2 * s_pair[0] + 1, (int)G, sp, hi);
+      } else {
+        const PairUnits pu = pair_units(g.units, (int)G / 2, s_pair[0]);
+        lo = pu.lo;
+        sp = pu.split;
+        hi = pu.hi;
+      }
+      if (pair_swap(lo, sp, hi, A.pair_t, s_pair[0])) {
+        s_pair[2] ^= 1;
+        if (g.pair_num) rsh = ranged_share(adj_tasks(g), 2 * s_pair[0] + (s_pair[1] ^ s_pair[2]), (int)G);
+      }
     }
     // Rows completed, each block a contiguous share of them (all blocks in
     // parallel, no serial tail): the column blocks' dL/dz partials summed in
@@ -684,26 +705,33 @@ AdjPlan plan_adj(int N, int M, int device, int layout) {
   g.ranged = 0;
   g.nch = (M + kAdjRows - 1) / kAdjRows;
   g.kmax = 0;
+  g.pair_num = 0;
   P.geo = g;
   P.grid = g.units < limit ? g.units : limit;
-  // AUTO: ranged tasks where their longest run (in 256-row chunks) is shorter
-  // than the slice plan's (its waves times the chunks of a slice).
+  // SM pairs (two blocks on every SM): slice units dealt to pairs (at least
+  // four units per pair), or the ranged tasks split within each pair
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const char* ev = getenv("CESA_SM_PAIRS");  // "0": equal shares (for comparisons)
+  const bool two_per_sm = sms > 0 && limit == 2 * sms && !(ev && ev[0] == '0');
+  // AUTO: ranged tasks for large clouds when SM pairs split them (the split
+  // is then finer than whole units), else where their longest run (in
+  // 256-row chunks) is shorter than the slice plan's (its waves times the
+  // chunks of a slice).
   const long T = (long)g.nb * g.nch;
   const long per = (T + limit - 1) / limit;
   const int waves = (g.units + limit - 1) / limit;
-  const bool ranged = layout == CESA_LAYOUT_RANGED ||
-                      (layout == CESA_LAYOUT_AUTO && T >= 8L * limit && (double)per < (double)waves * g.len / kAdjRows);
+  const bool ranged =
+      layout == CESA_LAYOUT_RANGED ||
+      (layout == CESA_LAYOUT_AUTO && T >= 8L * limit &&
+       (two_per_sm || (double)per < (double)waves * g.len / kAdjRows));
   if (ranged) {
     P.geo.ranged = 1;
+    P.geo.pair_num = two_per_sm ? kAdjRangedPairNum : 0;
     P.geo.kmax = ranged_kmax(adj_tasks(P.geo), limit);  // tasks of kAdjRows rows: g.nch as set above
     P.grid = limit;
   }
-  // SM pairs: two blocks on every SM and at least four units per pair
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  P.pairs = !P.geo.ranged && sms > 0 && limit == 2 * sms && P.grid == limit && P.geo.units >= 2 * P.grid;
-  const char* ev = getenv("CESA_SM_PAIRS");  // "0": deal the units evenly (for comparisons)
-  if (ev && ev[0] == '0') P.pairs = 0;
+  P.pairs = !P.geo.ranged && two_per_sm && P.grid == limit && P.geo.units >= 2 * P.grid;
   return P;
 }
 

@@ -71,7 +71,7 @@ struct SweepGeom {
   int pair_num;
 };
 
-constexpr int kPairDen = 16;
+constexpr int kPairDen = 256;
 constexpr int kPairCap = 1024;  // SM ids a pairing table covers
 
 // The split point of a pair's tasks [lo, hi).
