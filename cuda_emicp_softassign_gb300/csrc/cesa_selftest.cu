@@ -7,6 +7,7 @@
 
 #include "../../include/cesa.h"
 #include "cesa_common.cuh"
+#include "cesa_sweep.cuh"
 
 namespace {
 
@@ -75,4 +76,33 @@ extern "C" int cesa_self_test_waits(int which, int timeout_us, int* status_out, 
   *status_out = h.status;
   *where_out = h.where;
   return rc;
+}
+
+extern "C" int cesa_self_test_partition(int nblk, int nch, int grid, int pair_num, int* kmax_out) {
+  if (nblk < 1 || nch < 1 || grid < 1 || pair_num < 0 || pair_num >= cesa::kPairDen || !kmax_out ||
+      (pair_num > 0 && (grid & 1)) || (long)nblk * nch > 50000000L)
+    return CESA_ERR_INVALID_ARGUMENT;
+  cesa::SweepGeom g{};
+  g.nblk = nblk;
+  g.nch = nch;
+  g.ranged = 1;
+  g.pair_num = pair_num;
+  g.kmax = cesa::ranged_kmax(g, grid);
+  *kmax_out = g.kmax;
+  long next = 0;
+  for (int b = 0; b < grid; ++b) {
+    long t0 = 0, t1 = 0;
+    cesa::ranged_tasks(g, b, grid, t0, t1);
+    if (t0 != next || t1 < t0) return CESA_ERR_INTERNAL;
+    next = t1;
+    for (long t = t0; t < t1; ++t)
+      if (cesa::ranged_block_of(g, t, grid) != b) return CESA_ERR_INTERNAL;
+    if (t1 == t0) continue;
+    const long o_first = t0 / nch, o_last = (t1 - 1) / nch;
+    const int j_first = b - cesa::ranged_block_of(g, o_first * nch, grid);
+    if (j_first < 0 || j_first >= g.kmax) return CESA_ERR_INTERNAL;
+    for (long o = o_first + 1; o <= o_last; ++o)
+      if (cesa::ranged_block_of(g, o * nch, grid) != b) return CESA_ERR_INTERNAL;
+  }
+  return next == (long)nblk * nch ? CESA_OK : CESA_ERR_INTERNAL;
 }

@@ -397,6 +397,17 @@ const char* cesa_status_string(int status);
  * when the probe ran and the device is still usable afterwards. */
 int cesa_self_test_waits(int which, int timeout_us, int* status_out, int* where_out);
 
+/* Host-side check of the ranged sweeps' task partition (no counterpart in the
+ * reference; needs no GPU): nblk owned blocks of nch tasks each over `grid`
+ * blocks, split within SM pairs at pair_num / 256 (0: equal shares; else grid
+ * even). Checks, with the functions the kernels use, that the blocks' task
+ * ranges tile the tasks in order, that every task maps back to its block,
+ * and that every block's slot index among the blocks covering its first owned
+ * block is below the partition's kmax (it is the first to cover every later
+ * one). Returns CESA_OK, CESA_ERR_INTERNAL when a property fails, or
+ * CESA_ERR_INVALID_ARGUMENT; *kmax_out receives kmax. */
+int cesa_self_test_partition(int nblk, int nch, int grid, int pair_num, int* kmax_out);
+
 /* Library version as major*10000 + minor*100 + patch. */
 int cesa_version(void);
 
