@@ -53,6 +53,25 @@ def test_c3_registration_matches_fp64_oracle(cesa, c3):
         assert np.abs(tr[k, 27:30] - tro[k, 27:30]).max() < 1e-5 * ext, k
 
 
+def test_c3_sm_pairs_repeat_bitwise_and_hold_the_bounds(cesa, c3, monkeypatch):
+    """At config 3 each SM's two blocks split their task range 13 : 3, and
+    which block takes which part is decided at run time (order of arrival,
+    corrected from the sweep times). The partition itself is fixed, so
+    repeated registrations agree bitwise; with equal shares
+    (CESA_SM_PAIRS=0) the partial sums group differently, and both results
+    stay within the bounds against the FP64 oracle."""
+    X, Y = c3["X"], c3["Y"]
+    ext = _extent(X)
+    R1, t1 = cesa.emicp(X, Y)
+    R2, t2 = cesa.emicp(X, Y)
+    assert np.array_equal(R1, R2) and np.array_equal(t1, t2)
+    monkeypatch.setenv("CESA_SM_PAIRS", "0")
+    R3, t3 = cesa.emicp(X, Y)
+    monkeypatch.delenv("CESA_SM_PAIRS")
+    for R, t in ((R1, t1), (R3, t3)):
+        assert rot_err_deg(R, c3["R"]) < 1e-3 and np.abs(t - c3["t"]).max() / ext < 1e-5
+
+
 def test_c3_every_step_moments_from_the_oracle_pose(cesa, torch_cuda, c3):
     """Each of the 66 E-steps, taken from the oracle's input pose of that step
     at its sigma: sum lambda, Xc, Yc and S within 1e-5 of the oracle's."""
