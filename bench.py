@@ -1054,6 +1054,20 @@ def run_ours(args, rank, world, local):
                               "note": "both searches are exact and return the same matches"}
     if not args.no_adjoint and kind != "icp":
         adj = measure_adjoint(cesa, kind, dX, dY, N, M, p, pose0)
+        if kind == "emicp":
+            # the backward's own roofline: 19 FP32-pipe ops per element and sigma step
+            fp32_peak, _ = load_peaks()
+            ops = 19.0 * float(N) * float(M) * pose_updates(kind, p)
+            ach = ops / (adj["bwd_ms"] * 1e-3) / 1e12
+            adj["roofline"] = {
+                "bound": "fp32", "kernel": "emicp_adjoint_kernel", "achieved": ach,
+                "peak": fp32_peak / 1e12 if fp32_peak else None, "unit": "TFLOP/s",
+                "frac": ach / (fp32_peak / 1e12) if fp32_peak else None,
+                "executed_fp32_ops_per_registration": ops,
+                "note": ("19 FP32-pipe ops per affinity element and sigma step, executed as packed pairs (6 for "
+                         "the distance, 4 for ge, 3 for t = gB - ge (x - z) / s2, 3 each for dL/dx and dL/dz "
+                         "+= e t), over the N x M elements without padding, divided by the backward call's "
+                         "event time; peak as the forward's")}
         if kind == "softassign" and form_used != "matrix_free":
             # the tape comes from the matrix-free kernel; against the forward this
             # request actually runs (value's form) the ratio is higher
